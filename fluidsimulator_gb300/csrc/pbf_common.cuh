@@ -1,0 +1,119 @@
+// Shared device-side types of the GB300 PBF timestep.
+//
+// Layout in HBM (one solver, all scenes back to back, N particles):
+//   x[2], v[2]    float4 per slot, cell-sorted order of the current step;
+//                 x.w = caller index (int bits), v.w = scene (int bits).
+//                 Parity buffers: a step reads [p] and writes [1-p], so a
+//                 step that has to be re-run still has its input.
+//   slot[2]       int per caller index: its slot in x/v.
+//   p0, p1        float4 predicted positions (p.w = scene), ping-pong over
+//                 the Jacobi iterations.
+//   v2            float4 velocity scratch for XSPH; omega float4 (w = |omega|).
+//   lambda, rho[2] float per slot.
+//   keys/vals     radix-sort ping-pong (u32 cell key, int caller index).
+//   table         int2 (first, end) per cell of the per-scene bounding grids.
+//   cnt, nbr      neighbour lists in 32-wide slices: warp w (slots 32w..32w+31)
+//                 owns 32*depth[w] ints from wbase[w], entry k of lane l at
+//                 wbase[w] + 32k + l, so every list read is one coalesced
+//                 128-byte access per warp.
+#pragma once
+
+#include <cstdint>
+
+#include "fluid_gb300.h"
+
+namespace fgb {
+
+constexpr int kBlock = 256;
+constexpr int kRadixItems = 8;                      // keys per thread
+constexpr int kRadixTile = kBlock * kRadixItems;    // keys per CTA
+constexpr int kRadixMaxPasses = 4;                  // 8-bit digits of a u32
+constexpr unsigned kFull = 0xffffffffu;
+
+// Per-scene constants, each computed on the host with the same float
+// operations, in the same order, as the reference computes it
+// (core/src/core.cpp:138-148, 270-274 and the kernel helpers :35-71).
+struct SceneConst {
+  float h, inv_h, h2, min_r2;
+  float poly6_c;     // 315 / (64 pi h^9)
+  float w0;          // W(0) = poly6_c * h2^3
+  float spiky_c;     // -45 / (pi h^6)
+  float mass, inv_density, grad_scale, epsilon, density;
+  float scorr_inv_wdq, scorr_neg_k;
+  int scorr_n, scorr_on;
+  float dt, gdt_x, gdt_y, gdt_z;  // external force * dt
+  float visc_c;
+  int xsph_on;
+  float vort_eps, vort_norm_eps;
+  int vort_on;
+  float rest_neg_e, rest_scale;   // -restitution, 1 - friction
+  int rest_on;
+  int plane_count;
+  int iterations;
+  int first_slot, count;          // particle range of the scene
+  float4 planes[FLUID_MAX_PLANES];  // (nx, ny, nz, d)
+};
+
+// Bounding grid of one scene for the current step.
+struct GridInfo {
+  int minx, miny, minz;
+  int dimx, dimy, dimz;
+  uint32_t base;  // first key of the scene
+  int pad;
+};
+
+// Device status word. Kernels read `err` on entry and return when set, so
+// after a failure the rest of the enqueued work is a no-op and the failed
+// step's input buffers stay intact.
+struct DevStatus {
+  int err;        // fluid_status of the first failure
+  int started;    // steps started in this batch
+  int step;       // index within the batch of the step in progress
+  int fail_step;  // step index within the batch that failed
+  int npass;      // radix passes needed this step
+  int pad0;
+  unsigned long long total_cells;
+  unsigned long long need_grid;
+  unsigned long long need_nbr;
+  unsigned long long pairs;  // sum of neighbour counts, this step
+  int nbr_max;
+  int pad;
+};
+
+// Every pointer one step needs, parity already resolved.
+struct StepArgs {
+  const float4* x_old;
+  const float4* v_old;
+  const int* slot_old;
+  const float* rho_old;
+  float4* x;
+  float4* v;
+  float4* v2;
+  int* slot;
+  float4* p[2];
+  float4* omega;
+  float* lambda;
+  float* rho;
+  uint32_t* keys[2];
+  int* vals[2];
+  uint32_t* hist;         // 256 x tiles, digit-major
+  uint32_t* digit_total;  // kRadixMaxPasses x 256
+  int2* table;
+  int* cnt;
+  int* depth;             // per warp
+  long long* wbase;       // per warp
+  int* nbr;
+  int* bmin;              // 3 per scene
+  int* bmax;
+  GridInfo* grid;
+  DevStatus* status;
+  const SceneConst* sc;
+  int n;
+  int scenes;
+  int tiles;              // radix tiles
+  int warps;              // ceil(n / 32)
+  long long grid_capacity;
+  long long nbr_capacity;
+};
+
+}  // namespace fgb

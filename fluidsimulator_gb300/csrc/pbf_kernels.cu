@@ -1,0 +1,965 @@
+// GB300 (sm_103a) kernels of the Position Based Fluids timestep.
+//
+// One timestep, in launch order (reference: core/src/core.cpp:119-615):
+//   k_bounds        predicted cell of every particle, per-scene bounding box
+//   k_grid_setup    per-scene dense grid over that box, key base, radix passes
+//   k_keys          x-major linear cell key per particle, in caller order
+//   k_radix_*       stable LSD radix sort of (key, caller index), 8-bit digits
+//   k_reorder       gather into cell order, predict again (bit-identical),
+//                   cell (first, end) table by warp-shuffle boundary detection
+//   k_nbr_count     27-cell scan: per-particle neighbour counts, slice depths
+//   k_nbr_scan      slice offsets; capacity check
+//   k_nbr_fill      27-cell scan again: lists in scan order + first lambda
+//   k_lambda        density / lambda (iterations 2..n)
+//   k_delta         position correction, s_corr, plane projection (last
+//                   iteration also commits v = (p - x)/dt, x = p)
+//   k_xsph          XSPH viscosity over the step's lists
+//   k_omega, k_eta  vorticity confinement (+ plane restitution / friction)
+//
+// Arithmetic follows the reference's float operations one for one: the
+// library is compiled with -fmad=false (no contraction), IEEE division and
+// square root, and each neighbour sum runs in the reference's order (cells
+// dz, dy, dx; ascending caller index inside a cell), so on the same input the
+// results equal the reference CPU path bit for bit. Membership tests and the
+// prediction use explicit round-to-nearest intrinsics as well.
+
+#include <climits>
+#include <cstdint>
+
+#include "pbf_common.cuh"
+#include "pbf_launch.h"
+
+namespace fgb {
+namespace {
+
+__device__ __forceinline__ bool failed(const DevStatus* st) {
+  return *reinterpret_cast<const volatile int*>(&st->err) != 0;
+}
+
+__device__ __forceinline__ void set_error(DevStatus* st, int code) {
+  if (atomicCAS(&st->err, 0, code) == 0) st->fail_step = st->step;
+}
+
+__device__ __forceinline__ unsigned lanemask_lt(int lane) { return (1u << lane) - 1u; }
+
+// v += f dt; p = x + v dt  (core.cpp:154-160), each operation rounded.
+__device__ __forceinline__ float4 predict(const SceneConst& c, const float4 x, float4& v) {
+  v.x = __fadd_rn(v.x, c.gdt_x);
+  v.y = __fadd_rn(v.y, c.gdt_y);
+  v.z = __fadd_rn(v.z, c.gdt_z);
+  float4 p;
+  p.x = __fadd_rn(x.x, __fmul_rn(v.x, c.dt));
+  p.y = __fadd_rn(x.y, __fmul_rn(v.y, c.dt));
+  p.z = __fadd_rn(x.z, __fmul_rn(v.z, c.dt));
+  p.w = v.w;
+  return p;
+}
+
+// floor(p * (1/h)) per axis (core.cpp:28-34). False when out of range / NaN.
+__device__ __forceinline__ bool cell_of(const SceneConst& c, const float4 p, int& cx, int& cy, int& cz) {
+  const float fx = __fmul_rn(p.x, c.inv_h);
+  const float fy = __fmul_rn(p.y, c.inv_h);
+  const float fz = __fmul_rn(p.z, c.inv_h);
+  if (!(fabsf(fx) < 1.0e9f && fabsf(fy) < 1.0e9f && fabsf(fz) < 1.0e9f)) return false;
+  cx = static_cast<int>(floorf(fx));
+  cy = static_cast<int>(floorf(fy));
+  cz = static_cast<int>(floorf(fz));
+  return true;
+}
+
+// (dx*dx + dy*dy) + dz*dz, each operation rounded (core.cpp:234-237).
+__device__ __forceinline__ float dist2(float dx, float dy, float dz) {
+  return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+}
+
+// W_poly6 for r2 < h2 (core.cpp:35-46): coeff * ((d*d)*d), d = h2 - r2.
+__device__ __forceinline__ float poly6(const SceneConst& c, float r2) {
+  const float d = c.h2 - r2;
+  return c.poly6_c * (d * d * d);
+}
+
+// Spiky gradient factor (core.cpp:48-57): (coeff * (h - r)) * (h - r).
+__device__ __forceinline__ float spiky(const SceneConst& c, float r) {
+  if (r > c.h) return 0.0f;
+  const float d = c.h - r;
+  return c.spiky_c * d * d;
+}
+
+// r from r^2 with the 0.01 h floor (core.cpp:303).
+__device__ __forceinline__ float clamped_r(const SceneConst& c, float r2) {
+  return sqrtf(r2 < c.min_r2 ? c.min_r2 : r2);
+}
+
+// ratio^n (core.cpp:59-71).
+__device__ __forceinline__ float pow_n(float r, int n) {
+  if (n == 2) return r * r;
+  if (n == 3) return r * r * r;
+  if (n == 4) {
+    const float r2 = r * r;
+    return r2 * r2;
+  }
+  return powf(r, static_cast<float>(n));
+}
+
+// Plane restitution and friction on velocity (core.cpp:586-606).
+__device__ __forceinline__ void restitution(const SceneConst& c, float px, float py, float pz,
+                                            float& vx, float& vy, float& vz) {
+  for (int q = 0; q < c.plane_count; ++q) {
+    const float4 pl = c.planes[q];
+    const float sd = pl.x * px + pl.y * py + pl.z * pz - pl.w;
+    if (sd <= 0.0f) {
+      const float vn = pl.x * vx + pl.y * vy + pl.z * vz;
+      float vn_new = vn;
+      if (vn < 0.0f) vn_new = c.rest_neg_e * vn;
+      const float tx = vx - vn * pl.x;
+      const float ty = vy - vn * pl.y;
+      const float tz = vz - vn * pl.z;
+      vx = tx * c.rest_scale + vn_new * pl.x;
+      vy = ty * c.rest_scale + vn_new * pl.y;
+      vz = tz * c.rest_scale + vn_new * pl.z;
+    }
+  }
+}
+
+__device__ __forceinline__ uint32_t cell_key(const GridInfo& g, int cx, int cy, int cz) {
+  const long long l = (static_cast<long long>(cx - g.minx) * g.dimy + (cy - g.miny)) * g.dimz + (cz - g.minz);
+  return g.base + static_cast<uint32_t>(l);
+}
+
+__device__ __forceinline__ const uint32_t* sorted_keys(const StepArgs& a, int npass) {
+  return a.keys[npass & 1];
+}
+
+// Cell range from the table; entries left from earlier steps are rejected
+// because the first slot of a live entry holds that cell's key this step.
+__device__ __forceinline__ bool cell_range(const StepArgs& a, const uint32_t* ks, uint32_t key,
+                                           int& first, int& end) {
+  const int2 e = a.table[key];
+  if (e.x < 0 || e.x >= e.y || e.y > a.n) return false;
+  if (__ldg(ks + e.x) != key) return false;
+  first = e.x;
+  end = e.y;
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// Bounds, grid, keys
+
+__global__ void __launch_bounds__(kBlock) k_bounds(StepArgs a) {
+  if (failed(a.status)) return;
+  const int s = blockIdx.x * kBlock + threadIdx.x;
+  int scene = -1;
+  int cx = 0, cy = 0, cz = 0;
+  bool ok = false;
+  if (s < a.n) {
+    const float4 x = a.x_old[s];
+    float4 v = a.v_old[s];
+    scene = __float_as_int(v.w);
+    const SceneConst& c = a.sc[scene];
+    ok = cell_of(c, predict(c, x, v), cx, cy, cz);
+  }
+  const int s0 = __shfl_sync(kFull, scene, 0);
+  const bool uniform = __all_sync(kFull, scene == s0 || scene < 0);
+  if (uniform) {
+    if (s0 < 0) return;
+    const int mnx = __reduce_min_sync(kFull, ok ? cx : INT_MAX);
+    const int mny = __reduce_min_sync(kFull, ok ? cy : INT_MAX);
+    const int mnz = __reduce_min_sync(kFull, ok ? cz : INT_MAX);
+    const int mxx = __reduce_max_sync(kFull, ok ? cx : INT_MIN);
+    const int mxy = __reduce_max_sync(kFull, ok ? cy : INT_MIN);
+    const int mxz = __reduce_max_sync(kFull, ok ? cz : INT_MIN);
+    if ((threadIdx.x & 31) == 0 && mnx != INT_MAX) {
+      atomicMin(&a.bmin[3 * s0 + 0], mnx);
+      atomicMin(&a.bmin[3 * s0 + 1], mny);
+      atomicMin(&a.bmin[3 * s0 + 2], mnz);
+      atomicMax(&a.bmax[3 * s0 + 0], mxx);
+      atomicMax(&a.bmax[3 * s0 + 1], mxy);
+      atomicMax(&a.bmax[3 * s0 + 2], mxz);
+    }
+  } else if (ok) {
+    atomicMin(&a.bmin[3 * scene + 0], cx);
+    atomicMin(&a.bmin[3 * scene + 1], cy);
+    atomicMin(&a.bmin[3 * scene + 2], cz);
+    atomicMax(&a.bmax[3 * scene + 0], cx);
+    atomicMax(&a.bmax[3 * scene + 1], cy);
+    atomicMax(&a.bmax[3 * scene + 2], cz);
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_grid_setup(StepArgs a) {
+  if (failed(a.status)) return;
+  DevStatus* st = a.status;
+  for (int i = threadIdx.x; i < kRadixMaxPasses * 256; i += blockDim.x) a.digit_total[i] = 0;
+  if (threadIdx.x != 0) return;
+  st->step = st->started;
+  st->started = st->started + 1;
+  st->pairs = 0ull;
+  st->nbr_max = 0;
+  unsigned long long total = 0;
+  bool domain = false;
+  for (int s = 0; s < a.scenes; ++s) {
+    GridInfo g;
+    g.minx = a.bmin[3 * s + 0];
+    g.miny = a.bmin[3 * s + 1];
+    g.minz = a.bmin[3 * s + 2];
+    const int mxx = a.bmax[3 * s + 0], mxy = a.bmax[3 * s + 1], mxz = a.bmax[3 * s + 2];
+    g.base = static_cast<uint32_t>(total);
+    g.pad = 0;
+    if (g.minx > mxx || g.miny > mxy || g.minz > mxz) {
+      g.dimx = g.dimy = g.dimz = 0;
+    } else {
+      const double dx = double(mxx) - double(g.minx) + 1.0;
+      const double dy = double(mxy) - double(g.miny) + 1.0;
+      const double dz = double(mxz) - double(g.minz) + 1.0;
+      if (dx * dy * dz + double(total) > 2147483647.0) {
+        domain = true;
+        g.dimx = g.dimy = g.dimz = 0;
+      } else {
+        g.dimx = int(dx);
+        g.dimy = int(dy);
+        g.dimz = int(dz);
+        total += static_cast<unsigned long long>(g.dimx) * g.dimy * g.dimz;
+      }
+    }
+    a.grid[s] = g;
+    a.bmin[3 * s + 0] = a.bmin[3 * s + 1] = a.bmin[3 * s + 2] = INT_MAX;
+    a.bmax[3 * s + 0] = a.bmax[3 * s + 1] = a.bmax[3 * s + 2] = INT_MIN;
+  }
+  st->total_cells = total;
+  st->npass = total <= 1ull ? 0 : (32 - __clz(static_cast<int>(total - 1ull)) + 7) / 8;
+  if (domain) {
+    set_error(st, FLUID_ERR_DOMAIN);
+  } else if (static_cast<long long>(total) > a.grid_capacity) {
+    st->need_grid = total;
+    set_error(st, FLUID_ERR_CAPACITY);
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_keys(StepArgs a) {
+  if (failed(a.status)) return;
+  const int s = blockIdx.x * kBlock + threadIdx.x;
+  if (s >= a.n) return;
+  const float4 x = a.x_old[s];
+  float4 v = a.v_old[s];
+  const int scene = __float_as_int(v.w);
+  const SceneConst& c = a.sc[scene];
+  const float4 p = predict(c, x, v);
+  int cx, cy, cz;
+  if (!cell_of(c, p, cx, cy, cz)) {
+    const bool finite = isfinite(p.x) && isfinite(p.y) && isfinite(p.z);
+    set_error(a.status, finite ? FLUID_ERR_DOMAIN : FLUID_ERR_NONFINITE);
+    return;
+  }
+  a.keys[0][__float_as_int(x.w)] = cell_key(a.grid[scene], cx, cy, cz);
+}
+
+// ---------------------------------------------------------------------------
+// Stable LSD radix sort, 8-bit digits. Pass p reads keys[p&1] (pass 0: values
+// are the caller indices themselves) and writes keys[(p+1)&1].
+
+__global__ void __launch_bounds__(kBlock) k_radix_hist(StepArgs a, int pass) {
+  if (failed(a.status) || pass >= a.status->npass) return;
+  __shared__ uint32_t cnt[kBlock / 32][256];
+  const int warp = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < (kBlock / 32) * 256; i += kBlock) (&cnt[0][0])[i] = 0;
+  __syncthreads();
+  const uint32_t* kin = a.keys[pass & 1];
+  const int shift = 8 * pass;
+  const long long base = static_cast<long long>(blockIdx.x) * kRadixTile;
+#pragma unroll
+  for (int r = 0; r < kRadixItems; ++r) {
+    const long long idx = base + r * kBlock + threadIdx.x;
+    if (idx < a.n) atomicAdd(&cnt[warp][(kin[idx] >> shift) & 255u], 1u);
+  }
+  __syncthreads();
+  const int d = threadIdx.x;
+  uint32_t sum = 0;
+#pragma unroll
+  for (int w = 0; w < kBlock / 32; ++w) sum += cnt[w][d];
+  a.hist[static_cast<long long>(d) * a.tiles + blockIdx.x] = sum;
+  if (sum) atomicAdd(&a.digit_total[pass * 256 + d], sum);
+}
+
+// One CTA per digit: exclusive scan of that digit's tile counts plus the
+// number of keys with a smaller digit.
+__global__ void __launch_bounds__(kBlock) k_radix_scan(StepArgs a, int pass) {
+  if (failed(a.status) || pass >= a.status->npass) return;
+  __shared__ uint32_t warp_sums[kBlock / 32];
+  __shared__ uint32_t carry;
+  const int d = blockIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t below = (threadIdx.x < d) ? a.digit_total[pass * 256 + threadIdx.x] : 0u;
+  below = __reduce_add_sync(kFull, below);
+  if (lane == 0) warp_sums[warp] = below;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t s = 0;
+    for (int w = 0; w < kBlock / 32; ++w) s += warp_sums[w];
+    carry = s;
+  }
+  __syncthreads();
+  uint32_t* row = a.hist + static_cast<long long>(d) * a.tiles;
+  for (int chunk = 0; chunk < a.tiles; chunk += kBlock) {
+    const int t = chunk + threadIdx.x;
+    const uint32_t v = (t < a.tiles) ? row[t] : 0u;
+    uint32_t inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(kFull, inc, o);
+      if (lane >= o) inc += y;
+    }
+    __syncthreads();
+    if (lane == 31) warp_sums[warp] = inc;
+    __syncthreads();
+    uint32_t wpre = 0, all = 0;
+#pragma unroll
+    for (int w = 0; w < kBlock / 32; ++w) {
+      const uint32_t ws = warp_sums[w];
+      if (w < warp) wpre += ws;
+      all += ws;
+    }
+    const uint32_t c0 = carry;
+    if (t < a.tiles) row[t] = c0 + wpre + inc - v;
+    __syncthreads();
+    if (threadIdx.x == 0) carry = c0 + all;
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_radix_scatter(StepArgs a, int pass) {
+  if (failed(a.status) || pass >= a.status->npass) return;
+  __shared__ uint32_t wcnt[kBlock / 32][256];
+  __shared__ uint32_t goff[256];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < (kBlock / 32) * 256; i += kBlock) (&wcnt[0][0])[i] = 0;
+  goff[threadIdx.x] = a.hist[static_cast<long long>(threadIdx.x) * a.tiles + blockIdx.x];
+  __syncthreads();
+  const uint32_t* kin = a.keys[pass & 1];
+  const int* vin = a.vals[pass & 1];
+  uint32_t* kout = a.keys[(pass + 1) & 1];
+  int* vout = a.vals[(pass + 1) & 1];
+  const int shift = 8 * pass;
+  // Warp w ranks its contiguous 32*kRadixItems keys in order, 32 at a time.
+  const long long base = static_cast<long long>(blockIdx.x) * kRadixTile + warp * (32 * kRadixItems);
+  uint32_t key[kRadixItems];
+  int val[kRadixItems];
+  int dig[kRadixItems];
+  uint32_t rank[kRadixItems];
+#pragma unroll
+  for (int r = 0; r < kRadixItems; ++r) {
+    const long long idx = base + r * 32 + lane;
+    const bool ok = idx < a.n;
+    key[r] = ok ? kin[idx] : 0u;
+    val[r] = ok ? (pass == 0 ? static_cast<int>(idx) : vin[idx]) : 0;
+    const int d = ok ? static_cast<int>((key[r] >> shift) & 255u) : 256;
+    dig[r] = d;
+    const unsigned peers = __match_any_sync(kFull, d);
+    const uint32_t before = __popc(peers & lanemask_lt(lane));
+    const uint32_t run = (d < 256) ? wcnt[warp][d] : 0u;
+    __syncwarp();
+    if (d < 256 && before == 0) wcnt[warp][d] = run + __popc(peers);
+    __syncwarp();
+    rank[r] = run + before;
+  }
+  __syncthreads();
+  {
+    const int d = threadIdx.x;
+    uint32_t run = 0;
+#pragma unroll
+    for (int w = 0; w < kBlock / 32; ++w) {
+      const uint32_t t = wcnt[w][d];
+      wcnt[w][d] = run;
+      run += t;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < kRadixItems; ++r) {
+    const int d = dig[r];
+    if (d < 256) {
+      const uint32_t pos = goff[d] + wcnt[warp][d] + rank[r];
+      kout[pos] = key[r];
+      vout[pos] = val[r];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Reorder into cell order and cell table.
+
+__global__ void __launch_bounds__(kBlock) k_reorder(StepArgs a) {
+  if (failed(a.status)) return;
+  const int s = blockIdx.x * kBlock + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int npass = a.status->npass;
+  const uint32_t* ks = sorted_keys(a, npass);
+  const bool ok = s < a.n;
+  const uint32_t key = ok ? ks[s] : 0xffffffffu;
+  // Neighbouring keys through the warp; warp-edge lanes read memory.
+  uint32_t prev = __shfl_up_sync(kFull, key, 1);
+  uint32_t next = __shfl_down_sync(kFull, key, 1);
+  if (!ok) return;
+  if (lane == 0) prev = (s > 0) ? ks[s - 1] : ~key;
+  if (lane == 31 || s + 1 >= a.n) next = (s + 1 < a.n) ? ks[s + 1] : ~key;
+  int* table = reinterpret_cast<int*>(a.table);
+  if (prev != key) table[2ll * key] = s;
+  if (next != key) table[2ll * key + 1] = s + 1;
+
+  const int orig = npass ? a.vals[npass & 1][s] : s;
+  const int old = a.slot_old[orig];
+  const float4 x = a.x_old[old];
+  float4 v = a.v_old[old];
+  const int scene = __float_as_int(v.w);
+  const SceneConst& c = a.sc[scene];
+  const float4 p = predict(c, x, v);
+  a.x[s] = x;
+  a.v[s] = v;
+  a.p[0][s] = p;
+  a.slot[orig] = s;
+  if (c.iterations == 0) a.rho[s] = a.rho_old[old];
+}
+
+// ---------------------------------------------------------------------------
+// Neighbour lists.
+
+struct Cell27 {
+  int cx, cy, cz;
+};
+
+// Visits every j != i of the 27 cells around p in the reference's order
+// (core.cpp:211-243), calling f(j, q_j) for each candidate.
+template <typename F>
+__device__ __forceinline__ void for_each_candidate(const StepArgs& a, const uint32_t* ks, const GridInfo& g,
+                                                   const SceneConst& c, int i, const float4 p,
+                                                   const float4* __restrict__ pos, F&& f) {
+  int cx, cy, cz;
+  cell_of(c, p, cx, cy, cz);
+  for (int oz = -1; oz <= 1; ++oz) {
+    const int z = cz + oz;
+    if (z < g.minz || z >= g.minz + g.dimz) continue;
+    for (int oy = -1; oy <= 1; ++oy) {
+      const int y = cy + oy;
+      if (y < g.miny || y >= g.miny + g.dimy) continue;
+      for (int ox = -1; ox <= 1; ++ox) {
+        const int xx = cx + ox;
+        if (xx < g.minx || xx >= g.minx + g.dimx) continue;
+        int first, end;
+        if (!cell_range(a, ks, cell_key(g, xx, y, z), first, end)) continue;
+        for (int j = first; j < end; ++j) {
+          if (j == i) continue;
+          f(j, pos[j]);
+        }
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_nbr_count(StepArgs a) {
+  if (failed(a.status)) return;
+  const int i = blockIdx.x * kBlock + threadIdx.x;
+  int count = 0;
+  if (i < a.n) {
+    const uint32_t* ks = sorted_keys(a, a.status->npass);
+    const float4 p = a.p[0][i];
+    const int scene = __float_as_int(p.w);
+    const SceneConst& c = a.sc[scene];
+    const GridInfo g = a.grid[scene];
+    const float h2 = c.h2;
+    for_each_candidate(a, ks, g, c, i, p, a.p[0], [&](int, const float4 q) {
+      if (dist2(p.x - q.x, p.y - q.y, p.z - q.z) < h2) ++count;
+    });
+    a.cnt[i] = count;
+  }
+  const int mx = __reduce_max_sync(kFull, count);
+  const unsigned sum = __reduce_add_sync(kFull, static_cast<unsigned>(count));
+  if ((threadIdx.x & 31) == 0 && i < a.n) {
+    a.depth[i >> 5] = mx;
+    if (sum) atomicAdd(&a.status->pairs, static_cast<unsigned long long>(sum));
+    if (mx) atomicMax(&a.status->nbr_max, mx);
+  }
+}
+
+// Single CTA: exclusive scan of 32 * depth over warps.
+__global__ void __launch_bounds__(1024) k_nbr_scan(StepArgs a) {
+  if (failed(a.status)) return;
+  __shared__ long long warp_sums[32];
+  __shared__ long long carry;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int chunk = 0; chunk < a.warps; chunk += 1024) {
+    const int w = chunk + threadIdx.x;
+    const long long v = (w < a.warps) ? 32ll * a.depth[w] : 0ll;
+    long long inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long y = __shfl_up_sync(kFull, inc, o);
+      if (lane >= o) inc += y;
+    }
+    if (lane == 31) warp_sums[warp] = inc;
+    __syncthreads();
+    long long wpre = 0, all = 0;
+    for (int k = 0; k < 32; ++k) {
+      const long long ws = warp_sums[k];
+      if (k < warp) wpre += ws;
+      all += ws;
+    }
+    const long long c0 = carry;
+    if (w < a.warps) a.wbase[w] = c0 + wpre + inc - v;
+    __syncthreads();
+    if (threadIdx.x == 0) carry = c0 + all;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && carry > a.nbr_capacity) {
+    a.status->need_nbr = static_cast<unsigned long long>(carry);
+    set_error(a.status, FLUID_ERR_CAPACITY);
+  }
+}
+
+// Lambda from the accumulated sums (core.cpp:319-328).
+__device__ __forceinline__ float finish_lambda(const SceneConst& c, float rho, float gsx, float gsy, float gsz,
+                                               float sum_g2, float& rho_out) {
+  rho = rho + c.w0;
+  rho = rho * c.mass;
+  rho_out = rho;
+  const float C = rho * c.inv_density - 1.0f;
+  const float ix = c.grad_scale * gsx;
+  const float iy = c.grad_scale * gsy;
+  const float iz = c.grad_scale * gsz;
+  sum_g2 += ix * ix + iy * iy + iz * iz;
+  return -C / (sum_g2 + c.epsilon);
+}
+
+// Per-neighbour density / gradient terms (core.cpp:300-316).
+struct LambdaAcc {
+  float rho = 0.0f, gsx = 0.0f, gsy = 0.0f, gsz = 0.0f, sum_g2 = 0.0f;
+  __device__ __forceinline__ void add(const SceneConst& c, float dx, float dy, float dz, float r2) {
+    rho += poly6(c, r2);
+    const float gf = spiky(c, clamped_r(c, r2));
+    const float gx = gf * dx, gy = gf * dy, gz = gf * dz;
+    gsx += gx;
+    gsy += gy;
+    gsz += gz;
+    const float ng = -c.grad_scale;
+    const float jx = ng * gx, jy = ng * gy, jz = ng * gz;
+    sum_g2 += jx * jx + jy * jy + jz * jz;
+  }
+};
+
+__global__ void __launch_bounds__(kBlock) k_nbr_fill(StepArgs a) {
+  if (failed(a.status)) return;
+  const int i = blockIdx.x * kBlock + threadIdx.x;
+  if (i >= a.n) return;
+  const uint32_t* ks = sorted_keys(a, a.status->npass);
+  const float4 p = a.p[0][i];
+  const int scene = __float_as_int(p.w);
+  const SceneConst& c = a.sc[scene];
+  const GridInfo g = a.grid[scene];
+  const int lane = threadIdx.x & 31;
+  const int depth = a.depth[i >> 5];
+  int* out = a.nbr + a.wbase[i >> 5] + lane;
+  const bool lam = c.iterations > 0;
+  const float h2 = c.h2;
+  LambdaAcc acc;
+  int k = 0;
+  for_each_candidate(a, ks, g, c, i, p, a.p[0], [&](int j, const float4 q) {
+    const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+    const float r2 = dist2(dx, dy, dz);
+    if (r2 < h2) {
+      if (k < depth) out[32ll * k] = j;
+      ++k;
+      if (lam) acc.add(c, dx, dy, dz, r2);
+    }
+  });
+  a.cnt[i] = k < depth ? k : depth;  // entries actually written
+  if (lam) {
+    float rho;
+    a.lambda[i] = finish_lambda(c, acc.rho, acc.gsx, acc.gsy, acc.gsz, acc.sum_g2, rho);
+    a.rho[i] = rho;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Jacobi passes over the lists.
+
+__global__ void __launch_bounds__(kBlock) k_lambda(StepArgs a, int in) {
+  if (failed(a.status)) return;
+  const int i = blockIdx.x * kBlock + threadIdx.x;
+  if (i >= a.n) return;
+  const float4* __restrict__ pos = a.p[in];
+  const float4 p = pos[i];
+  const SceneConst& c = a.sc[__float_as_int(p.w)];
+  const int n = a.cnt[i];
+  const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
+  const float h2 = c.h2;
+  LambdaAcc acc;
+  for (int k = 0; k < n; ++k) {
+    const int j = __ldg(list + 32ll * k);
+    const float4 q = __ldg(pos + j);
+    const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+    const float r2 = dist2(dx, dy, dz);
+    if (r2 < h2) acc.add(c, dx, dy, dz, r2);
+  }
+  float rho;
+  a.lambda[i] = finish_lambda(c, acc.rho, acc.gsx, acc.gsy, acc.gsz, acc.sum_g2, rho);
+  a.rho[i] = rho;
+}
+
+// Commit v = (p - x)/dt, x = p (core.cpp:414-421); restitution when this is
+// the step's last velocity write.
+__device__ __forceinline__ void commit(const StepArgs& a, const SceneConst& c, int i, float px, float py, float pz,
+                                       float scene_bits, bool to_v2, bool rest) {
+  float4 x = a.x[i];
+  float vx = (px - x.x) / c.dt;
+  float vy = (py - x.y) / c.dt;
+  float vz = (pz - x.z) / c.dt;
+  x.x = px;
+  x.y = py;
+  x.z = pz;
+  a.x[i] = x;
+  if (rest && c.rest_on) restitution(c, px, py, pz, vx, vy, vz);
+  (to_v2 ? a.v2 : a.v)[i] = make_float4(vx, vy, vz, scene_bits);
+}
+
+__global__ void __launch_bounds__(kBlock) k_delta(StepArgs a, int in, int last, int to_v2, int rest) {
+  if (failed(a.status)) return;
+  const int i = blockIdx.x * kBlock + threadIdx.x;
+  if (i >= a.n) return;
+  const float4* __restrict__ pos = a.p[in];
+  const float4 p = pos[i];
+  const SceneConst& c = a.sc[__float_as_int(p.w)];
+  const int n = a.cnt[i];
+  const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
+  const float* __restrict__ lam = a.lambda;
+  const float li = lam[i];
+  const float h2 = c.h2;
+  float ax = 0.0f, ay = 0.0f, az = 0.0f;
+  for (int k = 0; k < n; ++k) {
+    const int j = __ldg(list + 32ll * k);
+    const float4 q = __ldg(pos + j);
+    const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+    const float r2 = dist2(dx, dy, dz);
+    if (r2 < h2) {
+      const float gf = spiky(c, clamped_r(c, r2));
+      float s = li + __ldg(lam + j);
+      if (c.scorr_on) {
+        const float ratio = poly6(c, r2) * c.scorr_inv_wdq;
+        s += c.scorr_neg_k * pow_n(ratio, c.scorr_n);
+      }
+      ax += s * gf * dx;
+      ay += s * gf * dy;
+      az += s * gf * dz;
+    }
+  }
+  ax *= c.inv_density;
+  ay *= c.inv_density;
+  az *= c.inv_density;
+  if (c.plane_count > 0) {  // core.cpp:372-393
+    float qx = p.x + ax, qy = p.y + ay, qz = p.z + az;
+    for (int q = 0; q < c.plane_count; ++q) {
+      const float4 pl = c.planes[q];
+      const float sd = pl.x * qx + pl.y * qy + pl.z * qz - pl.w;
+      const float pen = -sd;
+      if (pen > 0.0f) {
+        qx += pl.x * pen;
+        qy += pl.y * pen;
+        qz += pl.z * pen;
+      }
+    }
+    ax = qx - p.x;
+    ay = qy - p.y;
+    az = qz - p.z;
+  }
+  const float nx = p.x + ax, ny = p.y + ay, nz = p.z + az;  // core.cpp:404-406
+  if (!last) {
+    a.p[in ^ 1][i] = make_float4(nx, ny, nz, p.w);
+  } else {
+    commit(a, c, i, nx, ny, nz, p.w, to_v2 != 0, rest != 0);
+  }
+}
+
+// Commit without Jacobi iterations (solver_iterations == 0).
+__global__ void __launch_bounds__(kBlock) k_commit(StepArgs a, int to_v2, int rest) {
+  if (failed(a.status)) return;
+  const int i = blockIdx.x * kBlock + threadIdx.x;
+  if (i >= a.n) return;
+  const float4 p = a.p[0][i];
+  commit(a, a.sc[__float_as_int(p.w)], i, p.x, p.y, p.z, p.w, to_v2 != 0, rest != 0);
+}
+
+// XSPH (core.cpp:423-466): reads v2 (committed), writes v.
+__global__ void __launch_bounds__(kBlock) k_xsph(StepArgs a, int rest) {
+  if (failed(a.status)) return;
+  const int i = blockIdx.x * kBlock + threadIdx.x;
+  if (i >= a.n) return;
+  const float4* __restrict__ xs = a.x;
+  const float4* __restrict__ vs = a.v2;
+  const float4 xi = xs[i];
+  const float4 vi = vs[i];
+  const SceneConst& c = a.sc[__float_as_int(vi.w)];
+  float vx = vi.x, vy = vi.y, vz = vi.z;
+  if (c.xsph_on) {
+    const int n = a.cnt[i];
+    const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
+    const float* __restrict__ rho = a.rho;
+    const float h2 = c.h2;
+    float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+    for (int k = 0; k < n; ++k) {
+      const int j = __ldg(list + 32ll * k);
+      const float4 xj = __ldg(xs + j);
+      const float r2 = dist2(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
+      if (r2 < h2) {
+        const float W = poly6(c, r2);
+        const float rj = __ldg(rho + j);
+        const float inv_rho_j = (rj > 0.0f) ? (c.mass / rj) : 0.0f;
+        const float4 vj = __ldg(vs + j);
+        sx += (vj.x - vi.x) * W * inv_rho_j;
+        sy += (vj.y - vi.y) * W * inv_rho_j;
+        sz += (vj.z - vi.z) * W * inv_rho_j;
+      }
+    }
+    vx += c.visc_c * sx;
+    vy += c.visc_c * sy;
+    vz += c.visc_c * sz;
+  }
+  if (rest && c.rest_on) restitution(c, xi.x, xi.y, xi.z, vx, vy, vz);
+  a.v[i] = make_float4(vx, vy, vz, vi.w);
+}
+
+// Vorticity omega and |omega| (core.cpp:472-508).
+__global__ void __launch_bounds__(kBlock) k_omega(StepArgs a) {
+  if (failed(a.status)) return;
+  const int i = blockIdx.x * kBlock + threadIdx.x;
+  if (i >= a.n) return;
+  const float4* __restrict__ xs = a.x;
+  const float4* __restrict__ vs = a.v;
+  const float4 xi = xs[i];
+  const float4 vi = vs[i];
+  const SceneConst& c = a.sc[__float_as_int(vi.w)];
+  float ox = 0.0f, oy = 0.0f, oz = 0.0f;
+  if (c.vort_on) {
+    const int n = a.cnt[i];
+    const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
+    const float h2 = c.h2;
+    for (int k = 0; k < n; ++k) {
+      const int j = __ldg(list + 32ll * k);
+      const float4 xj = __ldg(xs + j);
+      const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+      const float r2 = dist2(dx, dy, dz);
+      if (r2 < h2) {
+        const float gf = spiky(c, clamped_r(c, r2));
+        const float gx = gf * dx, gy = gf * dy, gz = gf * dz;
+        const float4 vj = __ldg(vs + j);
+        const float ux = vj.x - vi.x, uy = vj.y - vi.y, uz = vj.z - vi.z;
+        ox += uy * gz - uz * gy;
+        oy += uz * gx - ux * gz;
+        oz += ux * gy - uy * gx;
+      }
+    }
+  }
+  a.omega[i] = make_float4(ox, oy, oz, sqrtf(ox * ox + oy * oy + oz * oz));
+}
+
+// Eta, confinement force, velocity update (core.cpp:512-570) and plane
+// restitution (core.cpp:573-612).
+__global__ void __launch_bounds__(kBlock) k_eta(StepArgs a, int rest) {
+  if (failed(a.status)) return;
+  const int i = blockIdx.x * kBlock + threadIdx.x;
+  if (i >= a.n) return;
+  const float4* __restrict__ xs = a.x;
+  const float4* __restrict__ om = a.omega;
+  const float4 xi = xs[i];
+  float4 v = a.v[i];
+  const SceneConst& c = a.sc[__float_as_int(v.w)];
+  if (c.vort_on) {
+    const float4 oi = om[i];
+    const int n = a.cnt[i];
+    const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
+    const float h2 = c.h2;
+    float ex = 0.0f, ey = 0.0f, ez = 0.0f;
+    for (int k = 0; k < n; ++k) {
+      const int j = __ldg(list + 32ll * k);
+      const float4 xj = __ldg(xs + j);
+      const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+      const float r2 = dist2(dx, dy, dz);
+      if (r2 < h2) {
+        const float gf = spiky(c, clamped_r(c, r2));
+        const float coeff = __ldg(&om[j].w) - oi.w;
+        ex += coeff * (gf * dx);
+        ey += coeff * (gf * dy);
+        ez += coeff * (gf * dz);
+      }
+    }
+    const float len = sqrtf(ex * ex + ey * ey + ez * ez);
+    float nx = 0.0f, ny = 0.0f, nz = 0.0f;
+    if (len > c.vort_norm_eps) {
+      const float inv = 1.0f / len;
+      nx = ex * inv;
+      ny = ey * inv;
+      nz = ez * inv;
+    }
+    const float fx = c.vort_eps * (ny * oi.z - nz * oi.y);
+    const float fy = c.vort_eps * (nz * oi.x - nx * oi.z);
+    const float fz = c.vort_eps * (nx * oi.y - ny * oi.x);
+    v.x += c.dt * fx;
+    v.y += c.dt * fy;
+    v.z += c.dt * fz;
+  }
+  if (rest && c.rest_on) restitution(c, xi.x, xi.y, xi.z, v.x, v.y, v.z);
+  a.v[i] = v;
+}
+
+// ---------------------------------------------------------------------------
+// Upload / download / reset.
+
+__global__ void __launch_bounds__(kBlock) k_upload(const float* px, const float* py, const float* pz,
+                                                   const float* vx, const float* vy, const float* vz,
+                                                   float4* x, float4* v, int* slot, float* rho,
+                                                   const SceneConst* sc, int scenes, int n) {
+  const int o = blockIdx.x * kBlock + threadIdx.x;
+  if (o >= n) return;
+  int lo = 0, hi = scenes - 1;  // last scene whose first slot <= o
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (sc[mid].first_slot <= o) lo = mid; else hi = mid - 1;
+  }
+  x[o] = make_float4(px[o], py[o], pz[o], __int_as_float(o));
+  v[o] = make_float4(vx[o], vy[o], vz[o], __int_as_float(lo));
+  slot[o] = o;
+  rho[o] = 0.0f;
+}
+
+__global__ void __launch_bounds__(kBlock) k_download(const float4* x, const float4* v, const int* slot,
+                                                     float* px, float* py, float* pz, float* vx, float* vy,
+                                                     float* vz, int n) {
+  const int o = blockIdx.x * kBlock + threadIdx.x;
+  if (o >= n) return;
+  const int s = slot[o];
+  const float4 xs = x[s];
+  const float4 vs = v[s];
+  px[o] = xs.x;
+  py[o] = xs.y;
+  pz[o] = xs.z;
+  vx[o] = vs.x;
+  vy[o] = vs.y;
+  vz[o] = vs.z;
+}
+
+__global__ void k_reset(DevStatus* st, int* bmin, int* bmax, int scenes) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t == 0) {
+    st->err = 0;
+    st->started = 0;
+    st->step = 0;
+    st->fail_step = 0;
+    st->need_grid = 0;
+    st->need_nbr = 0;
+  }
+  for (int k = t; k < 3 * scenes; k += gridDim.x * blockDim.x) {
+    bmin[k] = INT_MAX;
+    bmax[k] = INT_MIN;
+  }
+}
+
+inline int blocks_for(long long n, int threads) { return static_cast<int>((n + threads - 1) / threads); }
+
+}  // namespace
+
+void LaunchMarks::start() {
+  next = 0;
+  if (!on) return;
+  if (capturing) {
+    cudaEventRecordWithFlags((*events)[0], stream, cudaEventRecordExternal);
+  } else {
+    cudaEventRecord((*events)[0], stream);
+  }
+  next = 1;
+}
+
+void LaunchMarks::mark(int stage) {
+  ++launches;
+  if (!on) return;
+  if (next >= static_cast<int>(events->size())) return;
+  (*stages)[next] = stage;
+  if (capturing) {
+    cudaEventRecordWithFlags((*events)[next], stream, cudaEventRecordExternal);
+  } else {
+    cudaEventRecord((*events)[next], stream);
+  }
+  ++next;
+}
+
+cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t st, LaunchMarks& m) {
+  const int nb = blocks_for(a.n, kBlock);
+  m.start();
+  k_bounds<<<nb, kBlock, 0, st>>>(a);
+  m.mark(FLUID_STAGE_PREDICT);
+  k_grid_setup<<<1, kBlock, 0, st>>>(a);
+  m.mark(FLUID_STAGE_PREDICT);
+  k_keys<<<nb, kBlock, 0, st>>>(a);
+  m.mark(FLUID_STAGE_PREDICT);
+  for (int pass = 0; pass < plan.radix_passes; ++pass) {
+    k_radix_hist<<<a.tiles, kBlock, 0, st>>>(a, pass);
+    m.mark(FLUID_STAGE_SORT);
+    k_radix_scan<<<256, kBlock, 0, st>>>(a, pass);
+    m.mark(FLUID_STAGE_SORT);
+    k_radix_scatter<<<a.tiles, kBlock, 0, st>>>(a, pass);
+    m.mark(FLUID_STAGE_SORT);
+  }
+  k_reorder<<<nb, kBlock, 0, st>>>(a);
+  m.mark(FLUID_STAGE_REORDER);
+  k_nbr_count<<<nb, kBlock, 0, st>>>(a);
+  m.mark(FLUID_STAGE_NEIGHBORS);
+  k_nbr_scan<<<1, 1024, 0, st>>>(a);
+  m.mark(FLUID_STAGE_NEIGHBORS);
+  k_nbr_fill<<<nb, kBlock, 0, st>>>(a);
+  m.mark(FLUID_STAGE_NEIGHBORS);
+
+  const bool post = plan.xsph || plan.vorticity;
+  const int to_v2 = plan.xsph ? 1 : 0;
+  const int rest_commit = (!post && plan.restitution) ? 1 : 0;
+  if (plan.iterations == 0) {
+    k_commit<<<nb, kBlock, 0, st>>>(a, to_v2, rest_commit);
+    m.mark(FLUID_STAGE_DELTA);
+  }
+  for (int it = 0; it < plan.iterations; ++it) {
+    const int in = it & 1;
+    if (it > 0) {
+      k_lambda<<<nb, kBlock, 0, st>>>(a, in);
+      m.mark(FLUID_STAGE_LAMBDA);
+    }
+    const int last = (it == plan.iterations - 1) ? 1 : 0;
+    k_delta<<<nb, kBlock, 0, st>>>(a, in, last, to_v2, last ? rest_commit : 0);
+    m.mark(FLUID_STAGE_DELTA);
+  }
+  if (plan.xsph) {
+    k_xsph<<<nb, kBlock, 0, st>>>(a, (!plan.vorticity && plan.restitution) ? 1 : 0);
+    m.mark(FLUID_STAGE_XSPH);
+  }
+  if (plan.vorticity) {
+    k_omega<<<nb, kBlock, 0, st>>>(a);
+    m.mark(FLUID_STAGE_VORTICITY);
+    k_eta<<<nb, kBlock, 0, st>>>(a, plan.restitution ? 1 : 0);
+    m.mark(FLUID_STAGE_VORTICITY);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t enqueue_upload(const float* px, const float* py, const float* pz, const float* vx, const float* vy,
+                           const float* vz, float4* x, float4* v, int* slot, float* rho, const SceneConst* sc,
+                           int scenes, int n, cudaStream_t st) {
+  if (n > 0) k_upload<<<blocks_for(n, kBlock), kBlock, 0, st>>>(px, py, pz, vx, vy, vz, x, v, slot, rho, sc, scenes, n);
+  return cudaGetLastError();
+}
+
+cudaError_t enqueue_download(const float4* x, const float4* v, const int* slot, float* px, float* py, float* pz,
+                             float* vx, float* vy, float* vz, int n, cudaStream_t st) {
+  if (n > 0) k_download<<<blocks_for(n, kBlock), kBlock, 0, st>>>(x, v, slot, px, py, pz, vx, vy, vz, n);
+  return cudaGetLastError();
+}
+
+cudaError_t enqueue_reset(DevStatus* status, int* bmin, int* bmax, int scenes, cudaStream_t st) {
+  k_reset<<<1, kBlock, 0, st>>>(status, bmin, bmax, scenes);
+  return cudaGetLastError();
+}
+
+}  // namespace fgb

@@ -1,0 +1,56 @@
+// Host-side launch interface of the PBF step kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "pbf_common.cuh"
+
+namespace fgb {
+
+// What one step launches; fixed for a configuration, so a captured graph of
+// it stays valid until buffers are reallocated or the flags change.
+struct StepPlan {
+  int iterations = 0;
+  bool xsph = false;      // some scene runs XSPH
+  bool vorticity = false; // some scene runs vorticity confinement
+  bool restitution = false;
+  int radix_passes = 1;   // passes launched (cover the grid capacity)
+  int threads = kBlock;   // block size of the per-particle passes
+};
+
+// Records an event after selected launches when profiling is on.
+struct LaunchMarks {
+  bool on = false;
+  cudaStream_t stream = nullptr;
+  bool capturing = false;
+  std::vector<cudaEvent_t>* events = nullptr;  // events[0] recorded first
+  std::vector<int>* stages = nullptr;          // stage of the launch ending at events[k]
+  int next = 0;
+  long long launches = 0;
+  void start();
+  void mark(int stage);
+};
+
+// Enqueues one full timestep on `stream`.
+cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan,
+                         cudaStream_t stream, LaunchMarks& marks);
+
+// Packs caller-order SoA arrays (device) into slot-order x/v of one parity.
+cudaError_t enqueue_upload(const float* px, const float* py, const float* pz,
+                           const float* vx, const float* vy, const float* vz,
+                           float4* x, float4* v, int* slot, float* rho,
+                           const SceneConst* sc, int scenes, int n,
+                           cudaStream_t stream);
+
+// Gathers slot-order x/v of one parity into caller-order SoA arrays (device).
+cudaError_t enqueue_download(const float4* x, const float4* v, const int* slot,
+                             float* px, float* py, float* pz, float* vx,
+                             float* vy, float* vz, int n, cudaStream_t stream);
+
+// Resets the status word and the bounding-box accumulators.
+cudaError_t enqueue_reset(DevStatus* status, int* bmin, int* bmax, int scenes,
+                          cudaStream_t stream);
+
+}  // namespace fgb

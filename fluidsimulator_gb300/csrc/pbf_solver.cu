@@ -1,0 +1,976 @@
+// Host runtime of the GB300 PBF timestep and the C ABI of include/fluid_gb300.h.
+//
+// A Solver owns the device-resident state of one or more independent scenes
+// (all scenes run in the same launches; each particle carries its scene id),
+// the step scratch, capacity management for the neighbour lists and the cell
+// table, CUDA-graph capture of the step, and optional per-launch timing.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "fluid_gb300.h"
+#include "pbf_common.cuh"
+#include "pbf_launch.h"
+
+namespace fgb {
+namespace {
+
+constexpr float kPi = 3.14159265358979323846f;  // core/src/core.cpp:10
+
+template <typename T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  cudaError_t alloc(size_t count) {
+    release();
+    if (count == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&p), count * sizeof(T));
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return e;
+    }
+    n = count;
+    return cudaSuccess;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  ~DBuf() { release(); }
+};
+
+// poly6_kernel (core/src/core.cpp:35-46), host float arithmetic.
+float poly6_host(float r2, float h) {
+  const float h2 = h * h;
+  if (r2 > h2) return 0.0f;
+  const float diff = h2 - r2;
+  const float diff3 = diff * diff * diff;
+  const float h4 = h2 * h2;
+  const float h9 = h4 * h4 * h;
+  const float coeff = 315.0f / (64.0f * kPi * h9);
+  return coeff * diff3;
+}
+
+// Per-scene constants, each from the same float expression the reference
+// evaluates (core/src/core.cpp:138-148, :270-274, :35-57).
+SceneConst make_scene_const(const fluid_params& p, int first, int count) {
+  SceneConst c;
+  std::memset(&c, 0, sizeof(c));
+  const float h = p.h;
+  c.h = h;
+  c.inv_h = 1.0f / h;
+  c.h2 = h * h;
+  const float min_r = 0.01f * h;
+  c.min_r2 = min_r * min_r;
+  {
+    const float h2 = h * h;
+    const float h4 = h2 * h2;
+    const float h9 = h4 * h4 * h;
+    c.poly6_c = 315.0f / (64.0f * kPi * h9);
+    c.w0 = poly6_host(0.0f, h);
+    const float h6 = h2 * h2 * h2;
+    c.spiky_c = -45.0f / (kPi * h6);
+  }
+  c.mass = p.particle_mass;
+  c.density = p.density;
+  c.inv_density = 1.0f / p.density;
+  c.grad_scale = p.particle_mass * c.inv_density;
+  c.epsilon = p.epsilon;
+  const bool scorr = p.enable_scorr && p.scorr_k != 0.0f;
+  const float dq_coeff = (p.scorr_dq_coeff > 0.0f) ? p.scorr_dq_coeff : 0.3f;
+  const float dq = dq_coeff * h;
+  const float wdq = scorr ? poly6_host(dq * dq, h) : 0.0f;
+  c.scorr_inv_wdq = (wdq > 1e-12f) ? (1.0f / wdq) : 0.0f;
+  c.scorr_on = (scorr && c.scorr_inv_wdq > 0.0f) ? 1 : 0;
+  c.scorr_neg_k = -p.scorr_k;
+  c.scorr_n = p.scorr_n;
+  c.dt = p.dt;
+  c.gdt_x = p.external_force[0] * p.dt;
+  c.gdt_y = p.external_force[1] * p.dt;
+  c.gdt_z = p.external_force[2] * p.dt;
+  c.visc_c = p.visc_c;
+  c.xsph_on = (p.enable_xsph && p.visc_c != 0.0f) ? 1 : 0;
+  c.vort_eps = p.vort_epsilon;
+  c.vort_norm_eps = p.vort_norm_eps;
+  c.vort_on = (p.enable_vorticity && p.vort_epsilon != 0.0f) ? 1 : 0;
+  c.rest_neg_e = -p.plane_restitution;
+  c.rest_scale = 1.0f - p.plane_friction;
+  c.rest_on = ((p.plane_restitution > 0.0f || p.plane_friction > 0.0f) && p.plane_count > 0) ? 1 : 0;
+  c.plane_count = p.plane_count;
+  c.iterations = p.solver_iterations;
+  c.first_slot = first;
+  c.count = count;
+  for (int q = 0; q < p.plane_count; ++q) {
+    c.planes[q] = make_float4(p.plane_nx[q], p.plane_ny[q], p.plane_nz[q], p.plane_d[q]);
+  }
+  return c;
+}
+
+int validate_params(const fluid_params& p, std::string& why) {
+  auto bad = [&](const char* m) {
+    why = m;
+    return static_cast<int>(FLUID_ERR_INVALID_ARGUMENT);
+  };
+  if (!(p.dt > 0.0f) || !std::isfinite(p.dt)) return bad("dt must be finite and > 0");
+  if (!(p.h > 0.0f) || !std::isfinite(p.h)) return bad("h must be finite and > 0");
+  if (!(p.density > 0.0f) || !std::isfinite(p.density)) return bad("density must be finite and > 0");
+  if (!std::isfinite(p.particle_mass)) return bad("particle_mass must be finite");
+  if (p.solver_iterations < 0) return bad("solver_iterations must be >= 0");
+  if (p.plane_count < 0 || p.plane_count > FLUID_MAX_PLANES) return bad("plane_count out of range");
+  if (!p.use_uniform_grid) {
+    why = "use_uniform_grid = 0 (all-pairs lists) is not implemented on the GPU";
+    return FLUID_ERR_NOT_SUPPORTED;
+  }
+  return FLUID_OK;
+}
+
+long long round_up(long long v, long long m) { return (v + m - 1) / m * m; }
+
+int bits_for(long long cap) {
+  if (cap <= 1) return 0;
+  int b = 0;
+  unsigned long long v = static_cast<unsigned long long>(cap - 1);
+  while (v) {
+    ++b;
+    v >>= 1;
+  }
+  return b;
+}
+
+}  // namespace
+
+class Solver {
+ public:
+  explicit Solver(int device) : device_(device) {}
+  ~Solver() {
+    if (device_ >= 0) cudaSetDevice(device_);
+    destroy_graphs();
+    destroy_events();
+    if (status_host_) cudaFreeHost(status_host_);
+    if (own_) cudaStreamDestroy(own_);
+  }
+
+  int init() {
+    if (cudaSetDevice(device_) != cudaSuccess) return cuda_fail("cudaSetDevice");
+    if (cudaStreamCreateWithFlags(&own_, cudaStreamNonBlocking) != cudaSuccess) return cuda_fail("stream");
+    stream_ = own_;
+    if (cudaMallocHost(reinterpret_cast<void**>(&status_host_), sizeof(DevStatus)) != cudaSuccess)
+      return cuda_fail("cudaMallocHost");
+    if (status_.alloc(1) != cudaSuccess) return cuda_fail("cudaMalloc status");
+    cudaMemset(status_.p, 0, sizeof(DevStatus));
+    return FLUID_OK;
+  }
+
+  int set_stream(void* s) {
+    int rc = synchronize();
+    if (rc) return rc;
+    stream_ = s ? static_cast<cudaStream_t>(s) : own_;
+    invalidate_graphs();
+    return FLUID_OK;
+  }
+
+  int configure(int scenes, const fluid_params* params, const int64_t* counts) {
+    if (scenes < 1 || !params || !counts) return fail(FLUID_ERR_INVALID_ARGUMENT, "need >= 1 scene");
+    long long total = 0;
+    for (int s = 0; s < scenes; ++s) {
+      std::string why;
+      int rc = validate_params(params[s], why);
+      if (rc) return fail(rc, "scene " + std::to_string(s) + ": " + why);
+      if (counts[s] < 0) return fail(FLUID_ERR_INVALID_ARGUMENT, "negative particle count");
+      if (params[s].solver_iterations != params[0].solver_iterations)
+        return fail(FLUID_ERR_NOT_SUPPORTED, "all scenes must share solver_iterations");
+      total += counts[s];
+    }
+    if (total > (1ll << 30)) return fail(FLUID_ERR_INVALID_ARGUMENT, "more than 2^30 particles");
+    cudaSetDevice(device_);
+    int rc = synchronize_quiet();
+    (void)rc;
+    destroy_graphs();
+    S_ = scenes;
+    n_ = static_cast<int>(total);
+    params_.assign(params, params + scenes);
+    counts_.assign(counts, counts + scenes);
+    times_.assign(scenes, 0.0f);
+    steps_ = 0;
+    regrows_ = 0;
+    parity_ = 0;
+    pending_ = 0;
+    uploaded_ = false;
+    build_scene_consts();
+    warps_ = (n_ + 31) / 32;
+    tiles_ = std::max(1, (n_ + kRadixTile - 1) / kRadixTile);
+    const size_t n = static_cast<size_t>(std::max(n_, 1));
+    const size_t np = static_cast<size_t>(round_up(n, 32));
+    bool ok = true;
+    for (int k = 0; k < 2; ++k) {
+      ok &= x_[k].alloc(np) == cudaSuccess;
+      ok &= v_[k].alloc(np) == cudaSuccess;
+      ok &= p_[k].alloc(np) == cudaSuccess;
+      ok &= slot_[k].alloc(np) == cudaSuccess;
+      ok &= rho_[k].alloc(np) == cudaSuccess;
+      ok &= keys_[k].alloc(np) == cudaSuccess;
+      ok &= vals_[k].alloc(np) == cudaSuccess;
+    }
+    ok &= v2_.alloc(np) == cudaSuccess;
+    ok &= omega_.alloc(np) == cudaSuccess;
+    ok &= lambda_.alloc(np) == cudaSuccess;
+    ok &= cnt_.alloc(np) == cudaSuccess;
+    ok &= depth_.alloc(static_cast<size_t>(warps_) + 1) == cudaSuccess;
+    ok &= wbase_.alloc(static_cast<size_t>(warps_) + 1) == cudaSuccess;
+    ok &= hist_.alloc(static_cast<size_t>(tiles_) * 256) == cudaSuccess;
+    ok &= digit_total_.alloc(kRadixMaxPasses * 256) == cudaSuccess;
+    ok &= bmin_.alloc(3 * static_cast<size_t>(S_)) == cudaSuccess;
+    ok &= bmax_.alloc(3 * static_cast<size_t>(S_)) == cudaSuccess;
+    ok &= grid_.alloc(static_cast<size_t>(S_)) == cudaSuccess;
+    ok &= sc_.alloc(static_cast<size_t>(S_)) == cudaSuccess;
+    if (!ok) return fail(FLUID_ERR_OUT_OF_MEMORY, "device allocation failed");
+    grid_cap_ = std::max<long long>(1 << 16, 4ll * n_);
+    nbr_cap_ = 48ll * 32 * warps_;
+    if (table_.alloc(static_cast<size_t>(grid_cap_)) != cudaSuccess ||
+        nbr_.alloc(static_cast<size_t>(nbr_cap_)) != cudaSuccess)
+      return fail(FLUID_ERR_OUT_OF_MEMORY, "device allocation failed");
+    cudaMemsetAsync(table_.p, 0, table_.n * sizeof(int2), stream_);
+    if (cudaMemcpyAsync(sc_.p, sc_host_.data(), S_ * sizeof(SceneConst), cudaMemcpyHostToDevice, stream_) !=
+        cudaSuccess)
+      return cuda_fail("upload scene constants");
+    if (enqueue_reset(status_.p, bmin_.p, bmax_.p, S_, stream_) != cudaSuccess) return cuda_fail("reset");
+    if (cudaStreamSynchronize(stream_) != cudaSuccess) return cuda_fail("configure");
+    make_plan();
+    return FLUID_OK;
+  }
+
+  int set_params(const fluid_params* params) {
+    if (!S_) return fail(FLUID_ERR_STATE, "configure first");
+    for (int s = 0; s < S_; ++s) {
+      std::string why;
+      int rc = validate_params(params[s], why);
+      if (rc) return fail(rc, why);
+      if (params[s].solver_iterations != params[0].solver_iterations)
+        return fail(FLUID_ERR_NOT_SUPPORTED, "all scenes must share solver_iterations");
+    }
+    int rc = synchronize();
+    if (rc) return rc;
+    params_.assign(params, params + S_);
+    build_scene_consts();
+    if (cudaMemcpyAsync(sc_.p, sc_host_.data(), S_ * sizeof(SceneConst), cudaMemcpyHostToDevice, stream_) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(stream_) != cudaSuccess)
+      return cuda_fail("set_params");
+    StepPlan old = plan_;
+    make_plan();
+    if (old.iterations != plan_.iterations || old.xsph != plan_.xsph || old.vorticity != plan_.vorticity ||
+        old.restitution != plan_.restitution)
+      invalidate_graphs();
+    return FLUID_OK;
+  }
+
+  int upload(const float* px, const float* py, const float* pz, const float* vx, const float* vy,
+             const float* vz, int memory) {
+    if (!S_) return fail(FLUID_ERR_STATE, "configure first");
+    if (n_ > 0 && (!px || !py || !pz || !vx || !vy || !vz)) return fail(FLUID_ERR_INVALID_ARGUMENT, "null array");
+    int rc = synchronize();
+    if (rc) return rc;
+    if (n_ > 0) {
+      const float* src[6] = {px, py, pz, vx, vy, vz};
+      const float* dev[6];
+      if (memory == FLUID_MEMORY_HOST) {
+        float* stage = reinterpret_cast<float*>(p_[0].p);  // 4n floats
+        float* stage2 = reinterpret_cast<float*>(p_[1].p);
+        for (int k = 0; k < 6; ++k) {
+          float* dst = (k < 4 ? stage : stage2) + static_cast<size_t>(k % 4) * n_;
+          if (cudaMemcpyAsync(dst, src[k], sizeof(float) * n_, cudaMemcpyHostToDevice, stream_) != cudaSuccess)
+            return cuda_fail("upload copy");
+          dev[k] = dst;
+        }
+      } else {
+        for (int k = 0; k < 6; ++k) dev[k] = src[k];
+      }
+      if (enqueue_upload(dev[0], dev[1], dev[2], dev[3], dev[4], dev[5], x_[parity_].p, v_[parity_].p,
+                         slot_[parity_].p, rho_[parity_].p, sc_.p, S_, n_, stream_) != cudaSuccess)
+        return cuda_fail("upload kernel");
+      if (cudaStreamSynchronize(stream_) != cudaSuccess) return cuda_fail("upload");
+    }
+    uploaded_ = true;
+    return FLUID_OK;
+  }
+
+  int download(float* px, float* py, float* pz, float* vx, float* vy, float* vz, int memory) {
+    if (!uploaded_) return fail(FLUID_ERR_STATE, "no state uploaded");
+    if (n_ > 0 && (!px || !py || !pz || !vx || !vy || !vz)) return fail(FLUID_ERR_INVALID_ARGUMENT, "null array");
+    int rc = synchronize();
+    if (rc) return rc;
+    if (n_ == 0) return FLUID_OK;
+    float* dst[6] = {px, py, pz, vx, vy, vz};
+    float* dev[6];
+    if (memory == FLUID_MEMORY_HOST) {
+      float* stage = reinterpret_cast<float*>(p_[0].p);
+      float* stage2 = reinterpret_cast<float*>(p_[1].p);
+      for (int k = 0; k < 6; ++k) dev[k] = (k < 4 ? stage : stage2) + static_cast<size_t>(k % 4) * n_;
+    } else {
+      for (int k = 0; k < 6; ++k) dev[k] = dst[k];
+    }
+    if (enqueue_download(x_[parity_].p, v_[parity_].p, slot_[parity_].p, dev[0], dev[1], dev[2], dev[3], dev[4],
+                         dev[5], n_, stream_) != cudaSuccess)
+      return cuda_fail("download kernel");
+    if (memory == FLUID_MEMORY_HOST) {
+      for (int k = 0; k < 6; ++k) {
+        if (cudaMemcpyAsync(dst[k], dev[k], sizeof(float) * n_, cudaMemcpyDeviceToHost, stream_) != cudaSuccess)
+          return cuda_fail("download copy");
+      }
+    }
+    if (cudaStreamSynchronize(stream_) != cudaSuccess) return cuda_fail("download");
+    return FLUID_OK;
+  }
+
+  int step_async(int nsteps) {
+    if (!uploaded_) return fail(FLUID_ERR_STATE, "no state uploaded");
+    if (nsteps < 0) return fail(FLUID_ERR_INVALID_ARGUMENT, "negative step count");
+    if (n_ == 0) {
+      for (int k = 0; k < nsteps; ++k) advance_times(1);
+      steps_ += nsteps;
+      return FLUID_OK;
+    }
+    for (int k = 0; k < nsteps; ++k) {
+      int rc = launch_one();
+      if (rc) return rc;
+      if (profiling_) {
+        rc = synchronize();
+        if (rc) return rc;
+      }
+    }
+    return FLUID_OK;
+  }
+
+  int step(int nsteps) {
+    int rc = step_async(nsteps);
+    if (rc) return rc;
+    return synchronize();
+  }
+
+  // Waits for the enqueued steps; steps that overflowed a capacity are
+  // re-run after growing it.
+  int synchronize() {
+    for (;;) {
+      if (pending_ == 0) return FLUID_OK;
+      if (cudaStreamSynchronize(stream_) != cudaSuccess) return cuda_fail("step");
+      if (cudaMemcpy(status_host_, status_.p, sizeof(DevStatus), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return cuda_fail("status read");
+      const DevStatus st = *status_host_;
+      const int done = st.err ? st.fail_step : pending_;
+      const int remaining = pending_ - done;
+      if (profiling_ && done > 0) accumulate_profile((parity_ + done - 1) & 1);
+      commit_steps(done);
+      pending_ = 0;
+      last_pairs_ = static_cast<long long>(st.pairs);
+      last_max_ = st.nbr_max;
+      last_cells_ = static_cast<int>(st.total_cells);
+      if (enqueue_reset(status_.p, bmin_.p, bmax_.p, S_, stream_) != cudaSuccess) return cuda_fail("reset");
+      if (!st.err) return FLUID_OK;
+      if (st.err != FLUID_ERR_CAPACITY) {
+        cudaStreamSynchronize(stream_);
+        return fail(st.err, st.err == FLUID_ERR_NONFINITE ? "non-finite predicted position"
+                                                          : "particle cells span too large a grid");
+      }
+      int rc = grow(st.need_grid, st.need_nbr);
+      if (rc) return rc;
+      ++regrows_;
+      for (int k = 0; k < remaining; ++k) {
+        rc = launch_one();
+        if (rc) return rc;
+      }
+    }
+  }
+
+  int set_graphs(int on) {
+    int rc = synchronize();
+    if (rc) return rc;
+    use_graphs_ = on != 0;
+    invalidate_graphs();
+    return FLUID_OK;
+  }
+
+  int set_profiling(int on) {
+    int rc = synchronize();
+    if (rc) return rc;
+    profiling_ = on != 0;
+    invalidate_graphs();
+    if (profiling_) {
+      for (int k = 0; k < 2; ++k) {
+        if (events_[k].empty()) {
+          events_[k].resize(64);
+          stages_[k].assign(64, 0);
+          for (auto& e : events_[k]) cudaEventCreate(&e);
+        }
+      }
+    }
+    return FLUID_OK;
+  }
+
+  int stage_times(double* ms, int64_t* launches, int stages, int reset) {
+    for (int k = 0; k < stages && k < FLUID_STAGE_COUNT; ++k) {
+      if (ms) ms[k] = stage_ms_[k];
+      if (launches) launches[k] = stage_launches_[k];
+    }
+    if (reset) {
+      std::fill(std::begin(stage_ms_), std::end(stage_ms_), 0.0);
+      std::fill(std::begin(stage_launches_), std::end(stage_launches_), 0ll);
+    }
+    return FLUID_OK;
+  }
+
+  int get_time(int scene, float* t) {
+    if (scene < 0 || scene >= S_ || !t) return fail(FLUID_ERR_INVALID_ARGUMENT, "bad scene");
+    int rc = synchronize();
+    if (rc) return rc;
+    *t = times_[scene];
+    return FLUID_OK;
+  }
+
+  int set_time(int scene, float t) {
+    if (scene < 0 || scene >= S_) return fail(FLUID_ERR_INVALID_ARGUMENT, "bad scene");
+    int rc = synchronize();
+    if (rc) return rc;
+    times_[scene] = t;
+    return FLUID_OK;
+  }
+
+  int stats(fluid_stats* out) {
+    if (!out) return fail(FLUID_ERR_INVALID_ARGUMENT, "null stats");
+    int rc = synchronize();
+    if (rc) return rc;
+    out->particles = n_;
+    out->steps = steps_;
+    out->neighbor_pairs = last_pairs_;
+    out->neighbor_max = last_max_;
+    out->grid_cells = last_cells_;
+    out->neighbor_capacity = nbr_cap_;
+    out->grid_capacity = grid_cap_;
+    out->regrows = regrows_;
+    out->kernel_launches = launches_;
+    return FLUID_OK;
+  }
+
+  int read_debug(int what, void* out, int64_t capacity) {
+    if (!uploaded_ || steps_ == 0) return fail(FLUID_ERR_STATE, "no completed step");
+    int rc = synchronize();
+    if (rc) return rc;
+    const int n = n_;
+    const int64_t need = (what == FLUID_DEBUG_CELL_KEYS) ? 3ll * n : n;
+    if (capacity < need || !out) return fail(FLUID_ERR_INVALID_ARGUMENT, "debug buffer too small");
+    if (n == 0) return FLUID_OK;
+    // Current parity holds the last step's output; keys/vals/cnt/lambda/rho
+    // are the last step's scratch.
+    std::vector<int> slot(n);
+    if (cudaMemcpy(slot.data(), slot_[parity_].p, n * sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+      return cuda_fail("debug read");
+    DevStatus st;
+    cudaMemcpy(&st, status_.p, sizeof(st), cudaMemcpyDeviceToHost);
+    const int npass = last_npass();
+    if (what == FLUID_DEBUG_CELL_KEYS || what == FLUID_DEBUG_SORTED_ORDER) {
+      std::vector<uint32_t> keys(n);
+      std::vector<int> vals(n);
+      cudaMemcpy(keys.data(), keys_[npass & 1].p, n * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+      if (npass)
+        cudaMemcpy(vals.data(), vals_[npass & 1].p, n * sizeof(int), cudaMemcpyDeviceToHost);
+      else
+        for (int s = 0; s < n; ++s) vals[s] = s;
+      std::vector<GridInfo> grid(S_);
+      cudaMemcpy(grid.data(), grid_.p, S_ * sizeof(GridInfo), cudaMemcpyDeviceToHost);
+      if (what == FLUID_DEBUG_SORTED_ORDER) {
+        int32_t* o = static_cast<int32_t*>(out);
+        for (int s = 0; s < n; ++s) o[s] = vals[s] - sc_host_[scene_of(vals[s])].first_slot;
+      } else {
+        int32_t* o = static_cast<int32_t*>(out);
+        for (int s = 0; s < n; ++s) {
+          const int orig = vals[s];
+          const GridInfo& g = grid[scene_of(orig)];
+          const long long l = static_cast<long long>(keys[s]) - g.base;
+          const long long yz = static_cast<long long>(g.dimy) * g.dimz;
+          o[3 * orig + 0] = g.minx + static_cast<int>(l / yz);
+          o[3 * orig + 1] = g.miny + static_cast<int>((l % yz) / g.dimz);
+          o[3 * orig + 2] = g.minz + static_cast<int>(l % g.dimz);
+        }
+      }
+      return FLUID_OK;
+    }
+    std::vector<int32_t> buf(n);
+    const void* src = nullptr;
+    if (what == FLUID_DEBUG_NEIGHBOR_COUNTS) src = cnt_.p;
+    else if (what == FLUID_DEBUG_RHO) src = rho_[parity_].p;
+    else if (what == FLUID_DEBUG_LAMBDA) src = lambda_.p;
+    else return fail(FLUID_ERR_INVALID_ARGUMENT, "unknown debug record");
+    cudaMemcpy(buf.data(), src, n * sizeof(int32_t), cudaMemcpyDeviceToHost);
+    int32_t* o = static_cast<int32_t*>(out);
+    for (int orig = 0; orig < n; ++orig) o[orig] = buf[slot[orig]];
+    return FLUID_OK;
+  }
+
+  const char* last_error() const { return err_.c_str(); }
+
+ private:
+  int fail(int code, const std::string& msg) {
+    err_ = msg;
+    return code;
+  }
+  int cuda_fail(const char* what) {
+    cudaError_t e = cudaGetLastError();
+    err_ = std::string(what) + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation) return FLUID_ERR_OUT_OF_MEMORY;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return FLUID_ERR_NO_DEVICE;
+    return FLUID_ERR_CUDA;
+  }
+
+  int synchronize_quiet() {
+    if (stream_) cudaStreamSynchronize(stream_);
+    pending_ = 0;
+    return FLUID_OK;
+  }
+
+  void build_scene_consts() {
+    sc_host_.resize(S_);
+    long long first = 0;
+    for (int s = 0; s < S_; ++s) {
+      sc_host_[s] = make_scene_const(params_[s], static_cast<int>(first), static_cast<int>(counts_[s]));
+      first += counts_[s];
+    }
+  }
+
+  int scene_of(int orig) const {
+    int lo = 0, hi = S_ - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) / 2;
+      if (sc_host_[mid].first_slot <= orig) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+  }
+
+  int last_npass() const {
+    return last_cells_ <= 1 ? 0 : (bits_for(last_cells_) + 7) / 8;
+  }
+
+  void make_plan() {
+    plan_.iterations = params_[0].solver_iterations;
+    plan_.xsph = plan_.vorticity = plan_.restitution = false;
+    for (const auto& c : sc_host_) {
+      plan_.xsph |= c.xsph_on != 0;
+      plan_.vorticity |= c.vort_on != 0;
+      plan_.restitution |= c.rest_on != 0;
+    }
+    plan_.radix_passes = std::max(1, (bits_for(grid_cap_) + 7) / 8);
+  }
+
+  void advance_times(int steps) {
+    for (int k = 0; k < steps; ++k)
+      for (int s = 0; s < S_; ++s) times_[s] += params_[s].dt;  // core.cpp:614
+  }
+
+  void commit_steps(int done) {
+    advance_times(done);
+    steps_ += done;
+    parity_ = (parity_ + done) & 1;
+  }
+
+  StepArgs args(int par) {
+    StepArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.x_old = x_[par].p;
+    a.v_old = v_[par].p;
+    a.slot_old = slot_[par].p;
+    a.rho_old = rho_[par].p;
+    a.x = x_[par ^ 1].p;
+    a.v = v_[par ^ 1].p;
+    a.v2 = v2_.p;
+    a.slot = slot_[par ^ 1].p;
+    a.p[0] = p_[0].p;
+    a.p[1] = p_[1].p;
+    a.omega = omega_.p;
+    a.lambda = lambda_.p;
+    a.rho = rho_[par ^ 1].p;
+    a.keys[0] = keys_[0].p;
+    a.keys[1] = keys_[1].p;
+    a.vals[0] = vals_[0].p;
+    a.vals[1] = vals_[1].p;
+    a.hist = hist_.p;
+    a.digit_total = digit_total_.p;
+    a.table = table_.p;
+    a.cnt = cnt_.p;
+    a.depth = depth_.p;
+    a.wbase = wbase_.p;
+    a.nbr = nbr_.p;
+    a.bmin = bmin_.p;
+    a.bmax = bmax_.p;
+    a.grid = grid_.p;
+    a.status = status_.p;
+    a.sc = sc_.p;
+    a.n = n_;
+    a.scenes = S_;
+    a.tiles = tiles_;
+    a.warps = warps_;
+    a.grid_capacity = grid_cap_;
+    a.nbr_capacity = nbr_cap_;
+    return a;
+  }
+
+  LaunchMarks marks(int par, bool capturing) {
+    LaunchMarks m;
+    m.on = profiling_;
+    m.stream = stream_;
+    m.capturing = capturing;
+    m.events = &events_[par];
+    m.stages = &stages_[par];
+    return m;
+  }
+
+  int launch_one() {
+    const int par = (parity_ + pending_) & 1;
+    if (use_graphs_) {
+      if (!graphs_valid_) {
+        int rc = build_graphs();
+        if (rc) return rc;
+      }
+      if (cudaGraphLaunch(exec_[par], stream_) != cudaSuccess) return cuda_fail("graph launch");
+      launches_ += launches_per_step_;
+    } else {
+      LaunchMarks m = marks(par, false);
+      if (enqueue_step(args(par), plan_, stream_, m) != cudaSuccess) return cuda_fail("launch");
+      launches_ += m.launches;
+      launches_per_step_ = m.launches;
+      marks_used_[par] = m.next;
+    }
+    ++pending_;
+    return FLUID_OK;
+  }
+
+  int build_graphs() {
+    destroy_graphs();
+    for (int par = 0; par < 2; ++par) {
+      cudaGraph_t g = nullptr;
+      if (cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+        return cuda_fail("begin capture");
+      LaunchMarks m = marks(par, true);
+      cudaError_t e = enqueue_step(args(par), plan_, stream_, m);
+      cudaError_t e2 = cudaStreamEndCapture(stream_, &g);
+      if (e != cudaSuccess || e2 != cudaSuccess || !g) return cuda_fail("capture");
+      if (cudaGraphInstantiate(&exec_[par], g, 0) != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return cuda_fail("graph instantiate");
+      }
+      cudaGraphDestroy(g);
+      launches_per_step_ = m.launches;
+      marks_used_[par] = m.next;
+    }
+    graphs_valid_ = true;
+    return FLUID_OK;
+  }
+
+  void destroy_graphs() {
+    for (auto& e : exec_) {
+      if (e) cudaGraphExecDestroy(e);
+      e = nullptr;
+    }
+    graphs_valid_ = false;
+  }
+  void invalidate_graphs() { destroy_graphs(); }
+
+  void destroy_events() {
+    for (auto& v : events_)
+      for (auto& e : v) cudaEventDestroy(e);
+  }
+
+  void accumulate_profile(int par) {
+    const int used = marks_used_[par];
+    for (int k = 1; k < used; ++k) {
+      float ms = 0.0f;
+      if (cudaEventElapsedTime(&ms, events_[par][k - 1], events_[par][k]) == cudaSuccess) {
+        const int st = stages_[par][k];
+        stage_ms_[st] += ms;
+        stage_launches_[st] += 1;
+      }
+    }
+  }
+
+  int grow(unsigned long long need_grid, unsigned long long need_nbr) {
+    cudaStreamSynchronize(stream_);
+    float f = 1.5f;
+    for (const auto& p : params_) f = std::max(f, p.neighbor_reserve_factor);
+    bool changed = false;
+    if (need_grid > static_cast<unsigned long long>(grid_cap_)) {
+      long long cap = static_cast<long long>(std::ceil(double(need_grid) * f));
+      cap = std::min<long long>(cap, (1ll << 31) - 1);
+      if (table_.alloc(static_cast<size_t>(cap)) != cudaSuccess) return fail(FLUID_ERR_OUT_OF_MEMORY, "cell table");
+      cudaMemsetAsync(table_.p, 0, table_.n * sizeof(int2), stream_);
+      grid_cap_ = cap;
+      changed = true;
+    }
+    if (need_nbr > static_cast<unsigned long long>(nbr_cap_)) {
+      const long long cap = round_up(static_cast<long long>(std::ceil(double(need_nbr) * f)), 32);
+      nbr_.release();
+      if (nbr_.alloc(static_cast<size_t>(cap)) != cudaSuccess) {
+        nbr_cap_ = 0;
+        return fail(FLUID_ERR_OUT_OF_MEMORY, "neighbour lists of " + std::to_string(cap) + " entries");
+      }
+      nbr_cap_ = cap;
+      changed = true;
+    }
+    if (!changed) return fail(FLUID_ERR_CAPACITY, "capacity error without growth");
+    make_plan();
+    invalidate_graphs();
+    return FLUID_OK;
+  }
+
+  int device_;
+  cudaStream_t own_ = nullptr, stream_ = nullptr;
+  int S_ = 0, n_ = 0, warps_ = 0, tiles_ = 1;
+  std::vector<fluid_params> params_;
+  std::vector<int64_t> counts_;
+  std::vector<SceneConst> sc_host_;
+  std::vector<float> times_;
+  bool uploaded_ = false;
+  int parity_ = 0, pending_ = 0;
+  long long steps_ = 0, regrows_ = 0, launches_ = 0, launches_per_step_ = 0;
+  long long last_pairs_ = 0;
+  int last_max_ = 0, last_cells_ = 0;
+  DBuf<float4> x_[2], v_[2], p_[2], v2_, omega_;
+  DBuf<int> slot_[2], vals_[2], cnt_, depth_, nbr_, bmin_, bmax_;
+  DBuf<float> rho_[2], lambda_;
+  DBuf<uint32_t> keys_[2], hist_, digit_total_;
+  DBuf<long long> wbase_;
+  DBuf<int2> table_;
+  DBuf<GridInfo> grid_;
+  DBuf<DevStatus> status_;
+  DBuf<SceneConst> sc_;
+  DevStatus* status_host_ = nullptr;
+  long long grid_cap_ = 0, nbr_cap_ = 0;
+  StepPlan plan_;
+  bool use_graphs_ = true, graphs_valid_ = false, profiling_ = false;
+  cudaGraphExec_t exec_[2] = {nullptr, nullptr};
+  std::vector<cudaEvent_t> events_[2];
+  std::vector<int> stages_[2];
+  int marks_used_[2] = {0, 0};
+  double stage_ms_[FLUID_STAGE_COUNT] = {};
+  long long stage_launches_[FLUID_STAGE_COUNT] = {};
+  std::string err_;
+};
+
+}  // namespace fgb
+
+struct fluid_solver {
+  fgb::Solver impl;
+  explicit fluid_solver(int d) : impl(d) {}
+};
+
+extern "C" {
+
+void fluid_params_default(fluid_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  // core/include/fluid/core.h:12-43
+  p->dt = 1.0f / 60.0f;
+  p->density = 6000.0f;
+  p->particle_mass = 0.0f;
+  p->h = 0.0f;
+  p->particle_radius = 0.01f;
+  p->epsilon = 600.0f;
+  p->solver_iterations = 4;
+  p->neighbor_reserve_factor = 1.5f;
+  p->use_uniform_grid = 1;
+  p->enable_scorr = 0;
+  p->enable_xsph = 0;
+  p->enable_vorticity = 0;
+  p->scorr_k = 0.00005f;
+  p->scorr_n = 4;
+  p->scorr_dq_coeff = 0.3f;
+  p->visc_c = 0.0002f;
+  p->plane_restitution = 0.0f;
+  p->plane_friction = 0.0f;
+  p->vort_epsilon = 0.5f;
+  p->vort_norm_eps = 1e-6f;
+  p->external_force[0] = 0.0f;
+  p->external_force[1] = -9.8f;
+  p->external_force[2] = 0.0f;
+  p->plane_count = 0;
+}
+
+int fluid_gb300_version(void) { return FLUID_GB300_ABI_VERSION; }
+
+int fluid_gb300_device_available(int* count, const char** error) {
+  int n = 0;
+  const cudaError_t e = cudaGetDeviceCount(&n);
+  if (count) *count = 0;
+  if (error) *error = nullptr;
+  if (e == cudaErrorNoDevice) return 0;
+  if (e != cudaSuccess) {
+    if (error) *error = cudaGetErrorString(e);
+    return 0;
+  }
+  if (count) *count = n;
+  return n > 0 ? 1 : 0;
+}
+
+const char* fluid_status_string(int status) {
+  switch (status) {
+    case FLUID_OK: return "ok";
+    case FLUID_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case FLUID_ERR_CUDA: return "CUDA error";
+    case FLUID_ERR_CAPACITY: return "capacity exceeded";
+    case FLUID_ERR_DOMAIN: return "grid domain too large";
+    case FLUID_ERR_NONFINITE: return "non-finite position";
+    case FLUID_ERR_NO_DEVICE: return "no CUDA device";
+    case FLUID_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case FLUID_ERR_NOT_SUPPORTED: return "not supported";
+    case FLUID_ERR_STATE: return "invalid call order";
+    default: return "unknown status";
+  }
+}
+
+int fluid_solver_create(fluid_solver** out, int device) {
+  if (!out) return FLUID_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  int count = 0;
+  if (!fluid_gb300_device_available(&count, nullptr)) return FLUID_ERR_NO_DEVICE;
+  if (device < 0 || device >= count) return FLUID_ERR_INVALID_ARGUMENT;
+  auto s = std::make_unique<fluid_solver>(device);
+  const int rc = s->impl.init();
+  if (rc) return rc;
+  *out = s.release();
+  return FLUID_OK;
+}
+
+void fluid_solver_destroy(fluid_solver* s) { delete s; }
+
+#define FLUID_CHECK_SOLVER(s) \
+  if (!(s)) return FLUID_ERR_INVALID_ARGUMENT
+
+int fluid_solver_set_stream(fluid_solver* s, void* stream) {
+  FLUID_CHECK_SOLVER(s);
+  return s->impl.set_stream(stream);
+}
+
+int fluid_solver_configure(fluid_solver* s, int32_t scene_count, const fluid_params* params,
+                           const int64_t* counts) {
+  FLUID_CHECK_SOLVER(s);
+  return s->impl.configure(scene_count, params, counts);
+}
+
+int fluid_solver_set_params(fluid_solver* s, const fluid_params* params) {
+  FLUID_CHECK_SOLVER(s);
+  if (!params) return FLUID_ERR_INVALID_ARGUMENT;
+  return s->impl.set_params(params);
+}
+
+int fluid_solver_upload(fluid_solver* s, const float* px, const float* py, const float* pz, const float* vx,
+                        const float* vy, const float* vz, int32_t memory) {
+  FLUID_CHECK_SOLVER(s);
+  return s->impl.upload(px, py, pz, vx, vy, vz, memory);
+}
+
+int fluid_solver_download(fluid_solver* s, float* px, float* py, float* pz, float* vx, float* vy, float* vz,
+                          int32_t memory) {
+  FLUID_CHECK_SOLVER(s);
+  return s->impl.download(px, py, pz, vx, vy, vz, memory);
+}
+
+int fluid_solver_step(fluid_solver* s, int32_t nsteps) {
+  FLUID_CHECK_SOLVER(s);
+  return s->impl.step(nsteps);
+}
+
+int fluid_solver_step_async(fluid_solver* s, int32_t nsteps) {
+  FLUID_CHECK_SOLVER(s);
+  return s->impl.step_async(nsteps);
+}
+
+int fluid_solver_synchronize(fluid_solver* s) {
+  FLUID_CHECK_SOLVER(s);
+  return s->impl.synchronize();
+}
+
+int fluid_solver_set_graphs(fluid_solver* s, int32_t enable) {
+  FLUID_CHECK_SOLVER(s);
+  return s->impl.set_graphs(enable);
+}
+
+int fluid_solver_set_profiling(fluid_solver* s, int32_t enable) {
+  FLUID_CHECK_SOLVER(s);
+  return s->impl.set_profiling(enable);
+}
+
+int fluid_solver_stage_times(fluid_solver* s, double* ms, int64_t* launches, int32_t stages, int32_t reset) {
+  FLUID_CHECK_SOLVER(s);
+  return s->impl.stage_times(ms, launches, stages, reset);
+}
+
+int fluid_solver_get_time(fluid_solver* s, int32_t scene, float* time) {
+  FLUID_CHECK_SOLVER(s);
+  return s->impl.get_time(scene, time);
+}
+
+int fluid_solver_set_time(fluid_solver* s, int32_t scene, float time) {
+  FLUID_CHECK_SOLVER(s);
+  return s->impl.set_time(scene, time);
+}
+
+int fluid_solver_get_stats(fluid_solver* s, fluid_stats* out) {
+  FLUID_CHECK_SOLVER(s);
+  return s->impl.stats(out);
+}
+
+int fluid_solver_read_debug(fluid_solver* s, int32_t what, void* host_out, int64_t capacity) {
+  FLUID_CHECK_SOLVER(s);
+  return s->impl.read_debug(what, host_out, capacity);
+}
+
+const char* fluid_solver_last_error(const fluid_solver* s) {
+  return s ? s->impl.last_error() : "null solver";
+}
+
+int fluid_gb300_cuda_step(const fluid_params* params, int64_t count, float* px, float* py, float* pz, float* vx,
+                          float* vy, float* vz, float* time) {
+  if (!params || !time || count < 0) return FLUID_ERR_INVALID_ARGUMENT;
+  if (count == 0) {  // cuda_stub.cu:766-769
+    *time += params->dt;
+    return FLUID_OK;
+  }
+  struct Cache {
+    std::unique_ptr<fluid_solver> s;
+    int64_t count = -1;
+    int device = -1;
+  };
+  thread_local Cache cache;
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess) return FLUID_ERR_NO_DEVICE;
+  int rc;
+  if (!cache.s || cache.count != count || cache.device != device) {
+    cache.s.reset();
+    fluid_solver* raw = nullptr;
+    rc = fluid_solver_create(&raw, device);
+    if (rc) return rc;
+    cache.s.reset(raw);
+    rc = cache.s->impl.configure(1, params, &count);
+    if (rc) {
+      cache.s.reset();
+      return rc;
+    }
+    cache.count = count;
+    cache.device = device;
+  } else {
+    rc = cache.s->impl.set_params(params);
+    if (rc) return rc;
+  }
+  fgb::Solver& s = cache.s->impl;
+  if ((rc = s.upload(px, py, pz, vx, vy, vz, FLUID_MEMORY_HOST))) return rc;
+  if ((rc = s.set_time(0, *time))) return rc;
+  if ((rc = s.step(1))) return rc;
+  if ((rc = s.download(px, py, pz, vx, vy, vz, FLUID_MEMORY_HOST))) return rc;
+  return s.get_time(0, time);
+}
+
+}  // extern "C"

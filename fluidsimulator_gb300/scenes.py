@@ -1,0 +1,249 @@
+"""Scene construction for the PBF step: lattice blocks, box planes and the
+seeded benchmark scenes.
+
+`init_block` and `init_planes` restate the reference's scene helpers
+(core/src/init.cpp:72-107 and :109-117) in float32 arithmetic, so a scene built
+here is bit-identical to one built by the reference (checked by a CPU test
+against the reference compiled from source).
+
+Randomness (lattice jitter, scene sizes, initial velocities) comes from
+SplitMix64 (Steele, Lea & Flood, "Fast splittable pseudorandom number
+generators", OOPSLA 2014) keyed by an explicit seed, so every run on every
+machine builds the same scene. The reference publishes no dataset; all scenes
+are synthetic.
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from ._capi import MAX_PLANES, FluidParams, default_params
+
+_GOLDEN = np.uint64(0x9E3779B97F4A7C15)
+_M1 = np.uint64(0xBF58476D1CE4E5B9)
+_M2 = np.uint64(0x94D049BB133111EB)
+
+
+def splitmix64(seed: int, count: int, offset: int = 0) -> np.ndarray:
+    """Draws `count` 64-bit outputs of SplitMix64 seeded with `seed`,
+    starting after `offset` earlier draws."""
+    with np.errstate(over="ignore"):
+        k = np.arange(offset + 1, offset + count + 1, dtype=np.uint64)
+        z = np.uint64(seed) + k * _GOLDEN
+        z = (z ^ (z >> np.uint64(30))) * _M1
+        z = (z ^ (z >> np.uint64(27))) * _M2
+        return z ^ (z >> np.uint64(31))
+
+
+def uniform01(seed: int, count: int, offset: int = 0) -> np.ndarray:
+    """Float64 uniforms in [0, 1) with 53 random bits."""
+    return (splitmix64(seed, count, offset) >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+
+
+def normal(seed: int, count: int, offset: int = 0) -> np.ndarray:
+    """Standard normals by the Box-Muller transform of paired uniforms."""
+    m = (count + 1) // 2
+    u = uniform01(seed, 2 * m, offset)
+    u1 = 1.0 - u[0::2]  # (0, 1]
+    u2 = u[1::2]
+    r = np.sqrt(-2.0 * np.log(u1))
+    z = np.concatenate([r * np.cos(2.0 * np.pi * u2), r * np.sin(2.0 * np.pi * u2)])
+    out = np.empty(2 * m)
+    out[0::2] = z[:m]
+    out[1::2] = z[m:]
+    return out[:count]
+
+
+@dataclass
+class Scene:
+    """One scene: parameters plus SoA float32 state in caller order."""
+
+    name: str
+    params: FluidParams
+    pos: np.ndarray  # (3, N) float32
+    vel: np.ndarray  # (3, N) float32
+    steps: int = 1
+    info: dict = field(default_factory=dict)
+
+    @property
+    def count(self) -> int:
+        return int(self.pos.shape[1])
+
+    def copy(self) -> "Scene":
+        return Scene(self.name, self.params.copy(), self.pos.copy(), self.vel.copy(), self.steps, dict(self.info))
+
+
+def init_block(nx: int, ny: int, nz: int, origin, spacing: float) -> np.ndarray:
+    """Lattice of nx*ny*nz particles, z outermost and x innermost, each
+    coordinate origin + float(index) * spacing in float32
+    (core/src/init.cpp:96-106). Returns (3, N) float32."""
+    f32 = np.float32
+    step = f32(spacing)
+    ix = np.arange(nx, dtype=np.float32)
+    iy = np.arange(ny, dtype=np.float32)
+    iz = np.arange(nz, dtype=np.float32)
+    x = f32(origin[0]) + ix * step
+    y = f32(origin[1]) + iy * step
+    z = f32(origin[2]) + iz * step
+    zz, yy, xx = np.meshgrid(z, y, x, indexing="ij")
+    return np.stack([xx.ravel(), yy.ravel(), zz.ravel()]).astype(np.float32)
+
+
+def add_plane_normalized(p: FluidParams, nx: float, ny: float, nz: float, d: float) -> None:
+    """PlaneSoA::add_normalized (core/include/fluid/core.h:69-77) in float32."""
+    if p.plane_count >= MAX_PLANES:
+        raise ValueError("too many planes")
+    f32 = np.float32
+    nx, ny, nz, d = f32(nx), f32(ny), f32(nz), f32(d)
+    len_sq = nx * nx + ny * ny + nz * nz
+    if len_sq > f32(0):
+        inv = f32(1) / np.sqrt(len_sq, dtype=np.float32)
+        nx, ny, nz = nx * inv, ny * inv, nz * inv
+    i = p.plane_count
+    p.plane_nx[i], p.plane_ny[i], p.plane_nz[i], p.plane_d[i] = float(nx), float(ny), float(nz), float(d)
+    p.plane_count = i + 1
+
+
+def init_planes(p: FluidParams, bx: float, by: float, bz: float) -> None:
+    """Six inward planes of the box [0,bx]x[0,by]x[0,bz] (core/src/init.cpp:109-117)."""
+    p.plane_count = 0
+    add_plane_normalized(p, 1.0, 0.0, 0.0, 0.0)
+    add_plane_normalized(p, -1.0, 0.0, 0.0, -bx)
+    add_plane_normalized(p, 0.0, 1.0, 0.0, 0.0)
+    add_plane_normalized(p, 0.0, -1.0, 0.0, -by)
+    add_plane_normalized(p, 0.0, 0.0, 1.0, 0.0)
+    add_plane_normalized(p, 0.0, 0.0, -1.0, -bz)
+
+
+def jitter(pos: np.ndarray, amplitude: float, seed: int, offset: int = 0) -> np.ndarray:
+    """pos + U(-a, a) per coordinate; draw k = 3*i + axis, added in float32."""
+    n = pos.shape[1]
+    u = uniform01(seed, 3 * n, offset).reshape(n, 3).T
+    j = (amplitude * (2.0 * u - 1.0)).astype(np.float32)
+    return (pos + j).astype(np.float32)
+
+
+def base_params(spacing: float, h: float) -> FluidParams:
+    """Physics shared by the benchmark scenes: rho0 = 1000, m = rho0 * sp^3,
+    relaxation 100, dt = 1/120, 4 iterations, restitution 0.05, friction 0.1."""
+    p = default_params()
+    p.density = 1000.0
+    p.particle_mass = float(np.float32(1000.0) * np.float32(spacing) ** 3)
+    p.h = h
+    p.epsilon = 100.0
+    p.dt = 1.0 / 120.0
+    p.solver_iterations = 4
+    p.plane_restitution = 0.05
+    p.plane_friction = 0.1
+    return p
+
+
+def all_flags(p: FluidParams, h: float) -> None:
+    """s_corr k = 0.1, n = 4, dq = 0.2 h; XSPH c = 0.01; vorticity eps = 5e-4."""
+    p.enable_scorr = 1
+    p.scorr_k = 0.1
+    p.scorr_n = 4
+    p.scorr_dq_coeff = 0.2
+    p.enable_xsph = 1
+    p.visc_c = 0.01
+    p.enable_vorticity = 1
+    p.vort_epsilon = 0.0005
+
+
+def dam_break(n_side: int = 16, seed: int = 0, flags: bool = False) -> Scene:
+    """Plain dam break: n^3 lattice, spacing 0.05, corner (0.05,0.05,0.05),
+    jitter U(+-5e-4), box [0,1]^3, h = 0.1, flags off; 240 steps (n = 16:
+    4,096 particles)."""
+    sp, h = 0.05, 0.1
+    p = base_params(sp, h)
+    init_planes(p, 1.0, 1.0, 1.0)
+    if flags:
+        all_flags(p, h)
+    pos = jitter(init_block(n_side, n_side, n_side, (0.05, 0.05, 0.05), sp), 5e-4, seed)
+    vel = np.zeros_like(pos)
+    return Scene(f"dam_break_{n_side ** 3}", p, pos, vel, steps=240,
+                 info={"spacing": sp, "box": (1.0, 1.0, 1.0), "seed": seed})
+
+
+def double_dam_break(n_side: int = 50, seed: int = 0) -> Scene:
+    """Two n^3 blocks (2 x 125,000 at n = 50), spacing 0.025, h = 0.05, at the
+    two x-ends of a 4x2x2 box floor, centred in z; all three flags on; jitter
+    U(+-1e-4); 480 steps. Block placement is this builder's choice (the
+    benchmark leaves it open)."""
+    sp, h = 0.025, 0.05
+    bx, by, bz = 4.0, 2.0, 2.0
+    p = base_params(sp, h)
+    init_planes(p, bx, by, bz)
+    all_flags(p, h)
+    span = (n_side - 1) * sp
+    z0 = 0.5 * (bz - span)
+    a = init_block(n_side, n_side, n_side, (sp, sp, z0), sp)
+    b = init_block(n_side, n_side, n_side, (bx - sp - span, sp, z0), sp)
+    pos = jitter(np.concatenate([a, b], axis=1), 1e-4, seed)
+    vel = np.zeros_like(pos)
+    return Scene(f"double_dam_break_{2 * n_side ** 3}", p, pos, vel, steps=480,
+                 info={"spacing": sp, "box": (bx, by, bz), "seed": seed})
+
+
+def falling_block(n_side: int = 100, seed: int = 0) -> Scene:
+    """1M-particle throughput scene: an n^3 block (n = 100), spacing 0.02,
+    h = 0.04, in an 8x4x4 box, lower corner at (3, 1, 1) so it falls under
+    gravity; all three flags on; jitter U(+-1e-4); 600 steps. The corner is
+    this builder's choice (the benchmark leaves it open)."""
+    sp, h = 0.02, 0.04
+    bx, by, bz = 8.0, 4.0, 4.0
+    p = base_params(sp, h)
+    init_planes(p, bx, by, bz)
+    all_flags(p, h)
+    pos = jitter(init_block(n_side, n_side, n_side, (3.0, 1.0, 1.0), sp), 1e-4, seed)
+    vel = np.zeros_like(pos)
+    return Scene(f"falling_block_{n_side ** 3}", p, pos, vel, steps=600,
+                 info={"spacing": sp, "box": (bx, by, bz), "seed": seed, "origin": (3.0, 1.0, 1.0)})
+
+
+def batched_scenes(count: int = 64, seed: int = 0, n_min: int = 2000, n_max: int = 64000) -> list[Scene]:
+    """Batched dam breaks: `count` scenes, particle targets U[n_min, n_max]
+    and lattice aspect ratios x:y and z:y in U[0.5, 2] from the seed; spacing
+    0.05, h = 0.1, each in its own [0,2]x[0,1]x[0,1] box with the block's
+    corner at (0.05, 0.05, 0.05); flags on; jitter U(+-5e-4); 240 steps.
+    Blocks above ~16k particles do not fit the box at this spacing: the first
+    plane projection moves the overhang onto the walls, as the reference would."""
+    sp, h = 0.05, 0.1
+    u = uniform01(seed ^ 0xB47C4, 3 * count).reshape(count, 3)
+    scenes = []
+    off = 0
+    for s in range(count):
+        target = n_min + int(u[s, 0] * (n_max - n_min + 1))
+        rx = 0.5 + 1.5 * u[s, 1]
+        rz = 0.5 + 1.5 * u[s, 2]
+        base = (target / (rx * rz)) ** (1.0 / 3.0)
+        nx = max(1, int(round(rx * base)))
+        nz = max(1, int(round(rz * base)))
+        ny = max(1, int(round(target / (nx * nz))))
+        p = base_params(sp, h)
+        init_planes(p, 2.0, 1.0, 1.0)
+        all_flags(p, h)
+        pos = jitter(init_block(nx, ny, nz, (0.05, 0.05, 0.05), sp), 5e-4, seed, offset=off)
+        off += 3 * pos.shape[1]
+        scenes.append(Scene(f"batch_{s}", p, pos, np.zeros_like(pos), steps=240,
+                            info={"lattice": (nx, ny, nz), "target": target}))
+    return scenes
+
+
+def differentiable_block(n_side: int = 32, seed: int = 0) -> Scene:
+    """Differentiable scene: n^3 block (n = 32), spacing 0.05, h = 0.1, corner
+    (0.2, 0.05, 0.2) in a [0,2]^3 box, XSPH c = 0.01 and s_corr on (k = 0.1,
+    n = 4, dq = 0.2 h), vorticity off; initial velocity N(0, 0.1^2) per
+    component; 60 steps."""
+    sp, h = 0.05, 0.1
+    p = base_params(sp, h)
+    init_planes(p, 2.0, 2.0, 2.0)
+    all_flags(p, h)
+    p.enable_vorticity = 0
+    pos = init_block(n_side, n_side, n_side, (0.2, 0.05, 0.2), sp)
+    n = pos.shape[1]
+    vel = (0.1 * normal(seed ^ 0x5E1, 3 * n).reshape(n, 3).T).astype(np.float32)
+    return Scene(f"differentiable_{n}", p, pos, vel, steps=60,
+                 info={"spacing": sp, "box": (2.0, 2.0, 2.0), "seed": seed, "target": (1.5, 0.3, 1.0)})

@@ -1,0 +1,171 @@
+"""Python access to the device-resident solver of include/fluid_gb300.h.
+
+Thin ctypes plumbing over the C ABI, used by the tests and the benchmark:
+every step runs in the CUDA library; nothing here computes physics.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from ctypes import byref, c_char_p, c_double, c_float, c_int, c_int64, c_void_p
+
+import numpy as np
+
+from . import _capi
+from ._capi import FluidParams, FluidStats
+
+
+class FluidError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{_capi.STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+def device_available() -> tuple[bool, int, str | None]:
+    lib = _capi.load()
+    n = c_int(0)
+    err = c_char_p()
+    ok = lib.fluid_gb300_device_available(byref(n), byref(err))
+    return bool(ok), n.value, (err.value.decode() if err.value else None)
+
+
+def _rows(a):
+    """Row pointers of a (3, N) float32 array: numpy (host) or torch (host/device)."""
+    if isinstance(a, np.ndarray):
+        if a.dtype != np.float32 or a.ndim != 2 or a.shape[0] != 3 or not a.flags.c_contiguous:
+            raise ValueError("expected a C-contiguous (3, N) float32 array")
+        base = a.ctypes.data
+        stride = a.strides[0]
+        return [base + k * stride for k in range(3)], _capi.MEMORY_HOST
+    # torch.Tensor
+    if str(a.dtype) != "torch.float32" or a.dim() != 2 or a.shape[0] != 3 or not a.is_contiguous():
+        raise ValueError("expected a contiguous (3, N) float32 tensor")
+    base = a.data_ptr()
+    stride = a.stride(0) * 4
+    return [base + k * stride for k in range(3)], (_capi.MEMORY_DEVICE if a.is_cuda else _capi.MEMORY_HOST)
+
+
+class Solver:
+    """One device-resident solver for one or more independent scenes."""
+
+    def __init__(self, device: int = 0):
+        self.lib = _capi.load()
+        h = c_void_p()
+        self._check(self.lib.fluid_solver_create(byref(h), device), None)
+        self.h = h
+        self.n = 0
+        self.counts: list[int] = []
+
+    def _check(self, rc: int, h=...):
+        if rc != 0:
+            handle = self.h if h is ... else h
+            msg = self.lib.fluid_solver_last_error(handle).decode() if handle else ""
+            raise FluidError(rc, msg)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fluid_solver_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- configuration -----------------------------------------------------
+    def configure(self, params: list[FluidParams], counts: list[int]) -> None:
+        arr = (FluidParams * len(params))(*params)
+        cnt = (c_int64 * len(counts))(*counts)
+        self._check(self.lib.fluid_solver_configure(self.h, len(params), arr, cnt))
+        self.n = int(sum(counts))
+        self.counts = list(counts)
+
+    def set_params(self, params: list[FluidParams]) -> None:
+        arr = (FluidParams * len(params))(*params)
+        self._check(self.lib.fluid_solver_set_params(self.h, arr))
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        self._check(self.lib.fluid_solver_set_stream(self.h, c_void_p(stream_ptr or 0)))
+
+    def set_graphs(self, on: bool) -> None:
+        self._check(self.lib.fluid_solver_set_graphs(self.h, int(on)))
+
+    def set_profiling(self, on: bool) -> None:
+        self._check(self.lib.fluid_solver_set_profiling(self.h, int(on)))
+
+    # -- state ---------------------------------------------------------------
+    def upload(self, pos, vel) -> None:
+        pr, pm = _rows(pos)
+        vr, vm = _rows(vel)
+        if pm != vm:
+            raise ValueError("pos and vel must live in the same memory")
+        self._check(self.lib.fluid_solver_upload(self.h, *[c_void_p(p) for p in pr + vr], pm))
+
+    def download(self, pos=None, vel=None):
+        if pos is None:
+            pos = np.empty((3, self.n), np.float32)
+        if vel is None:
+            vel = np.empty((3, self.n), np.float32)
+        pr, pm = _rows(pos)
+        vr, vm = _rows(vel)
+        if pm != vm:
+            raise ValueError("pos and vel must live in the same memory")
+        self._check(self.lib.fluid_solver_download(self.h, *[c_void_p(p) for p in pr + vr], pm))
+        return pos, vel
+
+    def step(self, n: int = 1) -> None:
+        self._check(self.lib.fluid_solver_step(self.h, n))
+
+    def step_async(self, n: int = 1) -> None:
+        self._check(self.lib.fluid_solver_step_async(self.h, n))
+
+    def synchronize(self) -> None:
+        self._check(self.lib.fluid_solver_synchronize(self.h))
+
+    def time(self, scene: int = 0) -> float:
+        t = c_float()
+        self._check(self.lib.fluid_solver_get_time(self.h, scene, byref(t)))
+        return t.value
+
+    def set_time(self, t: float, scene: int = 0) -> None:
+        self._check(self.lib.fluid_solver_set_time(self.h, scene, c_float(t)))
+
+    def stats(self) -> dict:
+        s = FluidStats()
+        self._check(self.lib.fluid_solver_get_stats(self.h, byref(s)))
+        return {k: getattr(s, k) for k, _ in FluidStats._fields_}
+
+    def stage_times(self, reset: bool = False) -> dict:
+        n = len(_capi.STAGE_NAMES)
+        ms = (c_double * n)()
+        la = (c_int64 * n)()
+        self._check(self.lib.fluid_solver_stage_times(self.h, ms, la, n, int(reset)))
+        return {name: (ms[k], la[k]) for k, name in enumerate(_capi.STAGE_NAMES)}
+
+    def read_debug(self, what: int) -> np.ndarray:
+        if what == _capi.DEBUG_CELL_KEYS:
+            out = np.empty((self.n, 3), np.int32)
+        elif what in (_capi.DEBUG_RHO, _capi.DEBUG_LAMBDA):
+            out = np.empty(self.n, np.float32)
+        else:
+            out = np.empty(self.n, np.int32)
+        self._check(self.lib.fluid_solver_read_debug(self.h, what, out.ctypes.data_as(c_void_p), out.size))
+        return out
+
+
+def cuda_step(params: FluidParams, pos: np.ndarray, vel: np.ndarray, time: float) -> float:
+    """fluid::cuda_step semantics on host arrays: advances (pos, vel) in place
+    by one step and returns the new time."""
+    lib = _capi.load()
+    pr, _ = _rows(pos)
+    vr, _ = _rows(vel)
+    t = c_float(time)
+    f = ctypes.POINTER(c_float)
+    rc = lib.fluid_gb300_cuda_step(byref(params), pos.shape[1], *[ctypes.cast(p, f) for p in pr + vr], byref(t))
+    if rc != 0:
+        raise FluidError(rc, "fluid_gb300_cuda_step")
+    return t.value

@@ -1,0 +1,227 @@
+/*
+ * fluid_gb300.h — C ABI of the GB300 (sm_103a) Position Based Fluids timestep.
+ *
+ * This is the drop-in boundary for the CUDA backend of CTKnight/FluidSimulator.
+ * Every entry point names the reference interface it replaces (path:line within
+ * the reference project). All pointers are plain host or device pointers, all
+ * sizes are element counts, and every call returns a fluid_status code; no C++
+ * or torch types cross this boundary.
+ *
+ * Particle order at the boundary is always the caller's (original) order. The
+ * solver keeps particles sorted by grid cell on the device and undoes that
+ * permutation on download.
+ *
+ * Threading: a fluid_solver is single-threaded state; calls on one solver must
+ * not overlap. Different solvers may be used from different threads.
+ */
+#ifndef FLUID_GB300_H
+#define FLUID_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FLUID_GB300_ABI_VERSION 1
+/* Planes per scene. The reference keeps an unbounded std::vector SoA
+ * (core/include/fluid/core.h:44-78); every reference scene uses 6. */
+#define FLUID_MAX_PLANES 32
+
+typedef enum fluid_status {
+  FLUID_OK = 0,
+  FLUID_ERR_INVALID_ARGUMENT = 1, /* bad pointer, size or parameter */
+  FLUID_ERR_CUDA = 2,             /* a CUDA runtime call failed */
+  FLUID_ERR_CAPACITY = 3,         /* a device buffer could not grow enough */
+  FLUID_ERR_DOMAIN = 4,           /* grid over the particles' cells too large */
+  FLUID_ERR_NONFINITE = 5,        /* a predicted position was NaN or Inf */
+  FLUID_ERR_NO_DEVICE = 6,        /* no CUDA device */
+  FLUID_ERR_OUT_OF_MEMORY = 7,    /* device allocation failed */
+  FLUID_ERR_NOT_SUPPORTED = 8,    /* parameter combination not implemented */
+  FLUID_ERR_STATE = 9             /* call out of order (e.g. step before upload) */
+} fluid_status;
+
+/*
+ * Mirrors fluid::Params (core/include/fluid/core.h:11-79) field for field, same
+ * meaning and units. The plane SoA (core.h:44-78) becomes fixed arrays plus a
+ * count so the struct holds no pointers. Params::backend (core.h:13-17) is not
+ * carried: neither reference step function reads it.
+ */
+typedef struct fluid_params {
+  float dt;                      /* core.h:12 */
+  float density;                 /* core.h:18, rest density rho0 */
+  float particle_mass;           /* core.h:20 */
+  float h;                       /* core.h:22, kernel radius = grid cell size */
+  float particle_radius;         /* core.h:23, unused by the step */
+  float epsilon;                 /* core.h:24, lambda relaxation */
+  int32_t solver_iterations;     /* core.h:25 */
+  float neighbor_reserve_factor; /* core.h:26, neighbour-list growth factor */
+  int32_t use_uniform_grid;      /* core.h:27 */
+  int32_t enable_scorr;          /* core.h:28 */
+  int32_t enable_xsph;           /* core.h:29 */
+  int32_t enable_vorticity;      /* core.h:30 */
+  float scorr_k;                 /* core.h:31 */
+  int32_t scorr_n;               /* core.h:32 */
+  float scorr_dq_coeff;          /* core.h:33 */
+  float visc_c;                  /* core.h:34, XSPH c */
+  float plane_restitution;       /* core.h:35 */
+  float plane_friction;          /* core.h:36 */
+  float vort_epsilon;            /* core.h:37 */
+  float vort_norm_eps;           /* core.h:38 */
+  float external_force[3];       /* core.h:39-43 */
+  int32_t plane_count;           /* core.h:50 PlaneSoA::size() */
+  float plane_nx[FLUID_MAX_PLANES];
+  float plane_ny[FLUID_MAX_PLANES];
+  float plane_nz[FLUID_MAX_PLANES];
+  float plane_d[FLUID_MAX_PLANES]; /* signed distance = n.x - d */
+} fluid_params;
+
+/* Fills *p with the defaults of core/include/fluid/core.h:12-43 (no planes). */
+void fluid_params_default(fluid_params* p);
+
+/* Replaces fluid::cuda_version (cuda/include/fluid/cuda.h:7). */
+int fluid_gb300_version(void);
+
+/*
+ * Replaces fluid::cuda_device_available (cuda/include/fluid/cuda.h:8,
+ * cuda/src/cuda_stub.cu:740-762). Returns 1 when at least one device is
+ * present, else 0. *count receives the device count (0 on error); *error
+ * receives a static message or NULL. Either pointer may be NULL.
+ */
+int fluid_gb300_device_available(int* count, const char** error);
+
+/*
+ * Replaces fluid::cuda_step(const Params&, State&) (cuda/include/fluid/cuda.h:9,
+ * cuda/src/cuda_stub.cu:764-1099). Host SoA arrays of `count` particles in the
+ * caller's order are advanced by one timestep in place and *time += dt, exactly
+ * as the reference does. count == 0 only advances time (cuda_stub.cu:766-769).
+ * Device buffers are cached per calling thread between calls (keyed by count),
+ * so repeated calls allocate nothing; state still round-trips through the host
+ * arrays every call, like the reference.
+ */
+int fluid_gb300_cuda_step(const fluid_params* params, int64_t count,
+                          float* pos_x, float* pos_y, float* pos_z,
+                          float* vel_x, float* vel_y, float* vel_z,
+                          float* time);
+
+/* ---- Device-resident solver (no reference counterpart: the reference keeps
+ * no device state between steps; this is the handle the drop-in above uses). */
+
+typedef struct fluid_solver fluid_solver;
+
+enum { FLUID_MEMORY_HOST = 0, FLUID_MEMORY_DEVICE = 1 };
+
+/* Creates a solver on CUDA device `device` with its own non-blocking stream. */
+int fluid_solver_create(fluid_solver** out, int device);
+void fluid_solver_destroy(fluid_solver* solver);
+
+/* Runs all later work on `stream` (a cudaStream_t); NULL restores the solver's own. */
+int fluid_solver_set_stream(fluid_solver* solver, void* stream);
+
+/*
+ * Declares the scenes: `scene_count` independent scenes with params[s] and
+ * counts[s] particles each. Particle arrays at the boundary hold the scenes
+ * back to back (scene 0 first). A single simulation is scene_count == 1.
+ * All scenes must share solver_iterations, the three enable_* flags and
+ * use_uniform_grid; h, mass, planes and the rest may differ per scene.
+ * Resets the time of every scene to 0 and drops any uploaded state.
+ */
+int fluid_solver_configure(fluid_solver* solver, int32_t scene_count,
+                           const fluid_params* params, const int64_t* counts);
+
+/* Replaces the parameters of the configured scenes without touching state. */
+int fluid_solver_set_params(fluid_solver* solver, const fluid_params* params);
+
+/* Copies state in (caller order). memory selects host or device pointers. */
+int fluid_solver_upload(fluid_solver* solver,
+                        const float* pos_x, const float* pos_y, const float* pos_z,
+                        const float* vel_x, const float* vel_y, const float* vel_z,
+                        int32_t memory);
+
+/* Copies state out in caller order; synchronous. */
+int fluid_solver_download(fluid_solver* solver,
+                          float* pos_x, float* pos_y, float* pos_z,
+                          float* vel_x, float* vel_y, float* vel_z,
+                          int32_t memory);
+
+/*
+ * Advances every scene by `nsteps` timesteps and waits for the result. When a
+ * step needs a larger neighbour list or cell table than is allocated, the step
+ * is detected on the device, the buffers grow (by neighbor_reserve_factor, as
+ * core/src/core.cpp:128-136 reserves), and that step is re-run from its own
+ * untouched input, so results never depend on capacity.
+ */
+int fluid_solver_step(fluid_solver* solver, int32_t nsteps);
+
+/* Enqueues `nsteps` timesteps without waiting. */
+int fluid_solver_step_async(fluid_solver* solver, int32_t nsteps);
+
+/* Waits for enqueued steps, re-running any that overflowed a capacity. */
+int fluid_solver_synchronize(fluid_solver* solver);
+
+/* Capture each timestep as a CUDA graph (1) or launch kernels directly (0). */
+int fluid_solver_set_graphs(fluid_solver* solver, int32_t enable);
+
+/* Records CUDA events between stages of each step (adds no synchronisation). */
+int fluid_solver_set_profiling(fluid_solver* solver, int32_t enable);
+
+enum {
+  FLUID_STAGE_PREDICT = 0, /* bounds + cell keys */
+  FLUID_STAGE_SORT = 1,    /* radix sort */
+  FLUID_STAGE_REORDER = 2, /* gather into cell order + cell table */
+  FLUID_STAGE_NEIGHBORS = 3, /* neighbour count, slices, fill (+ first lambda) */
+  FLUID_STAGE_LAMBDA = 4,  /* density / lambda passes */
+  FLUID_STAGE_DELTA = 5,   /* position correction passes (+ commit) */
+  FLUID_STAGE_XSPH = 6,
+  FLUID_STAGE_VORTICITY = 7, /* omega, eta + apply + plane restitution */
+  FLUID_STAGE_COUNT = 8
+};
+
+/* Sums of per-stage GPU time (ms) and launch counts since the last reset. */
+int fluid_solver_stage_times(fluid_solver* solver, double* ms_out,
+                             int64_t* launches_out, int32_t stages,
+                             int32_t reset);
+
+/* Time of scene `scene` (float, accumulated as State::time, core.cpp:614). */
+int fluid_solver_get_time(fluid_solver* solver, int32_t scene, float* time);
+int fluid_solver_set_time(fluid_solver* solver, int32_t scene, float time);
+
+typedef struct fluid_stats {
+  int64_t particles;
+  int64_t steps;             /* completed steps since configure */
+  int64_t neighbor_pairs;    /* directed pairs in the last step's lists */
+  int32_t neighbor_max;      /* largest per-particle count, last step */
+  int32_t grid_cells;        /* cells in the last step's bounding grids */
+  int64_t neighbor_capacity; /* allocated list slots */
+  int64_t grid_capacity;     /* allocated cell-table entries */
+  int64_t regrows;           /* steps re-run after a capacity grew */
+  int64_t kernel_launches;   /* kernels launched since configure */
+} fluid_stats;
+
+int fluid_solver_get_stats(fluid_solver* solver, fluid_stats* out);
+
+/* Per-particle records of the last completed step, caller order. */
+enum {
+  FLUID_DEBUG_CELL_KEYS = 0,    /* int32 x3: floor(p* / h) per axis (core.cpp:28-34) */
+  FLUID_DEBUG_SORTED_ORDER = 1, /* int32: caller index at each sorted position
+                                   (core.cpp:173-183); per-scene local indices */
+  FLUID_DEBUG_NEIGHBOR_COUNTS = 2, /* int32 (core.cpp:245-246 differences) */
+  FLUID_DEBUG_RHO = 3,          /* float, last lambda pass (core.cpp:321) */
+  FLUID_DEBUG_LAMBDA = 4        /* float, last lambda pass (core.cpp:328) */
+};
+
+/* Copies a debug record to host memory of `capacity` elements (int32/float). */
+int fluid_solver_read_debug(fluid_solver* solver, int32_t what, void* host_out,
+                            int64_t capacity);
+
+/* Last error message of this solver (static storage owned by the solver). */
+const char* fluid_solver_last_error(const fluid_solver* solver);
+
+/* Message for a status code. */
+const char* fluid_status_string(int status);
+
+#ifdef __cplusplus
+}  /* extern "C" */
+#endif
+
+#endif /* FLUID_GB300_H */

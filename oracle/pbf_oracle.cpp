@@ -1,0 +1,640 @@
+// ORACLE — test infrastructure, not product code.
+//
+// A CPU restatement of the reference Position Based Fluids timestep
+// (CTKnight/FluidSimulator core/src/core.cpp:119-615), templated on the
+// arithmetic type. T = float is the checker the GPU path is compared against
+// (bit-exact with the reference when both are compiled with -ffp-contract=off);
+// T = double is the FP64 run used to report each path's error. Only the tests,
+// the smoke check and the bench's CPU-baseline leg load this library; the
+// product never links or calls it.
+//
+// Per-step scratch (neighbour list, rho, lambda, ...) lives in a workspace that
+// persists across steps, as fluid::CpuScratch does inside fluid::State
+// (core/include/fluid/core.h:81-132): with solver_iterations == 0 the XSPH pass
+// reads the previous step's rho, exactly like the reference.
+
+#include "fluid_gb300.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+template <typename T>
+struct Pi;
+template <>
+struct Pi<float> {
+  static constexpr float value = 3.14159265358979323846f;  // core.cpp:10
+};
+template <>
+struct Pi<double> {
+  static constexpr double value = 3.14159265358979323846;
+};
+
+// core.cpp:35-46
+template <typename T>
+T poly6(T r2, T h) {
+  const T h2 = h * h;
+  if (r2 > h2) return T(0);
+  const T diff = h2 - r2;
+  const T diff3 = diff * diff * diff;
+  const T h4 = h2 * h2;
+  const T h9 = h4 * h4 * h;
+  const T coeff = T(315) / (T(64) * Pi<T>::value * h9);
+  return coeff * diff3;
+}
+
+// core.cpp:48-57
+template <typename T>
+T spiky_factor(T r, T h) {
+  if (r > h) return T(0);
+  const T h2 = h * h;
+  const T h6 = h2 * h2 * h2;
+  const T diff = h - r;
+  const T coeff = T(-45) / (Pi<T>::value * h6);
+  return coeff * diff * diff;
+}
+
+// core.cpp:59-71
+template <typename T>
+T pow_n(T ratio, int n) {
+  if (n == 2) return ratio * ratio;
+  if (n == 3) return ratio * ratio * ratio;
+  if (n == 4) {
+    const T r2 = ratio * ratio;
+    return r2 * r2;
+  }
+  return std::pow(ratio, static_cast<T>(n));
+}
+
+struct Cell {
+  int x, y, z;
+};
+
+inline bool cell_less(const Cell& a, const Cell& b) {  // core.cpp:12-21
+  if (a.x != b.x) return a.x < b.x;
+  if (a.y != b.y) return a.y < b.y;
+  return a.z < b.z;
+}
+inline bool cell_eq(const Cell& a, const Cell& b) {  // core.cpp:23-26
+  return a.x == b.x && a.y == b.y && a.z == b.z;
+}
+
+// core.cpp:28-34: floor(p * (1/h)), the multiply by the rounded reciprocal.
+template <typename T>
+Cell cell_of(T x, T y, T z, T cell) {
+  const T inv = T(1) / cell;
+  return Cell{static_cast<int>(std::floor(x * inv)),
+              static_cast<int>(std::floor(y * inv)),
+              static_cast<int>(std::floor(z * inv))};
+}
+
+template <typename T>
+struct Workspace {
+  std::vector<T> px, py, pz;        // predicted positions p*
+  std::vector<T> dx, dy, dz;        // Jacobi corrections
+  std::vector<T> lambda, rho;
+  std::vector<T> dvx, dvy, dvz;     // XSPH
+  std::vector<T> ox, oy, oz, omag;  // vorticity omega, |omega|
+  std::vector<T> ex, ey, ez;        // eta
+  std::vector<Cell> key;            // cell of p* per particle
+  std::vector<int> order;           // particle at each sorted position
+  std::vector<Cell> run_key;        // occupied cells, ascending
+  std::vector<int> run_begin, run_end;
+  std::vector<int> nbr;             // neighbour lists, back to back
+  std::vector<int64_t> nbr_begin;   // count + 1 offsets into nbr
+
+  void resize(std::size_t n) {
+    for (auto* v : {&px, &py, &pz, &dx, &dy, &dz, &lambda, &rho, &dvx, &dvy,
+                    &dvz, &ox, &oy, &oz, &omag, &ex, &ey, &ez}) {
+      v->resize(n, T(0));
+    }
+    key.resize(n);
+    order.resize(n);
+    nbr_begin.resize(n + 1, 0);
+  }
+};
+
+template <typename T>
+struct Consts {
+  T dt, h, h2, min_r2, inv_density, mass, grad_scale, epsilon;
+  bool scorr;
+  T scorr_inv_wdq, scorr_k;
+  int scorr_n;
+};
+
+template <typename T>
+Consts<T> make_consts(const fluid_params& p) {
+  Consts<T> c{};
+  c.dt = T(p.dt);
+  c.h = T(p.h);
+  c.h2 = c.h * c.h;
+  const T min_r = T(0.01f) * c.h;  // core.cpp:141-142
+  c.min_r2 = min_r * min_r;
+  c.scorr = p.enable_scorr && p.scorr_k != 0.0f;  // core.cpp:143-148
+  const T dq_coeff = (p.scorr_dq_coeff > 0.0f) ? T(p.scorr_dq_coeff) : T(0.3f);
+  const T dq = dq_coeff * c.h;
+  const T wdq = c.scorr ? poly6<T>(dq * dq, c.h) : T(0);
+  c.scorr_inv_wdq = (wdq > T(1e-12f)) ? (T(1) / wdq) : T(0);
+  c.scorr_k = T(p.scorr_k);
+  c.scorr_n = p.scorr_n;
+  c.inv_density = T(1) / T(p.density);  // core.cpp:270-274
+  c.mass = T(p.particle_mass);
+  c.grad_scale = c.mass * c.inv_density;
+  c.epsilon = T(p.epsilon);
+  return c;
+}
+
+// Neighbour lists from p* on the uniform grid (core.cpp:163-247): cells of
+// size h, particles sorted by (cell x, y, z, index), each particle scanning the
+// 27 cells in dz, dy, dx order and keeping j != i with r^2 < h^2 in scan order.
+template <typename T>
+void build_grid_lists(Workspace<T>& w, std::size_t n, T h, T h2) {
+  for (std::size_t i = 0; i < n; ++i) {
+    w.key[i] = cell_of(w.px[i], w.py[i], w.pz[i], h);
+    w.order[i] = static_cast<int>(i);
+  }
+  std::sort(w.order.begin(), w.order.end(), [&](int a, int b) {
+    if (cell_less(w.key[a], w.key[b])) return true;
+    if (cell_less(w.key[b], w.key[a])) return false;
+    return a < b;
+  });
+  w.run_key.clear();
+  w.run_begin.clear();
+  w.run_end.clear();
+  for (std::size_t s = 0; s < n; ++s) {
+    const Cell& k = w.key[w.order[s]];
+    if (s == 0 || !cell_eq(k, w.run_key.back())) {
+      if (s != 0) w.run_end.push_back(static_cast<int>(s));
+      w.run_key.push_back(k);
+      w.run_begin.push_back(static_cast<int>(s));
+    }
+  }
+  w.run_end.push_back(static_cast<int>(n));
+
+  w.nbr.clear();
+  w.nbr_begin[0] = 0;
+  for (std::size_t i = 0; i < n; ++i) {
+    const T xi = w.px[i], yi = w.py[i], zi = w.pz[i];
+    const Cell base = cell_of(xi, yi, zi, h);
+    for (int oz = -1; oz <= 1; ++oz) {
+      for (int oy = -1; oy <= 1; ++oy) {
+        for (int ox = -1; ox <= 1; ++ox) {
+          const Cell want{base.x + ox, base.y + oy, base.z + oz};
+          auto it = std::lower_bound(w.run_key.begin(), w.run_key.end(), want,
+                                     cell_less);
+          if (it == w.run_key.end() || !cell_eq(*it, want)) continue;
+          const std::size_t r = static_cast<std::size_t>(it - w.run_key.begin());
+          for (int s = w.run_begin[r]; s < w.run_end[r]; ++s) {
+            const int j = w.order[s];
+            if (j == static_cast<int>(i)) continue;
+            const T ddx = xi - w.px[j];
+            const T ddy = yi - w.py[j];
+            const T ddz = zi - w.pz[j];
+            const T r2 = ddx * ddx + ddy * ddy + ddz * ddz;
+            if (r2 < h2) w.nbr.push_back(j);
+          }
+        }
+      }
+    }
+    w.nbr_begin[i + 1] = static_cast<int64_t>(w.nbr.size());
+  }
+}
+
+// All-pairs lists in ascending j (core.cpp:248-268), for use_uniform_grid == 0.
+template <typename T>
+void build_pair_lists(Workspace<T>& w, std::size_t n, T h2) {
+  w.nbr.clear();
+  w.nbr_begin[0] = 0;
+  for (std::size_t i = 0; i < n; ++i) {
+    for (std::size_t j = 0; j < n; ++j) {
+      if (i == j) continue;
+      const T ddx = w.px[i] - w.px[j];
+      const T ddy = w.py[i] - w.py[j];
+      const T ddz = w.pz[i] - w.pz[j];
+      const T r2 = ddx * ddx + ddy * ddy + ddz * ddz;
+      if (r2 < h2) w.nbr.push_back(static_cast<int>(j));
+    }
+    w.nbr_begin[i + 1] = static_cast<int64_t>(w.nbr.size());
+  }
+}
+
+template <typename T>
+struct Dump {
+  int32_t* cell_keys;
+  int32_t* sorted_order;
+  int32_t* neighbor_counts;
+  T* rho;
+  T* lambda;
+};
+
+template <typename T>
+int step(Workspace<T>& w, const fluid_params& p, std::size_t n, T* X, T* Y,
+         T* Z, T* VX, T* VY, T* VZ, T* time, const Dump<T>* dump,
+         int64_t* pairs_out, int32_t* max_out) {
+  w.resize(n);
+  if (n == 0) {  // core.cpp:122-125
+    *time += T(p.dt);
+    return 0;
+  }
+  const Consts<T> c = make_consts<T>(p);
+  const T h = c.h, h2 = c.h2, dt = c.dt;
+  const T fx = T(p.external_force[0]), fy = T(p.external_force[1]),
+          fz = T(p.external_force[2]);
+  const long long N = static_cast<long long>(n);
+
+  // Predict (core.cpp:150-161).
+#pragma omp parallel for
+  for (long long i = 0; i < N; ++i) {
+    VX[i] += fx * dt;
+    VY[i] += fy * dt;
+    VZ[i] += fz * dt;
+    w.px[i] = X[i] + VX[i] * dt;
+    w.py[i] = Y[i] + VY[i] * dt;
+    w.pz[i] = Z[i] + VZ[i] * dt;
+  }
+
+  const bool grid = p.use_uniform_grid && h > T(0);
+  if (grid) {
+    build_grid_lists(w, n, h, h2);
+  } else {
+    build_pair_lists(w, n, h2);
+  }
+
+  // Jacobi iterations (core.cpp:276-408).
+  for (int iter = 0; iter < p.solver_iterations; ++iter) {
+    // Density constraint and lambda (core.cpp:281-329).
+#pragma omp parallel for
+    for (long long i = 0; i < N; ++i) {
+      const T xi = w.px[i], yi = w.py[i], zi = w.pz[i];
+      T rho = T(0), gsx = T(0), gsy = T(0), gsz = T(0), sum_g2 = T(0);
+      for (int64_t k = w.nbr_begin[i]; k < w.nbr_begin[i + 1]; ++k) {
+        const int j = w.nbr[k];
+        const T ddx = xi - w.px[j];
+        const T ddy = yi - w.py[j];
+        const T ddz = zi - w.pz[j];
+        const T r2 = ddx * ddx + ddy * ddy + ddz * ddz;
+        rho += poly6<T>(r2, h);
+        if (r2 < h2) {
+          const T r = std::sqrt(r2 < c.min_r2 ? c.min_r2 : r2);
+          const T gf = spiky_factor<T>(r, h);
+          const T gx = gf * ddx, gy = gf * ddy, gz = gf * ddz;
+          gsx += gx;
+          gsy += gy;
+          gsz += gz;
+          const T jx = -c.grad_scale * gx;
+          const T jy = -c.grad_scale * gy;
+          const T jz = -c.grad_scale * gz;
+          sum_g2 += jx * jx + jy * jy + jz * jz;
+        }
+      }
+      rho += poly6<T>(T(0), h);
+      rho *= c.mass;
+      w.rho[i] = rho;
+      const T C = rho * c.inv_density - T(1);
+      const T ix = c.grad_scale * gsx;
+      const T iy = c.grad_scale * gsy;
+      const T iz = c.grad_scale * gsz;
+      sum_g2 += ix * ix + iy * iy + iz * iz;
+      w.lambda[i] = -C / (sum_g2 + c.epsilon);
+    }
+
+    // Position correction with s_corr and plane projection (core.cpp:334-398).
+#pragma omp parallel for
+    for (long long i = 0; i < N; ++i) {
+      const T xi = w.px[i], yi = w.py[i], zi = w.pz[i];
+      const T li = w.lambda[i];
+      T ax = T(0), ay = T(0), az = T(0);
+      for (int64_t k = w.nbr_begin[i]; k < w.nbr_begin[i + 1]; ++k) {
+        const int j = w.nbr[k];
+        const T ddx = xi - w.px[j];
+        const T ddy = yi - w.py[j];
+        const T ddz = zi - w.pz[j];
+        const T r2 = ddx * ddx + ddy * ddy + ddz * ddz;
+        if (r2 < h2) {
+          const T r = std::sqrt(r2 < c.min_r2 ? c.min_r2 : r2);
+          const T gf = spiky_factor<T>(r, h);
+          T s = li + w.lambda[j];
+          if (c.scorr && c.scorr_inv_wdq > T(0)) {
+            const T W = poly6<T>(r2, h);
+            const T ratio = W * c.scorr_inv_wdq;
+            s += -c.scorr_k * pow_n<T>(ratio, c.scorr_n);
+          }
+          ax += s * gf * ddx;
+          ay += s * gf * ddy;
+          az += s * gf * ddz;
+        }
+      }
+      ax *= c.inv_density;
+      ay *= c.inv_density;
+      az *= c.inv_density;
+      if (p.plane_count > 0) {
+        T qx = xi + ax, qy = yi + ay, qz = zi + az;
+        for (int q = 0; q < p.plane_count; ++q) {
+          const T nx = T(p.plane_nx[q]), ny = T(p.plane_ny[q]),
+                  nz = T(p.plane_nz[q]), d = T(p.plane_d[q]);
+          const T sd = nx * qx + ny * qy + nz * qz - d;
+          const T pen = -sd;
+          if (pen > T(0)) {
+            qx += nx * pen;
+            qy += ny * pen;
+            qz += nz * pen;
+          }
+        }
+        ax = qx - xi;
+        ay = qy - yi;
+        az = qz - zi;
+      }
+      w.dx[i] = ax;
+      w.dy[i] = ay;
+      w.dz[i] = az;
+    }
+#pragma omp parallel for
+    for (long long i = 0; i < N; ++i) {  // core.cpp:400-407
+      w.px[i] += w.dx[i];
+      w.py[i] += w.dy[i];
+      w.pz[i] += w.dz[i];
+    }
+  }
+
+  // Commit (core.cpp:410-421).
+#pragma omp parallel for
+  for (long long i = 0; i < N; ++i) {
+    VX[i] = (w.px[i] - X[i]) / dt;
+    VY[i] = (w.py[i] - Y[i]) / dt;
+    VZ[i] = (w.pz[i] - Z[i]) / dt;
+    X[i] = w.px[i];
+    Y[i] = w.py[i];
+    Z[i] = w.pz[i];
+  }
+
+  // XSPH viscosity over the step's lists at committed positions (core.cpp:423-466).
+  if (p.enable_xsph && p.visc_c != 0.0f) {
+    const T cvis = T(p.visc_c);
+#pragma omp parallel for
+    for (long long i = 0; i < N; ++i) {
+      const T vx = VX[i], vy = VY[i], vz = VZ[i];
+      T sx = T(0), sy = T(0), sz = T(0);
+      for (int64_t k = w.nbr_begin[i]; k < w.nbr_begin[i + 1]; ++k) {
+        const int j = w.nbr[k];
+        const T ddx = X[i] - X[j];
+        const T ddy = Y[i] - Y[j];
+        const T ddz = Z[i] - Z[j];
+        const T r2 = ddx * ddx + ddy * ddy + ddz * ddz;
+        if (r2 < h2) {
+          const T W = poly6<T>(r2, h);
+          const T inv_rho_j = (w.rho[j] > T(0)) ? (c.mass / w.rho[j]) : T(0);
+          sx += (VX[j] - vx) * W * inv_rho_j;
+          sy += (VY[j] - vy) * W * inv_rho_j;
+          sz += (VZ[j] - vz) * W * inv_rho_j;
+        }
+      }
+      w.dvx[i] = sx;
+      w.dvy[i] = sy;
+      w.dvz[i] = sz;
+    }
+#pragma omp parallel for
+    for (long long i = 0; i < N; ++i) {
+      VX[i] += cvis * w.dvx[i];
+      VY[i] += cvis * w.dvy[i];
+      VZ[i] += cvis * w.dvz[i];
+    }
+  }
+
+  // Vorticity confinement (core.cpp:468-571).
+  if (p.enable_vorticity && p.vort_epsilon != 0.0f) {
+#pragma omp parallel for
+    for (long long i = 0; i < N; ++i) {
+      const T xi = X[i], yi = Y[i], zi = Z[i];
+      const T vx = VX[i], vy = VY[i], vz = VZ[i];
+      T ax = T(0), ay = T(0), az = T(0);
+      for (int64_t k = w.nbr_begin[i]; k < w.nbr_begin[i + 1]; ++k) {
+        const int j = w.nbr[k];
+        const T ddx = xi - X[j];
+        const T ddy = yi - Y[j];
+        const T ddz = zi - Z[j];
+        const T r2 = ddx * ddx + ddy * ddy + ddz * ddz;
+        if (r2 < h2) {
+          const T r = std::sqrt(r2 < c.min_r2 ? c.min_r2 : r2);
+          const T gf = spiky_factor<T>(r, h);
+          const T gx = gf * ddx, gy = gf * ddy, gz = gf * ddz;
+          const T ux = VX[j] - vx, uy = VY[j] - vy, uz = VZ[j] - vz;
+          ax += uy * gz - uz * gy;
+          ay += uz * gx - ux * gz;
+          az += ux * gy - uy * gx;
+        }
+      }
+      w.ox[i] = ax;
+      w.oy[i] = ay;
+      w.oz[i] = az;
+      w.omag[i] = std::sqrt(ax * ax + ay * ay + az * az);
+    }
+#pragma omp parallel for
+    for (long long i = 0; i < N; ++i) {
+      const T xi = X[i], yi = Y[i], zi = Z[i];
+      const T mi = w.omag[i];
+      T ax = T(0), ay = T(0), az = T(0);
+      for (int64_t k = w.nbr_begin[i]; k < w.nbr_begin[i + 1]; ++k) {
+        const int j = w.nbr[k];
+        const T ddx = xi - X[j];
+        const T ddy = yi - Y[j];
+        const T ddz = zi - Z[j];
+        const T r2 = ddx * ddx + ddy * ddy + ddz * ddz;
+        if (r2 < h2) {
+          const T r = std::sqrt(r2 < c.min_r2 ? c.min_r2 : r2);
+          const T gf = spiky_factor<T>(r, h);
+          const T coeff = w.omag[j] - mi;
+          ax += coeff * (gf * ddx);
+          ay += coeff * (gf * ddy);
+          az += coeff * (gf * ddz);
+        }
+      }
+      w.ex[i] = ax;
+      w.ey[i] = ay;
+      w.ez[i] = az;
+    }
+    const T veps = T(p.vort_epsilon);
+    const T neps = T(p.vort_norm_eps);
+#pragma omp parallel for
+    for (long long i = 0; i < N; ++i) {
+      const T ex = w.ex[i], ey = w.ey[i], ez = w.ez[i];
+      const T len = std::sqrt(ex * ex + ey * ey + ez * ez);
+      T nx = T(0), ny = T(0), nz = T(0);
+      if (len > neps) {
+        const T inv = T(1) / len;
+        nx = ex * inv;
+        ny = ey * inv;
+        nz = ez * inv;
+      }
+      const T ox = w.ox[i], oy = w.oy[i], oz = w.oz[i];
+      const T fxv = veps * (ny * oz - nz * oy);
+      const T fyv = veps * (nz * ox - nx * oz);
+      const T fzv = veps * (nx * oy - ny * ox);
+      VX[i] += dt * fxv;
+      VY[i] += dt * fyv;
+      VZ[i] += dt * fzv;
+    }
+  }
+
+  // Plane restitution and friction (core.cpp:573-612).
+  if ((p.plane_restitution > 0.0f || p.plane_friction > 0.0f) &&
+      p.plane_count > 0) {
+    const T e = T(p.plane_restitution);
+    const T scale = T(1) - T(p.plane_friction);
+#pragma omp parallel for
+    for (long long i = 0; i < N; ++i) {
+      T vx = VX[i], vy = VY[i], vz = VZ[i];
+      const T xi = X[i], yi = Y[i], zi = Z[i];
+      for (int q = 0; q < p.plane_count; ++q) {
+        const T nx = T(p.plane_nx[q]), ny = T(p.plane_ny[q]),
+                nz = T(p.plane_nz[q]), d = T(p.plane_d[q]);
+        const T sd = nx * xi + ny * yi + nz * zi - d;
+        if (sd <= T(0)) {
+          const T vn = nx * vx + ny * vy + nz * vz;
+          T vn_new = vn;
+          if (vn < T(0)) vn_new = -e * vn;
+          const T tx = vx - vn * nx;
+          const T ty = vy - vn * ny;
+          const T tz = vz - vn * nz;
+          vx = tx * scale + vn_new * nx;
+          vy = ty * scale + vn_new * ny;
+          vz = tz * scale + vn_new * nz;
+        }
+      }
+      VX[i] = vx;
+      VY[i] = vy;
+      VZ[i] = vz;
+    }
+  }
+
+  *time += dt;  // core.cpp:614
+
+  int64_t pairs = static_cast<int64_t>(w.nbr.size());
+  int32_t mx = 0;
+  for (std::size_t i = 0; i < n; ++i) {
+    mx = std::max<int32_t>(mx, static_cast<int32_t>(w.nbr_begin[i + 1] - w.nbr_begin[i]));
+  }
+  if (pairs_out) *pairs_out = pairs;
+  if (max_out) *max_out = mx;
+  if (dump) {
+    for (std::size_t i = 0; i < n; ++i) {
+      if (dump->cell_keys) {
+        const Cell k = grid ? w.key[i] : cell_of(w.px[i], w.py[i], w.pz[i], h);
+        dump->cell_keys[3 * i + 0] = k.x;
+        dump->cell_keys[3 * i + 1] = k.y;
+        dump->cell_keys[3 * i + 2] = k.z;
+      }
+      if (dump->sorted_order) dump->sorted_order[i] = grid ? w.order[i] : int32_t(i);
+      if (dump->neighbor_counts)
+        dump->neighbor_counts[i] = static_cast<int32_t>(w.nbr_begin[i + 1] - w.nbr_begin[i]);
+      if (dump->rho) dump->rho[i] = w.rho[i];
+      if (dump->lambda) dump->lambda[i] = w.lambda[i];
+    }
+  }
+  return 0;
+}
+
+bool params_ok(const fluid_params* p) {
+  return p && p->plane_count >= 0 && p->plane_count <= FLUID_MAX_PLANES &&
+         p->solver_iterations >= 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+typedef struct pbf_oracle_dump_f32 {
+  int32_t* cell_keys;       // 3 per particle, cells of p* (core.cpp:165-171)
+  int32_t* sorted_order;    // particle at each sorted position (core.cpp:173-183)
+  int32_t* neighbor_counts; // per particle (core.cpp:245-246)
+  float* rho;               // last lambda pass (core.cpp:321)
+  float* lambda;            // last lambda pass (core.cpp:328)
+} pbf_oracle_dump_f32;
+
+typedef struct pbf_oracle_dump_f64 {
+  int32_t* cell_keys;
+  int32_t* sorted_order;
+  int32_t* neighbor_counts;
+  double* rho;
+  double* lambda;
+} pbf_oracle_dump_f64;
+
+void* pbf_oracle_create_f32(void) { return new Workspace<float>(); }
+void pbf_oracle_destroy_f32(void* ws) { delete static_cast<Workspace<float>*>(ws); }
+void* pbf_oracle_create_f64(void) { return new Workspace<double>(); }
+void pbf_oracle_destroy_f64(void* ws) { delete static_cast<Workspace<double>*>(ws); }
+
+int pbf_oracle_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+  return omp_get_max_threads();
+#else
+  (void)n;
+  return 1;
+#endif
+}
+
+// Runs `nsteps` steps. Optional per-step records (length nsteps, may be NULL):
+// neighbour pairs, largest neighbour count, and mean / max of rho_i/rho0 - 1
+// from the last lambda pass. The dump (may be NULL) describes the last step.
+int pbf_oracle_run_f32(void* ws, const fluid_params* p, int64_t count,
+                       float* px, float* py, float* pz, float* vx, float* vy,
+                       float* vz, float* time, int32_t nsteps,
+                       const pbf_oracle_dump_f32* dump, int64_t* pairs,
+                       int32_t* nmax, double* dens_mean, double* dens_max) {
+  if (!ws || !params_ok(p) || count < 0 || nsteps < 0) return FLUID_ERR_INVALID_ARGUMENT;
+  auto& w = *static_cast<Workspace<float>*>(ws);
+  const std::size_t n = static_cast<std::size_t>(count);
+  for (int s = 0; s < nsteps; ++s) {
+    Dump<float> d{};
+    if (dump) d = Dump<float>{dump->cell_keys, dump->sorted_order, dump->neighbor_counts, dump->rho, dump->lambda};
+    step<float>(w, *p, n, px, py, pz, vx, vy, vz, time, (dump && s == nsteps - 1) ? &d : nullptr,
+                pairs ? &pairs[s] : nullptr, nmax ? &nmax[s] : nullptr);
+    if (dens_mean || dens_max) {
+      double sum = 0.0, mx = -1e300;
+      for (std::size_t i = 0; i < n; ++i) {
+        const double e = double(w.rho[i]) / double(p->density) - 1.0;
+        sum += e;
+        mx = std::max(mx, e);
+      }
+      if (dens_mean) dens_mean[s] = n ? sum / double(n) : 0.0;
+      if (dens_max) dens_max[s] = n ? mx : 0.0;
+    }
+  }
+  return FLUID_OK;
+}
+
+int pbf_oracle_run_f64(void* ws, const fluid_params* p, int64_t count,
+                       double* px, double* py, double* pz, double* vx,
+                       double* vy, double* vz, double* time, int32_t nsteps,
+                       const pbf_oracle_dump_f64* dump, int64_t* pairs,
+                       int32_t* nmax, double* dens_mean, double* dens_max) {
+  if (!ws || !params_ok(p) || count < 0 || nsteps < 0) return FLUID_ERR_INVALID_ARGUMENT;
+  auto& w = *static_cast<Workspace<double>*>(ws);
+  const std::size_t n = static_cast<std::size_t>(count);
+  for (int s = 0; s < nsteps; ++s) {
+    Dump<double> d{};
+    if (dump) d = Dump<double>{dump->cell_keys, dump->sorted_order, dump->neighbor_counts, dump->rho, dump->lambda};
+    step<double>(w, *p, n, px, py, pz, vx, vy, vz, time, (dump && s == nsteps - 1) ? &d : nullptr,
+                 pairs ? &pairs[s] : nullptr, nmax ? &nmax[s] : nullptr);
+    if (dens_mean || dens_max) {
+      double sum = 0.0, mx = -1e300;
+      for (std::size_t i = 0; i < n; ++i) {
+        const double e = w.rho[i] / double(p->density) - 1.0;
+        sum += e;
+        mx = std::max(mx, e);
+      }
+      if (dens_mean) dens_mean[s] = n ? sum / double(n) : 0.0;
+      if (dens_max) dens_max[s] = n ? mx : 0.0;
+    }
+  }
+  return FLUID_OK;
+}
+
+}  // extern "C"

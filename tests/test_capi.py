@@ -1,0 +1,93 @@
+"""The C-ABI library without a GPU: it builds, loads, exports every entry
+point include/*.h declares, its struct layout matches the ctypes mirror, and
+its defaults match fluid::Params (core/include/fluid/core.h:11-43)."""
+
+import ctypes
+import glob
+import os
+import re
+import subprocess
+
+import pytest
+
+from conftest import ROOT
+from fluidsimulator_gb300 import _capi
+from fluidsimulator_gb300._capi import FluidParams, FluidStats, default_params
+
+
+def _declared_functions():
+    names = []
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names += re.findall(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(fluid_\w+)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+def test_library_exports_every_declared_symbol(cuda_lib):
+    names = _declared_functions()
+    assert len(names) >= 20
+    missing = [n for n in names if not hasattr(cuda_lib, n)]
+    assert not missing, missing
+
+
+def test_params_default_matches_mirror(cuda_lib):
+    p = FluidParams()
+    cuda_lib.fluid_params_default(ctypes.byref(p))
+    assert bytes(p) == bytes(default_params())
+
+
+def test_version(cuda_lib):
+    assert cuda_lib.fluid_gb300_version() == 1
+
+
+def test_struct_layout_matches_header(tmp_path):
+    src = tmp_path / "layout.c"
+    fields = [f for f, _ in FluidParams._fields_]
+    sfields = [f for f, _ in FluidStats._fields_]
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "fluid_gb300.h"', "int main(void) {",
+             'printf("%zu\\n", sizeof(fluid_params));', 'printf("%zu\\n", sizeof(fluid_stats));']
+    lines += [f'printf("%zu\\n", offsetof(fluid_params, {f}));' for f in fields]
+    lines += [f'printf("%zu\\n", offsetof(fluid_stats, {f}));' for f in sfields]
+    lines += ["return 0; }"]
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    assert out[0] == ctypes.sizeof(FluidParams)
+    assert out[1] == ctypes.sizeof(FluidStats)
+    assert out[2:2 + len(fields)] == [getattr(FluidParams, f).offset for f in fields]
+    assert out[2 + len(fields):] == [getattr(FluidStats, f).offset for f in sfields]
+
+
+def test_status_strings(cuda_lib):
+    for code in range(10):
+        assert cuda_lib.fluid_status_string(code)
+
+
+def test_device_query_without_gpu(cuda_lib):
+    torch = pytest.importorskip("torch")
+    n = ctypes.c_int(-1)
+    err = ctypes.c_char_p()
+    ok = cuda_lib.fluid_gb300_device_available(ctypes.byref(n), ctypes.byref(err))
+    assert bool(ok) == torch.cuda.is_available()
+    if not torch.cuda.is_available():
+        assert n.value == 0
+        h = ctypes.c_void_p()
+        assert cuda_lib.fluid_solver_create(ctypes.byref(h), 0) == 6  # FLUID_ERR_NO_DEVICE
+        assert not h.value
+
+
+def test_stateless_step_empty_state_advances_time(cuda_lib):
+    # count == 0 only advances time (cuda/src/cuda_stub.cu:766-769); no device needed.
+    p = default_params()
+    p.h = 0.1
+    t = ctypes.c_float(1.0)
+    assert cuda_lib.fluid_gb300_cuda_step(ctypes.byref(p), 0, None, None, None, None, None, None, ctypes.byref(t)) == 0
+    assert t.value == ctypes.c_float(1.0 + ctypes.c_float(p.dt).value).value
+
+
+def test_null_arguments_rejected(cuda_lib):
+    assert cuda_lib.fluid_solver_step(None, 1) == 1
+    assert cuda_lib.fluid_solver_configure(None, 1, None, None) == 1
+    assert cuda_lib.fluid_gb300_cuda_step(None, 0, None, None, None, None, None, None, None) == 1

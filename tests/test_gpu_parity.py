@@ -1,0 +1,244 @@
+"""GPU parity: the sm_103a step through the C ABI against the golden
+fixtures (written from the reference itself) and the live oracle.
+
+The bar is bit-exact: cell keys, sort order and neighbour counts at step 1
+(integer work) and, because the kernels follow the reference's float
+operations in the reference's order, positions, velocities, rho and lambda
+too. The stated floating-point tolerance (max |dx| <= 1e-5 h after one step)
+is checked as well, so a failure report shows both."""
+
+import numpy as np
+import pytest
+
+from conftest import golden_files, golden_scene, load_golden
+from fluidsimulator_gb300 import _capi, scenes
+from fluidsimulator_gb300.solver import FluidError, Solver, cuda_step
+
+pytestmark = pytest.mark.gpu
+
+STEP1_INT = ("cell_keys", "sorted_order", "neighbor_counts")
+DEBUG = {"cell_keys": _capi.DEBUG_CELL_KEYS, "sorted_order": _capi.DEBUG_SORTED_ORDER,
+         "neighbor_counts": _capi.DEBUG_NEIGHBOR_COUNTS, "rho": _capi.DEBUG_RHO, "lambda": _capi.DEBUG_LAMBDA}
+
+
+def run_gpu(sc, steps, graphs=True, profiling=False, records=False):
+    s = Solver(0)
+    s.configure([sc.params], [sc.count])
+    s.set_graphs(graphs)
+    s.set_profiling(profiling)
+    s.upload(sc.pos, sc.vel)
+    s.step(steps)
+    pos, vel = s.download()
+    out = {"pos": pos, "vel": vel, "time": s.time(), "stats": s.stats()}
+    if records:
+        for k, w in DEBUG.items():
+            out[k] = s.read_debug(w)
+    s.close()
+    return out
+
+
+def test_device_present(cuda_lib):
+    from fluidsimulator_gb300.solver import device_available
+
+    ok, n, err = device_available()
+    assert ok and n >= 1, err
+
+
+@pytest.mark.parametrize("name", golden_files())
+def test_step1_matches_golden(cuda_lib, name):
+    p, d = load_golden(name)
+    sc = golden_scene(name)
+    r = run_gpu(sc, 1, records=True)
+    for k in STEP1_INT:
+        np.testing.assert_array_equal(r[k], d[f"s1_{k}"], err_msg=k)
+    h = np.float32(p.h)
+    assert np.max(np.abs(r["pos"] - d["s1_pos"])) <= 1e-5 * h
+    for k in ("pos", "vel", "rho", "lambda"):
+        np.testing.assert_array_equal(r[k], d[f"s1_{k}"], err_msg=k)
+    assert np.float32(r["time"]) == d["s1_time"]
+
+
+@pytest.mark.parametrize("name", golden_files())
+def test_trajectory_matches_golden(cuda_lib, name):
+    p, d = load_golden(name)
+    sc = golden_scene(name)
+    snaps = sorted(int(k[1:].split("_")[0]) for k in d if k.startswith("s") and k.endswith("_pos") and k != "s1_pos")
+    for s in snaps:
+        r = run_gpu(sc, s)
+        np.testing.assert_array_equal(r["pos"], d[f"s{s}_pos"], err_msg=f"pos after {s} steps")
+        np.testing.assert_array_equal(r["vel"], d[f"s{s}_vel"], err_msg=f"vel after {s} steps")
+        assert np.float32(r["time"]) == d[f"s{s}_time"]
+
+
+def test_neighbor_statistics_match_golden(cuda_lib):
+    # Per-step neighbour pairs / max and density statistics over the whole
+    # 240-step plain dam break (SURVEY config 1) and 60 collapsing steps with
+    # all flags on.
+    for name in ("dam_break_4096.npz", "dam_break_flags_4096.npz"):
+        p, d = load_golden(name)
+        sc = golden_scene(name)
+        n = len(d["stats_neighbor_pairs"])
+        s = Solver(0)
+        s.configure([p], [sc.count])
+        s.upload(sc.pos, sc.vel)
+        pairs, mx, dmean, dmax = [], [], [], []
+        for _ in range(n):
+            s.step(1)
+            st = s.stats()
+            pairs.append(st["neighbor_pairs"])
+            mx.append(st["neighbor_max"])
+            rho = s.read_debug(_capi.DEBUG_RHO).astype(np.float64)
+            e = rho / np.float64(p.density) - 1.0
+            dmean.append(e.mean())
+            dmax.append(e.max())
+        s.close()
+        np.testing.assert_array_equal(pairs, d["stats_neighbor_pairs"])
+        np.testing.assert_array_equal(mx, d["stats_neighbor_max"])
+        # Same floats summed in a different order (numpy) -> tiny differences.
+        np.testing.assert_allclose(dmean, d["stats_density_mean"], rtol=1e-9, atol=1e-12)
+        np.testing.assert_array_equal(dmax, d["stats_density_max"])
+
+
+def test_graphs_eager_and_profiling_agree(cuda_lib):
+    sc = scenes.dam_break(12, seed=4, flags=True)
+    a = run_gpu(sc, 15, graphs=True)
+    b = run_gpu(sc, 15, graphs=False)
+    c = run_gpu(sc, 15, graphs=True, profiling=True)
+    for k in ("pos", "vel"):
+        np.testing.assert_array_equal(a[k], b[k])
+        np.testing.assert_array_equal(a[k], c[k])
+
+
+def test_batched_scenes_match_each_fixture(cuda_lib):
+    names = [n for n in golden_files() if n.startswith("batch")]
+    fixtures = [load_golden(n) for n in names]
+    scs = [golden_scene(n) for n in names]
+    s = Solver(0)
+    s.configure([f[0] for f in fixtures], [sc.count for sc in scs])
+    s.upload(np.concatenate([sc.pos for sc in scs], axis=1), np.concatenate([sc.vel for sc in scs], axis=1))
+    s.step(1)
+    order = s.read_debug(_capi.DEBUG_SORTED_ORDER)
+    counts = s.read_debug(_capi.DEBUG_NEIGHBOR_COUNTS)
+    off = 0
+    for (p, d), sc in zip(fixtures, scs):
+        np.testing.assert_array_equal(order[off:off + sc.count], d["s1_sorted_order"])
+        np.testing.assert_array_equal(counts[off:off + sc.count], d["s1_neighbor_counts"])
+        off += sc.count
+    s.step(9)
+    pos, vel = s.download()
+    off = 0
+    for k, ((p, d), sc) in enumerate(zip(fixtures, scs)):
+        np.testing.assert_array_equal(pos[:, off:off + sc.count], d["s10_pos"])
+        np.testing.assert_array_equal(vel[:, off:off + sc.count], d["s10_vel"])
+        assert np.float32(s.time(k)) == d["s10_time"]
+        off += sc.count
+    s.close()
+
+
+@pytest.mark.parametrize("builder,steps", [
+    (lambda: scenes.double_dam_break(24, seed=7), 12),
+    (lambda: scenes.falling_block(28, seed=7), 12),
+    (lambda: scenes.differentiable_block(20, seed=7), 20),
+])
+def test_matches_live_oracle(cuda_lib, oracle_lib, builder, steps):
+    sc = builder()
+    a = oracle_lib.Oracle().run(sc.params, sc.pos, sc.vel, 0.0, steps, dump=True)
+    b = run_gpu(sc, steps, records=True)
+    for k in ("pos", "vel", "neighbor_counts", "rho", "lambda", "cell_keys", "sorted_order"):
+        np.testing.assert_array_equal(b[k], a[k], err_msg=k)
+
+
+def test_full_size_first_step_1m(cuda_lib, oracle_lib):
+    """1,000,000 particles (the throughput scene) at full size: step-1 keys,
+    order, counts, positions and velocities equal the oracle's."""
+    sc = scenes.falling_block(100, seed=0)
+    a = oracle_lib.Oracle().run(sc.params, sc.pos, sc.vel, 0.0, 1, dump=True)
+    b = run_gpu(sc, 1, records=True)
+    for k in ("cell_keys", "sorted_order", "neighbor_counts", "pos", "vel", "rho", "lambda"):
+        np.testing.assert_array_equal(b[k], a[k], err_msg=k)
+    hist_a = np.bincount(a["neighbor_counts"])
+    hist_b = np.bincount(b["neighbor_counts"])
+    np.testing.assert_array_equal(hist_a, hist_b)
+
+
+def test_stateless_cuda_step_matches_golden(cuda_lib):
+    p, d = load_golden("dam_break_4096.npz")
+    sc = golden_scene("dam_break_4096.npz")
+    pos, vel = sc.pos.copy(), sc.vel.copy()
+    t = cuda_step(p, pos, vel, 0.0)
+    np.testing.assert_array_equal(pos, d["s1_pos"])
+    np.testing.assert_array_equal(vel, d["s1_vel"])
+    assert np.float32(t) == d["s1_time"]
+    # second call reuses the cached device buffers
+    for _ in range(9):
+        t = cuda_step(p, pos, vel, t)
+    np.testing.assert_array_equal(pos, d["s10_pos"])
+
+
+def test_capacity_regrow_keeps_results(cuda_lib, oracle_lib):
+    # The flags scene collapses from ~25 to ~500 neighbours: the lists grow
+    # several times and every re-run step must still match the oracle.
+    sc = scenes.dam_break(12, seed=9, flags=True)
+    a = oracle_lib.Oracle().run(sc.params, sc.pos, sc.vel, 0.0, 50)
+    b = run_gpu(sc, 50)
+    assert b["stats"]["regrows"] >= 1
+    np.testing.assert_array_equal(b["pos"], a["pos"])
+    np.testing.assert_array_equal(b["vel"], a["vel"])
+
+
+def test_nonfinite_input_reports_error_and_keeps_state(cuda_lib):
+    sc = scenes.dam_break(6, seed=1)
+    pos = sc.pos.copy()
+    pos[1, 17] = np.nan
+    s = Solver(0)
+    s.configure([sc.params], [sc.count])
+    s.upload(pos, sc.vel)
+    with pytest.raises(FluidError) as e:
+        s.step(1)
+    assert e.value.status == 5  # FLUID_ERR_NONFINITE
+    p2, v2 = s.download()
+    np.testing.assert_array_equal(p2, pos)
+    # the solver stays usable
+    s.upload(sc.pos, sc.vel)
+    s.step(2)
+    s.close()
+
+
+def test_invalid_parameters_rejected(cuda_lib):
+    s = Solver(0)
+    p = scenes.dam_break(4).params
+    bad = p.copy()
+    bad.h = 0.0
+    with pytest.raises(FluidError) as e:
+        s.configure([bad], [64])
+    assert e.value.status == 1
+    bad = p.copy()
+    bad.use_uniform_grid = 0
+    with pytest.raises(FluidError) as e:
+        s.configure([bad], [64])
+    assert e.value.status == 8
+    with pytest.raises(FluidError):
+        s.step(1)  # nothing configured / uploaded
+    s.close()
+
+
+def test_empty_and_tiny_scenes(cuda_lib, oracle_lib):
+    p = scenes.dam_break(2).params
+    s = Solver(0)
+    s.configure([p], [0])
+    s.upload(np.zeros((3, 0), np.float32), np.zeros((3, 0), np.float32))
+    s.step(3)
+    assert s.time() > 0
+    s.close()
+    for n in (1, 2, 31, 33):
+        sc = scenes.dam_break(4, seed=n)
+        pos, vel = sc.pos[:, :n].copy(), sc.vel[:, :n].copy()
+        s = Solver(0)
+        s.configure([sc.params], [n])
+        s.upload(pos, vel)
+        s.step(5)
+        got = s.download()
+        s.close()
+        ref = oracle_lib.Oracle().run(sc.params, pos, vel, 0.0, 5)
+        np.testing.assert_array_equal(got[0], ref["pos"])
+        np.testing.assert_array_equal(got[1], ref["vel"])

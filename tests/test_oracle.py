@@ -1,0 +1,146 @@
+"""The oracle (CPU restatement of core/src/core.cpp:119-615) against the
+golden fixtures written from the reference itself, and, where the reference
+tree exists, against the reference compiled from source."""
+
+import hashlib
+
+import numpy as np
+import pytest
+
+from conftest import golden_files, golden_scene, load_golden
+from fluidsimulator_gb300 import scenes
+from fluidsimulator_gb300._capi import default_params
+
+STEP1 = ("pos", "vel", "cell_keys", "sorted_order", "neighbor_counts", "rho", "lambda")
+
+
+def _sha(pos, vel):
+    h = hashlib.sha256()
+    h.update(np.ascontiguousarray(pos, np.float32).tobytes())
+    h.update(np.ascontiguousarray(vel, np.float32).tobytes())
+    return h.hexdigest()
+
+
+@pytest.mark.parametrize("name", golden_files())
+def test_scene_builder_reproduces_fixture_state(name):
+    sc = golden_scene(name)
+    _, d = load_golden(name)
+    assert _sha(sc.pos, sc.vel) == str(d["init_sha256"])
+    assert bytes(sc.params) == d["params"].tobytes()
+
+
+@pytest.mark.parametrize("name", golden_files())
+def test_oracle_matches_golden(oracle_lib, name):
+    p, d = load_golden(name)
+    sc = golden_scene(name)
+    r = oracle_lib.Oracle().run(p, sc.pos, sc.vel, 0.0, 1, dump=True)
+    for k in STEP1:
+        np.testing.assert_array_equal(r[k], d[f"s1_{k}"], err_msg=k)
+    assert np.float32(r["time"]) == d["s1_time"]
+    snaps = sorted(int(k[1:].split("_")[0]) for k in d if k.startswith("s") and k.endswith("_pos") and k != "s1_pos")
+    for s in snaps:
+        r = oracle_lib.Oracle().run(p, sc.pos, sc.vel, 0.0, s)
+        np.testing.assert_array_equal(r["pos"], d[f"s{s}_pos"], err_msg=f"pos after {s}")
+        np.testing.assert_array_equal(r["vel"], d[f"s{s}_vel"], err_msg=f"vel after {s}")
+    if "stats_neighbor_pairs" in d:
+        n = len(d["stats_neighbor_pairs"])
+        r = oracle_lib.Oracle().run(p, sc.pos, sc.vel, 0.0, n, records=True)
+        np.testing.assert_array_equal(r["neighbor_pairs"], d["stats_neighbor_pairs"])
+        np.testing.assert_array_equal(r["neighbor_max"], d["stats_neighbor_max"])
+        np.testing.assert_array_equal(r["density_mean"], d["stats_density_mean"])
+        np.testing.assert_array_equal(r["density_max"], d["stats_density_max"])
+
+
+def test_oracle_thread_count_invariant(oracle_lib):
+    sc = scenes.dam_break(10, seed=5, flags=True)
+    outs = []
+    for t in (1, 3):
+        oracle_lib.set_threads(t)
+        outs.append(oracle_lib.Oracle().run(sc.params, sc.pos, sc.vel, 0.0, 8))
+    oracle_lib.set_threads(0)
+    np.testing.assert_array_equal(outs[0]["pos"], outs[1]["pos"])
+    np.testing.assert_array_equal(outs[0]["vel"], outs[1]["vel"])
+
+
+def test_oracle_fp64_tracks_fp32_first_step(oracle_lib):
+    sc = scenes.dam_break(12, seed=2, flags=True)
+    a = oracle_lib.Oracle(np.float32).run(sc.params, sc.pos, sc.vel, 0.0, 1, dump=True)
+    b = oracle_lib.Oracle(np.float64).run(sc.params, sc.pos.astype(np.float64), sc.vel.astype(np.float64), 0.0, 1,
+                                          dump=True)
+    np.testing.assert_array_equal(a["neighbor_counts"], b["neighbor_counts"])
+    # The reference's FP32 step sits ~1e-3 h from FP64 after one step (four
+    # Jacobi iterations amplify rounding by 1/m); the 1e-5 h parity bar is
+    # FP32 GPU against FP32 CPU, which the GPU tests check bit for bit.
+    assert np.max(np.abs(a["pos"] - b["pos"])) < 5e-3 * sc.params.h
+
+
+def _variants():
+    """Parameter corners the reference's step branches on."""
+    out = []
+    base = scenes.dam_break(8, seed=11, flags=True)
+    out.append(("all_flags", base))
+    for n in (2, 3, 5):
+        v = base.copy()
+        v.params.scorr_n = n
+        out.append((f"scorr_n{n}", v))
+    v = base.copy()
+    v.params.plane_restitution = 0.0
+    out.append(("friction_only", v))
+    v = base.copy()
+    v.params.plane_friction = 0.0
+    out.append(("restitution_only", v))
+    v = base.copy()
+    v.params.plane_count = 0
+    out.append(("no_planes", v))
+    v = base.copy()
+    v.params.scorr_dq_coeff = 0.0
+    out.append(("dq_fallback", v))
+    v = base.copy()
+    v.params.solver_iterations = 1
+    out.append(("one_iteration", v))
+    v = base.copy()
+    v.params.use_uniform_grid = 0
+    out.append(("all_pairs", v))
+    return out
+
+
+@pytest.mark.parametrize("name,sc", _variants(), ids=[n for n, _ in _variants()])
+def test_oracle_matches_reference_live(oracle_lib, name, sc):
+    if not oracle_lib.ref_available():
+        pytest.skip("reference tree not present")
+    a = oracle_lib.Oracle().run(sc.params, sc.pos, sc.vel, 0.0, 12, dump=True, records=True)
+    b = oracle_lib.Reference().run(sc.params, sc.pos, sc.vel, 0.0, 12, dump=True, records=True)
+    for k in ("pos", "vel", "neighbor_counts", "rho", "lambda", "neighbor_pairs"):
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+    if sc.params.use_uniform_grid:
+        np.testing.assert_array_equal(a["cell_keys"], b["cell_keys"])
+        np.testing.assert_array_equal(a["sorted_order"], b["sorted_order"])
+
+
+def test_empty_state_advances_time(oracle_lib):
+    p = scenes.dam_break(2).params
+    r = oracle_lib.Oracle().run(p, np.zeros((3, 0), np.float32), np.zeros((3, 0), np.float32), 0.5, 3)
+    t = np.float32(0.5)
+    for _ in range(3):
+        t = np.float32(t + np.float32(p.dt))
+    assert np.float32(r["time"]) == t
+
+
+def test_scene_builders_match_reference(oracle_lib):
+    if not oracle_lib.ref_available():
+        pytest.skip("reference tree not present")
+    p = default_params()
+    for dims, origin, sp in [((16, 16, 16), (0.05, 0.05, 0.05), 0.05), ((7, 3, 5), (3.0, 1.0, 1.0), 0.02),
+                             ((50, 2, 3), (0.025, 0.025, 0.6125), 0.025)]:
+        np.testing.assert_array_equal(scenes.init_block(*dims, origin, sp), oracle_lib.ref_init_block(p, *dims, origin, sp))
+    for box in [(1.0, 1.0, 1.0), (8.0, 4.0, 4.0), (2.0, 1.0, 1.0)]:
+        q = default_params()
+        scenes.init_planes(q, *box)
+        r = oracle_lib.ref_init_planes(default_params(), *box)
+        assert q.planes() == r.planes()
+
+
+def test_default_params_match_reference(oracle_lib):
+    if not oracle_lib.ref_available():
+        pytest.skip("reference tree not present")
+    assert bytes(default_params()) == bytes(oracle_lib.ref_default_params())
