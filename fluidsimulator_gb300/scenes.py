@@ -67,6 +67,10 @@ class Scene:
     steps: int = 1
     info: dict = field(default_factory=dict)
 
+    def __post_init__(self):
+        self.pos = np.ascontiguousarray(self.pos, dtype=np.float32)
+        self.vel = np.ascontiguousarray(self.vel, dtype=np.float32)
+
     @property
     def count(self) -> int:
         return int(self.pos.shape[1])
