@@ -1,0 +1,446 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 PBF timestep (particle-steps/s on the 1M scene).
+
+Workload: the 1,000,000-particle falling block (100^3 lattice, spacing 0.02,
+h = 0.04, 8x4x4 box, s_corr + XSPH + vorticity, 4 Jacobi iterations),
+synthetic and seeded. One timed step = one full PBF timestep over that
+scene's initial batch: before every step the initial state is restored
+device-to-device (outside the timed region), so every step does the same
+work (the lattice phase, ~28 neighbours per particle). The reference's own
+run of this scene collapses to ~10^4 neighbours per particle within ~30
+steps; `trajectory` reports that regime separately.
+
+  value   particle-steps/s, inputs resident in HBM, L2 flushed between steps,
+          per-step CUDA events on the solver's stream, max over ranks.
+  e2e     the same metric through the reference-facing call
+          fluid_gb300_cuda_step (host SoA arrays in pinned memory copied in,
+          stepped, copied out every step), host wall clock.
+  roofline / pair_roofline  the dominant kernel against HBM bandwidth and
+          against the FP32 issue rate, from per-launch CUDA events.
+  cpu_baseline  the oracle (a CPU restatement of the reference step) on the
+          host cores on a bounded sample, rank 0 at N = 1.
+
+`--impl reference` times the reference's CPU step (the oracle restatement;
+the reference binary is not buildable on the GPU host) on the host cores.
+Multi-GPU (torchrun): independent replicas, one per rank, no collective on
+the data path; scaling "weak".
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+N_SIDE = 100
+METRIC = "particle-steps/s @1M"
+UNIT = "particle-steps/s"
+
+# Algorithmic bytes per particle per launch (compulsory per-particle array
+# traffic; vec3 = 12 B, scalar / index = 4 B; neighbour gathers on chip).
+ALGO_BYTES_PER_PARTICLE = {
+    "k_bounds": 24,        # R x 12, v 12
+    "k_keys": 28,          # R x 12, v 12; W key 4
+    "k_reorder": 76,       # R key 4, index 4, slot 4, x 12, v 12; W x 12, v 12, p* 12, slot 4
+    "k_nbr_count": 16,     # R p* 12; W count 4 (lists excluded)
+    "k_nbr_fill": 24,      # R p* 12; W count 4, lambda 4, rho 4 (lists excluded)
+    "k_lambda": 20,        # R p* 12; W lambda 4, rho 4
+    "k_delta": 28,         # R p* 12, lambda 4; W p* 12
+    "k_xsph": 40,          # R x 12, v 12, rho 4; W v 12
+    "k_omega": 40,         # R x 12, v 12; W omega + |omega| 16
+    "k_eta": 52,           # R x 12, omega 16, v 12; W v 12
+}
+# Per step, all three flags and 4 iterations (predict 44, sort 16, reorder 56,
+# 4 x (lambda 16 + delta 28) + rho 4, commit + XSPH 52, omega 40, eta 52,
+# permutation 12).
+ALGO_BYTES_PER_STEP = 452
+# FP32 operations per neighbour pair in k_delta (s_corr on): difference 3,
+# r^2 5, sqrt 1, spiky factor 3, lambda sum 1, s_corr 9, accumulate 7.
+DELTA_OPS_PER_PAIR = 29
+FP32_LANES_PER_SM = 128
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def profile_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summaries."""
+    import glob
+    import re
+
+    for path in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
+        with open(path) as f:
+            for line in f:
+                m = re.match(r"^traffic_bytes_per_launch\s+(\S+)\s+(\d+)", line)
+                if m and m.group(1) == kernel:
+                    return int(m.group(2))
+    return None
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured", d
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback", {}
+
+
+# --------------------------------------------------------------------------
+# distributed helpers (replicas only)
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def reduce_max(value: float, world: int, device=None) -> float:
+    """Max over ranks (no-op at world size 1)."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+# --------------------------------------------------------------------------
+# clocks
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------
+# our arm
+
+def run_ours(args, world, rank, local):
+    import numpy as np
+    import torch
+
+    from fluidsimulator_gb300 import _capi, scenes
+    from fluidsimulator_gb300 import build as lib_build
+    from fluidsimulator_gb300.solver import Solver, cuda_step
+
+    lib_build.build()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+    stream = torch.cuda.Stream(dev)  # a real stream: the legacy NULL stream would not order with the solver
+    torch.cuda.set_stream(stream)
+
+    sc = scenes.falling_block(N_SIDE, seed=0)
+    n = sc.count
+    pos0 = torch.from_numpy(sc.pos).to(dev)
+    vel0 = torch.from_numpy(sc.vel).to(dev)
+    l2_flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > 129 MB L2
+    torch.cuda.synchronize(dev)
+
+    solver = Solver(local)
+    solver.configure([sc.params], [n])
+    solver.set_stream(stream.cuda_stream)
+    solver.set_graphs(True)
+
+    def restore():
+        solver.upload(pos0, vel0)
+
+    # warm-up (also sizes the neighbour lists and captures the graphs)
+    for _ in range(args.warmup):
+        restore()
+        solver.step(1)
+    solver.set_profiling(True)
+    solver.kernel_times(reset=True)
+    launches0 = solver.stats()["kernel_launches"]
+
+    barrier(world)
+    torch.cuda.synchronize(dev)
+    clocks = ClockSampler(local)
+    clocks.start()
+    step_ms = []
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    for _ in range(args.steps):
+        restore()
+        l2_flush.zero_()
+        ev0.record(stream)
+        solver.step_async(1)
+        ev1.record(stream)
+        solver.synchronize()
+        step_ms.append(ev0.elapsed_time(ev1))
+    torch.cuda.synchronize(dev)
+    barrier(world)
+    clk = clocks.stop()
+    stats = solver.stats()
+    stage = solver.kernel_times(reset=True)
+    launches = stats["kernel_launches"] - launches0
+    total_ms = reduce_max(sum(step_ms), world, dev)
+    value = world * n * args.steps / (total_ms / 1e3)
+
+    # dominant kernel and its rooflines
+    peak_gbs, peak_kind, peaks = measured_peaks()
+    dom = max(stage, key=lambda k: stage[k][0])
+    dom_ms, dom_launches = stage[dom]
+    avg_ms = dom_ms / max(dom_launches, 1)
+    roofline = None
+    if dom in ALGO_BYTES_PER_PARTICLE and dom_launches:
+        bytes_per_launch = ALGO_BYTES_PER_PARTICLE[dom] * n
+        achieved = bytes_per_launch / (avg_ms / 1e3) / 1e9
+        roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2), "peak": peak_gbs,
+                    "unit": "GB/s", "frac": round(achieved / peak_gbs, 5),
+                    "traffic": args.traffic if args.traffic is not None else profile_traffic(dom),
+                    "bytes_per_launch": bytes_per_launch, "avg_launch_ms": round(avg_ms, 4),
+                    "launches": dom_launches, "share": round(dom_ms / max(sum(v[0] for v in stage.values()), 1e-9), 3),
+                    "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)" if peak_kind == "measured" else "fallback"}
+    pair_roofline = None
+    sm_mhz = clk["sm_mhz"] if clk else None
+    if stage["k_delta"][1]:
+        pairs = stats["neighbor_pairs"]
+        d_ms = stage["k_delta"][0] / stage["k_delta"][1]
+        props = torch.cuda.get_device_properties(dev)
+        max_mhz = (clk or {}).get("sm_max_mhz") or float(peaks.get("sm_max_mhz", 2070.0))
+        peak_ops = props.multi_processor_count * FP32_LANES_PER_SM * max_mhz * 1e6
+        ops = pairs * DELTA_OPS_PER_PAIR / (d_ms / 1e3)
+        pair_roofline = {"bound": "fp32_issue", "kernel": "k_delta", "pairs_per_launch": pairs,
+                         "ops_per_pair": DELTA_OPS_PER_PAIR, "achieved": round(ops / 1e12, 3),
+                         "peak": round(peak_ops / 1e12, 2), "unit": "TFLOP/s (non-FMA FP32)",
+                         "frac": round(ops / peak_ops, 4), "avg_launch_ms": round(d_ms, 4)}
+    step_frac = ALGO_BYTES_PER_STEP * n / (statistics.mean(step_ms) / 1e3) / 1e9 / peak_gbs
+
+    # e2e through the reference-facing call, host arrays in pinned memory
+    e2e = None
+    if not args.no_e2e:
+        hp = torch.empty((3, n), dtype=torch.float32, pin_memory=True)
+        hv = torch.empty((3, n), dtype=torch.float32, pin_memory=True)
+        hpn, hvn = hp.numpy(), hv.numpy()
+        torch.cuda.set_device(local)
+        for _ in range(args.warmup):
+            np.copyto(hpn, sc.pos)
+            np.copyto(hvn, sc.vel)
+            cuda_step(sc.params, hpn, hvn, 0.0)
+        e2e_s = []
+        for _ in range(args.steps):
+            np.copyto(hpn, sc.pos)
+            np.copyto(hvn, sc.vel)
+            l2_flush.zero_()
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            cuda_step(sc.params, hpn, hvn, 0.0)
+            e2e_s.append(time.perf_counter() - t0)
+        e2e_total = reduce_max(sum(e2e_s), world, dev)
+        e2e = {"value": round(world * n * args.steps / e2e_total, 1), "unit": UNIT,
+               "h2d_bytes_per_step": 24 * n, "d2h_bytes_per_step": 24 * n,
+               "ms_per_step": round(1e3 * e2e_total / args.steps, 4),
+               "call": "fluid_gb300_cuda_step (fluid::cuda_step semantics)"}
+
+    # the real trajectory: lattice phase and collapse
+    traj = None
+    if args.trajectory > 0:
+        restore()
+        solver.kernel_times(reset=True)
+        t_ms, t_pairs = [], []
+        for _ in range(args.trajectory):
+            ev0.record(stream)
+            solver.step(1)
+            ev1.record(stream)
+            ev1.synchronize()
+            t_ms.append(ev0.elapsed_time(ev1))
+            t_pairs.append(solver.stats()["neighbor_pairs"])
+        st = solver.stats()
+        traj = {"steps": args.trajectory, "ms_per_step_first5": round(statistics.mean(t_ms[:5]), 3),
+                "ms_per_step_last5": round(statistics.mean(t_ms[-5:]), 3),
+                "neighbors_per_particle_step1": round(t_pairs[0] / n, 2),
+                "neighbors_per_particle_last": round(t_pairs[-1] / n, 2), "neighbor_max_last": st["neighbor_max"],
+                "particle_steps_per_s": round(n * len(t_ms) / (sum(t_ms) / 1e3), 1),
+                "regrows": st["regrows"]}
+        tail = solver.kernel_times(reset=True)
+        traj["kernel_ms_total"] = {k: round(v[0], 2) for k, v in tail.items() if v[1]}
+    solver.close()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(sc, budget_s=args.cpu_budget)
+
+    out = {
+        "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "falling_block_1M: 100^3 lattice, sp 0.02, h 0.04, 8x4x4 box, s_corr+XSPH+vorticity, "
+                               "4 iterations, one step over the initial batch per timed step",
+                   "particles": n, "neighbors_per_particle": round(stats["neighbor_pairs"] / n, 2),
+                   "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{world}",
+                   "graphs": True, "exact_fp32": True},
+        "roofline": roofline, "pair_roofline": pair_roofline,
+        "step_roofline": {"bytes_per_particle_step": ALGO_BYTES_PER_STEP, "frac": round(step_frac, 5)},
+        "kernel_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in stage.items() if v[1]},
+        "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches, "trajectory": traj,
+    }
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+# --------------------------------------------------------------------------
+# CPU: oracle restatement of the reference step
+
+def _cpu_sample(sc, particles):
+    """The first `particles` particles of the lattice (whole z-layers)."""
+    from fluidsimulator_gb300 import scenes
+
+    layer = N_SIDE * N_SIDE
+    k = max(1, min(N_SIDE, particles // layer)) * layer
+    return scenes.Scene(sc.name, sc.params, sc.pos[:, :k].copy(), sc.vel[:, :k].copy())
+
+
+def cpu_baseline(sc, budget_s=20.0, steps=None):
+    from oracle import pyoracle
+
+    pyoracle.build(ref=False)
+    threads = os.cpu_count() or 1
+    pyoracle.set_threads(threads)
+    probe = _cpu_sample(sc, 100_000)
+    t0 = time.perf_counter()
+    pyoracle.Oracle().run(probe.params, probe.pos, probe.vel, 0.0, 1)
+    per_particle = (time.perf_counter() - t0) / probe.count
+    reps = steps or 2
+    particles = int(min(sc.count, budget_s / reps / max(per_particle, 1e-12)))
+    sample = _cpu_sample(sc, particles)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        pyoracle.Oracle().run(sample.params, sample.pos, sample.vel, 0.0, 1)
+    dt = time.perf_counter() - t0
+    return {"value": round(sample.count * reps / dt, 1), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{reps} x step 1 of the first {sample.count} particles (whole z-layers) of the 1M scene, "
+                      f"oracle/pbf_oracle.cpp (restatement of core/src/core.cpp:119-615), OpenMP {threads} threads, "
+                      f"{os.uname().machine}"}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    from fluidsimulator_gb300 import scenes
+    from oracle import pyoracle
+
+    pyoracle.build(ref=False)
+    threads = os.cpu_count() or 1
+    pyoracle.set_threads(threads)
+    sc = scenes.falling_block(N_SIDE, seed=0)
+    probe = _cpu_sample(sc, 100_000)
+    t0 = time.perf_counter()
+    pyoracle.Oracle().run(probe.params, probe.pos, probe.vel, 0.0, 1)
+    per_particle = (time.perf_counter() - t0) / probe.count
+    budget = args.cpu_budget * 6  # whole run within a few minutes
+    particles = int(min(sc.count, budget / max(args.steps + args.warmup, 1) / max(per_particle, 1e-12)))
+    sample = _cpu_sample(sc, particles)
+    for _ in range(args.warmup):
+        pyoracle.Oracle().run(sample.params, sample.pos, sample.vel, 0.0, 1)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        pyoracle.Oracle().run(sample.params, sample.pos, sample.vel, 0.0, 1)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = sample.count * args.steps / total
+    desc = (f"each step: one PBF step (step 1) of the first {sample.count} particles (whole z-layers) of the 1M "
+            f"scene on the host CPU, oracle/pbf_oracle.cpp (CPU restatement of core/src/core.cpp:119-615; the "
+            f"reference binary itself builds only where its source tree is), OpenMP {threads} threads, "
+            f"{os.uname().machine}")
+    out = {"metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 3), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+           "config": {"workload": "falling_block_1M (CPU sample)", "particles": sample.count},
+           "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": threads, "kind": "port", "sample": desc},
+           "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--trajectory", type=int, default=24, help="steps of the real run to report (0 = skip)")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU work for cpu_baseline")
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="DRAM bytes per launch of the dominant kernel from an ncu capture")
+    args = ap.parse_args(argv)
+    world, rank, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+    run_ours(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -892,54 +892,54 @@ cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t s
   const int nb = blocks_for(a.n, kBlock);
   m.start();
   k_bounds<<<nb, kBlock, 0, st>>>(a);
-  m.mark(FLUID_STAGE_PREDICT);
+  m.mark(FLUID_KERNEL_BOUNDS);
   k_grid_setup<<<1, kBlock, 0, st>>>(a);
-  m.mark(FLUID_STAGE_PREDICT);
+  m.mark(FLUID_KERNEL_GRID);
   k_keys<<<nb, kBlock, 0, st>>>(a);
-  m.mark(FLUID_STAGE_PREDICT);
+  m.mark(FLUID_KERNEL_KEYS);
   for (int pass = 0; pass < plan.radix_passes; ++pass) {
     k_radix_hist<<<a.tiles, kBlock, 0, st>>>(a, pass);
-    m.mark(FLUID_STAGE_SORT);
+    m.mark(FLUID_KERNEL_RADIX_HIST);
     k_radix_scan<<<256, kBlock, 0, st>>>(a, pass);
-    m.mark(FLUID_STAGE_SORT);
+    m.mark(FLUID_KERNEL_RADIX_SCAN);
     k_radix_scatter<<<a.tiles, kBlock, 0, st>>>(a, pass);
-    m.mark(FLUID_STAGE_SORT);
+    m.mark(FLUID_KERNEL_RADIX_SCATTER);
   }
   k_reorder<<<nb, kBlock, 0, st>>>(a);
-  m.mark(FLUID_STAGE_REORDER);
+  m.mark(FLUID_KERNEL_REORDER);
   k_nbr_count<<<nb, kBlock, 0, st>>>(a);
-  m.mark(FLUID_STAGE_NEIGHBORS);
+  m.mark(FLUID_KERNEL_NBR_COUNT);
   k_nbr_scan<<<1, 1024, 0, st>>>(a);
-  m.mark(FLUID_STAGE_NEIGHBORS);
+  m.mark(FLUID_KERNEL_NBR_SCAN);
   k_nbr_fill<<<nb, kBlock, 0, st>>>(a);
-  m.mark(FLUID_STAGE_NEIGHBORS);
+  m.mark(FLUID_KERNEL_NBR_FILL);
 
   const bool post = plan.xsph || plan.vorticity;
   const int to_v2 = plan.xsph ? 1 : 0;
   const int rest_commit = (!post && plan.restitution) ? 1 : 0;
   if (plan.iterations == 0) {
     k_commit<<<nb, kBlock, 0, st>>>(a, to_v2, rest_commit);
-    m.mark(FLUID_STAGE_DELTA);
+    m.mark(FLUID_KERNEL_COMMIT);
   }
   for (int it = 0; it < plan.iterations; ++it) {
     const int in = it & 1;
     if (it > 0) {
       k_lambda<<<nb, kBlock, 0, st>>>(a, in);
-      m.mark(FLUID_STAGE_LAMBDA);
+      m.mark(FLUID_KERNEL_LAMBDA);
     }
     const int last = (it == plan.iterations - 1) ? 1 : 0;
     k_delta<<<nb, kBlock, 0, st>>>(a, in, last, to_v2, last ? rest_commit : 0);
-    m.mark(FLUID_STAGE_DELTA);
+    m.mark(FLUID_KERNEL_DELTA);
   }
   if (plan.xsph) {
     k_xsph<<<nb, kBlock, 0, st>>>(a, (!plan.vorticity && plan.restitution) ? 1 : 0);
-    m.mark(FLUID_STAGE_XSPH);
+    m.mark(FLUID_KERNEL_XSPH);
   }
   if (plan.vorticity) {
     k_omega<<<nb, kBlock, 0, st>>>(a);
-    m.mark(FLUID_STAGE_VORTICITY);
+    m.mark(FLUID_KERNEL_OMEGA);
     k_eta<<<nb, kBlock, 0, st>>>(a, plan.restitution ? 1 : 0);
-    m.mark(FLUID_STAGE_VORTICITY);
+    m.mark(FLUID_KERNEL_ETA);
   }
   return cudaGetLastError();
 }

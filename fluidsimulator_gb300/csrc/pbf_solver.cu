@@ -341,10 +341,6 @@ class Solver {
     for (int k = 0; k < nsteps; ++k) {
       int rc = launch_one();
       if (rc) return rc;
-      if (profiling_) {
-        rc = synchronize();
-        if (rc) return rc;
-      }
     }
     return FLUID_OK;
   }
@@ -366,7 +362,10 @@ class Solver {
       const DevStatus st = *status_host_;
       const int done = st.err ? st.fail_step : pending_;
       const int remaining = pending_ - done;
-      if (profiling_ && done > 0) accumulate_profile((parity_ + done - 1) & 1);
+      // Each parity's events hold its latest step: the last two completed
+      // steps are timed (every step when the caller synchronises each step).
+      if (profiling_)
+        for (int k = std::max(0, done - 2); k < done; ++k) accumulate_profile((parity_ + k) & 1);
       commit_steps(done);
       pending_ = 0;
       last_pairs_ = static_cast<long long>(st.pairs);
@@ -414,8 +413,8 @@ class Solver {
     return FLUID_OK;
   }
 
-  int stage_times(double* ms, int64_t* launches, int stages, int reset) {
-    for (int k = 0; k < stages && k < FLUID_STAGE_COUNT; ++k) {
+  int kernel_times(double* ms, int64_t* launches, int kernels, int reset) {
+    for (int k = 0; k < kernels && k < FLUID_KERNEL_COUNT; ++k) {
       if (ms) ms[k] = stage_ms_[k];
       if (launches) launches[k] = stage_launches_[k];
     }
@@ -755,8 +754,8 @@ class Solver {
   std::vector<cudaEvent_t> events_[2];
   std::vector<int> stages_[2];
   int marks_used_[2] = {0, 0};
-  double stage_ms_[FLUID_STAGE_COUNT] = {};
-  long long stage_launches_[FLUID_STAGE_COUNT] = {};
+  double stage_ms_[FLUID_KERNEL_COUNT] = {};
+  long long stage_launches_[FLUID_KERNEL_COUNT] = {};
   std::string err_;
 };
 
@@ -903,9 +902,17 @@ int fluid_solver_set_profiling(fluid_solver* s, int32_t enable) {
   return s->impl.set_profiling(enable);
 }
 
-int fluid_solver_stage_times(fluid_solver* s, double* ms, int64_t* launches, int32_t stages, int32_t reset) {
+int fluid_solver_kernel_times(fluid_solver* s, double* ms, int64_t* launches, int32_t kernels, int32_t reset) {
   FLUID_CHECK_SOLVER(s);
-  return s->impl.stage_times(ms, launches, stages, reset);
+  return s->impl.kernel_times(ms, launches, kernels, reset);
+}
+
+const char* fluid_kernel_name(int kernel) {
+  static const char* const names[FLUID_KERNEL_COUNT] = {
+      "k_bounds", "k_grid_setup", "k_keys", "k_radix_hist", "k_radix_scan", "k_radix_scatter",
+      "k_reorder", "k_nbr_count", "k_nbr_scan", "k_nbr_fill", "k_lambda", "k_delta",
+      "k_commit", "k_xsph", "k_omega", "k_eta"};
+  return (kernel >= 0 && kernel < FLUID_KERNEL_COUNT) ? names[kernel] : nullptr;
 }
 
 int fluid_solver_get_time(fluid_solver* s, int32_t scene, float* time) {

@@ -139,12 +139,13 @@ class Solver:
         self._check(self.lib.fluid_solver_get_stats(self.h, byref(s)))
         return {k: getattr(s, k) for k, _ in FluidStats._fields_}
 
-    def stage_times(self, reset: bool = False) -> dict:
-        n = len(_capi.STAGE_NAMES)
+    def kernel_times(self, reset: bool = False) -> dict:
+        """{kernel name: (total ms, launches)} since the last reset."""
+        n = len(_capi.KERNEL_NAMES)
         ms = (c_double * n)()
         la = (c_int64 * n)()
-        self._check(self.lib.fluid_solver_stage_times(self.h, ms, la, n, int(reset)))
-        return {name: (ms[k], la[k]) for k, name in enumerate(_capi.STAGE_NAMES)}
+        self._check(self.lib.fluid_solver_kernel_times(self.h, ms, la, n, int(reset)))
+        return {name: (ms[k], la[k]) for k, name in enumerate(_capi.KERNEL_NAMES)}
 
     def read_debug(self, what: int) -> np.ndarray:
         if what == _capi.DEBUG_CELL_KEYS:

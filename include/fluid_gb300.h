@@ -162,25 +162,41 @@ int fluid_solver_synchronize(fluid_solver* solver);
 /* Capture each timestep as a CUDA graph (1) or launch kernels directly (0). */
 int fluid_solver_set_graphs(fluid_solver* solver, int32_t enable);
 
-/* Records CUDA events between stages of each step (adds no synchronisation). */
+/* Records a CUDA event after every kernel of each step (adds no
+ * synchronisation). Times accumulate at fluid_solver_synchronize for the
+ * last completed step of each parity, i.e. for every step when the caller
+ * synchronises after each step. */
 int fluid_solver_set_profiling(fluid_solver* solver, int32_t enable);
 
+/* Kernels of one step, in launch order (per-kernel timing buckets). */
 enum {
-  FLUID_STAGE_PREDICT = 0, /* bounds + cell keys */
-  FLUID_STAGE_SORT = 1,    /* radix sort */
-  FLUID_STAGE_REORDER = 2, /* gather into cell order + cell table */
-  FLUID_STAGE_NEIGHBORS = 3, /* neighbour count, slices, fill (+ first lambda) */
-  FLUID_STAGE_LAMBDA = 4,  /* density / lambda passes */
-  FLUID_STAGE_DELTA = 5,   /* position correction passes (+ commit) */
-  FLUID_STAGE_XSPH = 6,
-  FLUID_STAGE_VORTICITY = 7, /* omega, eta + apply + plane restitution */
-  FLUID_STAGE_COUNT = 8
+  FLUID_KERNEL_BOUNDS = 0,   /* predicted cells, per-scene bounding box */
+  FLUID_KERNEL_GRID = 1,     /* per-scene grid over the box */
+  FLUID_KERNEL_KEYS = 2,     /* linear cell keys */
+  FLUID_KERNEL_RADIX_HIST = 3,
+  FLUID_KERNEL_RADIX_SCAN = 4,
+  FLUID_KERNEL_RADIX_SCATTER = 5,
+  FLUID_KERNEL_REORDER = 6,  /* gather into cell order + cell table */
+  FLUID_KERNEL_NBR_COUNT = 7,
+  FLUID_KERNEL_NBR_SCAN = 8,
+  FLUID_KERNEL_NBR_FILL = 9, /* lists + first lambda */
+  FLUID_KERNEL_LAMBDA = 10,
+  FLUID_KERNEL_DELTA = 11,   /* position correction (+ commit on the last) */
+  FLUID_KERNEL_COMMIT = 12,  /* commit when solver_iterations == 0 */
+  FLUID_KERNEL_XSPH = 13,
+  FLUID_KERNEL_OMEGA = 14,
+  FLUID_KERNEL_ETA = 15,     /* eta + confinement + plane restitution */
+  FLUID_KERNEL_COUNT = 16
 };
 
-/* Sums of per-stage GPU time (ms) and launch counts since the last reset. */
-int fluid_solver_stage_times(fluid_solver* solver, double* ms_out,
-                             int64_t* launches_out, int32_t stages,
-                             int32_t reset);
+/* Name of a kernel id ("k_delta", ...); NULL when out of range. */
+const char* fluid_kernel_name(int kernel);
+
+/* Sums of per-kernel GPU time (ms) and launch counts since the last reset,
+ * indexed by FLUID_KERNEL_*. */
+int fluid_solver_kernel_times(fluid_solver* solver, double* ms_out,
+                              int64_t* launches_out, int32_t kernels,
+                              int32_t reset);
 
 /* Time of scene `scene` (float, accumulated as State::time, core.cpp:614). */
 int fluid_solver_get_time(fluid_solver* solver, int32_t scene, float* time);
