@@ -147,6 +147,9 @@ def _declare(lib):
     lib.fluid_gb300_device_available.restype = c_int
     lib.fluid_gb300_cuda_step.argtypes = [POINTER(FluidParams), c_int64, f, f, f, f, f, f, f]
     lib.fluid_gb300_cuda_step.restype = c_int
+    lib.fluid_gb300_step_noalloc.argtypes = [POINTER(FluidParams), c_int64, c_void_p, c_void_p, c_void_p, c_void_p,
+                                             c_void_p, c_void_p, POINTER(c_float), c_void_p]
+    lib.fluid_gb300_step_noalloc.restype = c_int
     lib.fluid_solver_create.argtypes = [POINTER(c_void_p), c_int]
     lib.fluid_solver_create.restype = c_int
     lib.fluid_solver_destroy.argtypes = [c_void_p]

@@ -981,3 +981,15 @@ int fluid_gb300_cuda_step(const fluid_params* params, int64_t count, float* px, 
 }
 
 }  // extern "C"
+
+namespace fgb {
+
+// Exported for the no-allocation entry point (pbf_noalloc.cu).
+SceneConst scene_const_for(const fluid_params& p, int first, int count) { return make_scene_const(p, first, count); }
+
+int params_status(const fluid_params& p) {
+  std::string why;
+  return validate_params(p, why);
+}
+
+}  // namespace fgb

@@ -104,6 +104,34 @@ int fluid_gb300_cuda_step(const fluid_params* params, int64_t count,
                           float* vel_x, float* vel_y, float* vel_z,
                           float* time);
 
+/*
+ * No counterpart in the reference: one timestep that allocates no device
+ * memory, for callers that cannot allocate where they step the fluid (an
+ * application that owns all device memory through its own pool or budget,
+ * a frame-time loop where an allocation would stall, a plugin that must not
+ * grow the process's footprint). The six arrays are the caller's DEVICE
+ * arrays of `count` particles in caller order, advanced in place; *time +=
+ * dt. Work is enqueued on `stream` (a cudaStream_t, NULL = legacy default)
+ * and the call returns when it is done.
+ *
+ * All scratch lives in one fixed device array inside this library (about
+ * 7.3 MiB, held on every GPU that loads the library until the process
+ * exits). Limits: count <= FLUID_NOALLOC_MAX_PARTICLES, at most
+ * FLUID_NOALLOC_MAX_NEIGHBOR_SLOTS neighbour-list entries (32-wide slices)
+ * and FLUID_NOALLOC_MAX_CELLS grid cells per step; beyond any of them the
+ * call returns FLUID_ERR_CAPACITY and leaves the arrays untouched. Every call
+ * shares that scratch, so calls whose work overlaps on the GPU race: do not
+ * run two at once. The first call on a device looks up the scratch address
+ * on that device; make that first call before any stream capture.
+ */
+#define FLUID_NOALLOC_MAX_PARTICLES 8192
+#define FLUID_NOALLOC_MAX_NEIGHBOR_SLOTS (1 << 20)
+#define FLUID_NOALLOC_MAX_CELLS (1 << 18)
+int fluid_gb300_step_noalloc(const fluid_params* params, int64_t count,
+                             float* pos_x, float* pos_y, float* pos_z,
+                             float* vel_x, float* vel_y, float* vel_z,
+                             float* time, void* stream);
+
 /* ---- Device-resident solver (no reference counterpart: the reference keeps
  * no device state between steps; this is the handle the drop-in above uses). */
 
