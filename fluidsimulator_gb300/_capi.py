@@ -15,7 +15,8 @@ from ctypes import POINTER, c_char_p, c_double, c_float, c_int, c_int32, c_int64
 MAX_PLANES = 32
 
 LIB_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib")
-LIB_PATH = os.path.join(LIB_DIR, "libfluid_gb300.so")
+# FLUID_GB300_LIB selects another build of the same library (e.g. a tuning variant).
+LIB_PATH = os.environ.get("FLUID_GB300_LIB") or os.path.join(LIB_DIR, "libfluid_gb300.so")
 
 FLUID_OK = 0
 STATUS_NAMES = {
@@ -41,7 +42,7 @@ DEBUG_RHO = 3
 DEBUG_LAMBDA = 4
 
 KERNEL_NAMES = ["k_bounds", "k_grid_setup", "k_keys", "k_radix_hist", "k_radix_scan", "k_radix_scatter",
-                "k_reorder", "k_nbr_count", "k_nbr_scan", "k_nbr_fill", "k_lambda", "k_delta", "k_commit",
+                "k_reorder", "k_nbr_count", "k_nbr_fill", "k_lambda", "k_delta", "k_commit",
                 "k_xsph", "k_omega", "k_eta"]
 
 

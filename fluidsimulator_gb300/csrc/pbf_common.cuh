@@ -13,7 +13,8 @@
 //   keys/vals     radix-sort ping-pong (u32 cell key, int caller index).
 //   table         int2 (first, end) per cell of the per-scene bounding grids.
 //   cnt, nbr      neighbour lists in 32-wide slices: warp w (slots 32w..32w+31)
-//                 owns 32*depth[w] ints from wbase[w], entry k of lane l at
+//                 owns 32*depth[w] ints from wbase[w] (claimed by one atomic
+//                 per block), entry k of lane l at
 //                 wbase[w] + 32k + l, so every list read is one coalesced
 //                 128-byte access per warp.
 #pragma once
@@ -76,6 +77,7 @@ struct DevStatus {
   unsigned long long need_grid;
   unsigned long long need_nbr;
   unsigned long long pairs;  // sum of neighbour counts, this step
+  unsigned long long cursor; // list entries claimed by the slices, this step
   int nbr_max;
   int pad;
 };

@@ -7,8 +7,8 @@
 //   k_radix_*       stable LSD radix sort of (key, caller index), 8-bit digits
 //   k_reorder       gather into cell order, predict again (bit-identical),
 //                   cell (first, end) table by warp-shuffle boundary detection
-//   k_nbr_count     27-cell scan: per-particle neighbour counts, slice depths
-//   k_nbr_scan      slice offsets; capacity check
+//   k_nbr_count     27-cell scan: per-particle neighbour counts, slice depths,
+//                   slice offsets (one atomic per block), capacity check
 //   k_nbr_fill      27-cell scan again: lists in scan order + first lambda
 //   k_lambda        density / lambda (iterations 2..n)
 //   k_delta         position correction, s_corr, plane projection (last
@@ -158,24 +158,20 @@ __global__ void __launch_bounds__(kBlock) k_bounds(StepArgs a) {
     const SceneConst& c = a.sc[scene];
     ok = cell_of(c, predict(c, x, v), cx, cy, cz);
   }
+  // Warp, then block reduction when the block is one scene; mixed blocks
+  // (scene boundaries) fall back to per-warp or per-lane atomics.
+  __shared__ int wmin[kBlock / 32][3], wmax[kBlock / 32][3], wscene[kBlock / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int s0 = __shfl_sync(kFull, scene, 0);
   const bool uniform = __all_sync(kFull, scene == s0 || scene < 0);
+  int mn[3] = {INT_MAX, INT_MAX, INT_MAX}, mx[3] = {INT_MIN, INT_MIN, INT_MIN};
   if (uniform) {
-    if (s0 < 0) return;
-    const int mnx = __reduce_min_sync(kFull, ok ? cx : INT_MAX);
-    const int mny = __reduce_min_sync(kFull, ok ? cy : INT_MAX);
-    const int mnz = __reduce_min_sync(kFull, ok ? cz : INT_MAX);
-    const int mxx = __reduce_max_sync(kFull, ok ? cx : INT_MIN);
-    const int mxy = __reduce_max_sync(kFull, ok ? cy : INT_MIN);
-    const int mxz = __reduce_max_sync(kFull, ok ? cz : INT_MIN);
-    if ((threadIdx.x & 31) == 0 && mnx != INT_MAX) {
-      atomicMin(&a.bmin[3 * s0 + 0], mnx);
-      atomicMin(&a.bmin[3 * s0 + 1], mny);
-      atomicMin(&a.bmin[3 * s0 + 2], mnz);
-      atomicMax(&a.bmax[3 * s0 + 0], mxx);
-      atomicMax(&a.bmax[3 * s0 + 1], mxy);
-      atomicMax(&a.bmax[3 * s0 + 2], mxz);
-    }
+    mn[0] = __reduce_min_sync(kFull, ok ? cx : INT_MAX);
+    mn[1] = __reduce_min_sync(kFull, ok ? cy : INT_MAX);
+    mn[2] = __reduce_min_sync(kFull, ok ? cz : INT_MAX);
+    mx[0] = __reduce_max_sync(kFull, ok ? cx : INT_MIN);
+    mx[1] = __reduce_max_sync(kFull, ok ? cy : INT_MIN);
+    mx[2] = __reduce_max_sync(kFull, ok ? cz : INT_MIN);
   } else if (ok) {
     atomicMin(&a.bmin[3 * scene + 0], cx);
     atomicMin(&a.bmin[3 * scene + 1], cy);
@@ -183,6 +179,43 @@ __global__ void __launch_bounds__(kBlock) k_bounds(StepArgs a) {
     atomicMax(&a.bmax[3 * scene + 0], cx);
     atomicMax(&a.bmax[3 * scene + 1], cy);
     atomicMax(&a.bmax[3 * scene + 2], cz);
+  }
+  if (lane == 0) {
+    wscene[warp] = (uniform && mn[0] != INT_MAX) ? s0 : -1;
+    for (int d = 0; d < 3; ++d) {
+      wmin[warp][d] = mn[d];
+      wmax[warp][d] = mx[d];
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  int bs = -1;
+  bool same = true;
+  for (int w = 0; w < kBlock / 32; ++w) {
+    if (wscene[w] < 0) continue;
+    if (bs < 0) bs = wscene[w];
+    else if (wscene[w] != bs) same = false;
+  }
+  if (bs < 0) return;
+  if (same) {
+    for (int d = 0; d < 3; ++d) {
+      int lo = INT_MAX, hi = INT_MIN;
+      for (int w = 0; w < kBlock / 32; ++w) {
+        if (wscene[w] < 0) continue;
+        lo = min(lo, wmin[w][d]);
+        hi = max(hi, wmax[w][d]);
+      }
+      atomicMin(&a.bmin[3 * bs + d], lo);
+      atomicMax(&a.bmax[3 * bs + d], hi);
+    }
+  } else {
+    for (int w = 0; w < kBlock / 32; ++w) {
+      if (wscene[w] < 0) continue;
+      for (int d = 0; d < 3; ++d) {
+        atomicMin(&a.bmin[3 * wscene[w] + d], wmin[w][d]);
+        atomicMax(&a.bmax[3 * wscene[w] + d], wmax[w][d]);
+      }
+    }
   }
 }
 
@@ -194,6 +227,7 @@ __global__ void __launch_bounds__(kBlock) k_grid_setup(StepArgs a) {
   st->step = st->started;
   st->started = st->started + 1;
   st->pairs = 0ull;
+  st->cursor = 0ull;
   st->nbr_max = 0;
   unsigned long long total = 0;
   bool domain = false;
@@ -471,47 +505,33 @@ __global__ void __launch_bounds__(kBlock) k_nbr_count(StepArgs a) {
   }
   const int mx = __reduce_max_sync(kFull, count);
   const unsigned sum = __reduce_add_sync(kFull, static_cast<unsigned>(count));
-  if ((threadIdx.x & 31) == 0 && i < a.n) {
-    a.depth[i >> 5] = mx;
-    if (sum) atomicAdd(&a.status->pairs, static_cast<unsigned long long>(sum));
-    if (mx) atomicMax(&a.status->nbr_max, mx);
-  }
-}
-
-// Single CTA: exclusive scan of 32 * depth over warps.
-__global__ void __launch_bounds__(1024) k_nbr_scan(StepArgs a) {
-  if (failed(a.status)) return;
-  __shared__ long long warp_sums[32];
-  __shared__ long long carry;
+  // Slices: each block takes one contiguous range for its warps with a single
+  // atomic on the list cursor. Placement varies run to run; every list's
+  // content and order do not.
+  __shared__ int wdepth[kBlock / 32];
+  __shared__ unsigned long long block_base;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (threadIdx.x == 0) carry = 0;
-  __syncthreads();
-  for (int chunk = 0; chunk < a.warps; chunk += 1024) {
-    const int w = chunk + threadIdx.x;
-    const long long v = (w < a.warps) ? 32ll * a.depth[w] : 0ll;
-    long long inc = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const long long y = __shfl_up_sync(kFull, inc, o);
-      if (lane >= o) inc += y;
+  if (lane == 0) {
+    wdepth[warp] = (i < a.n) ? mx : 0;
+    if (i < a.n) {
+      if (sum) atomicAdd(&a.status->pairs, static_cast<unsigned long long>(sum));
+      if (mx) atomicMax(&a.status->nbr_max, mx);
     }
-    if (lane == 31) warp_sums[warp] = inc;
-    __syncthreads();
-    long long wpre = 0, all = 0;
-    for (int k = 0; k < 32; ++k) {
-      const long long ws = warp_sums[k];
-      if (k < warp) wpre += ws;
-      all += ws;
-    }
-    const long long c0 = carry;
-    if (w < a.warps) a.wbase[w] = c0 + wpre + inc - v;
-    __syncthreads();
-    if (threadIdx.x == 0) carry = c0 + all;
-    __syncthreads();
   }
-  if (threadIdx.x == 0 && carry > a.nbr_capacity) {
-    a.status->need_nbr = static_cast<unsigned long long>(carry);
-    set_error(a.status, FLUID_ERR_CAPACITY);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long total = 0;
+    for (int w = 0; w < kBlock / 32; ++w) total += 32ull * wdepth[w];
+    const unsigned long long base = atomicAdd(&a.status->cursor, total);
+    if (base + total > static_cast<unsigned long long>(a.nbr_capacity)) set_error(a.status, FLUID_ERR_CAPACITY);
+    block_base = base;
+  }
+  __syncthreads();
+  if (lane == 0 && i < a.n) {
+    unsigned long long off = block_base;
+    for (int w = 0; w < warp; ++w) off += 32ull * wdepth[w];
+    a.wbase[i >> 5] = static_cast<long long>(off);
+    a.depth[i >> 5] = mx;
   }
 }
 
@@ -581,6 +601,48 @@ __global__ void __launch_bounds__(kBlock) k_nbr_fill(StepArgs a) {
 // ---------------------------------------------------------------------------
 // Jacobi passes over the lists.
 
+// Walks this lane's list entries k = 0..n-1 in order. kUnroll indices and the
+// records they point at are fetched before any is used, so every warp keeps
+// several independent gathers in flight; the body still sees the entries in
+// list order, so sums accumulate in the reference's order.
+#ifndef FGB_UNROLL
+#define FGB_UNROLL 4
+#endif
+constexpr int kUnroll = FGB_UNROLL;
+
+template <typename Load, typename Body>
+__device__ __forceinline__ void for_each_neighbor(const int* __restrict__ list, int n, Load&& load, Body&& body) {
+  using Rec = decltype(load(0));
+  int k = 0;
+  for (; k + kUnroll <= n; k += kUnroll) {
+    int j[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) j[u] = __ldg(list + 32ll * (k + u));
+    Rec r[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) r[u] = load(j[u]);
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) body(r[u]);
+  }
+  for (; k < n; ++k) body(load(__ldg(list + 32ll * k)));
+}
+
+struct PosLam {
+  float4 q;
+  float l;
+};
+struct PosVelRho {
+  float4 x, v;
+  float rho;
+};
+struct PosVel {
+  float4 x, v;
+};
+struct PosOmega {
+  float4 x;
+  float om;
+};
+
 __global__ void __launch_bounds__(kBlock) k_lambda(StepArgs a, int in) {
   if (failed(a.status)) return;
   const int i = blockIdx.x * kBlock + threadIdx.x;
@@ -592,13 +654,11 @@ __global__ void __launch_bounds__(kBlock) k_lambda(StepArgs a, int in) {
   const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
   const float h2 = c.h2;
   LambdaAcc acc;
-  for (int k = 0; k < n; ++k) {
-    const int j = __ldg(list + 32ll * k);
-    const float4 q = __ldg(pos + j);
+  for_each_neighbor(list, n, [&](int j) { return __ldg(pos + j); }, [&](const float4 q) {
     const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
     const float r2 = dist2(dx, dy, dz);
     if (r2 < h2) acc.add(c, dx, dy, dz, r2);
-  }
+  });
   float rho;
   a.lambda[i] = finish_lambda(c, acc.rho, acc.gsx, acc.gsy, acc.gsz, acc.sum_g2, rho);
   a.rho[i] = rho;
@@ -633,15 +693,14 @@ __global__ void __launch_bounds__(kBlock) k_delta(StepArgs a, int in, int last, 
   const float li = lam[i];
   const float h2 = c.h2;
   float ax = 0.0f, ay = 0.0f, az = 0.0f;
-  for (int k = 0; k < n; ++k) {
-    const int j = __ldg(list + 32ll * k);
-    const float4 q = __ldg(pos + j);
-    const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+  const bool scorr = c.scorr_on != 0;
+  for_each_neighbor(list, n, [&](int j) { return PosLam{__ldg(pos + j), __ldg(lam + j)}; }, [&](const PosLam r) {
+    const float dx = p.x - r.q.x, dy = p.y - r.q.y, dz = p.z - r.q.z;
     const float r2 = dist2(dx, dy, dz);
     if (r2 < h2) {
       const float gf = spiky(c, clamped_r(c, r2));
-      float s = li + __ldg(lam + j);
-      if (c.scorr_on) {
+      float s = li + r.l;
+      if (scorr) {
         const float ratio = poly6(c, r2) * c.scorr_inv_wdq;
         s += c.scorr_neg_k * pow_n(ratio, c.scorr_n);
       }
@@ -649,7 +708,7 @@ __global__ void __launch_bounds__(kBlock) k_delta(StepArgs a, int in, int last, 
       ay += s * gf * dy;
       az += s * gf * dz;
     }
-  }
+  });
   ax *= c.inv_density;
   ay *= c.inv_density;
   az *= c.inv_density;
@@ -703,20 +762,18 @@ __global__ void __launch_bounds__(kBlock) k_xsph(StepArgs a, int rest) {
     const float* __restrict__ rho = a.rho;
     const float h2 = c.h2;
     float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-    for (int k = 0; k < n; ++k) {
-      const int j = __ldg(list + 32ll * k);
-      const float4 xj = __ldg(xs + j);
-      const float r2 = dist2(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
-      if (r2 < h2) {
-        const float W = poly6(c, r2);
-        const float rj = __ldg(rho + j);
-        const float inv_rho_j = (rj > 0.0f) ? (c.mass / rj) : 0.0f;
-        const float4 vj = __ldg(vs + j);
-        sx += (vj.x - vi.x) * W * inv_rho_j;
-        sy += (vj.y - vi.y) * W * inv_rho_j;
-        sz += (vj.z - vi.z) * W * inv_rho_j;
-      }
-    }
+    for_each_neighbor(
+        list, n, [&](int j) { return PosVelRho{__ldg(xs + j), __ldg(vs + j), __ldg(rho + j)}; },
+        [&](const PosVelRho r) {
+          const float r2 = dist2(xi.x - r.x.x, xi.y - r.x.y, xi.z - r.x.z);
+          if (r2 < h2) {
+            const float W = poly6(c, r2);
+            const float inv_rho_j = (r.rho > 0.0f) ? (c.mass / r.rho) : 0.0f;
+            sx += (r.v.x - vi.x) * W * inv_rho_j;
+            sy += (r.v.y - vi.y) * W * inv_rho_j;
+            sz += (r.v.z - vi.z) * W * inv_rho_j;
+          }
+        });
     vx += c.visc_c * sx;
     vy += c.visc_c * sy;
     vz += c.visc_c * sz;
@@ -740,21 +797,18 @@ __global__ void __launch_bounds__(kBlock) k_omega(StepArgs a) {
     const int n = a.cnt[i];
     const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
     const float h2 = c.h2;
-    for (int k = 0; k < n; ++k) {
-      const int j = __ldg(list + 32ll * k);
-      const float4 xj = __ldg(xs + j);
-      const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+    for_each_neighbor(list, n, [&](int j) { return PosVel{__ldg(xs + j), __ldg(vs + j)}; }, [&](const PosVel r) {
+      const float dx = xi.x - r.x.x, dy = xi.y - r.x.y, dz = xi.z - r.x.z;
       const float r2 = dist2(dx, dy, dz);
       if (r2 < h2) {
         const float gf = spiky(c, clamped_r(c, r2));
         const float gx = gf * dx, gy = gf * dy, gz = gf * dz;
-        const float4 vj = __ldg(vs + j);
-        const float ux = vj.x - vi.x, uy = vj.y - vi.y, uz = vj.z - vi.z;
+        const float ux = r.v.x - vi.x, uy = r.v.y - vi.y, uz = r.v.z - vi.z;
         ox += uy * gz - uz * gy;
         oy += uz * gx - ux * gz;
         oz += ux * gy - uy * gx;
       }
-    }
+    });
   }
   a.omega[i] = make_float4(ox, oy, oz, sqrtf(ox * ox + oy * oy + oz * oz));
 }
@@ -776,19 +830,18 @@ __global__ void __launch_bounds__(kBlock) k_eta(StepArgs a, int rest) {
     const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
     const float h2 = c.h2;
     float ex = 0.0f, ey = 0.0f, ez = 0.0f;
-    for (int k = 0; k < n; ++k) {
-      const int j = __ldg(list + 32ll * k);
-      const float4 xj = __ldg(xs + j);
-      const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
-      const float r2 = dist2(dx, dy, dz);
-      if (r2 < h2) {
-        const float gf = spiky(c, clamped_r(c, r2));
-        const float coeff = __ldg(&om[j].w) - oi.w;
-        ex += coeff * (gf * dx);
-        ey += coeff * (gf * dy);
-        ez += coeff * (gf * dz);
-      }
-    }
+    for_each_neighbor(list, n, [&](int j) { return PosOmega{__ldg(xs + j), __ldg(&om[j].w)}; },
+                      [&](const PosOmega r) {
+                        const float dx = xi.x - r.x.x, dy = xi.y - r.x.y, dz = xi.z - r.x.z;
+                        const float r2 = dist2(dx, dy, dz);
+                        if (r2 < h2) {
+                          const float gf = spiky(c, clamped_r(c, r2));
+                          const float coeff = r.om - oi.w;
+                          ex += coeff * (gf * dx);
+                          ey += coeff * (gf * dy);
+                          ez += coeff * (gf * dz);
+                        }
+                      });
     const float len = sqrtf(ex * ex + ey * ey + ez * ez);
     float nx = 0.0f, ny = 0.0f, nz = 0.0f;
     if (len > c.vort_norm_eps) {
@@ -909,8 +962,6 @@ cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t s
   m.mark(FLUID_KERNEL_REORDER);
   k_nbr_count<<<nb, kBlock, 0, st>>>(a);
   m.mark(FLUID_KERNEL_NBR_COUNT);
-  k_nbr_scan<<<1, 1024, 0, st>>>(a);
-  m.mark(FLUID_KERNEL_NBR_SCAN);
   k_nbr_fill<<<nb, kBlock, 0, st>>>(a);
   m.mark(FLUID_KERNEL_NBR_FILL);
 

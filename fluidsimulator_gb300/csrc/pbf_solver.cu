@@ -378,7 +378,7 @@ class Solver {
         return fail(st.err, st.err == FLUID_ERR_NONFINITE ? "non-finite predicted position"
                                                           : "particle cells span too large a grid");
       }
-      int rc = grow(st.need_grid, st.need_nbr);
+      int rc = grow(st.need_grid, st.cursor);
       if (rc) return rc;
       ++regrows_;
       for (int k = 0; k < remaining; ++k) {
@@ -910,7 +910,7 @@ int fluid_solver_kernel_times(fluid_solver* s, double* ms, int64_t* launches, in
 const char* fluid_kernel_name(int kernel) {
   static const char* const names[FLUID_KERNEL_COUNT] = {
       "k_bounds", "k_grid_setup", "k_keys", "k_radix_hist", "k_radix_scan", "k_radix_scatter",
-      "k_reorder", "k_nbr_count", "k_nbr_scan", "k_nbr_fill", "k_lambda", "k_delta",
+      "k_reorder", "k_nbr_count", "k_nbr_fill", "k_lambda", "k_delta",
       "k_commit", "k_xsph", "k_omega", "k_eta"};
   return (kernel >= 0 && kernel < FLUID_KERNEL_COUNT) ? names[kernel] : nullptr;
 }

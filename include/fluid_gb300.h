@@ -205,16 +205,15 @@ enum {
   FLUID_KERNEL_RADIX_SCAN = 4,
   FLUID_KERNEL_RADIX_SCATTER = 5,
   FLUID_KERNEL_REORDER = 6,  /* gather into cell order + cell table */
-  FLUID_KERNEL_NBR_COUNT = 7,
-  FLUID_KERNEL_NBR_SCAN = 8,
-  FLUID_KERNEL_NBR_FILL = 9, /* lists + first lambda */
-  FLUID_KERNEL_LAMBDA = 10,
-  FLUID_KERNEL_DELTA = 11,   /* position correction (+ commit on the last) */
-  FLUID_KERNEL_COMMIT = 12,  /* commit when solver_iterations == 0 */
-  FLUID_KERNEL_XSPH = 13,
-  FLUID_KERNEL_OMEGA = 14,
-  FLUID_KERNEL_ETA = 15,     /* eta + confinement + plane restitution */
-  FLUID_KERNEL_COUNT = 16
+  FLUID_KERNEL_NBR_COUNT = 7, /* counts + list slices */
+  FLUID_KERNEL_NBR_FILL = 8, /* lists + first lambda */
+  FLUID_KERNEL_LAMBDA = 9,
+  FLUID_KERNEL_DELTA = 10,   /* position correction (+ commit on the last) */
+  FLUID_KERNEL_COMMIT = 11,  /* commit when solver_iterations == 0 */
+  FLUID_KERNEL_XSPH = 12,
+  FLUID_KERNEL_OMEGA = 13,
+  FLUID_KERNEL_ETA = 14,     /* eta + confinement + plane restitution */
+  FLUID_KERNEL_COUNT = 15
 };
 
 /* Name of a kernel id ("k_delta", ...); NULL when out of range. */
