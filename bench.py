@@ -195,7 +195,7 @@ def run_ours(args, world, rank, local):
     stream = torch.cuda.Stream(dev)  # a real stream: the legacy NULL stream would not order with the solver
     torch.cuda.set_stream(stream)
 
-    sc = scenes.falling_block(N_SIDE, seed=0)
+    sc = scenes.falling_block(args.side, seed=0)
     n = sc.count
     pos0 = torch.from_numpy(sc.pos).to(dev)
     vel0 = torch.from_numpy(sc.vel).to(dev)
@@ -322,6 +322,10 @@ def run_ours(args, world, rank, local):
         traj["kernel_ms_total"] = {k: round(v[0], 2) for k, v in tail.items() if v[1]}
     solver.close()
 
+    batched = None
+    if not args.no_batched:
+        batched = run_batched(args, dev, stream, l2_flush)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(sc, budget_s=args.cpu_budget)
@@ -339,6 +343,7 @@ def run_ours(args, world, rank, local):
         "step_roofline": {"bytes_per_particle_step": ALGO_BYTES_PER_STEP, "frac": round(step_frac, 5)},
         "kernel_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in stage.items() if v[1]},
         "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches, "trajectory": traj,
+        "batched": batched,
     }
     if world > 1:
         import torch.distributed as dist
@@ -346,6 +351,98 @@ def run_ours(args, world, rank, local):
         dist.destroy_process_group()
     if rank == 0:
         print(json.dumps(out), flush=True)
+
+
+def run_batched(args, dev, stream, l2_flush):
+    """64 independent dam-break scenes (2k-64k particles each, all flags):
+    one batched solver (all scenes in the same launches, one CUDA graph per
+    step, autotuned launch shapes) against the same scenes stepped serially by
+    64 single-scene solvers enqueued back to back on one stream."""
+    import torch
+
+    from fluidsimulator_gb300 import scenes
+    from fluidsimulator_gb300.solver import Solver
+
+    scs = scenes.batched_scenes(args.batch_scenes, seed=0)
+    counts = [sc.count for sc in scs]
+    pos = torch.from_numpy(__import__("numpy").concatenate([sc.pos for sc in scs], axis=1)).to(dev)
+    vel = torch.from_numpy(__import__("numpy").concatenate([sc.vel for sc in scs], axis=1)).to(dev)
+    parts_p = [torch.from_numpy(sc.pos).to(dev) for sc in scs]
+    parts_v = [torch.from_numpy(sc.vel).to(dev) for sc in scs]
+    torch.cuda.synchronize(dev)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+
+    big = Solver(dev.index)
+    big.configure([sc.params for sc in scs], counts)
+    big.set_stream(stream.cuda_stream)
+    big.upload(pos, vel)
+    shapes = big.autotune(1)
+    small = []
+    for sc, pp, vv in zip(scs, parts_p, parts_v):
+        s = Solver(dev.index)
+        s.configure([sc.params], [sc.count])
+        s.set_stream(stream.cuda_stream)
+        s.upload(pp, vv)
+        s.set_tuning(shapes)
+        small.append(s)
+
+    def time_batched(steps, restore):
+        ms = []
+        if not restore:
+            big.upload(pos, vel)
+        for _ in range(steps):
+            if restore:
+                big.upload(pos, vel)
+            l2_flush.zero_()
+            ev0.record(stream)
+            big.step_async(1)
+            ev1.record(stream)
+            big.synchronize()
+            ms.append(ev0.elapsed_time(ev1))
+        return ms
+
+    def time_serial(steps, restore):
+        ms = []
+        if not restore:
+            for s, pp, vv in zip(small, parts_p, parts_v):
+                s.upload(pp, vv)
+        for _ in range(steps):
+            if restore:
+                for s, pp, vv in zip(small, parts_p, parts_v):
+                    s.upload(pp, vv)
+            l2_flush.zero_()
+            ev0.record(stream)
+            for s in small:
+                s.step_async(1)
+            ev1.record(stream)
+            for s in small:
+                s.synchronize()
+            ms.append(ev0.elapsed_time(ev1))
+        return ms
+
+    time_batched(args.warmup, True)
+    time_serial(args.warmup, True)
+    b = time_batched(args.steps, True)
+    sr = time_serial(args.steps, True)
+    out = {"scenes": len(scs), "particles": int(sum(counts)), "steps": args.steps,
+           "batched_ms_per_step": round(statistics.mean(b), 4), "serial_ms_per_step": round(statistics.mean(sr), 4),
+           "batched_scene_steps_per_s": round(len(scs) * 1e3 / statistics.mean(b), 1),
+           "serial_scene_steps_per_s": round(len(scs) * 1e3 / statistics.mean(sr), 1),
+           "speedup": round(statistics.mean(sr) / statistics.mean(b), 3),
+           "workload": "one step over each scene's initial batch per timed step, L2 flushed between steps",
+           "tuning": shapes, }
+    if args.batch_trajectory > 0:
+        tb = time_batched(args.batch_trajectory, False)
+        ts = time_serial(args.batch_trajectory, False)
+        st = big.stats()
+        out["trajectory"] = {"steps": args.batch_trajectory, "batched_ms_total": round(sum(tb), 3),
+                             "serial_ms_total": round(sum(ts), 3), "speedup": round(sum(ts) / sum(tb), 3),
+                             "neighbors_per_particle_last": round(st["neighbor_pairs"] / st["particles"], 2)}
+    for s in small:
+        s.close()
+    big.close()
+    return out
 
 
 # --------------------------------------------------------------------------
@@ -432,6 +529,10 @@ def main(argv=None):
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU work for cpu_baseline")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 64-scene batched vs serial measurement")
+    ap.add_argument("--batch-scenes", type=int, default=64)
+    ap.add_argument("--batch-trajectory", type=int, default=30)
+    ap.add_argument("--side", type=int, default=100, help="lattice side of the throughput scene (100 = 1M)")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per launch of the dominant kernel from an ncu capture")
     args = ap.parse_args(argv)

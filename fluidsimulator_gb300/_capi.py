@@ -44,6 +44,7 @@ DEBUG_LAMBDA = 4
 KERNEL_NAMES = ["k_bounds", "k_grid_setup", "k_keys", "k_radix_hist", "k_radix_scan", "k_radix_scatter",
                 "k_reorder", "k_nbr_count", "k_nbr_fill", "k_lambda", "k_delta", "k_commit",
                 "k_xsph", "k_omega", "k_eta"]
+TUNABLE = ("k_nbr_count", "k_nbr_fill", "k_lambda", "k_delta", "k_xsph", "k_omega", "k_eta")
 
 
 class FluidParams(ctypes.Structure):
@@ -177,6 +178,12 @@ def _declare(lib):
     lib.fluid_solver_set_profiling.restype = c_int
     lib.fluid_solver_kernel_times.argtypes = [c_void_p, POINTER(c_double), POINTER(c_int64), c_int32, c_int32]
     lib.fluid_solver_kernel_times.restype = c_int
+    lib.fluid_solver_autotune.argtypes = [c_void_p, c_int32]
+    lib.fluid_solver_autotune.restype = c_int
+    lib.fluid_solver_get_tuning.argtypes = [c_void_p, POINTER(c_int32), POINTER(c_int32), c_int32]
+    lib.fluid_solver_get_tuning.restype = c_int
+    lib.fluid_solver_set_tuning.argtypes = [c_void_p, POINTER(c_int32), POINTER(c_int32), c_int32]
+    lib.fluid_solver_set_tuning.restype = c_int
     lib.fluid_kernel_name.argtypes = [c_int]
     lib.fluid_kernel_name.restype = c_char_p
     lib.fluid_solver_get_time.argtypes = [c_void_p, c_int32, POINTER(c_float)]

@@ -23,7 +23,7 @@ LIB_DIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIB_DIR, "libfluid_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["pbf_kernels.cu", "pbf_solver.cu", "pbf_noalloc.cu"]
+SOURCES = ["pbf_kernels.cu", "pbf_solver.cu", "pbf_noalloc.cu", "host/fluid_gb300.cpp"]
 
 
 def nvcc() -> str:
@@ -40,7 +40,8 @@ def cuda_flags() -> list[str]:
 
 def _headers() -> list[str]:
     hs = [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
-    hs += [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh", ".hpp"))]
+    for d in (CSRC, os.path.join(CSRC, "host")):
+        hs += [os.path.join(d, f) for f in os.listdir(d) if f.endswith((".h", ".cuh", ".hpp"))]
     return hs
 
 
@@ -71,7 +72,7 @@ def build(verbose: bool = False, force: bool = False, extra: list[str] | None = 
     objs = []
     for src in SOURCES:
         path = os.path.join(CSRC, src)
-        obj = os.path.join(BUILD_DIR, src.rsplit(".", 1)[0] + ".o")
+        obj = os.path.join(BUILD_DIR, os.path.basename(src).rsplit(".", 1)[0] + ".o")
         objs.append(obj)
         if force or _stale(obj, [path, __file__] + headers):
             jobs.append([nv, *cuda_flags(), *(extra or []), "-c", path, "-o", obj])

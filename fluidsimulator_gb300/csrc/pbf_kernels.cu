@@ -32,6 +32,8 @@
 namespace fgb {
 namespace {
 
+constexpr int kMaxBlock = 512;  // largest block the tuner may pick
+
 __device__ __forceinline__ bool failed(const DevStatus* st) {
   return *reinterpret_cast<const volatile int*>(&st->err) != 0;
 }
@@ -487,9 +489,9 @@ __device__ __forceinline__ void for_each_candidate(const StepArgs& a, const uint
   }
 }
 
-__global__ void __launch_bounds__(kBlock) k_nbr_count(StepArgs a) {
+__global__ void __launch_bounds__(kMaxBlock) k_nbr_count(StepArgs a) {
   if (failed(a.status)) return;
-  const int i = blockIdx.x * kBlock + threadIdx.x;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
   int count = 0;
   if (i < a.n) {
     const uint32_t* ks = sorted_keys(a, a.status->npass);
@@ -508,7 +510,7 @@ __global__ void __launch_bounds__(kBlock) k_nbr_count(StepArgs a) {
   // Slices: each block takes one contiguous range for its warps with a single
   // atomic on the list cursor. Placement varies run to run; every list's
   // content and order do not.
-  __shared__ int wdepth[kBlock / 32];
+  __shared__ int wdepth[kMaxBlock / 32];
   __shared__ unsigned long long block_base;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (lane == 0) {
@@ -521,7 +523,7 @@ __global__ void __launch_bounds__(kBlock) k_nbr_count(StepArgs a) {
   __syncthreads();
   if (threadIdx.x == 0) {
     unsigned long long total = 0;
-    for (int w = 0; w < kBlock / 32; ++w) total += 32ull * wdepth[w];
+    for (int w = 0; w < static_cast<int>(blockDim.x / 32); ++w) total += 32ull * wdepth[w];
     const unsigned long long base = atomicAdd(&a.status->cursor, total);
     if (base + total > static_cast<unsigned long long>(a.nbr_capacity)) set_error(a.status, FLUID_ERR_CAPACITY);
     block_base = base;
@@ -565,9 +567,9 @@ struct LambdaAcc {
   }
 };
 
-__global__ void __launch_bounds__(kBlock) k_nbr_fill(StepArgs a) {
+__global__ void __launch_bounds__(kMaxBlock) k_nbr_fill(StepArgs a) {
   if (failed(a.status)) return;
-  const int i = blockIdx.x * kBlock + threadIdx.x;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   const uint32_t* ks = sorted_keys(a, a.status->npass);
   const float4 p = a.p[0][i];
@@ -605,12 +607,7 @@ __global__ void __launch_bounds__(kBlock) k_nbr_fill(StepArgs a) {
 // records they point at are fetched before any is used, so every warp keeps
 // several independent gathers in flight; the body still sees the entries in
 // list order, so sums accumulate in the reference's order.
-#ifndef FGB_UNROLL
-#define FGB_UNROLL 4
-#endif
-constexpr int kUnroll = FGB_UNROLL;
-
-template <typename Load, typename Body>
+template <int kUnroll, typename Load, typename Body>
 __device__ __forceinline__ void for_each_neighbor(const int* __restrict__ list, int n, Load&& load, Body&& body) {
   using Rec = decltype(load(0));
   int k = 0;
@@ -643,9 +640,10 @@ struct PosOmega {
   float om;
 };
 
-__global__ void __launch_bounds__(kBlock) k_lambda(StepArgs a, int in) {
+template <int U>
+__global__ void __launch_bounds__(kMaxBlock) k_lambda(StepArgs a, int in) {
   if (failed(a.status)) return;
-  const int i = blockIdx.x * kBlock + threadIdx.x;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   const float4* __restrict__ pos = a.p[in];
   const float4 p = pos[i];
@@ -654,7 +652,7 @@ __global__ void __launch_bounds__(kBlock) k_lambda(StepArgs a, int in) {
   const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
   const float h2 = c.h2;
   LambdaAcc acc;
-  for_each_neighbor(list, n, [&](int j) { return __ldg(pos + j); }, [&](const float4 q) {
+  for_each_neighbor<U>(list, n, [&](int j) { return __ldg(pos + j); }, [&](const float4 q) {
     const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
     const float r2 = dist2(dx, dy, dz);
     if (r2 < h2) acc.add(c, dx, dy, dz, r2);
@@ -680,9 +678,10 @@ __device__ __forceinline__ void commit(const StepArgs& a, const SceneConst& c, i
   (to_v2 ? a.v2 : a.v)[i] = make_float4(vx, vy, vz, scene_bits);
 }
 
-__global__ void __launch_bounds__(kBlock) k_delta(StepArgs a, int in, int last, int to_v2, int rest) {
+template <int U>
+__global__ void __launch_bounds__(kMaxBlock) k_delta(StepArgs a, int in, int last, int to_v2, int rest) {
   if (failed(a.status)) return;
-  const int i = blockIdx.x * kBlock + threadIdx.x;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   const float4* __restrict__ pos = a.p[in];
   const float4 p = pos[i];
@@ -694,7 +693,7 @@ __global__ void __launch_bounds__(kBlock) k_delta(StepArgs a, int in, int last, 
   const float h2 = c.h2;
   float ax = 0.0f, ay = 0.0f, az = 0.0f;
   const bool scorr = c.scorr_on != 0;
-  for_each_neighbor(list, n, [&](int j) { return PosLam{__ldg(pos + j), __ldg(lam + j)}; }, [&](const PosLam r) {
+  for_each_neighbor<U>(list, n, [&](int j) { return PosLam{__ldg(pos + j), __ldg(lam + j)}; }, [&](const PosLam r) {
     const float dx = p.x - r.q.x, dy = p.y - r.q.y, dz = p.z - r.q.z;
     const float r2 = dist2(dx, dy, dz);
     if (r2 < h2) {
@@ -737,18 +736,19 @@ __global__ void __launch_bounds__(kBlock) k_delta(StepArgs a, int in, int last, 
 }
 
 // Commit without Jacobi iterations (solver_iterations == 0).
-__global__ void __launch_bounds__(kBlock) k_commit(StepArgs a, int to_v2, int rest) {
+__global__ void __launch_bounds__(kMaxBlock) k_commit(StepArgs a, int to_v2, int rest) {
   if (failed(a.status)) return;
-  const int i = blockIdx.x * kBlock + threadIdx.x;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   const float4 p = a.p[0][i];
   commit(a, a.sc[__float_as_int(p.w)], i, p.x, p.y, p.z, p.w, to_v2 != 0, rest != 0);
 }
 
 // XSPH (core.cpp:423-466): reads v2 (committed), writes v.
-__global__ void __launch_bounds__(kBlock) k_xsph(StepArgs a, int rest) {
+template <int U>
+__global__ void __launch_bounds__(kMaxBlock) k_xsph(StepArgs a, int rest) {
   if (failed(a.status)) return;
-  const int i = blockIdx.x * kBlock + threadIdx.x;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   const float4* __restrict__ xs = a.x;
   const float4* __restrict__ vs = a.v2;
@@ -762,7 +762,7 @@ __global__ void __launch_bounds__(kBlock) k_xsph(StepArgs a, int rest) {
     const float* __restrict__ rho = a.rho;
     const float h2 = c.h2;
     float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-    for_each_neighbor(
+    for_each_neighbor<U>(
         list, n, [&](int j) { return PosVelRho{__ldg(xs + j), __ldg(vs + j), __ldg(rho + j)}; },
         [&](const PosVelRho r) {
           const float r2 = dist2(xi.x - r.x.x, xi.y - r.x.y, xi.z - r.x.z);
@@ -783,9 +783,10 @@ __global__ void __launch_bounds__(kBlock) k_xsph(StepArgs a, int rest) {
 }
 
 // Vorticity omega and |omega| (core.cpp:472-508).
-__global__ void __launch_bounds__(kBlock) k_omega(StepArgs a) {
+template <int U>
+__global__ void __launch_bounds__(kMaxBlock) k_omega(StepArgs a) {
   if (failed(a.status)) return;
-  const int i = blockIdx.x * kBlock + threadIdx.x;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   const float4* __restrict__ xs = a.x;
   const float4* __restrict__ vs = a.v;
@@ -797,7 +798,7 @@ __global__ void __launch_bounds__(kBlock) k_omega(StepArgs a) {
     const int n = a.cnt[i];
     const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
     const float h2 = c.h2;
-    for_each_neighbor(list, n, [&](int j) { return PosVel{__ldg(xs + j), __ldg(vs + j)}; }, [&](const PosVel r) {
+    for_each_neighbor<U>(list, n, [&](int j) { return PosVel{__ldg(xs + j), __ldg(vs + j)}; }, [&](const PosVel r) {
       const float dx = xi.x - r.x.x, dy = xi.y - r.x.y, dz = xi.z - r.x.z;
       const float r2 = dist2(dx, dy, dz);
       if (r2 < h2) {
@@ -815,9 +816,10 @@ __global__ void __launch_bounds__(kBlock) k_omega(StepArgs a) {
 
 // Eta, confinement force, velocity update (core.cpp:512-570) and plane
 // restitution (core.cpp:573-612).
-__global__ void __launch_bounds__(kBlock) k_eta(StepArgs a, int rest) {
+template <int U>
+__global__ void __launch_bounds__(kMaxBlock) k_eta(StepArgs a, int rest) {
   if (failed(a.status)) return;
-  const int i = blockIdx.x * kBlock + threadIdx.x;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   const float4* __restrict__ xs = a.x;
   const float4* __restrict__ om = a.omega;
@@ -830,7 +832,7 @@ __global__ void __launch_bounds__(kBlock) k_eta(StepArgs a, int rest) {
     const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
     const float h2 = c.h2;
     float ex = 0.0f, ey = 0.0f, ez = 0.0f;
-    for_each_neighbor(list, n, [&](int j) { return PosOmega{__ldg(xs + j), __ldg(&om[j].w)}; },
+    for_each_neighbor<U>(list, n, [&](int j) { return PosOmega{__ldg(xs + j), __ldg(&om[j].w)}; },
                       [&](const PosOmega r) {
                         const float dx = xi.x - r.x.x, dy = xi.y - r.x.y, dz = xi.z - r.x.z;
                         const float r2 = dist2(dx, dy, dz);
@@ -915,6 +917,17 @@ __global__ void k_reset(DevStatus* st, int* bmin, int* bmax, int scenes) {
 
 inline int blocks_for(long long n, int threads) { return static_cast<int>((n + threads - 1) / threads); }
 
+// Launches KERNEL<U> for the tuned unroll U of the plan.
+#define FGB_DISPATCH_UNROLL(u, KERNEL, grid, block, stream, ...)          \
+  do {                                                                  \
+    switch (u) {                                                        \
+      case 1: KERNEL<1><<<grid, block, 0, stream>>>(__VA_ARGS__); break;  \
+      case 2: KERNEL<2><<<grid, block, 0, stream>>>(__VA_ARGS__); break;  \
+      case 8: KERNEL<8><<<grid, block, 0, stream>>>(__VA_ARGS__); break;  \
+      default: KERNEL<4><<<grid, block, 0, stream>>>(__VA_ARGS__); break; \
+    }                                                                   \
+  } while (0)
+
 }  // namespace
 
 void LaunchMarks::start() {
@@ -960,9 +973,11 @@ cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t s
   }
   k_reorder<<<nb, kBlock, 0, st>>>(a);
   m.mark(FLUID_KERNEL_REORDER);
-  k_nbr_count<<<nb, kBlock, 0, st>>>(a);
+  const int bc = plan.block[FLUID_KERNEL_NBR_COUNT];
+  k_nbr_count<<<blocks_for(a.n, bc), bc, 0, st>>>(a);
   m.mark(FLUID_KERNEL_NBR_COUNT);
-  k_nbr_fill<<<nb, kBlock, 0, st>>>(a);
+  const int bf = plan.block[FLUID_KERNEL_NBR_FILL];
+  k_nbr_fill<<<blocks_for(a.n, bf), bf, 0, st>>>(a);
   m.mark(FLUID_KERNEL_NBR_FILL);
 
   const bool post = plan.xsph || plan.vorticity;
@@ -975,21 +990,29 @@ cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t s
   for (int it = 0; it < plan.iterations; ++it) {
     const int in = it & 1;
     if (it > 0) {
-      k_lambda<<<nb, kBlock, 0, st>>>(a, in);
+      const int b = plan.block[FLUID_KERNEL_LAMBDA];
+      FGB_DISPATCH_UNROLL(plan.unroll[FLUID_KERNEL_LAMBDA], k_lambda, blocks_for(a.n, b), b, st, a, in);
       m.mark(FLUID_KERNEL_LAMBDA);
     }
     const int last = (it == plan.iterations - 1) ? 1 : 0;
-    k_delta<<<nb, kBlock, 0, st>>>(a, in, last, to_v2, last ? rest_commit : 0);
+    const int b = plan.block[FLUID_KERNEL_DELTA];
+    FGB_DISPATCH_UNROLL(plan.unroll[FLUID_KERNEL_DELTA], k_delta, blocks_for(a.n, b), b, st, a, in, last, to_v2,
+                        last ? rest_commit : 0);
     m.mark(FLUID_KERNEL_DELTA);
   }
   if (plan.xsph) {
-    k_xsph<<<nb, kBlock, 0, st>>>(a, (!plan.vorticity && plan.restitution) ? 1 : 0);
+    const int b = plan.block[FLUID_KERNEL_XSPH];
+    FGB_DISPATCH_UNROLL(plan.unroll[FLUID_KERNEL_XSPH], k_xsph, blocks_for(a.n, b), b, st, a,
+                        (!plan.vorticity && plan.restitution) ? 1 : 0);
     m.mark(FLUID_KERNEL_XSPH);
   }
   if (plan.vorticity) {
-    k_omega<<<nb, kBlock, 0, st>>>(a);
+    const int bo = plan.block[FLUID_KERNEL_OMEGA];
+    FGB_DISPATCH_UNROLL(plan.unroll[FLUID_KERNEL_OMEGA], k_omega, blocks_for(a.n, bo), bo, st, a);
     m.mark(FLUID_KERNEL_OMEGA);
-    k_eta<<<nb, kBlock, 0, st>>>(a, plan.restitution ? 1 : 0);
+    const int be = plan.block[FLUID_KERNEL_ETA];
+    FGB_DISPATCH_UNROLL(plan.unroll[FLUID_KERNEL_ETA], k_eta, blocks_for(a.n, be), be, st, a,
+                        plan.restitution ? 1 : 0);
     m.mark(FLUID_KERNEL_ETA);
   }
   return cudaGetLastError();

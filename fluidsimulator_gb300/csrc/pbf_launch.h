@@ -17,8 +17,27 @@ struct StepPlan {
   bool vorticity = false; // some scene runs vorticity confinement
   bool restitution = false;
   int radix_passes = 1;   // passes launched (cover the grid capacity)
-  int threads = kBlock;   // block size of the per-particle passes
+  // Per-kernel launch shape (indexed by FLUID_KERNEL_*), chosen by the
+  // autotuner: neighbour entries fetched ahead (1, 2, 4, 8) in the list
+  // passes, and threads per block (128, 256, 512) for the neighbour kernels.
+  int unroll[FLUID_KERNEL_COUNT];
+  int block[FLUID_KERNEL_COUNT];
+  StepPlan() {
+    for (int k = 0; k < FLUID_KERNEL_COUNT; ++k) {
+      unroll[k] = 4;
+      block[k] = kBlock;
+    }
+  }
 };
+
+// Kernels whose launch shape the autotuner chooses.
+inline bool tunable_unroll(int k) {
+  return k == FLUID_KERNEL_LAMBDA || k == FLUID_KERNEL_DELTA || k == FLUID_KERNEL_XSPH || k == FLUID_KERNEL_OMEGA ||
+         k == FLUID_KERNEL_ETA;
+}
+inline bool tunable_block(int k) {
+  return tunable_unroll(k) || k == FLUID_KERNEL_NBR_COUNT || k == FLUID_KERNEL_NBR_FILL;
+}
 
 // Records an event after selected launches when profiling is on.
 struct LaunchMarks {

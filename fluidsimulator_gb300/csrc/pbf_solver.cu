@@ -205,6 +205,7 @@ class Solver {
     pending_ = 0;
     uploaded_ = false;
     build_scene_consts();
+    plan_ = StepPlan();
     warps_ = (n_ + 31) / 32;
     tiles_ = std::max(1, (n_ + kRadixTile - 1) / kRadixTile);
     const size_t n = static_cast<size_t>(std::max(n_, 1));
@@ -410,6 +411,98 @@ class Solver {
         }
       }
     }
+    return FLUID_OK;
+  }
+
+  // Times every tunable kernel under each (unroll, block) shape on the
+  // current state and keeps the fastest shape per kernel. Trial steps are
+  // discarded (the step's input stays in the current parity buffers), so the
+  // state is not advanced. All shapes compute identical results.
+  int autotune(int trials) {
+    if (!uploaded_) return fail(FLUID_ERR_STATE, "no state uploaded");
+    int rc = synchronize();
+    if (rc) return rc;
+    if (n_ == 0) return FLUID_OK;
+    trials = std::max(1, trials);
+    const int parity0 = parity_;
+    const long long steps0 = steps_;
+    const std::vector<float> times0 = times_;
+    auto revert = [&] {
+      parity_ = parity0;
+      steps_ = steps0;
+      times_ = times0;
+    };
+    rc = step(1);  // sizes the lists and the cell table for this state
+    revert();
+    if (rc) return rc;
+    const bool prof = profiling_;
+    rc = set_profiling(1);
+    if (rc) return rc;
+    StepPlan best = plan_;
+    double best_ms[FLUID_KERNEL_COUNT];
+    std::fill(std::begin(best_ms), std::end(best_ms), 1e300);
+    const int unrolls[] = {1, 2, 4, 8};
+    const int blocks[] = {128, 256, 512};
+    for (int u : unrolls) {
+      for (int b : blocks) {
+        for (int k = 0; k < FLUID_KERNEL_COUNT; ++k) {
+          if (tunable_unroll(k)) plan_.unroll[k] = u;
+          if (tunable_block(k)) plan_.block[k] = b;
+        }
+        invalidate_graphs();
+        kernel_times(nullptr, nullptr, 0, 1);
+        for (int t = 0; t < trials; ++t) {
+          rc = launch_one();
+          if (!rc) rc = synchronize();
+          revert();
+          if (rc) {
+            plan_ = best;
+            set_profiling(prof);
+            return rc;
+          }
+        }
+        for (int k = 0; k < FLUID_KERNEL_COUNT; ++k) {
+          if (!tunable_block(k) || stage_launches_[k] == 0) continue;
+          const double avg = stage_ms_[k] / static_cast<double>(stage_launches_[k]);
+          if (avg < best_ms[k]) {
+            best_ms[k] = avg;
+            if (tunable_unroll(k)) best.unroll[k] = u;
+            best.block[k] = b;
+          }
+        }
+      }
+    }
+    for (int k = 0; k < FLUID_KERNEL_COUNT; ++k) {
+      plan_.unroll[k] = best.unroll[k];
+      plan_.block[k] = best.block[k];
+    }
+    kernel_times(nullptr, nullptr, 0, 1);
+    invalidate_graphs();
+    return set_profiling(prof);
+  }
+
+  int get_tuning(int32_t* unroll, int32_t* block, int kernels) {
+    for (int k = 0; k < kernels && k < FLUID_KERNEL_COUNT; ++k) {
+      if (unroll) unroll[k] = plan_.unroll[k];
+      if (block) block[k] = plan_.block[k];
+    }
+    return FLUID_OK;
+  }
+
+  int set_tuning(const int32_t* unroll, const int32_t* block, int kernels) {
+    for (int k = 0; k < kernels && k < FLUID_KERNEL_COUNT; ++k) {
+      if (unroll && !(unroll[k] == 1 || unroll[k] == 2 || unroll[k] == 4 || unroll[k] == 8))
+        return fail(FLUID_ERR_INVALID_ARGUMENT, "unroll must be 1, 2, 4 or 8");
+      if (block && !(block[k] == 128 || block[k] == 256 || block[k] == 512))
+        return fail(FLUID_ERR_INVALID_ARGUMENT, "block must be 128, 256 or 512");
+    }
+    int rc = synchronize();
+    if (rc) return rc;
+    for (int k = 0; k < kernels && k < FLUID_KERNEL_COUNT; ++k) {
+      if (unroll && tunable_unroll(k)) plan_.unroll[k] = unroll[k];
+      if (block && tunable_block(k)) plan_.block[k] = block[k];
+    }
+    invalidate_graphs();
     return FLUID_OK;
   }
 
@@ -913,6 +1006,21 @@ const char* fluid_kernel_name(int kernel) {
       "k_reorder", "k_nbr_count", "k_nbr_fill", "k_lambda", "k_delta",
       "k_commit", "k_xsph", "k_omega", "k_eta"};
   return (kernel >= 0 && kernel < FLUID_KERNEL_COUNT) ? names[kernel] : nullptr;
+}
+
+int fluid_solver_autotune(fluid_solver* s, int32_t trials) {
+  FLUID_CHECK_SOLVER(s);
+  return s->impl.autotune(trials);
+}
+
+int fluid_solver_get_tuning(fluid_solver* s, int32_t* unroll, int32_t* block, int32_t kernels) {
+  FLUID_CHECK_SOLVER(s);
+  return s->impl.get_tuning(unroll, block, kernels);
+}
+
+int fluid_solver_set_tuning(fluid_solver* s, const int32_t* unroll, const int32_t* block, int32_t kernels) {
+  FLUID_CHECK_SOLVER(s);
+  return s->impl.set_tuning(unroll, block, kernels);
 }
 
 int fluid_solver_get_time(fluid_solver* s, int32_t scene, float* time) {

@@ -147,6 +147,31 @@ class Solver:
         self._check(self.lib.fluid_solver_kernel_times(self.h, ms, la, n, int(reset)))
         return {name: (ms[k], la[k]) for k, name in enumerate(_capi.KERNEL_NAMES)}
 
+    def autotune(self, trials: int = 2) -> dict:
+        """Picks the fastest launch shape per kernel on the current state
+        (state not advanced); returns the chosen shapes."""
+        self._check(self.lib.fluid_solver_autotune(self.h, trials))
+        return self.tuning()
+
+    def tuning(self) -> dict:
+        n = len(_capi.KERNEL_NAMES)
+        u = (ctypes.c_int32 * n)()
+        b = (ctypes.c_int32 * n)()
+        self._check(self.lib.fluid_solver_get_tuning(self.h, u, b, n))
+        return {name: {"unroll": u[k], "block": b[k]} for k, name in enumerate(_capi.KERNEL_NAMES)
+                if name in _capi.TUNABLE}
+
+    def set_tuning(self, shapes: dict) -> None:
+        n = len(_capi.KERNEL_NAMES)
+        cur = self.tuning()
+        u = (ctypes.c_int32 * n)(*([4] * n))
+        b = (ctypes.c_int32 * n)(*([256] * n))
+        for k, name in enumerate(_capi.KERNEL_NAMES):
+            shape = shapes.get(name, cur.get(name))
+            if shape:
+                u[k], b[k] = shape["unroll"], shape["block"]
+        self._check(self.lib.fluid_solver_set_tuning(self.h, u, b, n))
+
     def read_debug(self, what: int) -> np.ndarray:
         if what == _capi.DEBUG_CELL_KEYS:
             out = np.empty((self.n, 3), np.int32)

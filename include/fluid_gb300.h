@@ -225,6 +225,23 @@ int fluid_solver_kernel_times(fluid_solver* solver, double* ms_out,
                               int64_t* launches_out, int32_t kernels,
                               int32_t reset);
 
+/*
+ * Autotuner (no reference counterpart). Times each tunable kernel (the
+ * neighbour-list passes and the list build) under every launch shape --
+ * neighbour entries fetched ahead in {1, 2, 4, 8}, threads per block in
+ * {128, 256, 512} -- over `trials` discarded steps of the current state, and
+ * keeps the fastest shape per kernel. The state and time are not advanced.
+ * Every shape computes identical results; only speed differs.
+ */
+int fluid_solver_autotune(fluid_solver* solver, int32_t trials);
+
+/* Launch shape per kernel id (FLUID_KERNEL_*): entries fetched ahead and
+ * threads per block. Arrays of `kernels` entries; either may be NULL. */
+int fluid_solver_get_tuning(fluid_solver* solver, int32_t* unroll, int32_t* block,
+                            int32_t kernels);
+int fluid_solver_set_tuning(fluid_solver* solver, const int32_t* unroll,
+                            const int32_t* block, int32_t kernels);
+
 /* Time of scene `scene` (float, accumulated as State::time, core.cpp:614). */
 int fluid_solver_get_time(fluid_solver* solver, int32_t scene, float* time);
 int fluid_solver_set_time(fluid_solver* solver, int32_t scene, float time);

@@ -242,3 +242,32 @@ def test_empty_and_tiny_scenes(cuda_lib, oracle_lib):
         ref = oracle_lib.Oracle().run(sc.params, pos, vel, 0.0, 5)
         np.testing.assert_array_equal(got[0], ref["pos"])
         np.testing.assert_array_equal(got[1], ref["vel"])
+
+
+def test_autotune_keeps_state_and_results(cuda_lib, oracle_lib):
+    sc = scenes.dam_break(12, seed=9, flags=True)
+    s = Solver(0)
+    s.configure([sc.params], [sc.count])
+    s.upload(sc.pos, sc.vel)
+    s.step(20)
+    before = s.download()
+    t0 = s.time()
+    steps0 = s.stats()["steps"]
+    shapes = s.autotune(1)
+    after = s.download()
+    np.testing.assert_array_equal(before[0], after[0])
+    np.testing.assert_array_equal(before[1], after[1])
+    assert s.time() == t0 and s.stats()["steps"] == steps0
+    assert set(shapes) >= {"k_delta", "k_lambda"}
+    s.step(10)
+    ref = oracle_lib.Oracle().run(sc.params, sc.pos, sc.vel, 0.0, 30)
+    got = s.download()
+    np.testing.assert_array_equal(got[0], ref["pos"])
+    np.testing.assert_array_equal(got[1], ref["vel"])
+    # extreme shapes give the same numbers
+    s.upload(sc.pos, sc.vel)
+    s.set_tuning({k: {"unroll": 1, "block": 512} for k in shapes})
+    s.step(30)
+    got = s.download()
+    np.testing.assert_array_equal(got[0], ref["pos"])
+    s.close()
