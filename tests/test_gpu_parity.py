@@ -72,7 +72,7 @@ def test_trajectory_matches_golden(cuda_lib, name):
 
 def test_neighbor_statistics_match_golden(cuda_lib):
     # Per-step neighbour pairs / max and density statistics over the whole
-    # 240-step plain dam break (SURVEY config 1) and 60 collapsing steps with
+    # 240-step plain dam break (4,096 particles) and 60 collapsing steps with
     # all flags on.
     for name in ("dam_break_4096.npz", "dam_break_flags_4096.npz"):
         p, d = load_golden(name)
