@@ -184,6 +184,12 @@ def _declare(lib):
     lib.fluid_solver_get_tuning.restype = c_int
     lib.fluid_solver_set_tuning.argtypes = [c_void_p, POINTER(c_int32), POINTER(c_int32), c_int32]
     lib.fluid_solver_set_tuning.restype = c_int
+    lib.fluid_solver_step_backward.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int32]
+    lib.fluid_solver_step_backward.restype = c_int
+    lib.fluid_solver_record.argtypes = [c_void_p, c_int32, c_int32]
+    lib.fluid_solver_record.restype = c_int
+    lib.fluid_solver_backward.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int32]
+    lib.fluid_solver_backward.restype = c_int
     lib.fluid_kernel_name.argtypes = [c_int]
     lib.fluid_kernel_name.restype = c_char_p
     lib.fluid_solver_get_time.argtypes = [c_void_p, c_int32, POINTER(c_float)]

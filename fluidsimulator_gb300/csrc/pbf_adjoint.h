@@ -1,0 +1,34 @@
+// Launch interface of the adjoint kernels (pbf_adjoint.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "pbf_common.cuh"
+#include "pbf_launch.h"
+
+namespace fgb {
+
+struct AdjArgs {
+  StepArgs s;        // the recorded step: lists, scene constants, status
+  StepRecord rec;    // its internals
+  int iters;
+  float4* v2;        // committed velocity
+  float4* gx;        // cotangent of the committed positions (accumulates)
+  float4* gv;        // cotangent of the output velocity
+  float4* gv3;       // ... before restitution
+  float4* gp;        // cotangent of p^k
+  float4* gd;        // cotangent of the correction of iteration k
+  float4* gx0;       // cotangent of the input positions through the commit
+  float4* aux;       // (G_i, dL/dS_i) of the density constraint
+  float* grt;        // dL/drho_i (total)
+  float* grho;       // dL/drho_i from XSPH
+  float* cc;         // per-particle share of dL/dc (XSPH coefficient)
+  const float* g_pos_out;  // caller order, 3n floats: x block, y block, z block
+  const float* g_vel_out;
+  float* g_pos_in;
+  float* g_vel_in;
+};
+
+cudaError_t enqueue_adjoint(const AdjArgs& a, cudaStream_t stream);
+
+}  // namespace fgb

@@ -679,7 +679,7 @@ __device__ __forceinline__ void commit(const StepArgs& a, const SceneConst& c, i
 }
 
 template <int U>
-__global__ void __launch_bounds__(kMaxBlock) k_delta(StepArgs a, int in, int last, int to_v2, int rest) {
+__global__ void __launch_bounds__(kMaxBlock) k_delta(StepArgs a, int in, int last, int to_v2, int rest, float4* q_out) {
   if (failed(a.status)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
@@ -711,6 +711,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_delta(StepArgs a, int in, int las
   ax *= c.inv_density;
   ay *= c.inv_density;
   az *= c.inv_density;
+  if (q_out) q_out[i] = make_float4(p.x + ax, p.y + ay, p.z + az, 0.0f);  // recorded for the adjoint
   if (c.plane_count > 0) {  // core.cpp:372-393
     float qx = p.x + ax, qy = p.y + ay, qz = p.z + az;
     for (int q = 0; q < c.plane_count; ++q) {
@@ -954,7 +955,8 @@ void LaunchMarks::mark(int stage) {
   ++next;
 }
 
-cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t st, LaunchMarks& m) {
+cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t st, LaunchMarks& m,
+                         const StepRecord* rec) {
   const int nb = blocks_for(a.n, kBlock);
   m.start();
   k_bounds<<<nb, kBlock, 0, st>>>(a);
@@ -973,12 +975,19 @@ cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t s
   }
   k_reorder<<<nb, kBlock, 0, st>>>(a);
   m.mark(FLUID_KERNEL_REORDER);
+  const size_t n4 = sizeof(float4) * static_cast<size_t>(a.n);
+  const size_t n1 = sizeof(float) * static_cast<size_t>(a.n);
+  if (rec) {
+    cudaMemcpyAsync(rec->x0, a.x, n4, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(rec->p, a.p[0], n4, cudaMemcpyDeviceToDevice, st);
+  }
   const int bc = plan.block[FLUID_KERNEL_NBR_COUNT];
   k_nbr_count<<<blocks_for(a.n, bc), bc, 0, st>>>(a);
   m.mark(FLUID_KERNEL_NBR_COUNT);
   const int bf = plan.block[FLUID_KERNEL_NBR_FILL];
   k_nbr_fill<<<blocks_for(a.n, bf), bf, 0, st>>>(a);
   m.mark(FLUID_KERNEL_NBR_FILL);
+  if (rec && plan.iterations > 0) cudaMemcpyAsync(rec->lambda, a.lambda, n1, cudaMemcpyDeviceToDevice, st);
 
   const bool post = plan.xsph || plan.vorticity;
   const int to_v2 = plan.xsph ? 1 : 0;
@@ -993,13 +1002,20 @@ cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t s
       const int b = plan.block[FLUID_KERNEL_LAMBDA];
       FGB_DISPATCH_UNROLL(plan.unroll[FLUID_KERNEL_LAMBDA], k_lambda, blocks_for(a.n, b), b, st, a, in);
       m.mark(FLUID_KERNEL_LAMBDA);
+      if (rec)
+        cudaMemcpyAsync(rec->lambda + static_cast<size_t>(it) * a.n, a.lambda, n1, cudaMemcpyDeviceToDevice, st);
     }
     const int last = (it == plan.iterations - 1) ? 1 : 0;
     const int b = plan.block[FLUID_KERNEL_DELTA];
+    float4* q_out = rec ? rec->q + static_cast<size_t>(it) * a.n : nullptr;
     FGB_DISPATCH_UNROLL(plan.unroll[FLUID_KERNEL_DELTA], k_delta, blocks_for(a.n, b), b, st, a, in, last, to_v2,
-                        last ? rest_commit : 0);
+                        last ? rest_commit : 0, q_out);
     m.mark(FLUID_KERNEL_DELTA);
+    if (rec)  // p^(it+1); the last iteration's lands in x (commit)
+      cudaMemcpyAsync(rec->p + static_cast<size_t>(it + 1) * a.n, last ? a.x : a.p[in ^ 1], n4,
+                      cudaMemcpyDeviceToDevice, st);
   }
+  if (rec) cudaMemcpyAsync(rec->rho, a.rho, n1, cudaMemcpyDeviceToDevice, st);
   if (plan.xsph) {
     const int b = plan.block[FLUID_KERNEL_XSPH];
     FGB_DISPATCH_UNROLL(plan.unroll[FLUID_KERNEL_XSPH], k_xsph, blocks_for(a.n, b), b, st, a,

@@ -52,9 +52,23 @@ struct LaunchMarks {
   void mark(int stage);
 };
 
-// Enqueues one full timestep on `stream`.
+// Forward internals of one step kept for the adjoint (slot order of the
+// step's output): x0 input positions, p = p^0..p^K (K+1 blocks of n),
+// q = pre-projection positions of each iteration (K blocks), lambda (K
+// blocks), rho of the last lambda pass.
+struct StepRecord {
+  float4* x0 = nullptr;
+  float4* p = nullptr;
+  float4* q = nullptr;
+  float* lambda = nullptr;
+  float* rho = nullptr;
+};
+
+// Enqueues one full timestep on `stream`; with `rec`, also records the
+// internals the adjoint needs (device-to-device copies after the kernels).
 cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan,
-                         cudaStream_t stream, LaunchMarks& marks);
+                         cudaStream_t stream, LaunchMarks& marks,
+                         const StepRecord* rec = nullptr);
 
 // Packs caller-order SoA arrays (device) into slot-order x/v of one parity.
 cudaError_t enqueue_upload(const float* px, const float* py, const float* pz,

@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "fluid_gb300.h"
+#include "pbf_adjoint.h"
 #include "pbf_common.cuh"
 #include "pbf_launch.h"
 
@@ -206,6 +207,9 @@ class Solver {
     uploaded_ = false;
     build_scene_consts();
     plan_ = StepPlan();
+    checkpoints_.clear();
+    rec_steps_ = 0;
+    adj_n_ = 0;
     warps_ = (n_ + 31) / 32;
     tiles_ = std::max(1, (n_ + kRadixTile - 1) / kRadixTile);
     const size_t n = static_cast<size_t>(std::max(n_, 1));
@@ -479,6 +483,171 @@ class Solver {
     kernel_times(nullptr, nullptr, 0, 1);
     invalidate_graphs();
     return set_profiling(prof);
+  }
+
+  // ---- Adjoint -----------------------------------------------------------
+
+  // Vector-Jacobian product of the step the current state would take, all
+  // pointers on the device (3n floats: x, y, z blocks, caller order). The
+  // state, time and step count are left unchanged.
+  int vjp_device(const float* gpo, const float* gvo, float* gpi, float* gvi, std::vector<double>& gc) {
+    if (!uploaded_) return fail(FLUID_ERR_STATE, "no state uploaded");
+    if (plan_.vorticity)
+      return fail(FLUID_ERR_NOT_SUPPORTED, "the adjoint does not cover vorticity confinement");
+    int rc = synchronize();
+    if (rc) return rc;
+    gc.assign(S_, 0.0);
+    if (n_ == 0) return FLUID_OK;
+    if ((rc = ensure_adjoint_buffers())) return rc;
+    const int parity0 = parity_;
+    const long long steps0 = steps_;
+    const std::vector<float> times0 = times_;
+    rc = step(1);  // sizes the lists and the cell table for this state
+    parity_ = parity0;
+    steps_ = steps0;
+    times_ = times0;
+    if (rc) return rc;
+    StepRecord rec;
+    rec.x0 = rec_x0_.p;
+    rec.p = rec_p_.p;
+    rec.q = rec_q_.p;
+    rec.lambda = rec_lam_.p;
+    rec.rho = rec_rho_.p;
+    LaunchMarks m;
+    const StepArgs sa = args(parity_);
+    if (enqueue_step(sa, plan_, stream_, m, &rec) != cudaSuccess) return cuda_fail("record step");
+    launches_ += m.launches;
+    AdjArgs aa;
+    aa.s = sa;
+    aa.rec = rec;
+    aa.iters = plan_.iterations;
+    aa.v2 = a_v2_.p;
+    aa.gx = a_gx_.p;
+    aa.gv = a_gv_.p;
+    aa.gv3 = a_gv3_.p;
+    aa.gp = a_gp_.p;
+    aa.gd = a_gd_.p;
+    aa.gx0 = a_gx0_.p;
+    aa.aux = a_aux_.p;
+    aa.grt = a_grt_.p;
+    aa.grho = a_grho_.p;
+    aa.cc = a_cc_.p;
+    aa.g_pos_out = gpo;
+    aa.g_vel_out = gvo;
+    aa.g_pos_in = gpi;
+    aa.g_vel_in = gvi;
+    if (enqueue_adjoint(aa, stream_) != cudaSuccess) return cuda_fail("adjoint launch");
+    launches_ += 4 + 3ll * plan_.iterations;
+    if (cudaStreamSynchronize(stream_) != cudaSuccess) return cuda_fail("adjoint");
+    DevStatus st;
+    cudaMemcpy(&st, status_.p, sizeof(st), cudaMemcpyDeviceToHost);
+    enqueue_reset(status_.p, bmin_.p, bmax_.p, S_, stream_);
+    if (st.err) {
+      cudaStreamSynchronize(stream_);
+      return fail(st.err, "recorded step failed");
+    }
+    std::vector<float> cc(n_);
+    if (cudaMemcpy(cc.data(), a_cc_.p, sizeof(float) * n_, cudaMemcpyDeviceToHost) != cudaSuccess)
+      return cuda_fail("adjoint read");
+    for (int sc = 0; sc < S_; ++sc) {
+      double acc = 0.0;
+      for (int i = sc_host_[sc].first_slot; i < sc_host_[sc].first_slot + sc_host_[sc].count; ++i) acc += cc[i];
+      gc[sc] = acc;
+    }
+    return FLUID_OK;
+  }
+
+  int step_backward(const float* gpo, const float* gvo, float* gpi, float* gvi, float* gvisc, int memory) {
+    if (!gpo || !gvo || !gpi || !gvi) return fail(FLUID_ERR_INVALID_ARGUMENT, "null cotangent");
+    int rc = synchronize();
+    if (rc) return rc;
+    if ((rc = ensure_adjoint_buffers())) return rc;
+    const size_t b = 3 * static_cast<size_t>(n_) * sizeof(float);
+    float* io = a_io_.p;
+    const size_t m3 = 3 * static_cast<size_t>(n_);
+    const float *dpo = gpo, *dvo = gvo;
+    float *dpi = gpi, *dvi = gvi;
+    if (memory == FLUID_MEMORY_HOST) {
+      cudaMemcpy(io, gpo, b, cudaMemcpyHostToDevice);
+      cudaMemcpy(io + m3, gvo, b, cudaMemcpyHostToDevice);
+      dpo = io;
+      dvo = io + m3;
+      dpi = io + 2 * m3;
+      dvi = io + 3 * m3;
+    }
+    std::vector<double> gc;
+    if ((rc = vjp_device(dpo, dvo, dpi, dvi, gc))) return rc;
+    if (memory == FLUID_MEMORY_HOST) {
+      cudaMemcpy(gpi, dpi, b, cudaMemcpyDeviceToHost);
+      cudaMemcpy(gvi, dvi, b, cudaMemcpyDeviceToHost);
+    }
+    if (gvisc)
+      for (int sc = 0; sc < S_; ++sc) gvisc[sc] = static_cast<float>(gc[sc]);
+    return FLUID_OK;
+  }
+
+  // Forward nsteps from the current state keeping a snapshot every
+  // `every` steps, for backward().
+  int record(int nsteps, int every) {
+    if (!uploaded_) return fail(FLUID_ERR_STATE, "no state uploaded");
+    if (nsteps < 1 || every < 1) return fail(FLUID_ERR_INVALID_ARGUMENT, "nsteps and checkpoint interval must be >= 1");
+    int rc = synchronize();
+    if (rc) return rc;
+    checkpoints_.clear();
+    checkpoints_.resize((nsteps + every - 1) / every);
+    for (int t = 0; t < nsteps; ++t) {
+      if (t % every == 0 && (rc = snap_save(checkpoints_[t / every]))) return rc;
+      if ((rc = step(1))) return rc;
+    }
+    if ((rc = snap_save(final_))) return rc;
+    rec_steps_ = nsteps;
+    rec_every_ = every;
+    return FLUID_OK;
+  }
+
+  // Back-propagates the cotangent of the final recorded state to the state
+  // record() started from: each checkpoint segment is re-run forward to get
+  // its step inputs, then stepped back in reverse. Leaves the solver at the
+  // final state.
+  int backward(const float* gpf, const float* gvf, float* gpi, float* gvi, float* gvisc, int memory) {
+    if (rec_steps_ == 0) return fail(FLUID_ERR_STATE, "record() first");
+    if (!gpf || !gvf || !gpi || !gvi) return fail(FLUID_ERR_INVALID_ARGUMENT, "null cotangent");
+    int rc = synchronize();
+    if (rc) return rc;
+    if ((rc = ensure_adjoint_buffers())) return rc;
+    const size_t m3 = 3 * static_cast<size_t>(n_);
+    const size_t b = m3 * sizeof(float);
+    float* cur[2] = {a_io_.p, a_io_.p + m3};
+    float* nxt[2] = {a_io_.p + 2 * m3, a_io_.p + 3 * m3};
+    const cudaMemcpyKind in = memory == FLUID_MEMORY_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+    cudaMemcpy(cur[0], gpf, b, in);
+    cudaMemcpy(cur[1], gvf, b, in);
+    std::vector<double> total(S_, 0.0), gc;
+    const int segs = static_cast<int>(checkpoints_.size());
+    for (int seg = segs - 1; seg >= 0; --seg) {
+      const int t0 = seg * rec_every_;
+      const int t1 = std::min(rec_steps_, t0 + rec_every_);
+      if ((rc = snap_load(checkpoints_[seg]))) return rc;
+      std::vector<Snap> states(t1 - t0);
+      for (int t = t0; t < t1; ++t) {
+        if ((rc = snap_save(states[t - t0]))) return rc;
+        if (t + 1 < t1 && (rc = step(1))) return rc;
+      }
+      for (int t = t1 - 1; t >= t0; --t) {
+        if ((rc = snap_load(states[t - t0]))) return rc;
+        if ((rc = vjp_device(cur[0], cur[1], nxt[0], nxt[1], gc))) return rc;
+        for (int sc = 0; sc < S_; ++sc) total[sc] += gc[sc];
+        std::swap(cur[0], nxt[0]);
+        std::swap(cur[1], nxt[1]);
+      }
+    }
+    if ((rc = snap_load(final_))) return rc;
+    const cudaMemcpyKind out = memory == FLUID_MEMORY_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    cudaMemcpy(gpi, cur[0], b, out);
+    cudaMemcpy(gvi, cur[1], b, out);
+    if (gvisc)
+      for (int sc = 0; sc < S_; ++sc) gvisc[sc] = static_cast<float>(total[sc]);
+    return FLUID_OK;
   }
 
   int get_tuning(int32_t* unroll, int32_t* block, int kernels) {
@@ -818,6 +987,69 @@ class Solver {
     return FLUID_OK;
   }
 
+  struct Snap {
+    DBuf<float4> x, v;
+    DBuf<int> slot;
+    DBuf<float> rho;
+    std::vector<float> times;
+    long long steps = 0;
+  };
+
+  int snap_save(Snap& sn) {
+    const size_t n = static_cast<size_t>(std::max(n_, 1));
+    if (sn.x.n != n) {
+      if (sn.x.alloc(n) || sn.v.alloc(n) || sn.slot.alloc(n) || sn.rho.alloc(n))
+        return fail(FLUID_ERR_OUT_OF_MEMORY, "snapshot");
+    }
+    cudaMemcpyAsync(sn.x.p, x_[parity_].p, n * sizeof(float4), cudaMemcpyDeviceToDevice, stream_);
+    cudaMemcpyAsync(sn.v.p, v_[parity_].p, n * sizeof(float4), cudaMemcpyDeviceToDevice, stream_);
+    cudaMemcpyAsync(sn.slot.p, slot_[parity_].p, n * sizeof(int), cudaMemcpyDeviceToDevice, stream_);
+    cudaMemcpyAsync(sn.rho.p, rho_[parity_].p, n * sizeof(float), cudaMemcpyDeviceToDevice, stream_);
+    sn.times = times_;
+    sn.steps = steps_;
+    return cudaStreamSynchronize(stream_) == cudaSuccess ? FLUID_OK : cuda_fail("snapshot");
+  }
+
+  int snap_load(const Snap& sn) {
+    const size_t n = static_cast<size_t>(std::max(n_, 1));
+    cudaMemcpyAsync(x_[parity_].p, sn.x.p, n * sizeof(float4), cudaMemcpyDeviceToDevice, stream_);
+    cudaMemcpyAsync(v_[parity_].p, sn.v.p, n * sizeof(float4), cudaMemcpyDeviceToDevice, stream_);
+    cudaMemcpyAsync(slot_[parity_].p, sn.slot.p, n * sizeof(int), cudaMemcpyDeviceToDevice, stream_);
+    cudaMemcpyAsync(rho_[parity_].p, sn.rho.p, n * sizeof(float), cudaMemcpyDeviceToDevice, stream_);
+    times_ = sn.times;
+    steps_ = sn.steps;
+    return cudaStreamSynchronize(stream_) == cudaSuccess ? FLUID_OK : cuda_fail("restore");
+  }
+
+  int ensure_adjoint_buffers() {
+    const size_t n = static_cast<size_t>(std::max(n_, 1));
+    const int k = plan_.iterations;
+    if (adj_n_ == n && adj_k_ == k) return FLUID_OK;
+    const size_t kk = static_cast<size_t>(std::max(k, 1));
+    bool ok = rec_x0_.alloc(n) == cudaSuccess && rec_p_.alloc((k + 1) * n) == cudaSuccess &&
+              rec_q_.alloc(kk * n) == cudaSuccess && rec_lam_.alloc(kk * n) == cudaSuccess &&
+              rec_rho_.alloc(n) == cudaSuccess && a_v2_.alloc(n) == cudaSuccess && a_gx_.alloc(n) == cudaSuccess &&
+              a_gv_.alloc(n) == cudaSuccess && a_gv3_.alloc(n) == cudaSuccess && a_gp_.alloc(n) == cudaSuccess &&
+              a_gd_.alloc(n) == cudaSuccess && a_gx0_.alloc(n) == cudaSuccess && a_aux_.alloc(n) == cudaSuccess &&
+              a_grt_.alloc(n) == cudaSuccess && a_grho_.alloc(n) == cudaSuccess && a_cc_.alloc(n) == cudaSuccess &&
+              a_io_.alloc(12 * n) == cudaSuccess;
+    if (!ok) {
+      adj_n_ = 0;
+      return fail(FLUID_ERR_OUT_OF_MEMORY, "adjoint buffers");
+    }
+    adj_n_ = n;
+    adj_k_ = k;
+    return FLUID_OK;
+  }
+
+  DBuf<float4> rec_x0_, rec_p_, rec_q_, a_v2_, a_gx_, a_gv_, a_gv3_, a_gp_, a_gd_, a_gx0_, a_aux_;
+  DBuf<float> rec_lam_, rec_rho_, a_grt_, a_grho_, a_cc_, a_io_;
+  size_t adj_n_ = 0;
+  int adj_k_ = -1;
+  std::vector<Snap> checkpoints_;
+  Snap final_;
+  int rec_steps_ = 0, rec_every_ = 1;
+
   int device_;
   cudaStream_t own_ = nullptr, stream_ = nullptr;
   int S_ = 0, n_ = 0, warps_ = 0, tiles_ = 1;
@@ -1021,6 +1253,23 @@ int fluid_solver_get_tuning(fluid_solver* s, int32_t* unroll, int32_t* block, in
 int fluid_solver_set_tuning(fluid_solver* s, const int32_t* unroll, const int32_t* block, int32_t kernels) {
   FLUID_CHECK_SOLVER(s);
   return s->impl.set_tuning(unroll, block, kernels);
+}
+
+int fluid_solver_step_backward(fluid_solver* s, const float* g_pos_out, const float* g_vel_out, float* g_pos_in,
+                               float* g_vel_in, float* g_visc_c, int32_t memory) {
+  FLUID_CHECK_SOLVER(s);
+  return s->impl.step_backward(g_pos_out, g_vel_out, g_pos_in, g_vel_in, g_visc_c, memory);
+}
+
+int fluid_solver_record(fluid_solver* s, int32_t nsteps, int32_t checkpoint_every) {
+  FLUID_CHECK_SOLVER(s);
+  return s->impl.record(nsteps, checkpoint_every);
+}
+
+int fluid_solver_backward(fluid_solver* s, const float* g_pos_final, const float* g_vel_final, float* g_pos_initial,
+                          float* g_vel_initial, float* g_visc_c, int32_t memory) {
+  FLUID_CHECK_SOLVER(s);
+  return s->impl.backward(g_pos_final, g_vel_final, g_pos_initial, g_vel_initial, g_visc_c, memory);
 }
 
 int fluid_solver_get_time(fluid_solver* s, int32_t scene, float* time) {

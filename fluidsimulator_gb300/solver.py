@@ -172,6 +172,37 @@ class Solver:
                 u[k], b[k] = shape["unroll"], shape["block"]
         self._check(self.lib.fluid_solver_set_tuning(self.h, u, b, n))
 
+    def _cot(self, a):
+        a = np.ascontiguousarray(a, dtype=np.float32).reshape(3, self.n)
+        return a
+
+    def step_backward(self, g_pos_out, g_vel_out):
+        """VJP of the step the current state would take (state unchanged).
+        Returns (g_pos_in, g_vel_in, g_visc_c per scene)."""
+        gpo, gvo = self._cot(g_pos_out), self._cot(g_vel_out)
+        gpi = np.zeros((3, self.n), np.float32)
+        gvi = np.zeros((3, self.n), np.float32)
+        gc = np.zeros(max(1, len(self.counts)), np.float32)
+        self._check(self.lib.fluid_solver_step_backward(self.h, gpo.ctypes.data_as(c_void_p),
+                                                        gvo.ctypes.data_as(c_void_p), gpi.ctypes.data_as(c_void_p),
+                                                        gvi.ctypes.data_as(c_void_p), gc.ctypes.data_as(c_void_p),
+                                                        _capi.MEMORY_HOST))
+        return gpi, gvi, gc
+
+    def record(self, nsteps: int, checkpoint_every: int) -> None:
+        self._check(self.lib.fluid_solver_record(self.h, nsteps, checkpoint_every))
+
+    def backward(self, g_pos_final, g_vel_final):
+        """dL/d(initial state) and dL/d(visc_c) of the last record()."""
+        gpf, gvf = self._cot(g_pos_final), self._cot(g_vel_final)
+        gpi = np.zeros((3, self.n), np.float32)
+        gvi = np.zeros((3, self.n), np.float32)
+        gc = np.zeros(max(1, len(self.counts)), np.float32)
+        self._check(self.lib.fluid_solver_backward(self.h, gpf.ctypes.data_as(c_void_p), gvf.ctypes.data_as(c_void_p),
+                                                   gpi.ctypes.data_as(c_void_p), gvi.ctypes.data_as(c_void_p),
+                                                   gc.ctypes.data_as(c_void_p), _capi.MEMORY_HOST))
+        return gpi, gvi, gc
+
     def read_debug(self, what: int) -> np.ndarray:
         if what == _capi.DEBUG_CELL_KEYS:
             out = np.empty((self.n, 3), np.int32)

@@ -242,6 +242,35 @@ int fluid_solver_get_tuning(fluid_solver* solver, int32_t* unroll, int32_t* bloc
 int fluid_solver_set_tuning(fluid_solver* solver, const int32_t* unroll,
                             const int32_t* block, int32_t kernels);
 
+/*
+ * Reverse-mode derivative (no reference counterpart: the reference has no
+ * adjoint). Cotangent arrays hold 3 * particles floats in caller order: all
+ * x, then all y, then all z. Neighbour sets and every branch (r < h, the
+ * 0.01 h clamp, plane contacts, restitution's vn < 0) are held at the forward
+ * step's values. Vorticity confinement is not differentiated
+ * (FLUID_ERR_NOT_SUPPORTED when a scene enables it).
+ *
+ * fluid_solver_step_backward: vector-Jacobian product of the step the current
+ * state would take: given dL/d(positions, velocities) after that step, writes
+ * dL/d(positions, velocities) of the current state and dL/d(visc_c) per scene
+ * (g_visc_c, scene_count floats, may be NULL). The state, time and step
+ * count are unchanged; the step is recomputed internally.
+ */
+int fluid_solver_step_backward(fluid_solver* solver, const float* g_pos_out,
+                               const float* g_vel_out, float* g_pos_in,
+                               float* g_vel_in, float* g_visc_c, int32_t memory);
+
+/* Runs nsteps forward from the current state keeping a state snapshot every
+ * checkpoint_every steps (for fluid_solver_backward); leaves the final state. */
+int fluid_solver_record(fluid_solver* solver, int32_t nsteps, int32_t checkpoint_every);
+
+/* Back-propagates dL/d(final state) of the last record() to dL/d(the state
+ * record() started from) and dL/d(visc_c): each checkpoint segment is
+ * recomputed forward, then stepped back in reverse. Leaves the final state. */
+int fluid_solver_backward(fluid_solver* solver, const float* g_pos_final,
+                          const float* g_vel_final, float* g_pos_initial,
+                          float* g_vel_initial, float* g_visc_c, int32_t memory);
+
 /* Time of scene `scene` (float, accumulated as State::time, core.cpp:614). */
 int fluid_solver_get_time(fluid_solver* solver, int32_t scene, float* time);
 int fluid_solver_set_time(fluid_solver* solver, int32_t scene, float time);

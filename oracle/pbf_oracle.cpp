@@ -225,6 +225,26 @@ void build_pair_lists(Workspace<T>& w, std::size_t n, T h2) {
   }
 }
 
+// Forward internals of one step, for the adjoint (SoA blocks: x | y | z).
+template <typename T>
+struct Record {
+  std::size_t n = 0;
+  int iters = 0;
+  bool vorticity = false;
+  std::vector<T> x0, x1, v2, rho;          // input x, committed x, committed v, last rho
+  std::vector<std::vector<T>> P, Q, LAM;   // p^k (iters+1), pre-projection q^k (iters), lambda^k (iters)
+  std::vector<int> nbr;
+  std::vector<int64_t> nbr_begin;
+};
+
+template <typename T>
+void put3(std::vector<T>& dst, std::size_t n, const T* a, const T* b, const T* c) {
+  dst.resize(3 * n);
+  std::copy(a, a + n, dst.begin());
+  std::copy(b, b + n, dst.begin() + n);
+  std::copy(c, c + n, dst.begin() + 2 * n);
+}
+
 template <typename T>
 struct Dump {
   int32_t* cell_keys;
@@ -237,7 +257,7 @@ struct Dump {
 template <typename T>
 int step(Workspace<T>& w, const fluid_params& p, std::size_t n, T* X, T* Y,
          T* Z, T* VX, T* VY, T* VZ, T* time, const Dump<T>* dump,
-         int64_t* pairs_out, int32_t* max_out) {
+         int64_t* pairs_out, int32_t* max_out, Record<T>* rec = nullptr) {
   w.resize(n);
   if (n == 0) {  // core.cpp:122-125
     *time += T(p.dt);
@@ -248,6 +268,16 @@ int step(Workspace<T>& w, const fluid_params& p, std::size_t n, T* X, T* Y,
   const T fx = T(p.external_force[0]), fy = T(p.external_force[1]),
           fz = T(p.external_force[2]);
   const long long N = static_cast<long long>(n);
+
+  if (rec) {
+    rec->n = n;
+    rec->iters = p.solver_iterations;
+    rec->vorticity = p.enable_vorticity && p.vort_epsilon != 0.0f;
+    put3(rec->x0, n, X, Y, Z);
+    rec->P.assign(p.solver_iterations + 1, {});
+    rec->Q.assign(p.solver_iterations, std::vector<T>(3 * n));
+    rec->LAM.assign(p.solver_iterations, {});
+  }
 
   // Predict (core.cpp:150-161).
 #pragma omp parallel for
@@ -265,6 +295,11 @@ int step(Workspace<T>& w, const fluid_params& p, std::size_t n, T* X, T* Y,
     build_grid_lists(w, n, h, h2);
   } else {
     build_pair_lists(w, n, h2);
+  }
+  if (rec) {
+    put3(rec->P[0], n, w.px.data(), w.py.data(), w.pz.data());
+    rec->nbr = w.nbr;
+    rec->nbr_begin = w.nbr_begin;
   }
 
   // Jacobi iterations (core.cpp:276-408).
@@ -304,6 +339,7 @@ int step(Workspace<T>& w, const fluid_params& p, std::size_t n, T* X, T* Y,
       sum_g2 += ix * ix + iy * iy + iz * iz;
       w.lambda[i] = -C / (sum_g2 + c.epsilon);
     }
+    if (rec) rec->LAM[iter] = w.lambda;
 
     // Position correction with s_corr and plane projection (core.cpp:334-398).
 #pragma omp parallel for
@@ -334,6 +370,11 @@ int step(Workspace<T>& w, const fluid_params& p, std::size_t n, T* X, T* Y,
       ax *= c.inv_density;
       ay *= c.inv_density;
       az *= c.inv_density;
+      if (rec) {
+        rec->Q[iter][i] = xi + ax;
+        rec->Q[iter][n + i] = yi + ay;
+        rec->Q[iter][2 * n + i] = zi + az;
+      }
       if (p.plane_count > 0) {
         T qx = xi + ax, qy = yi + ay, qz = zi + az;
         for (int q = 0; q < p.plane_count; ++q) {
@@ -361,7 +402,9 @@ int step(Workspace<T>& w, const fluid_params& p, std::size_t n, T* X, T* Y,
       w.py[i] += w.dy[i];
       w.pz[i] += w.dz[i];
     }
+    if (rec) put3(rec->P[iter + 1], n, w.px.data(), w.py.data(), w.pz.data());
   }
+  if (rec) rec->rho = w.rho;
 
   // Commit (core.cpp:410-421).
 #pragma omp parallel for
@@ -372,6 +415,10 @@ int step(Workspace<T>& w, const fluid_params& p, std::size_t n, T* X, T* Y,
     X[i] = w.px[i];
     Y[i] = w.py[i];
     Z[i] = w.pz[i];
+  }
+  if (rec) {
+    put3(rec->x1, n, X, Y, Z);
+    put3(rec->v2, n, VX, VY, VZ);
   }
 
   // XSPH viscosity over the step's lists at committed positions (core.cpp:423-466).
@@ -540,6 +587,255 @@ int step(Workspace<T>& w, const fluid_params& p, std::size_t n, T* X, T* Y,
   return 0;
 }
 
+template <typename A, typename B>
+Record<B> convert_record(const Record<A>& r) {
+  Record<B> o;
+  o.n = r.n;
+  o.iters = r.iters;
+  o.vorticity = r.vorticity;
+  auto cv = [](const std::vector<A>& v) { return std::vector<B>(v.begin(), v.end()); };
+  o.x0 = cv(r.x0);
+  o.x1 = cv(r.x1);
+  o.v2 = cv(r.v2);
+  o.rho = cv(r.rho);
+  for (const auto& v : r.P) o.P.push_back(cv(v));
+  for (const auto& v : r.Q) o.Q.push_back(cv(v));
+  for (const auto& v : r.LAM) o.LAM.push_back(cv(v));
+  o.nbr = r.nbr;
+  o.nbr_begin = r.nbr_begin;
+  return o;
+}
+
+// Reverse-mode derivative of one recorded step. Given the cotangents of the
+// step's outputs (positions gxo, velocities gvo; SoA 3n), accumulates those of
+// its inputs (gxi, gvi) and of the XSPH coefficient (*gc). Neighbour sets and
+// every branch (r < h, the min_r clamp, plane contacts, restitution's
+// vn < 0) are held at the recorded forward's values. Membership is symmetric
+// (r^2 of (i, j) and (j, i) are the same float), so each transposed sum is a
+// gather over i's own list.
+template <typename T>
+int adjoint(const Record<T>& R, const fluid_params& p, const T* gxo, const T* gvo, T* gxi, T* gvi, T* gc) {
+  if (R.vorticity) return FLUID_ERR_NOT_SUPPORTED;
+  const std::size_t n = R.n;
+  const long long N = static_cast<long long>(n);
+  const int K = R.iters;
+  const Consts<T> c = make_consts<T>(p);
+  const T h = c.h, h2 = c.h2, dt = c.dt, m = c.mass, gs = c.grad_scale, ir = c.inv_density;
+  const T pi = Pi<T>::value;
+  const T h2_ = h * h, h4 = h2_ * h2_, h9 = h4 * h4 * h;
+  const T c6 = T(315) / (T(64) * pi * h9);
+  const T csp = T(-45) / (pi * h2_ * h2_ * h2_);
+  const T W0 = c6 * h2 * h2 * h2;
+  const bool scorr = c.scorr && c.scorr_inv_wdq > T(0);
+  const T nk = -c.scorr_k, iw = c.scorr_inv_wdq;
+  const int sn = c.scorr_n;
+  const bool xsph = p.enable_xsph && p.visc_c != 0.0f;
+  const T cv = T(p.visc_c);
+  const bool rest = (p.plane_restitution > 0.0f || p.plane_friction > 0.0f) && p.plane_count > 0;
+  const T e = T(p.plane_restitution), mu_s = T(1) - T(p.plane_friction);
+  auto W = [&](T r2) { const T d = h2 - r2; return c6 * d * d * d; };
+  auto dW = [&](T r2) { const T d = h2 - r2; return T(-3) * c6 * d * d; };
+  auto F = [&](T r) { const T d = h - r; return csp * d * d; };
+  auto dF = [&](T r) { return T(-2) * csp * (h - r); };
+  auto powr = [&](T x, int k) { T y = T(1); for (int q = 0; q < k; ++q) y *= x; return y; };
+  auto at = [n](const std::vector<T>& a, std::size_t i, int d) { return a[d * n + i]; };
+
+  std::vector<T> gx1(gxo, gxo + 3 * n), gv3(3 * n), gv2(3 * n), dv(3 * n, T(0)), grho(n, T(0));
+  std::vector<T> aj(n);
+  for (std::size_t i = 0; i < n; ++i) aj[i] = (R.rho[i] > T(0)) ? m / R.rho[i] : T(0);
+
+  // XSPH sums, then restitution reversed (core.cpp:423-466, 573-612).
+#pragma omp parallel for
+  for (long long ii = 0; ii < N; ++ii) {
+    const std::size_t i = static_cast<std::size_t>(ii);
+    T s[3] = {0, 0, 0};
+    if (xsph) {
+      for (int64_t k = R.nbr_begin[i]; k < R.nbr_begin[i + 1]; ++k) {
+        const std::size_t j = static_cast<std::size_t>(R.nbr[k]);
+        T d[3], r2 = 0;
+        for (int a = 0; a < 3; ++a) { d[a] = at(R.x1, i, a) - at(R.x1, j, a); r2 += d[a] * d[a]; }
+        if (r2 < h2) {
+          const T w = W(r2);
+          for (int a = 0; a < 3; ++a) s[a] += (at(R.v2, j, a) - at(R.v2, i, a)) * w * aj[j];
+        }
+      }
+    }
+    T v[3], g[3];
+    for (int a = 0; a < 3; ++a) {
+      dv[a * n + i] = s[a];
+      v[a] = at(R.v2, i, a) + cv * s[a];
+      g[a] = gvo[a * n + i];
+    }
+    if (rest) {
+      bool act[FLUID_MAX_PLANES];
+      T sc[FLUID_MAX_PLANES];
+      for (int q = 0; q < p.plane_count; ++q) {
+        const T nq[3] = {T(p.plane_nx[q]), T(p.plane_ny[q]), T(p.plane_nz[q])};
+        const T sd = nq[0] * at(R.x1, i, 0) + nq[1] * at(R.x1, i, 1) + nq[2] * at(R.x1, i, 2) - T(p.plane_d[q]);
+        act[q] = sd <= T(0);
+        if (act[q]) {
+          const T vn = nq[0] * v[0] + nq[1] * v[1] + nq[2] * v[2];
+          sc[q] = (vn < T(0)) ? -e : T(1);
+          for (int a = 0; a < 3; ++a) v[a] = (v[a] - vn * nq[a]) * mu_s + sc[q] * vn * nq[a];
+        }
+      }
+      for (int q = p.plane_count - 1; q >= 0; --q) {
+        if (!act[q]) continue;
+        const T nq[3] = {T(p.plane_nx[q]), T(p.plane_ny[q]), T(p.plane_nz[q])};
+        const T gn = nq[0] * g[0] + nq[1] * g[1] + nq[2] * g[2];
+        for (int a = 0; a < 3; ++a) g[a] = mu_s * g[a] + (sc[q] - mu_s) * gn * nq[a];
+      }
+    }
+    for (int a = 0; a < 3; ++a) gv3[a * n + i] = g[a];
+  }
+  if (xsph) {
+    T acc = 0;
+    for (std::size_t i = 0; i < 3 * n; ++i) acc += gv3[i] * dv[i];
+    *gc += cv == T(0) ? T(0) : acc;
+  }
+
+  // XSPH reversed.
+#pragma omp parallel for
+  for (long long ii = 0; ii < N; ++ii) {
+    const std::size_t i = static_cast<std::size_t>(ii);
+    T g2[3], gx[3] = {0, 0, 0}, rsum = 0;
+    for (int a = 0; a < 3; ++a) g2[a] = gv3[a * n + i];
+    if (xsph) {
+      T wsum = 0, vsum[3] = {0, 0, 0};
+      for (int64_t k = R.nbr_begin[i]; k < R.nbr_begin[i + 1]; ++k) {
+        const std::size_t j = static_cast<std::size_t>(R.nbr[k]);
+        T d[3], r2 = 0;
+        for (int a = 0; a < 3; ++a) { d[a] = at(R.x1, i, a) - at(R.x1, j, a); r2 += d[a] * d[a]; }
+        if (!(r2 < h2)) continue;
+        const T w = W(r2), w1 = dW(r2);
+        T ti = 0, tj = 0, tr = 0;
+        for (int a = 0; a < 3; ++a) {
+          const T dvij = at(R.v2, j, a) - at(R.v2, i, a);
+          ti += dvij * gv3[a * n + i];
+          tj += -dvij * gv3[a * n + j];
+          tr += -dvij * gv3[a * n + j];
+        }
+        wsum += w * aj[j];
+        for (int a = 0; a < 3; ++a) vsum[a] += w * gv3[a * n + j];
+        const T coef = T(2) * w1 * cv * (aj[j] * ti + aj[i] * tj);
+        for (int a = 0; a < 3; ++a) gx[a] += coef * d[a];
+        rsum += w * tr;
+      }
+      for (int a = 0; a < 3; ++a) g2[a] = gv3[a * n + i] - cv * wsum * gv3[a * n + i] + cv * aj[i] * vsum[a];
+      grho[i] = (R.rho[i] > T(0)) ? -(m / (R.rho[i] * R.rho[i])) * cv * rsum : T(0);
+    }
+    for (int a = 0; a < 3; ++a) {
+      gv2[a * n + i] = g2[a];
+      gx1[a * n + i] += gx[a];
+    }
+  }
+
+  // Commit reversed: v2 = (p^K - x0)/dt, x1 = p^K.
+  std::vector<T> gP(3 * n), gx0(3 * n), gD(3 * n), gL(n), G(3 * n), gS(n), gRT(n);
+  for (std::size_t i = 0; i < 3 * n; ++i) {
+    gP[i] = gx1[i] + gv2[i] / dt;
+    gx0[i] = -gv2[i] / dt;
+  }
+
+  for (int it = K - 1; it >= 0; --it) {
+    const auto& P = R.P[it];
+    const auto& Q = R.Q[it];
+    const auto& L = R.LAM[it];
+    // Plane projection reversed (core.cpp:372-393): q -> q + n max(0, -(n.q - d)).
+#pragma omp parallel for
+    for (long long ii = 0; ii < N; ++ii) {
+      const std::size_t i = static_cast<std::size_t>(ii);
+      T q[3] = {at(Q, i, 0), at(Q, i, 1), at(Q, i, 2)}, g[3];
+      for (int a = 0; a < 3; ++a) g[a] = gP[a * n + i];
+      bool act[FLUID_MAX_PLANES];
+      for (int k = 0; k < p.plane_count; ++k) {
+        const T nq[3] = {T(p.plane_nx[k]), T(p.plane_ny[k]), T(p.plane_nz[k])};
+        const T pen = -(nq[0] * q[0] + nq[1] * q[1] + nq[2] * q[2] - T(p.plane_d[k]));
+        act[k] = pen > T(0);
+        if (act[k]) for (int a = 0; a < 3; ++a) q[a] += nq[a] * pen;
+      }
+      for (int k = p.plane_count - 1; k >= 0; --k) {
+        if (!act[k]) continue;
+        const T nq[3] = {T(p.plane_nx[k]), T(p.plane_ny[k]), T(p.plane_nz[k])};
+        const T gn = nq[0] * g[0] + nq[1] * g[1] + nq[2] * g[2];
+        for (int a = 0; a < 3; ++a) g[a] -= gn * nq[a];
+      }
+      for (int a = 0; a < 3; ++a) gD[a * n + i] = g[a];
+    }
+    // Position correction reversed (core.cpp:334-370) and lambda recomputed.
+#pragma omp parallel for
+    for (long long ii = 0; ii < N; ++ii) {
+      const std::size_t i = static_cast<std::size_t>(ii);
+      T gp[3], gl = 0, rs = 0, Gi[3] = {0, 0, 0}, s1 = 0;
+      for (int a = 0; a < 3; ++a) gp[a] = gD[a * n + i];
+      for (int64_t k = R.nbr_begin[i]; k < R.nbr_begin[i + 1]; ++k) {
+        const std::size_t j = static_cast<std::size_t>(R.nbr[k]);
+        T d[3], r2 = 0;
+        for (int a = 0; a < 3; ++a) { d[a] = at(P, i, a) - at(P, j, a); r2 += d[a] * d[a]; }
+        if (!(r2 < h2)) continue;
+        const bool clamp = r2 < c.min_r2;
+        const T r = std::sqrt(clamp ? c.min_r2 : r2);
+        const T f = F(r), fpr = clamp ? T(0) : dF(r) / r;
+        T s = L[i] + L[j], alpha = s * fpr;
+        if (scorr) {
+          const T x = W(r2) * iw;
+          s += nk * powr(x, sn);
+          alpha = s * fpr + T(2) * f * nk * T(sn) * powr(x, sn - 1) * iw * dW(r2);
+        }
+        T de = 0;
+        for (int a = 0; a < 3; ++a) de += d[a] * (gD[a * n + i] - gD[a * n + j]);
+        for (int a = 0; a < 3; ++a) gp[a] += ir * (s * f * (gD[a * n + i] - gD[a * n + j]) + alpha * de * d[a]);
+        gl += ir * f * de;
+        rs += W(r2);
+        for (int a = 0; a < 3; ++a) Gi[a] += f * d[a];
+        s1 += f * f * r2;
+      }
+      const T rho = m * (rs + W0);
+      const T C = rho * ir - T(1);
+      const T S = gs * gs * (s1 + Gi[0] * Gi[0] + Gi[1] * Gi[1] + Gi[2] * Gi[2]);
+      const T lam = -C / (S + c.epsilon);
+      const T gC = -gl / (S + c.epsilon);
+      gS[i] = -gl * lam / (S + c.epsilon);
+      gRT[i] = (it == K - 1 ? grho[i] : T(0)) + gC * ir;
+      for (int a = 0; a < 3; ++a) {
+        G[a * n + i] = Gi[a];
+        gP[a * n + i] = gp[a];  // partial: direct + correction terms; lambda terms next
+      }
+      gL[i] = gl;
+    }
+    // Lambda reversed (core.cpp:281-329), gathered over i's list.
+#pragma omp parallel for
+    for (long long ii = 0; ii < N; ++ii) {
+      const std::size_t i = static_cast<std::size_t>(ii);
+      T add[3] = {0, 0, 0};
+      for (int64_t k = R.nbr_begin[i]; k < R.nbr_begin[i + 1]; ++k) {
+        const std::size_t j = static_cast<std::size_t>(R.nbr[k]);
+        T d[3], r2 = 0;
+        for (int a = 0; a < 3; ++a) { d[a] = at(P, i, a) - at(P, j, a); r2 += d[a] * d[a]; }
+        if (!(r2 < h2)) continue;
+        const bool clamp = r2 < c.min_r2;
+        const T r = std::sqrt(clamp ? c.min_r2 : r2);
+        const T f = F(r), fpr = clamp ? T(0) : dF(r) / r;
+        T dGi = 0, dGj = 0;
+        for (int a = 0; a < 3; ++a) { dGi += d[a] * G[a * n + i]; dGj += d[a] * G[a * n + j]; }
+        const T t1 = T(2) * m * dW(r2) * (gRT[i] + gRT[j]);
+        const T t2 = gs * gs * (gS[i] + gS[j]) * (T(2) * f * fpr * r2 + T(2) * f * f);
+        const T t4 = T(2) * gs * gs * fpr * (gS[i] * dGi - gS[j] * dGj);
+        for (int a = 0; a < 3; ++a)
+          add[a] += (t1 + t2 + t4) * d[a] + T(2) * f * gs * gs * (gS[i] * G[a * n + i] - gS[j] * G[a * n + j]);
+      }
+      for (int a = 0; a < 3; ++a) gP[a * n + i] += add[a];
+    }
+  }
+
+  // Predict reversed: p^0 = x0 + (v + f dt) dt.
+  for (std::size_t i = 0; i < 3 * n; ++i) {
+    gxi[i] += gx0[i] + gP[i];
+    gvi[i] += gP[i] * dt;
+  }
+  return FLUID_OK;
+}
+
 bool params_ok(const fluid_params* p) {
   return p && p->plane_count >= 0 && p->plane_count <= FLUID_MAX_PLANES &&
          p->solver_iterations >= 0;
@@ -635,6 +931,44 @@ int pbf_oracle_run_f64(void* ws, const fluid_params* p, int64_t count,
     }
   }
   return FLUID_OK;
+}
+
+// One step's vector-Jacobian product. Runs the forward step from (x, v)
+// (SoA 3n each) in float (fwd32 != 0, the trajectory the GPU computes) or
+// double, writes its outputs to (x_out, v_out) (same type as the forward),
+// then back-propagates the cotangents (gx_out, gv_out) in double arithmetic,
+// adding into gx_in, gv_in and *gc (XSPH coefficient).
+int pbf_oracle_vjp(const fluid_params* p, int64_t count, int32_t fwd32, const void* x, const void* v,
+                   void* x_out, void* v_out, const double* gx_out, const double* gv_out, double* gx_in,
+                   double* gv_in, double* gc) {
+  if (!params_ok(p) || count < 0) return FLUID_ERR_INVALID_ARGUMENT;
+  const std::size_t n = static_cast<std::size_t>(count);
+  Record<double> rd;
+  if (fwd32) {
+    Workspace<float> w;
+    std::vector<float> s(6 * n);
+    std::copy(static_cast<const float*>(x), static_cast<const float*>(x) + 3 * n, s.begin());
+    std::copy(static_cast<const float*>(v), static_cast<const float*>(v) + 3 * n, s.begin() + 3 * n);
+    float t = 0.0f;
+    Record<float> rf;
+    step<float>(w, *p, n, s.data(), s.data() + n, s.data() + 2 * n, s.data() + 3 * n, s.data() + 4 * n,
+                s.data() + 5 * n, &t, nullptr, nullptr, nullptr, &rf);
+    if (x_out) std::copy(s.begin(), s.begin() + 3 * n, static_cast<float*>(x_out));
+    if (v_out) std::copy(s.begin() + 3 * n, s.end(), static_cast<float*>(v_out));
+    rd = convert_record<float, double>(rf);
+  } else {
+    Workspace<double> w;
+    std::vector<double> s(6 * n);
+    std::copy(static_cast<const double*>(x), static_cast<const double*>(x) + 3 * n, s.begin());
+    std::copy(static_cast<const double*>(v), static_cast<const double*>(v) + 3 * n, s.begin() + 3 * n);
+    double t = 0.0;
+    step<double>(w, *p, n, s.data(), s.data() + n, s.data() + 2 * n, s.data() + 3 * n, s.data() + 4 * n,
+                 s.data() + 5 * n, &t, nullptr, nullptr, nullptr, &rd);
+    if (x_out) std::copy(s.begin(), s.begin() + 3 * n, static_cast<double*>(x_out));
+    if (v_out) std::copy(s.begin() + 3 * n, s.end(), static_cast<double*>(v_out));
+  }
+  if (n == 0) return FLUID_OK;
+  return adjoint<double>(rd, *p, gx_out, gv_out, gx_in, gv_in, gc);
 }
 
 }  // extern "C"

@@ -227,3 +227,31 @@ def ref_load_scene(path: str):
     if rc != 0:
         raise ValueError(err.value.decode())
     return p, pos, vel
+
+
+def vjp(params: FluidParams, pos, vel, gx_out, gv_out, fwd32: bool = False):
+    """One step's vector-Jacobian product by the oracle (double arithmetic).
+
+    Runs the forward step from (pos, vel) in float32 (fwd32) or float64,
+    then back-propagates the output cotangents. Returns (gx_in, gv_in, gc,
+    pos_out, vel_out)."""
+    lib = _lib(ORACLE_SO)
+    fp = c_void_p
+    lib.pbf_oracle_vjp.argtypes = [POINTER(FluidParams), c_int64, c_int32, fp, fp, fp, fp, fp, fp, fp, fp, fp]
+    lib.pbf_oracle_vjp.restype = c_int
+    dt = np.float32 if fwd32 else np.float64
+    n = pos.shape[1]
+    x = np.ascontiguousarray(pos, dt)
+    v = np.ascontiguousarray(vel, dt)
+    xo = np.zeros_like(x)
+    vo = np.zeros_like(v)
+    gxo = np.ascontiguousarray(gx_out, np.float64)
+    gvo = np.ascontiguousarray(gv_out, np.float64)
+    gxi = np.zeros((3, n))
+    gvi = np.zeros((3, n))
+    gc = np.zeros(1)
+    rc = lib.pbf_oracle_vjp(ctypes.byref(params), n, int(fwd32), _ptr(x), _ptr(v), _ptr(xo), _ptr(vo), _ptr(gxo),
+                            _ptr(gvo), _ptr(gxi), _ptr(gvi), _ptr(gc))
+    if rc != 0:
+        raise RuntimeError(f"oracle vjp failed with status {rc}")
+    return gxi, gvi, float(gc[0]), xo, vo
