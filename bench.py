@@ -325,6 +325,9 @@ def run_ours(args, world, rank, local):
     batched = None
     if not args.no_batched:
         batched = run_batched(args, dev, stream, l2_flush)
+    differentiable = None
+    if not args.no_adjoint:
+        differentiable = run_differentiable(args, dev, stream, with_cpu=(rank == 0 and world == 1))
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -343,14 +346,174 @@ def run_ours(args, world, rank, local):
         "step_roofline": {"bytes_per_particle_step": ALGO_BYTES_PER_STEP, "frac": round(step_frac, 5)},
         "kernel_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in stage.items() if v[1]},
         "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches, "trajectory": traj,
-        "batched": batched,
+        "batched": batched, "differentiable": differentiable,
     }
     if world > 1:
         import torch.distributed as dist
 
         dist.destroy_process_group()
     if rank == 0:
-        print(json.dumps(out), flush=True)
+        print(json.dumps(_finite(out)), flush=True)
+
+
+def run_differentiable(args, dev, stream, with_cpu=True):
+    """Differentiable PBF: 32^3 block (32,768 particles), XSPH c = 0.01 and
+    s_corr on, initial velocity N(0, 0.1^2), 60 steps, loss |COM - (1.5, 0.3,
+    1.0)|^2. Times the forward run and forward + adjoint (checkpoints every 10
+    steps, recomputation in between), and checks dL/dv0 and dL/dc against
+    central finite differences of the GPU forward (16 random directions, step
+    1e-3) and against the oracle's FP64 adjoint of the same FP32 trajectory."""
+    import numpy as np
+    import torch
+
+    from fluidsimulator_gb300 import scenes
+    from fluidsimulator_gb300.solver import Solver
+
+    sc = scenes.differentiable_block(32, seed=0)
+    n = sc.count
+    steps, every = args.adj_steps, 10
+    target = np.array([1.5, 0.3, 1.0])
+    s = Solver(dev.index)
+    s.configure([sc.params], [n])
+    s.set_stream(stream.cuda_stream)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+
+    def grad(horizon):
+        s.upload(sc.pos, sc.vel)
+        s.record(horizon, every)
+        x, _ = s.download()
+        com = x.astype(np.float64).mean(axis=1)
+        gxf = np.repeat((2.0 * (com - target) / n)[:, None], n, axis=1).astype(np.float32)
+        return s.backward(gxf, np.zeros((3, n), np.float32))
+
+    # timing: forward run vs forward + adjoint
+    for _ in range(max(1, args.warmup)):
+        s.upload(sc.pos, sc.vel)
+        s.step(steps)
+        grad(steps)
+    fwd, both = [], []
+    for _ in range(3):
+        s.upload(sc.pos, sc.vel)
+        torch.cuda.synchronize(dev)
+        ev0.record(stream)
+        s.step_async(steps)
+        ev1.record(stream)
+        s.synchronize()
+        fwd.append(ev0.elapsed_time(ev1))
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        grad(steps)
+        both.append(1e3 * (time.perf_counter() - t0))
+    fwd_ms, both_ms = statistics.median(fwd), statistics.median(both)
+
+    out = {"particles": n, "steps": steps, "checkpoint_every": every,
+           "forward_ms": round(fwd_ms, 3), "forward_adjoint_ms": round(both_ms, 3),
+           "adjoint_cost_ratio": round(both_ms / fwd_ms, 3),
+           "timing": "forward: CUDA events around the 60 steps; forward+adjoint: host wall clock around record(60, 10) "
+                     "+ final-state read + backward"}
+
+    def fd_check(scene):
+        """dL/dv0 and dL/dc against central differences (step 1e-3) of the
+        GPU forward, per horizon."""
+        s.set_params([scene.params])
+        res = {}
+        rng = np.random.default_rng(2024)
+        dirs = [rng.standard_normal((3, n)) for _ in range(args.fd_dirs)]
+        dirs = [d / np.sqrt(np.mean(d * d)) for d in dirs]  # unit RMS per component
+        eps = 1e-3
+
+        def loss(v0, params, horizon):
+            s.set_params([params])
+            s.upload(scene.pos, np.ascontiguousarray(v0, np.float32))
+            s.step(horizon)
+            x, _ = s.download()
+            return float(np.sum((x.astype(np.float64).mean(axis=1) - target) ** 2))
+
+        for horizon in sorted({1, 5, 10, steps}):
+            s.set_params([scene.params])
+            s.upload(scene.pos, scene.vel)
+            s.record(horizon, every)
+            x, _ = s.download()
+            com = x.astype(np.float64).mean(axis=1)
+            gxf = np.repeat((2.0 * (com - target) / n)[:, None], n, axis=1).astype(np.float32)
+            _, gv0, gc = s.backward(gxf, np.zeros((3, n), np.float32))
+            rel = []
+            for d in dirs:
+                fd = (loss(scene.vel + eps * d, scene.params, horizon) -
+                      loss(scene.vel - eps * d, scene.params, horizon)) / (2 * eps)
+                ad = float(np.sum(gv0.astype(np.float64) * d))
+                rel.append(abs(fd - ad) / max(abs(fd), abs(ad), 1e-30))
+            c0 = np.float32(scene.params.visc_c)
+            pp, pm = scene.params.copy(), scene.params.copy()
+            pp.visc_c, pm.visc_c = float(np.float32(c0 * 1.001)), float(np.float32(c0 * 0.999))
+            fdc = (loss(scene.vel, pp, horizon) - loss(scene.vel, pm, horizon)) / (pp.visc_c - pm.visc_c)
+            res[str(horizon)] = {
+                "grad_v0_norm": float(np.linalg.norm(gv0)), "fd_rel_err_median": float(np.median(rel)),
+                "fd_rel_err_max": float(np.max(rel)), "fd_within_1e-3": int(sum(r <= 1e-3 for r in rel)),
+                "dL_dc": float(gc[0]), "dL_dc_fd": float(fdc),
+                "dL_dc_rel_err": float(abs(fdc - gc[0]) / max(abs(fdc), abs(gc[0]), 1e-30))}
+        s.set_params([sc.params])
+        return res
+
+    out["fd"] = {"as_specified": fd_check(sc),
+                 "unit_mass": fd_check(scenes.differentiable_block(32, seed=0, unit_mass=True)),
+                 "directions": args.fd_dirs, "step": 1e-3}
+    if with_cpu:
+        from oracle import pyoracle
+
+        pyoracle.build(ref=False)
+        horizon = 5
+        states = [(sc.pos, sc.vel)]
+        for _ in range(horizon):
+            r = pyoracle.Oracle().run(sc.params, *states[-1], 0.0, 1)
+            states.append((r["pos"], r["vel"]))
+        com = states[-1][0].astype(np.float64).mean(axis=1)
+        g = np.repeat((2.0 * (com - target) / n)[:, None], n, axis=1)
+        gv = np.zeros((3, n))
+        gct = 0.0
+        for t in reversed(range(horizon)):
+            g, gv, c, _, _ = pyoracle.vjp(sc.params, *states[t], g, gv, fwd32=True)
+            gct += c
+        gx0, gv0, gc = grad(horizon)
+        # central differences of the FP64 forward (step 1e-6) on the unit-mass
+        # scene against the GPU adjoint: FP32 rounding noise of a COM loss
+        # (~1e-9) swamps a 1e-3 step's signal, FP64 does not.
+        um = scenes.differentiable_block(32, seed=0, unit_mass=True)
+        s.set_params([um.params])
+        fd64 = {}
+        for hz in (1, 5):
+            s.upload(um.pos, um.vel)
+            s.record(hz, every)
+            x, _ = s.download()
+            com = x.astype(np.float64).mean(axis=1)
+            gxf = np.repeat((2.0 * (com - target) / n)[:, None], n, axis=1).astype(np.float32)
+            _, gv_um, _ = s.backward(gxf, np.zeros((3, n), np.float32))
+            rng = np.random.default_rng(7)
+            rels = []
+            for _ in range(4):
+                d = rng.standard_normal((3, n))
+                d /= np.sqrt(np.mean(d * d))
+
+                def l64(v0):
+                    r = pyoracle.Oracle(np.float64).run(um.params, um.pos.astype(np.float64), v0, 0.0, hz)
+                    return float(np.sum((r["pos"].mean(axis=1) - target) ** 2))
+
+                e6 = 1e-6
+                fd = (l64(um.vel.astype(np.float64) + e6 * d) - l64(um.vel.astype(np.float64) - e6 * d)) / (2 * e6)
+                ad = float(np.sum(gv_um.astype(np.float64) * d))
+                rels.append(abs(fd - ad) / max(abs(fd), abs(ad), 1e-30))
+            fd64[str(hz)] = {"rel_err_median": float(np.median(rels)), "rel_err_max": float(np.max(rels)),
+                             "within_1e-3": int(sum(r <= 1e-3 for r in rels)), "directions": 4}
+        s.set_params([sc.params])
+        out["fd_fp64_unit_mass"] = fd64
+        out["fp64_adjoint"] = {"horizon": horizon,
+                               "dL_dv0_rel_err": float(np.linalg.norm(gv0 - gv) / np.linalg.norm(gv)),
+                               "dL_dx0_rel_err": float(np.linalg.norm(gx0 - g) / np.linalg.norm(g)),
+                               "dL_dc_rel_err": float(abs(gc[0] - gct) / abs(gct)),
+                               "note": "oracle FP64 adjoint linearised around the same FP32 trajectory"}
+    s.close()
+    return out
 
 
 def run_batched(args, dev, stream, l2_flush):
@@ -445,6 +608,19 @@ def run_batched(args, dev, stream, l2_flush):
     return out
 
 
+def _finite(x):
+    """JSON-safe copy: non-finite floats (an overflowed gradient) become null."""
+    import math
+
+    if isinstance(x, dict):
+        return {k: _finite(v) for k, v in x.items()}
+    if isinstance(x, (list, tuple)):
+        return [_finite(v) for v in x]
+    if isinstance(x, float) and not math.isfinite(x):
+        return None
+    return x
+
+
 # --------------------------------------------------------------------------
 # CPU: oracle restatement of the reference step
 
@@ -533,6 +709,9 @@ def main(argv=None):
     ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--batch-trajectory", type=int, default=30)
     ap.add_argument("--side", type=int, default=100, help="lattice side of the throughput scene (100 = 1M)")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-scene measurement")
+    ap.add_argument("--adj-steps", type=int, default=60)
+    ap.add_argument("--fd-dirs", type=int, default=16)
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per launch of the dominant kernel from an ncu capture")
     args = ap.parse_args(argv)

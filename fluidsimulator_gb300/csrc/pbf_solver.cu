@@ -25,10 +25,28 @@ namespace {
 
 constexpr float kPi = 3.14159265358979323846f;  // core/src/core.cpp:10
 
+// Owning device buffer; move-only so containers never double-free.
 template <typename T>
 struct DBuf {
   T* p = nullptr;
   size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  DBuf(DBuf&& o) noexcept : p(o.p), n(o.n) {
+    o.p = nullptr;
+    o.n = 0;
+  }
+  DBuf& operator=(DBuf&& o) noexcept {
+    if (this != &o) {
+      release();
+      p = o.p;
+      n = o.n;
+      o.p = nullptr;
+      o.n = 0;
+    }
+    return *this;
+  }
   cudaError_t alloc(size_t count) {
     release();
     if (count == 0) return cudaSuccess;
@@ -208,6 +226,7 @@ class Solver {
     build_scene_consts();
     plan_ = StepPlan();
     checkpoints_.clear();
+    tapes_.clear();
     rec_steps_ = 0;
     adj_n_ = 0;
     warps_ = (n_ + 31) / 32;
@@ -499,62 +518,16 @@ class Solver {
     gc.assign(S_, 0.0);
     if (n_ == 0) return FLUID_OK;
     if ((rc = ensure_adjoint_buffers())) return rc;
+    if (tapes_.empty()) tapes_.resize(1);
     const int parity0 = parity_;
     const long long steps0 = steps_;
     const std::vector<float> times0 = times_;
-    rc = step(1);  // sizes the lists and the cell table for this state
-    parity_ = parity0;
+    rc = taped_step(tapes_[0]);
+    parity_ = parity0;  // the step's input is still in these buffers
     steps_ = steps0;
     times_ = times0;
     if (rc) return rc;
-    StepRecord rec;
-    rec.x0 = rec_x0_.p;
-    rec.p = rec_p_.p;
-    rec.q = rec_q_.p;
-    rec.lambda = rec_lam_.p;
-    rec.rho = rec_rho_.p;
-    LaunchMarks m;
-    const StepArgs sa = args(parity_);
-    if (enqueue_step(sa, plan_, stream_, m, &rec) != cudaSuccess) return cuda_fail("record step");
-    launches_ += m.launches;
-    AdjArgs aa;
-    aa.s = sa;
-    aa.rec = rec;
-    aa.iters = plan_.iterations;
-    aa.v2 = a_v2_.p;
-    aa.gx = a_gx_.p;
-    aa.gv = a_gv_.p;
-    aa.gv3 = a_gv3_.p;
-    aa.gp = a_gp_.p;
-    aa.gd = a_gd_.p;
-    aa.gx0 = a_gx0_.p;
-    aa.aux = a_aux_.p;
-    aa.grt = a_grt_.p;
-    aa.grho = a_grho_.p;
-    aa.cc = a_cc_.p;
-    aa.g_pos_out = gpo;
-    aa.g_vel_out = gvo;
-    aa.g_pos_in = gpi;
-    aa.g_vel_in = gvi;
-    if (enqueue_adjoint(aa, stream_) != cudaSuccess) return cuda_fail("adjoint launch");
-    launches_ += 4 + 3ll * plan_.iterations;
-    if (cudaStreamSynchronize(stream_) != cudaSuccess) return cuda_fail("adjoint");
-    DevStatus st;
-    cudaMemcpy(&st, status_.p, sizeof(st), cudaMemcpyDeviceToHost);
-    enqueue_reset(status_.p, bmin_.p, bmax_.p, S_, stream_);
-    if (st.err) {
-      cudaStreamSynchronize(stream_);
-      return fail(st.err, "recorded step failed");
-    }
-    std::vector<float> cc(n_);
-    if (cudaMemcpy(cc.data(), a_cc_.p, sizeof(float) * n_, cudaMemcpyDeviceToHost) != cudaSuccess)
-      return cuda_fail("adjoint read");
-    for (int sc = 0; sc < S_; ++sc) {
-      double acc = 0.0;
-      for (int i = sc_host_[sc].first_slot; i < sc_host_[sc].first_slot + sc_host_[sc].count; ++i) acc += cc[i];
-      gc[sc] = acc;
-    }
-    return FLUID_OK;
+    return tape_adjoint(tapes_[0], gpo, gvo, gpi, gvi, gc);
   }
 
   int step_backward(const float* gpo, const float* gvo, float* gpi, float* gvi, float* gvisc, int memory) {
@@ -624,18 +597,15 @@ class Solver {
     cudaMemcpy(cur[1], gvf, b, in);
     std::vector<double> total(S_, 0.0), gc;
     const int segs = static_cast<int>(checkpoints_.size());
+    if (static_cast<int>(tapes_.size()) < rec_every_) tapes_.resize(rec_every_);
     for (int seg = segs - 1; seg >= 0; --seg) {
       const int t0 = seg * rec_every_;
       const int t1 = std::min(rec_steps_, t0 + rec_every_);
       if ((rc = snap_load(checkpoints_[seg]))) return rc;
-      std::vector<Snap> states(t1 - t0);
-      for (int t = t0; t < t1; ++t) {
-        if ((rc = snap_save(states[t - t0]))) return rc;
-        if (t + 1 < t1 && (rc = step(1))) return rc;
-      }
+      for (int t = t0; t < t1; ++t)  // recompute the segment once, taping every step
+        if ((rc = taped_step(tapes_[t - t0]))) return rc;
       for (int t = t1 - 1; t >= t0; --t) {
-        if ((rc = snap_load(states[t - t0]))) return rc;
-        if ((rc = vjp_device(cur[0], cur[1], nxt[0], nxt[1], gc))) return rc;
+        if ((rc = tape_adjoint(tapes_[t - t0], cur[0], cur[1], nxt[0], nxt[1], gc))) return rc;
         for (int sc = 0; sc < S_; ++sc) total[sc] += gc[sc];
         std::swap(cur[0], nxt[0]);
         std::swap(cur[1], nxt[1]);
@@ -1021,31 +991,133 @@ class Solver {
     return cudaStreamSynchronize(stream_) == cudaSuccess ? FLUID_OK : cuda_fail("restore");
   }
 
-  int ensure_adjoint_buffers() {
+  // One step's forward internals and neighbour lists, for the adjoint.
+  struct Tape {
+    DBuf<float4> x0, p, q;
+    DBuf<float> lam, rho;
+    DBuf<int> cnt, nbr;
+    DBuf<long long> wbase;
+    size_t n = 0;
+    int k = -1;
+  };
+
+  // Runs one step from the current state (advancing it like step(1)) and
+  // tapes what the adjoint needs. Capacity overflows regrow and re-run.
+  int taped_step(Tape& tp) {
     const size_t n = static_cast<size_t>(std::max(n_, 1));
     const int k = plan_.iterations;
-    if (adj_n_ == n && adj_k_ == k) return FLUID_OK;
-    const size_t kk = static_cast<size_t>(std::max(k, 1));
-    bool ok = rec_x0_.alloc(n) == cudaSuccess && rec_p_.alloc((k + 1) * n) == cudaSuccess &&
-              rec_q_.alloc(kk * n) == cudaSuccess && rec_lam_.alloc(kk * n) == cudaSuccess &&
-              rec_rho_.alloc(n) == cudaSuccess && a_v2_.alloc(n) == cudaSuccess && a_gx_.alloc(n) == cudaSuccess &&
-              a_gv_.alloc(n) == cudaSuccess && a_gv3_.alloc(n) == cudaSuccess && a_gp_.alloc(n) == cudaSuccess &&
-              a_gd_.alloc(n) == cudaSuccess && a_gx0_.alloc(n) == cudaSuccess && a_aux_.alloc(n) == cudaSuccess &&
-              a_grt_.alloc(n) == cudaSuccess && a_grho_.alloc(n) == cudaSuccess && a_cc_.alloc(n) == cudaSuccess &&
-              a_io_.alloc(12 * n) == cudaSuccess;
+    if (tp.n != n || tp.k != k) {
+      const size_t kk = static_cast<size_t>(std::max(k, 1));
+      if (tp.x0.alloc(n) || tp.p.alloc((k + 1) * n) || tp.q.alloc(kk * n) || tp.lam.alloc(kk * n) ||
+          tp.rho.alloc(n) || tp.cnt.alloc(n) || tp.wbase.alloc(static_cast<size_t>(warps_) + 1)) {
+        tp.n = 0;
+        return fail(FLUID_ERR_OUT_OF_MEMORY, "adjoint tape");
+      }
+      tp.n = n;
+      tp.k = k;
+    }
+    for (;;) {
+      StepRecord rec;
+      rec.x0 = tp.x0.p;
+      rec.p = tp.p.p;
+      rec.q = tp.q.p;
+      rec.lambda = tp.lam.p;
+      rec.rho = tp.rho.p;
+      LaunchMarks m;
+      if (enqueue_step(args(parity_), plan_, stream_, m, &rec) != cudaSuccess) return cuda_fail("taped step");
+      launches_ += m.launches;
+      if (cudaStreamSynchronize(stream_) != cudaSuccess) return cuda_fail("taped step");
+      DevStatus st;
+      cudaMemcpy(&st, status_.p, sizeof(st), cudaMemcpyDeviceToHost);
+      enqueue_reset(status_.p, bmin_.p, bmax_.p, S_, stream_);
+      if (st.err == FLUID_ERR_CAPACITY) {
+        int rc = grow(st.need_grid, st.cursor);
+        if (rc) return rc;
+        ++regrows_;
+        continue;
+      }
+      if (st.err) {
+        cudaStreamSynchronize(stream_);
+        return fail(st.err, "taped step failed");
+      }
+      const size_t len = static_cast<size_t>(st.cursor);
+      if (tp.nbr.n < len && tp.nbr.alloc(len + len / 4 + 32)) return fail(FLUID_ERR_OUT_OF_MEMORY, "adjoint tape");
+      cudaMemcpyAsync(tp.nbr.p, nbr_.p, len * sizeof(int), cudaMemcpyDeviceToDevice, stream_);
+      cudaMemcpyAsync(tp.cnt.p, cnt_.p, n * sizeof(int), cudaMemcpyDeviceToDevice, stream_);
+      cudaMemcpyAsync(tp.wbase.p, wbase_.p, (static_cast<size_t>(warps_) + 1) * sizeof(long long),
+                      cudaMemcpyDeviceToDevice, stream_);
+      last_pairs_ = static_cast<long long>(st.pairs);
+      last_max_ = st.nbr_max;
+      last_cells_ = static_cast<int>(st.total_cells);
+      commit_steps(1);
+      return FLUID_OK;
+    }
+  }
+
+  // Adjoint kernels over one tape; cotangents on the device (3n blocks).
+  int tape_adjoint(const Tape& tp, const float* gpo, const float* gvo, float* gpi, float* gvi,
+                   std::vector<double>& gc) {
+    StepArgs sa = args(parity_);
+    sa.cnt = tp.cnt.p;
+    sa.nbr = tp.nbr.p;
+    sa.wbase = tp.wbase.p;
+    AdjArgs aa;
+    aa.s = sa;
+    aa.rec.x0 = tp.x0.p;
+    aa.rec.p = tp.p.p;
+    aa.rec.q = tp.q.p;
+    aa.rec.lambda = tp.lam.p;
+    aa.rec.rho = tp.rho.p;
+    aa.iters = tp.k;
+    aa.v2 = a_v2_.p;
+    aa.gx = a_gx_.p;
+    aa.gv = a_gv_.p;
+    aa.gv3 = a_gv3_.p;
+    aa.gp = a_gp_.p;
+    aa.gd = a_gd_.p;
+    aa.gx0 = a_gx0_.p;
+    aa.aux = a_aux_.p;
+    aa.grt = a_grt_.p;
+    aa.grho = a_grho_.p;
+    aa.cc = a_cc_.p;
+    aa.g_pos_out = gpo;
+    aa.g_vel_out = gvo;
+    aa.g_pos_in = gpi;
+    aa.g_vel_in = gvi;
+    if (enqueue_adjoint(aa, stream_) != cudaSuccess) return cuda_fail("adjoint launch");
+    launches_ += 4 + 3ll * tp.k;
+    std::vector<float> cc(n_);
+    if (cudaMemcpyAsync(cc.data(), a_cc_.p, sizeof(float) * n_, cudaMemcpyDeviceToHost, stream_) != cudaSuccess ||
+        cudaStreamSynchronize(stream_) != cudaSuccess)
+      return cuda_fail("adjoint");
+    gc.assign(S_, 0.0);
+    for (int sc = 0; sc < S_; ++sc) {
+      double acc = 0.0;
+      for (int i = sc_host_[sc].first_slot; i < sc_host_[sc].first_slot + sc_host_[sc].count; ++i) acc += cc[i];
+      gc[sc] = acc;
+    }
+    return FLUID_OK;
+  }
+
+  int ensure_adjoint_buffers() {
+    const size_t n = static_cast<size_t>(std::max(n_, 1));
+    if (adj_n_ == n) return FLUID_OK;
+    bool ok = a_v2_.alloc(n) == cudaSuccess && a_gx_.alloc(n) == cudaSuccess && a_gv_.alloc(n) == cudaSuccess &&
+              a_gv3_.alloc(n) == cudaSuccess && a_gp_.alloc(n) == cudaSuccess && a_gd_.alloc(n) == cudaSuccess &&
+              a_gx0_.alloc(n) == cudaSuccess && a_aux_.alloc(n) == cudaSuccess && a_grt_.alloc(n) == cudaSuccess &&
+              a_grho_.alloc(n) == cudaSuccess && a_cc_.alloc(n) == cudaSuccess && a_io_.alloc(12 * n) == cudaSuccess;
     if (!ok) {
       adj_n_ = 0;
       return fail(FLUID_ERR_OUT_OF_MEMORY, "adjoint buffers");
     }
     adj_n_ = n;
-    adj_k_ = k;
     return FLUID_OK;
   }
 
-  DBuf<float4> rec_x0_, rec_p_, rec_q_, a_v2_, a_gx_, a_gv_, a_gv3_, a_gp_, a_gd_, a_gx0_, a_aux_;
-  DBuf<float> rec_lam_, rec_rho_, a_grt_, a_grho_, a_cc_, a_io_;
+  DBuf<float4> a_v2_, a_gx_, a_gv_, a_gv3_, a_gp_, a_gd_, a_gx0_, a_aux_;
+  DBuf<float> a_grt_, a_grho_, a_cc_, a_io_;
   size_t adj_n_ = 0;
-  int adj_k_ = -1;
+  std::vector<Tape> tapes_;
   std::vector<Snap> checkpoints_;
   Snap final_;
   int rec_steps_ = 0, rec_every_ = 1;

@@ -236,18 +236,25 @@ def batched_scenes(count: int = 64, seed: int = 0, n_min: int = 2000, n_max: int
     return scenes
 
 
-def differentiable_block(n_side: int = 32, seed: int = 0) -> Scene:
+def differentiable_block(n_side: int = 32, seed: int = 0, unit_mass: bool = False) -> Scene:
     """Differentiable scene: n^3 block (n = 32), spacing 0.05, h = 0.1, corner
     (0.2, 0.05, 0.2) in a [0,2]^3 box, XSPH c = 0.01 and s_corr on (k = 0.1,
     n = 4, dq = 0.2 h), vorticity off; initial velocity N(0, 0.1^2) per
-    component; 60 steps."""
+    component; 60 steps.
+
+    unit_mass: the well-conditioned variant with m = 1 and rho0 = 1/sp^3 (the
+    convention of the reference's own scene files), where the Jacobi update
+    is not scaled by 1/m."""
     sp, h = 0.05, 0.1
     p = base_params(sp, h)
+    if unit_mass:
+        p.particle_mass = 1.0
+        p.density = float(np.float32(1.0) / np.float32(sp) ** 3)
     init_planes(p, 2.0, 2.0, 2.0)
     all_flags(p, h)
     p.enable_vorticity = 0
     pos = init_block(n_side, n_side, n_side, (0.2, 0.05, 0.2), sp)
     n = pos.shape[1]
     vel = (0.1 * normal(seed ^ 0x5E1, 3 * n).reshape(n, 3).T).astype(np.float32)
-    return Scene(f"differentiable_{n}", p, pos, vel, steps=60,
+    return Scene(f"differentiable_{n}" + ("_unit_mass" if unit_mass else ""), p, pos, vel, steps=60,
                  info={"spacing": sp, "box": (2.0, 2.0, 2.0), "seed": seed, "target": (1.5, 0.3, 1.0)})
