@@ -11,7 +11,10 @@
 // Launch order (slot order of the step's output):
 //   k_adj_prepare  committed velocity v2 = (p^K - x0)/dt, output cotangents
 //                  gathered from caller order
-//   k_adj_out      XSPH sum recomputed, restitution reversed (core.cpp:573-612)
+//   k_adj_out      XSPH sum and vorticity force recomputed, restitution
+//                  reversed (core.cpp:573-612), confinement force reversed
+//   k_adj_eta      eta reversed (core.cpp:512-543)      } vorticity
+//   k_adj_omega    omega reversed (core.cpp:472-508)    } confinement
 //   k_adj_xsph     XSPH reversed (core.cpp:423-466), commit reversed
 //   per iteration k = K-1 .. 0:
 //     k_adj_proj    plane projection reversed (core.cpp:372-393)
@@ -115,6 +118,39 @@ __global__ void __launch_bounds__(kAdjBlock) k_adj_out(AdjArgs a) {
     });
   }
   float v[3] = {vi.x + c.visc_c * sx, vi.y + c.visc_c * sy, vi.z + c.visc_c * sz};
+  a.dv[i] = make_float4(sx, sy, sz, 0.0f);
+  a.v3[i] = make_float4(v[0], v[1], v[2], vi.w);
+  // Vorticity confinement recomputed (core.cpp:512-570): eta from the
+  // recorded |omega|, N = eta/|eta|, f = eps N x omega.
+  float N[3] = {0.0f, 0.0f, 0.0f}, om[3] = {0.0f, 0.0f, 0.0f}, elen = 0.0f;
+  const bool vort = a.vorticity && c.vort_on;
+  if (vort) {
+    const float4 oi = a.rec.omega[i];
+    om[0] = oi.x;
+    om[1] = oi.y;
+    om[2] = oi.z;
+    float ex = 0.0f, ey = 0.0f, ez = 0.0f;
+    for_list(a.s, i, [&](int j) {
+      const float4 xj = __ldg(x1 + j);
+      const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+      const float r2 = d2(dx, dy, dz);
+      if (!(r2 < c.h2)) return;
+      const float f = Fs(c, sqrtf(r2 < c.min_r2 ? c.min_r2 : r2));
+      const float dm = __ldg(&a.rec.omega[j].w) - oi.w;
+      ex += dm * (f * dx);
+      ey += dm * (f * dy);
+      ez += dm * (f * dz);
+    });
+    elen = sqrtf(ex * ex + ey * ey + ez * ez);
+    if (elen > c.vort_norm_eps) {
+      N[0] = ex / elen;
+      N[1] = ey / elen;
+      N[2] = ez / elen;
+    }
+    v[0] += c.dt * (c.vort_eps * (N[1] * om[2] - N[2] * om[1]));
+    v[1] += c.dt * (c.vort_eps * (N[2] * om[0] - N[0] * om[2]));
+    v[2] += c.dt * (c.vort_eps * (N[0] * om[1] - N[1] * om[0]));
+  }
   const float4 go = a.gv[i];
   float g[3] = {go.x, go.y, go.z};
   if (c.rest_on) {
@@ -142,8 +178,119 @@ __global__ void __launch_bounds__(kAdjBlock) k_adj_out(AdjArgs a) {
       g[2] = c.rest_scale * g[2] + k * pl.z;
     }
   }
-  a.gv3[i] = make_float4(g[0], g[1], g[2], 0.0f);
-  a.cc[i] = c.xsph_on ? g[0] * sx + g[1] * sy + g[2] * sz : 0.0f;
+  if (!a.vorticity) {
+    a.gv3[i] = make_float4(g[0], g[1], g[2], 0.0f);
+    a.cc[i] = c.xsph_on ? g[0] * sx + g[1] * sy + g[2] * sz : 0.0f;
+    return;
+  }
+  a.gv4[i] = make_float4(g[0], g[1], g[2], 0.0f);
+  float ebx = 0.0f, eby = 0.0f, ebz = 0.0f, obx = 0.0f, oby = 0.0f, obz = 0.0f;
+  if (vort) {  // f = eps N x omega and N = eta/|eta| reversed
+    const float fb[3] = {c.dt * g[0], c.dt * g[1], c.dt * g[2]};
+    const float Nb[3] = {c.vort_eps * (om[1] * fb[2] - om[2] * fb[1]), c.vort_eps * (om[2] * fb[0] - om[0] * fb[2]),
+                         c.vort_eps * (om[0] * fb[1] - om[1] * fb[0])};
+    obx = c.vort_eps * (fb[1] * N[2] - fb[2] * N[1]);
+    oby = c.vort_eps * (fb[2] * N[0] - fb[0] * N[2]);
+    obz = c.vort_eps * (fb[0] * N[1] - fb[1] * N[0]);
+    if (elen > c.vort_norm_eps) {
+      const float nn = N[0] * Nb[0] + N[1] * Nb[1] + N[2] * Nb[2];
+      ebx = (Nb[0] - N[0] * nn) / elen;
+      eby = (Nb[1] - N[1] * nn) / elen;
+      ebz = (Nb[2] - N[2] * nn) / elen;
+    }
+  }
+  a.eb[i] = make_float4(ebx, eby, ebz, 0.0f);
+  a.obd[i] = make_float4(obx, oby, obz, 0.0f);
+}
+
+// eta_i = sum_j (|w_j| - |w_i|) g_ij reversed: cotangent of |omega| and of
+// positions; omega's total cotangent.
+__global__ void __launch_bounds__(kAdjBlock) k_adj_eta(AdjArgs a) {
+  if (adj_failed(a.s.status)) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = a.s.n;
+  if (i >= n) return;
+  const float4* __restrict__ x1 = a.rec.p + static_cast<size_t>(a.iters) * n;
+  const float4 xi = x1[i];
+  const SceneConst& c = a.s.sc[__float_as_int(a.v2[i].w)];
+  const float4 ebi = a.eb[i];
+  const float4 oi = c.vort_on ? a.rec.omega[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  float mb = 0.0f, ax = 0.0f, ay = 0.0f, az = 0.0f;
+  if (c.vort_on) {
+    for_list(a.s, i, [&](int j) {
+      const float4 xj = __ldg(x1 + j);
+      const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+      const float r2 = d2(dx, dy, dz);
+      if (!(r2 < c.h2)) return;
+      const bool clamp = r2 < c.min_r2;
+      const float r = sqrtf(clamp ? c.min_r2 : r2);
+      const float f = Fs(c, r), fpr = clamp ? 0.0f : dFs(c, r) / r;
+      const float4 ebj = __ldg(a.eb + j);
+      const float ex = ebi.x + ebj.x, ey = ebi.y + ebj.y, ez = ebi.z + ebj.z;
+      const float de = dx * ex + dy * ey + dz * ez;
+      mb -= f * de;
+      const float dm = __ldg(&a.rec.omega[j].w) - oi.w;
+      ax += dm * (f * ex + fpr * de * dx);
+      ay += dm * (f * ey + fpr * de * dy);
+      az += dm * (f * ez + fpr * de * dz);
+    });
+  }
+  const float4 od = a.obd[i];
+  const float k = oi.w > 0.0f ? mb / oi.w : 0.0f;
+  a.ob[i] = make_float4(od.x + k * oi.x, od.y + k * oi.y, od.z + k * oi.z, 0.0f);
+  float4 gx = a.gx[i];
+  gx.x += ax;
+  gx.y += ay;
+  gx.z += az;
+  a.gx[i] = gx;
+}
+
+// omega_i = sum_j (u_j - u_i) x g_ij reversed: cotangent of the velocity
+// after XSPH and of positions; then dL/dc's per-particle share.
+__global__ void __launch_bounds__(kAdjBlock) k_adj_omega(AdjArgs a) {
+  if (adj_failed(a.s.status)) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = a.s.n;
+  if (i >= n) return;
+  const float4* __restrict__ x1 = a.rec.p + static_cast<size_t>(a.iters) * n;
+  const float4 xi = x1[i];
+  const float4 ui = a.v3[i];
+  const SceneConst& c = a.s.sc[__float_as_int(ui.w)];
+  const float4 obi = a.ob[i];
+  const float4 g4 = a.gv4[i];
+  float gu[3] = {g4.x, g4.y, g4.z}, ax = 0.0f, ay = 0.0f, az = 0.0f;
+  if (c.vort_on) {
+    for_list(a.s, i, [&](int j) {
+      const float4 xj = __ldg(x1 + j);
+      const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+      const float r2 = d2(dx, dy, dz);
+      if (!(r2 < c.h2)) return;
+      const bool clamp = r2 < c.min_r2;
+      const float r = sqrtf(clamp ? c.min_r2 : r2);
+      const float f = Fs(c, r), fpr = clamp ? 0.0f : dFs(c, r) / r;
+      const float4 obj = __ldg(a.ob + j);
+      const float4 uj = __ldg(a.v3 + j);
+      const float o[3] = {obi.x + obj.x, obi.y + obj.y, obi.z + obj.z};
+      const float g[3] = {f * dx, f * dy, f * dz};
+      gu[0] -= g[1] * o[2] - g[2] * o[1];
+      gu[1] -= g[2] * o[0] - g[0] * o[2];
+      gu[2] -= g[0] * o[1] - g[1] * o[0];
+      const float w[3] = {uj.x - ui.x, uj.y - ui.y, uj.z - ui.z};
+      const float C[3] = {o[1] * w[2] - o[2] * w[1], o[2] * w[0] - o[0] * w[2], o[0] * w[1] - o[1] * w[0]};
+      const float cd = C[0] * dx + C[1] * dy + C[2] * dz;
+      ax += f * C[0] + fpr * cd * dx;
+      ay += f * C[1] + fpr * cd * dy;
+      az += f * C[2] + fpr * cd * dz;
+    });
+  }
+  a.gv3[i] = make_float4(gu[0], gu[1], gu[2], 0.0f);
+  const float4 s = a.dv[i];
+  a.cc[i] = c.xsph_on ? gu[0] * s.x + gu[1] * s.y + gu[2] * s.z : 0.0f;
+  float4 gx = a.gx[i];
+  gx.x += ax;
+  gx.y += ay;
+  gx.z += az;
+  a.gx[i] = gx;
 }
 
 __global__ void __launch_bounds__(kAdjBlock) k_adj_xsph(AdjArgs a) {
@@ -347,6 +494,10 @@ cudaError_t enqueue_adjoint(const AdjArgs& a, cudaStream_t st) {
   if (a.s.n == 0) return cudaSuccess;
   k_adj_prepare<<<nb, kAdjBlock, 0, st>>>(a);
   k_adj_out<<<nb, kAdjBlock, 0, st>>>(a);
+  if (a.vorticity) {
+    k_adj_eta<<<nb, kAdjBlock, 0, st>>>(a);
+    k_adj_omega<<<nb, kAdjBlock, 0, st>>>(a);
+  }
   k_adj_xsph<<<nb, kAdjBlock, 0, st>>>(a);
   for (int it = a.iters - 1; it >= 0; --it) {
     k_adj_proj<<<nb, kAdjBlock, 0, st>>>(a, it);

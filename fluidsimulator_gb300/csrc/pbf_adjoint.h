@@ -23,6 +23,13 @@ struct AdjArgs {
   float* grt;        // dL/drho_i (total)
   float* grho;       // dL/drho_i from XSPH
   float* cc;         // per-particle share of dL/dc (XSPH coefficient)
+  int vorticity;     // some scene runs vorticity confinement
+  float4* v3;        // velocity after XSPH (recomputed)
+  float4* dv;        // XSPH sum (recomputed)
+  float4* gv4;       // cotangent of the velocity after vorticity, before restitution
+  float4* eb;        // cotangent of eta
+  float4* obd;       // cotangent of omega through the confinement force
+  float4* ob;        // cotangent of omega (total)
   const float* g_pos_out;  // caller order, 3n floats: x block, y block, z block
   const float* g_vel_out;
   float* g_pos_in;

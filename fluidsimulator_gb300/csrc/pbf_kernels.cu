@@ -1026,6 +1026,7 @@ cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t s
     const int bo = plan.block[FLUID_KERNEL_OMEGA];
     FGB_DISPATCH_UNROLL(plan.unroll[FLUID_KERNEL_OMEGA], k_omega, blocks_for(a.n, bo), bo, st, a);
     m.mark(FLUID_KERNEL_OMEGA);
+    if (rec && rec->omega) cudaMemcpyAsync(rec->omega, a.omega, n4, cudaMemcpyDeviceToDevice, st);
     const int be = plan.block[FLUID_KERNEL_ETA];
     FGB_DISPATCH_UNROLL(plan.unroll[FLUID_KERNEL_ETA], k_eta, blocks_for(a.n, be), be, st, a,
                         plan.restitution ? 1 : 0);

@@ -62,6 +62,7 @@ struct StepRecord {
   float4* q = nullptr;
   float* lambda = nullptr;
   float* rho = nullptr;
+  float4* omega = nullptr;  // omega and |omega| (when vorticity runs)
 };
 
 // Enqueues one full timestep on `stream`; with `rec`, also records the

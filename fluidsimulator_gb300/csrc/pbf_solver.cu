@@ -511,8 +511,6 @@ class Solver {
   // state, time and step count are left unchanged.
   int vjp_device(const float* gpo, const float* gvo, float* gpi, float* gvi, std::vector<double>& gc) {
     if (!uploaded_) return fail(FLUID_ERR_STATE, "no state uploaded");
-    if (plan_.vorticity)
-      return fail(FLUID_ERR_NOT_SUPPORTED, "the adjoint does not cover vorticity confinement");
     int rc = synchronize();
     if (rc) return rc;
     gc.assign(S_, 0.0);
@@ -993,7 +991,7 @@ class Solver {
 
   // One step's forward internals and neighbour lists, for the adjoint.
   struct Tape {
-    DBuf<float4> x0, p, q;
+    DBuf<float4> x0, p, q, omega;
     DBuf<float> lam, rho;
     DBuf<int> cnt, nbr;
     DBuf<long long> wbase;
@@ -1009,7 +1007,8 @@ class Solver {
     if (tp.n != n || tp.k != k) {
       const size_t kk = static_cast<size_t>(std::max(k, 1));
       if (tp.x0.alloc(n) || tp.p.alloc((k + 1) * n) || tp.q.alloc(kk * n) || tp.lam.alloc(kk * n) ||
-          tp.rho.alloc(n) || tp.cnt.alloc(n) || tp.wbase.alloc(static_cast<size_t>(warps_) + 1)) {
+          tp.rho.alloc(n) || tp.omega.alloc(n) || tp.cnt.alloc(n) ||
+          tp.wbase.alloc(static_cast<size_t>(warps_) + 1)) {
         tp.n = 0;
         return fail(FLUID_ERR_OUT_OF_MEMORY, "adjoint tape");
       }
@@ -1023,6 +1022,7 @@ class Solver {
       rec.q = tp.q.p;
       rec.lambda = tp.lam.p;
       rec.rho = tp.rho.p;
+      rec.omega = tp.omega.p;
       LaunchMarks m;
       if (enqueue_step(args(parity_), plan_, stream_, m, &rec) != cudaSuccess) return cuda_fail("taped step");
       launches_ += m.launches;
@@ -1068,7 +1068,15 @@ class Solver {
     aa.rec.q = tp.q.p;
     aa.rec.lambda = tp.lam.p;
     aa.rec.rho = tp.rho.p;
+    aa.rec.omega = tp.omega.p;
     aa.iters = tp.k;
+    aa.vorticity = plan_.vorticity ? 1 : 0;
+    aa.v3 = a_v3_.p;
+    aa.dv = a_dv_.p;
+    aa.gv4 = a_gv4_.p;
+    aa.eb = a_eb_.p;
+    aa.obd = a_obd_.p;
+    aa.ob = a_ob_.p;
     aa.v2 = a_v2_.p;
     aa.gx = a_gx_.p;
     aa.gv = a_gv_.p;
@@ -1085,7 +1093,7 @@ class Solver {
     aa.g_pos_in = gpi;
     aa.g_vel_in = gvi;
     if (enqueue_adjoint(aa, stream_) != cudaSuccess) return cuda_fail("adjoint launch");
-    launches_ += 4 + 3ll * tp.k;
+    launches_ += 4 + 3ll * tp.k + (plan_.vorticity ? 2 : 0);
     std::vector<float> cc(n_);
     if (cudaMemcpyAsync(cc.data(), a_cc_.p, sizeof(float) * n_, cudaMemcpyDeviceToHost, stream_) != cudaSuccess ||
         cudaStreamSynchronize(stream_) != cudaSuccess)
@@ -1105,7 +1113,9 @@ class Solver {
     bool ok = a_v2_.alloc(n) == cudaSuccess && a_gx_.alloc(n) == cudaSuccess && a_gv_.alloc(n) == cudaSuccess &&
               a_gv3_.alloc(n) == cudaSuccess && a_gp_.alloc(n) == cudaSuccess && a_gd_.alloc(n) == cudaSuccess &&
               a_gx0_.alloc(n) == cudaSuccess && a_aux_.alloc(n) == cudaSuccess && a_grt_.alloc(n) == cudaSuccess &&
-              a_grho_.alloc(n) == cudaSuccess && a_cc_.alloc(n) == cudaSuccess && a_io_.alloc(12 * n) == cudaSuccess;
+              a_grho_.alloc(n) == cudaSuccess && a_cc_.alloc(n) == cudaSuccess && a_io_.alloc(12 * n) == cudaSuccess &&
+              a_v3_.alloc(n) == cudaSuccess && a_dv_.alloc(n) == cudaSuccess && a_gv4_.alloc(n) == cudaSuccess &&
+              a_eb_.alloc(n) == cudaSuccess && a_obd_.alloc(n) == cudaSuccess && a_ob_.alloc(n) == cudaSuccess;
     if (!ok) {
       adj_n_ = 0;
       return fail(FLUID_ERR_OUT_OF_MEMORY, "adjoint buffers");
@@ -1114,7 +1124,7 @@ class Solver {
     return FLUID_OK;
   }
 
-  DBuf<float4> a_v2_, a_gx_, a_gv_, a_gv3_, a_gp_, a_gd_, a_gx0_, a_aux_;
+  DBuf<float4> a_v2_, a_gx_, a_gv_, a_gv3_, a_gp_, a_gd_, a_gx0_, a_aux_, a_v3_, a_dv_, a_gv4_, a_eb_, a_obd_, a_ob_;
   DBuf<float> a_grt_, a_grho_, a_cc_, a_io_;
   size_t adj_n_ = 0;
   std::vector<Tape> tapes_;

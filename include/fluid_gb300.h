@@ -247,8 +247,8 @@ int fluid_solver_set_tuning(fluid_solver* solver, const int32_t* unroll,
  * adjoint). Cotangent arrays hold 3 * particles floats in caller order: all
  * x, then all y, then all z. Neighbour sets and every branch (r < h, the
  * 0.01 h clamp, plane contacts, restitution's vn < 0) are held at the forward
- * step's values. Vorticity confinement is not differentiated
- * (FLUID_ERR_NOT_SUPPORTED when a scene enables it).
+ * step's values, and so is the |eta| > vort_norm_eps test of vorticity
+ * confinement.
  *
  * fluid_solver_step_backward: vector-Jacobian product of the step the current
  * state would take: given dL/d(positions, velocities) after that step, writes

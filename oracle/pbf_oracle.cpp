@@ -232,6 +232,7 @@ struct Record {
   int iters = 0;
   bool vorticity = false;
   std::vector<T> x0, x1, v2, rho;          // input x, committed x, committed v, last rho
+  std::vector<T> v3, om, omag;             // velocity after XSPH, omega (3n), |omega| (n)
   std::vector<std::vector<T>> P, Q, LAM;   // p^k (iters+1), pre-projection q^k (iters), lambda^k (iters)
   std::vector<int> nbr;
   std::vector<int64_t> nbr_begin;
@@ -454,6 +455,8 @@ int step(Workspace<T>& w, const fluid_params& p, std::size_t n, T* X, T* Y,
     }
   }
 
+  if (rec) put3(rec->v3, n, VX, VY, VZ);
+
   // Vorticity confinement (core.cpp:468-571).
   if (p.enable_vorticity && p.vort_epsilon != 0.0f) {
 #pragma omp parallel for
@@ -481,6 +484,10 @@ int step(Workspace<T>& w, const fluid_params& p, std::size_t n, T* X, T* Y,
       w.oy[i] = ay;
       w.oz[i] = az;
       w.omag[i] = std::sqrt(ax * ax + ay * ay + az * az);
+    }
+    if (rec) {
+      put3(rec->om, n, w.ox.data(), w.oy.data(), w.oz.data());
+      rec->omag = w.omag;
     }
 #pragma omp parallel for
     for (long long i = 0; i < N; ++i) {
@@ -598,6 +605,9 @@ Record<B> convert_record(const Record<A>& r) {
   o.x1 = cv(r.x1);
   o.v2 = cv(r.v2);
   o.rho = cv(r.rho);
+  o.v3 = cv(r.v3);
+  o.om = cv(r.om);
+  o.omag = cv(r.omag);
   for (const auto& v : r.P) o.P.push_back(cv(v));
   for (const auto& v : r.Q) o.Q.push_back(cv(v));
   for (const auto& v : r.LAM) o.LAM.push_back(cv(v));
@@ -615,7 +625,6 @@ Record<B> convert_record(const Record<A>& r) {
 // gather over i's own list.
 template <typename T>
 int adjoint(const Record<T>& R, const fluid_params& p, const T* gxo, const T* gvo, T* gxi, T* gvi, T* gc) {
-  if (R.vorticity) return FLUID_ERR_NOT_SUPPORTED;
   const std::size_t n = R.n;
   const long long N = static_cast<long long>(n);
   const int K = R.iters;
@@ -640,7 +649,10 @@ int adjoint(const Record<T>& R, const fluid_params& p, const T* gxo, const T* gv
   auto powr = [&](T x, int k) { T y = T(1); for (int q = 0; q < k; ++q) y *= x; return y; };
   auto at = [n](const std::vector<T>& a, std::size_t i, int d) { return a[d * n + i]; };
 
+  const bool vort = R.vorticity;
+  const T ve = T(p.vort_epsilon), vne = T(p.vort_norm_eps);
   std::vector<T> gx1(gxo, gxo + 3 * n), gv3(3 * n), gv2(3 * n), dv(3 * n, T(0)), grho(n, T(0));
+  std::vector<T> gv4(3 * n), eb(3 * n, T(0)), obd(3 * n, T(0)), ob(3 * n, T(0));
   std::vector<T> aj(n);
   for (std::size_t i = 0; i < n; ++i) aj[i] = (R.rho[i] > T(0)) ? m / R.rho[i] : T(0);
 
@@ -660,11 +672,28 @@ int adjoint(const Record<T>& R, const fluid_params& p, const T* gxo, const T* gv
         }
       }
     }
-    T v[3], g[3];
+    T v[3], g[3], Nv[3] = {0, 0, 0}, eta[3] = {0, 0, 0}, elen = 0;
     for (int a = 0; a < 3; ++a) {
       dv[a * n + i] = s[a];
       v[a] = at(R.v2, i, a) + cv * s[a];
       g[a] = gvo[a * n + i];
+    }
+    const T om[3] = {vort ? at(R.om, i, 0) : T(0), vort ? at(R.om, i, 1) : T(0), vort ? at(R.om, i, 2) : T(0)};
+    if (vort) {  // eta, N, confinement force (core.cpp:512-570)
+      for (int64_t k = R.nbr_begin[i]; k < R.nbr_begin[i + 1]; ++k) {
+        const std::size_t j = static_cast<std::size_t>(R.nbr[k]);
+        T d[3], r2 = 0;
+        for (int a = 0; a < 3; ++a) { d[a] = at(R.x1, i, a) - at(R.x1, j, a); r2 += d[a] * d[a]; }
+        if (!(r2 < h2)) continue;
+        const T f = F(std::sqrt(r2 < c.min_r2 ? c.min_r2 : r2));
+        for (int a = 0; a < 3; ++a) eta[a] += (R.omag[j] - R.omag[i]) * (f * d[a]);
+      }
+      elen = std::sqrt(eta[0] * eta[0] + eta[1] * eta[1] + eta[2] * eta[2]);
+      if (elen > vne)
+        for (int a = 0; a < 3; ++a) Nv[a] = eta[a] / elen;
+      const T fv[3] = {ve * (Nv[1] * om[2] - Nv[2] * om[1]), ve * (Nv[2] * om[0] - Nv[0] * om[2]),
+                       ve * (Nv[0] * om[1] - Nv[1] * om[0])};
+      for (int a = 0; a < 3; ++a) v[a] += dt * fv[a];
     }
     if (rest) {
       bool act[FLUID_MAX_PLANES];
@@ -686,7 +715,77 @@ int adjoint(const Record<T>& R, const fluid_params& p, const T* gxo, const T* gv
         for (int a = 0; a < 3; ++a) g[a] = mu_s * g[a] + (sc[q] - mu_s) * gn * nq[a];
       }
     }
-    for (int a = 0; a < 3; ++a) gv3[a * n + i] = g[a];
+    for (int a = 0; a < 3; ++a) gv4[a * n + i] = g[a];
+    if (vort) {  // f = eps N x omega reversed; N = eta/|eta| reversed
+      const T fb[3] = {dt * g[0], dt * g[1], dt * g[2]};
+      const T Nb[3] = {ve * (om[1] * fb[2] - om[2] * fb[1]), ve * (om[2] * fb[0] - om[0] * fb[2]),
+                       ve * (om[0] * fb[1] - om[1] * fb[0])};
+      obd[i] = ve * (fb[1] * Nv[2] - fb[2] * Nv[1]);
+      obd[n + i] = ve * (fb[2] * Nv[0] - fb[0] * Nv[2]);
+      obd[2 * n + i] = ve * (fb[0] * Nv[1] - fb[1] * Nv[0]);
+      if (elen > vne) {
+        const T nn = Nv[0] * Nb[0] + Nv[1] * Nb[1] + Nv[2] * Nb[2];
+        for (int a = 0; a < 3; ++a) eb[a * n + i] = (Nb[a] - Nv[a] * nn) / elen;
+      }
+    }
+  }
+  if (vort) {
+    // eta = sum (|w_j| - |w_i|) g_ij reversed: |w| and positions.
+#pragma omp parallel for
+    for (long long ii = 0; ii < N; ++ii) {
+      const std::size_t i = static_cast<std::size_t>(ii);
+      T mb = 0, add[3] = {0, 0, 0};
+      for (int64_t k = R.nbr_begin[i]; k < R.nbr_begin[i + 1]; ++k) {
+        const std::size_t j = static_cast<std::size_t>(R.nbr[k]);
+        T d[3], r2 = 0;
+        for (int a = 0; a < 3; ++a) { d[a] = at(R.x1, i, a) - at(R.x1, j, a); r2 += d[a] * d[a]; }
+        if (!(r2 < h2)) continue;
+        const bool clamp = r2 < c.min_r2;
+        const T r = std::sqrt(clamp ? c.min_r2 : r2);
+        const T f = F(r), fpr = clamp ? T(0) : dF(r) / r;
+        T e[3], de = 0;
+        for (int a = 0; a < 3; ++a) { e[a] = eb[a * n + i] + eb[a * n + j]; de += d[a] * e[a]; }
+        mb -= f * de;
+        const T dm = R.omag[j] - R.omag[i];
+        for (int a = 0; a < 3; ++a) add[a] += dm * (f * e[a] + fpr * de * d[a]);
+      }
+      const T m = R.omag[i];
+      for (int a = 0; a < 3; ++a) {
+        ob[a * n + i] = obd[a * n + i] + (m > T(0) ? mb * at(R.om, i, a) / m : T(0));
+        gx1[a * n + i] += add[a];
+      }
+    }
+    // omega = sum (u_j - u_i) x g_ij reversed: velocities after XSPH and positions.
+#pragma omp parallel for
+    for (long long ii = 0; ii < N; ++ii) {
+      const std::size_t i = static_cast<std::size_t>(ii);
+      T gu[3] = {gv4[i], gv4[n + i], gv4[2 * n + i]}, add[3] = {0, 0, 0};
+      for (int64_t k = R.nbr_begin[i]; k < R.nbr_begin[i + 1]; ++k) {
+        const std::size_t j = static_cast<std::size_t>(R.nbr[k]);
+        T d[3], r2 = 0;
+        for (int a = 0; a < 3; ++a) { d[a] = at(R.x1, i, a) - at(R.x1, j, a); r2 += d[a] * d[a]; }
+        if (!(r2 < h2)) continue;
+        const bool clamp = r2 < c.min_r2;
+        const T r = std::sqrt(clamp ? c.min_r2 : r2);
+        const T f = F(r), fpr = clamp ? T(0) : dF(r) / r;
+        const T o[3] = {ob[i] + ob[j], ob[n + i] + ob[n + j], ob[2 * n + i] + ob[2 * n + j]};
+        const T g[3] = {f * d[0], f * d[1], f * d[2]};
+        gu[0] -= g[1] * o[2] - g[2] * o[1];
+        gu[1] -= g[2] * o[0] - g[0] * o[2];
+        gu[2] -= g[0] * o[1] - g[1] * o[0];
+        const T w[3] = {at(R.v3, j, 0) - at(R.v3, i, 0), at(R.v3, j, 1) - at(R.v3, i, 1),
+                        at(R.v3, j, 2) - at(R.v3, i, 2)};
+        const T C[3] = {o[1] * w[2] - o[2] * w[1], o[2] * w[0] - o[0] * w[2], o[0] * w[1] - o[1] * w[0]};
+        const T cd = C[0] * d[0] + C[1] * d[1] + C[2] * d[2];
+        for (int a = 0; a < 3; ++a) add[a] += f * C[a] + fpr * cd * d[a];
+      }
+      for (int a = 0; a < 3; ++a) {
+        gv3[a * n + i] = gu[a];
+        gx1[a * n + i] += add[a];
+      }
+    }
+  } else {
+    gv3 = gv4;
   }
   if (xsph) {
     T acc = 0;
