@@ -104,6 +104,7 @@ struct StepArgs {
   int* cnt;
   int* depth;             // per warp
   long long* wbase;       // per warp
+  int* ovf;               // per warp: list longer than the shared-memory staging
   int* nbr;
   int* bmin;              // 3 per scene
   int* bmax;

@@ -7,10 +7,11 @@
 //   k_radix_*       stable LSD radix sort of (key, caller index), 8-bit digits
 //   k_reorder       gather into cell order, predict again (bit-identical),
 //                   cell (first, end) table by warp-shuffle boundary detection
-//   k_nbr_count     27-cell scan: per-particle neighbour counts, slice depths,
-//                   slice offsets (one atomic per block), capacity check
-//   k_nbr_fill      27-cell scan again: lists in scan order + first lambda
-//   k_lambda        density / lambda (iterations 2..n)
+//   k_nbr_build     27-cell scan: lists in scan order staged in shared memory,
+//                   slices claimed by one atomic per block, coalesced copy-out;
+//                   capacity check
+//   k_nbr_overflow  re-scan for warps whose lists outgrew the staging
+//   k_lambda        density / lambda
 //   k_delta         position correction, s_corr, plane projection (last
 //                   iteration also commits v = (p - x)/dt, x = p)
 //   k_xsph          XSPH viscosity over the step's lists
@@ -33,6 +34,8 @@ namespace fgb {
 namespace {
 
 constexpr int kMaxBlock = 512;  // largest block the tuner may pick
+constexpr int kMaxBuildBlock = 256;  // k_nbr_build: kStage ints per thread of shared memory
+constexpr int kStage = 40;           // list entries per lane staged in shared memory
 
 __device__ __forceinline__ bool failed(const DevStatus* st) {
   return *reinterpret_cast<const volatile int*>(&st->err) != 0;
@@ -489,54 +492,6 @@ __device__ __forceinline__ void for_each_candidate(const StepArgs& a, const uint
   }
 }
 
-__global__ void __launch_bounds__(kMaxBlock) k_nbr_count(StepArgs a) {
-  if (failed(a.status)) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  int count = 0;
-  if (i < a.n) {
-    const uint32_t* ks = sorted_keys(a, a.status->npass);
-    const float4 p = a.p[0][i];
-    const int scene = __float_as_int(p.w);
-    const SceneConst& c = a.sc[scene];
-    const GridInfo g = a.grid[scene];
-    const float h2 = c.h2;
-    for_each_candidate(a, ks, g, c, i, p, a.p[0], [&](int, const float4 q) {
-      if (dist2(p.x - q.x, p.y - q.y, p.z - q.z) < h2) ++count;
-    });
-    a.cnt[i] = count;
-  }
-  const int mx = __reduce_max_sync(kFull, count);
-  const unsigned sum = __reduce_add_sync(kFull, static_cast<unsigned>(count));
-  // Slices: each block takes one contiguous range for its warps with a single
-  // atomic on the list cursor. Placement varies run to run; every list's
-  // content and order do not.
-  __shared__ int wdepth[kMaxBlock / 32];
-  __shared__ unsigned long long block_base;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (lane == 0) {
-    wdepth[warp] = (i < a.n) ? mx : 0;
-    if (i < a.n) {
-      if (sum) atomicAdd(&a.status->pairs, static_cast<unsigned long long>(sum));
-      if (mx) atomicMax(&a.status->nbr_max, mx);
-    }
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned long long total = 0;
-    for (int w = 0; w < static_cast<int>(blockDim.x / 32); ++w) total += 32ull * wdepth[w];
-    const unsigned long long base = atomicAdd(&a.status->cursor, total);
-    if (base + total > static_cast<unsigned long long>(a.nbr_capacity)) set_error(a.status, FLUID_ERR_CAPACITY);
-    block_base = base;
-  }
-  __syncthreads();
-  if (lane == 0 && i < a.n) {
-    unsigned long long off = block_base;
-    for (int w = 0; w < warp; ++w) off += 32ull * wdepth[w];
-    a.wbase[i >> 5] = static_cast<long long>(off);
-    a.depth[i >> 5] = mx;
-  }
-}
-
 // Lambda from the accumulated sums (core.cpp:319-328).
 __device__ __forceinline__ float finish_lambda(const SceneConst& c, float rho, float gsx, float gsy, float gsz,
                                                float sum_g2, float& rho_out) {
@@ -567,37 +522,92 @@ struct LambdaAcc {
   }
 };
 
-__global__ void __launch_bounds__(kMaxBlock) k_nbr_fill(StepArgs a) {
+// Neighbour lists in one scan (core.cpp:205-247). Each lane stages its first
+// kStage list entries in
+// shared memory while it scans; the block then claims its warps' 32-wide
+// slices with one atomic on the list cursor (placement varies run to run,
+// every list's content and order do not) and writes the staged entries out
+// as coalesced 128-byte rows. Warps with a longer list set ovf[w] and
+// k_nbr_overflow writes their remaining entries.
+__global__ void __launch_bounds__(kMaxBuildBlock) k_nbr_build(StepArgs a) {
+  extern __shared__ int stage[];
   if (failed(a.status)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n) return;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int* mine = stage + warp * (kStage * 32) + lane;  // entry k at mine[32 k]
+  int count = 0;
+  if (i < a.n) {
+    const uint32_t* ks = sorted_keys(a, a.status->npass);
+    const float4 p = a.p[0][i];
+    const int scene = __float_as_int(p.w);
+    const SceneConst& c = a.sc[scene];
+    const GridInfo g = a.grid[scene];
+    const float h2 = c.h2;
+    for_each_candidate(a, ks, g, c, i, p, a.p[0], [&](int j, const float4 q) {
+      if (dist2(p.x - q.x, p.y - q.y, p.z - q.z) < h2) {
+        if (count < kStage) mine[32 * count] = j;
+        ++count;
+      }
+    });
+    a.cnt[i] = count;
+  }
+  const int mx = __reduce_max_sync(kFull, count);
+  const unsigned sum = __reduce_add_sync(kFull, static_cast<unsigned>(count));
+  __shared__ int wdepth[kMaxBuildBlock / 32];
+  __shared__ unsigned long long block_base;
+  __shared__ int block_ok;
+  const bool warp_live = (i - lane) < a.n;
+  if (lane == 0) {
+    wdepth[warp] = warp_live ? mx : 0;
+    if (warp_live) {
+      if (sum) atomicAdd(&a.status->pairs, static_cast<unsigned long long>(sum));
+      if (mx) atomicMax(&a.status->nbr_max, mx);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long total = 0;
+    for (int w = 0; w < static_cast<int>(blockDim.x / 32); ++w) total += 32ull * wdepth[w];
+    const unsigned long long base = atomicAdd(&a.status->cursor, total);
+    block_ok = base + total <= static_cast<unsigned long long>(a.nbr_capacity);
+    if (!block_ok) set_error(a.status, FLUID_ERR_CAPACITY);
+    block_base = base;
+  }
+  __syncthreads();
+  if (!warp_live || !block_ok) return;
+  unsigned long long off = block_base;
+  for (int w = 0; w < warp; ++w) off += 32ull * wdepth[w];
+  int* out = a.nbr + off + lane;
+  const int staged = mx < kStage ? mx : kStage;
+  for (int k = 0; k < staged; ++k)
+    if (k < count) out[32ll * k] = mine[32 * k];
+  if (lane == 0) {
+    a.wbase[i >> 5] = static_cast<long long>(off);
+    a.depth[i >> 5] = mx;
+    a.ovf[i >> 5] = mx > kStage ? 1 : 0;
+  }
+}
+
+// List entries kStage and above, for the warps k_nbr_build flagged.
+__global__ void __launch_bounds__(kMaxBlock) k_nbr_overflow(StepArgs a) {
+  if (failed(a.status)) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n || !a.ovf[i >> 5]) return;
   const uint32_t* ks = sorted_keys(a, a.status->npass);
   const float4 p = a.p[0][i];
   const int scene = __float_as_int(p.w);
   const SceneConst& c = a.sc[scene];
   const GridInfo g = a.grid[scene];
-  const int lane = threadIdx.x & 31;
   const int depth = a.depth[i >> 5];
-  int* out = a.nbr + a.wbase[i >> 5] + lane;
-  const bool lam = c.iterations > 0;
+  int* out = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
   const float h2 = c.h2;
-  LambdaAcc acc;
   int k = 0;
   for_each_candidate(a, ks, g, c, i, p, a.p[0], [&](int j, const float4 q) {
-    const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
-    const float r2 = dist2(dx, dy, dz);
-    if (r2 < h2) {
-      if (k < depth) out[32ll * k] = j;
+    if (dist2(p.x - q.x, p.y - q.y, p.z - q.z) < h2) {
+      if (k >= kStage && k < depth) out[32ll * k] = j;
       ++k;
-      if (lam) acc.add(c, dx, dy, dz, r2);
     }
   });
-  a.cnt[i] = k < depth ? k : depth;  // entries actually written
-  if (lam) {
-    float rho;
-    a.lambda[i] = finish_lambda(c, acc.rho, acc.gsx, acc.gsy, acc.gsz, acc.sum_g2, rho);
-    a.rho[i] = rho;
-  }
 }
 
 // ---------------------------------------------------------------------------
@@ -981,13 +991,12 @@ cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t s
     cudaMemcpyAsync(rec->x0, a.x, n4, cudaMemcpyDeviceToDevice, st);
     cudaMemcpyAsync(rec->p, a.p[0], n4, cudaMemcpyDeviceToDevice, st);
   }
-  const int bc = plan.block[FLUID_KERNEL_NBR_COUNT];
-  k_nbr_count<<<blocks_for(a.n, bc), bc, 0, st>>>(a);
-  m.mark(FLUID_KERNEL_NBR_COUNT);
-  const int bf = plan.block[FLUID_KERNEL_NBR_FILL];
-  k_nbr_fill<<<blocks_for(a.n, bf), bf, 0, st>>>(a);
-  m.mark(FLUID_KERNEL_NBR_FILL);
-  if (rec && plan.iterations > 0) cudaMemcpyAsync(rec->lambda, a.lambda, n1, cudaMemcpyDeviceToDevice, st);
+  const int bc = plan.block[FLUID_KERNEL_NBR_BUILD] > kMaxBuildBlock ? kMaxBuildBlock : plan.block[FLUID_KERNEL_NBR_BUILD];
+  k_nbr_build<<<blocks_for(a.n, bc), bc, sizeof(int) * kStage * bc, st>>>(a);
+  m.mark(FLUID_KERNEL_NBR_BUILD);
+  const int bf = plan.block[FLUID_KERNEL_NBR_OVERFLOW];
+  k_nbr_overflow<<<blocks_for(a.n, bf), bf, 0, st>>>(a);
+  m.mark(FLUID_KERNEL_NBR_OVERFLOW);
 
   const bool post = plan.xsph || plan.vorticity;
   const int to_v2 = plan.xsph ? 1 : 0;
@@ -998,7 +1007,7 @@ cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t s
   }
   for (int it = 0; it < plan.iterations; ++it) {
     const int in = it & 1;
-    if (it > 0) {
+    {
       const int b = plan.block[FLUID_KERNEL_LAMBDA];
       FGB_DISPATCH_UNROLL(plan.unroll[FLUID_KERNEL_LAMBDA], k_lambda, blocks_for(a.n, b), b, st, a, in);
       m.mark(FLUID_KERNEL_LAMBDA);

@@ -36,7 +36,7 @@ inline bool tunable_unroll(int k) {
          k == FLUID_KERNEL_ETA;
 }
 inline bool tunable_block(int k) {
-  return tunable_unroll(k) || k == FLUID_KERNEL_NBR_COUNT || k == FLUID_KERNEL_NBR_FILL;
+  return tunable_unroll(k) || k == FLUID_KERNEL_NBR_BUILD || k == FLUID_KERNEL_NBR_OVERFLOW;
 }
 
 // Records an event after selected launches when profiling is on.

@@ -52,7 +52,8 @@ constexpr size_t kSlot0 = kOmega + kF4, kSlot1 = kSlot0 + kI32, kRho0 = kSlot1 +
 constexpr size_t kLambda = kRho1 + kI32, kKeys0 = kLambda + kI32, kKeys1 = kKeys0 + kI32;
 constexpr size_t kVals0 = kKeys1 + kI32, kVals1 = kVals0 + kI32, kCnt = kVals1 + kI32;
 constexpr size_t kDepth = kCnt + kI32, kWbase = kDepth + up(sizeof(int) * (kMaxWarps + 1));
-constexpr size_t kHist = kWbase + up(sizeof(long long) * (kMaxWarps + 1));
+constexpr size_t kOvf = kWbase + up(sizeof(long long) * (kMaxWarps + 1));
+constexpr size_t kHist = kOvf + up(sizeof(int) * (kMaxWarps + 1));
 constexpr size_t kDigits = kHist + up(sizeof(uint32_t) * 256 * kMaxTiles);
 constexpr size_t kBmin = kDigits + up(sizeof(uint32_t) * 256 * kRadixMaxPasses);
 constexpr size_t kBmax = kBmin + up(3 * sizeof(int));
@@ -116,6 +117,7 @@ StepArgs carve(unsigned char* b, int n) {
   a.cnt = at<int>(b, kCnt);
   a.depth = at<int>(b, kDepth);
   a.wbase = at<long long>(b, kWbase);
+  a.ovf = at<int>(b, kOvf);
   a.nbr = at<int>(b, kNbr);
   a.bmin = at<int>(b, kBmin);
   a.bmax = at<int>(b, kBmax);

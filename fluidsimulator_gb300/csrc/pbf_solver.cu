@@ -248,6 +248,7 @@ class Solver {
     ok &= lambda_.alloc(np) == cudaSuccess;
     ok &= cnt_.alloc(np) == cudaSuccess;
     ok &= depth_.alloc(static_cast<size_t>(warps_) + 1) == cudaSuccess;
+    ok &= ovf_.alloc(static_cast<size_t>(warps_) + 1) == cudaSuccess;
     ok &= wbase_.alloc(static_cast<size_t>(warps_) + 1) == cudaSuccess;
     ok &= hist_.alloc(static_cast<size_t>(tiles_) * 256) == cudaSuccess;
     ok &= digit_total_.alloc(kRadixMaxPasses * 256) == cudaSuccess;
@@ -486,6 +487,7 @@ class Solver {
         }
         for (int k = 0; k < FLUID_KERNEL_COUNT; ++k) {
           if (!tunable_block(k) || stage_launches_[k] == 0) continue;
+          if (k == FLUID_KERNEL_NBR_BUILD && b > 256) continue;  // launched at 256 regardless
           const double avg = stage_ms_[k] / static_cast<double>(stage_launches_[k]);
           if (avg < best_ms[k]) {
             best_ms[k] = avg;
@@ -832,6 +834,7 @@ class Solver {
     a.table = table_.p;
     a.cnt = cnt_.p;
     a.depth = depth_.p;
+    a.ovf = ovf_.p;
     a.wbase = wbase_.p;
     a.nbr = nbr_.p;
     a.bmin = bmin_.p;
@@ -1145,7 +1148,7 @@ class Solver {
   long long last_pairs_ = 0;
   int last_max_ = 0, last_cells_ = 0;
   DBuf<float4> x_[2], v_[2], p_[2], v2_, omega_;
-  DBuf<int> slot_[2], vals_[2], cnt_, depth_, nbr_, bmin_, bmax_;
+  DBuf<int> slot_[2], vals_[2], cnt_, depth_, ovf_, nbr_, bmin_, bmax_;
   DBuf<float> rho_[2], lambda_;
   DBuf<uint32_t> keys_[2], hist_, digit_total_;
   DBuf<long long> wbase_;
@@ -1317,7 +1320,7 @@ int fluid_solver_kernel_times(fluid_solver* s, double* ms, int64_t* launches, in
 const char* fluid_kernel_name(int kernel) {
   static const char* const names[FLUID_KERNEL_COUNT] = {
       "k_bounds", "k_grid_setup", "k_keys", "k_radix_hist", "k_radix_scan", "k_radix_scatter",
-      "k_reorder", "k_nbr_count", "k_nbr_fill", "k_lambda", "k_delta",
+      "k_reorder", "k_nbr_build", "k_nbr_overflow", "k_lambda", "k_delta",
       "k_commit", "k_xsph", "k_omega", "k_eta"};
   return (kernel >= 0 && kernel < FLUID_KERNEL_COUNT) ? names[kernel] : nullptr;
 }

@@ -205,8 +205,8 @@ enum {
   FLUID_KERNEL_RADIX_SCAN = 4,
   FLUID_KERNEL_RADIX_SCATTER = 5,
   FLUID_KERNEL_REORDER = 6,  /* gather into cell order + cell table */
-  FLUID_KERNEL_NBR_COUNT = 7, /* counts + list slices */
-  FLUID_KERNEL_NBR_FILL = 8, /* lists + first lambda */
+  FLUID_KERNEL_NBR_BUILD = 7, /* lists (one scan) + slices */
+  FLUID_KERNEL_NBR_OVERFLOW = 8, /* long lists' remaining entries */
   FLUID_KERNEL_LAMBDA = 9,
   FLUID_KERNEL_DELTA = 10,   /* position correction (+ commit on the last) */
   FLUID_KERNEL_COMMIT = 11,  /* commit when solver_iterations == 0 */
