@@ -190,6 +190,14 @@ def _declare(lib):
     lib.fluid_solver_record.restype = c_int
     lib.fluid_solver_backward.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int32]
     lib.fluid_solver_backward.restype = c_int
+    lib.fluid_solver_frame_begin.argtypes = [c_void_p, c_int32, c_void_p, c_void_p]
+    lib.fluid_solver_frame_begin.restype = c_int
+    lib.fluid_solver_frame_wait.argtypes = [c_void_p, c_int32]
+    lib.fluid_solver_frame_wait.restype = c_int
+    lib.fluid_write_vtp.argtypes = [c_char_p, c_void_p, c_void_p, c_void_p, c_int64, c_int32]
+    lib.fluid_write_vtp.restype = c_int
+    lib.fluid_write_pvd.argtypes = [c_char_p, POINTER(c_double), POINTER(c_char_p), c_int64]
+    lib.fluid_write_pvd.restype = c_int
     lib.fluid_kernel_name.argtypes = [c_int]
     lib.fluid_kernel_name.restype = c_char_p
     lib.fluid_solver_get_time.argtypes = [c_void_p, c_int32, POINTER(c_float)]

@@ -51,6 +51,7 @@ struct SceneConst {
   int rest_on;
   int plane_count;
   int iterations;
+  int all_pairs;                  // use_uniform_grid == 0: lists from all pairs
   int first_slot, count;          // particle range of the scene
   float4 planes[FLUID_MAX_PLANES];  // (nx, ny, nz, d)
 };

@@ -522,6 +522,19 @@ struct LambdaAcc {
   }
 };
 
+// All-pairs candidates (core.cpp:248-268, use_uniform_grid == 0): every other
+// particle of the scene in ascending caller index, as the reference's
+// fallback visits them. O(N^2) per scene; meant for small scenes.
+template <typename F>
+__device__ __forceinline__ void for_each_pair_candidate(const StepArgs& a, const SceneConst& c, int i,
+                                                        const float4* __restrict__ pos, F&& f) {
+  for (int o = c.first_slot; o < c.first_slot + c.count; ++o) {
+    const int j = a.slot[o];
+    if (j == i) continue;
+    f(j, pos[j]);
+  }
+}
+
 // Neighbour lists in one scan (core.cpp:205-247). Each lane stages its first
 // kStage list entries in
 // shared memory while it scans; the block then claims its warps' 32-wide
@@ -543,12 +556,14 @@ __global__ void __launch_bounds__(kMaxBuildBlock) k_nbr_build(StepArgs a) {
     const SceneConst& c = a.sc[scene];
     const GridInfo g = a.grid[scene];
     const float h2 = c.h2;
-    for_each_candidate(a, ks, g, c, i, p, a.p[0], [&](int j, const float4 q) {
+    auto test = [&](int j, const float4 q) {
       if (dist2(p.x - q.x, p.y - q.y, p.z - q.z) < h2) {
         if (count < kStage) mine[32 * count] = j;
         ++count;
       }
-    });
+    };
+    if (c.all_pairs) for_each_pair_candidate(a, c, i, a.p[0], test);
+    else for_each_candidate(a, ks, g, c, i, p, a.p[0], test);
     a.cnt[i] = count;
   }
   const int mx = __reduce_max_sync(kFull, count);
@@ -602,12 +617,14 @@ __global__ void __launch_bounds__(kMaxBlock) k_nbr_overflow(StepArgs a) {
   int* out = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
   const float h2 = c.h2;
   int k = 0;
-  for_each_candidate(a, ks, g, c, i, p, a.p[0], [&](int j, const float4 q) {
+  auto test = [&](int j, const float4 q) {
     if (dist2(p.x - q.x, p.y - q.y, p.z - q.z) < h2) {
       if (k >= kStage && k < depth) out[32ll * k] = j;
       ++k;
     }
-  });
+  };
+  if (c.all_pairs) for_each_pair_candidate(a, c, i, a.p[0], test);
+  else for_each_candidate(a, ks, g, c, i, p, a.p[0], test);
 }
 
 // ---------------------------------------------------------------------------

@@ -125,6 +125,7 @@ SceneConst make_scene_const(const fluid_params& p, int first, int count) {
   c.rest_on = ((p.plane_restitution > 0.0f || p.plane_friction > 0.0f) && p.plane_count > 0) ? 1 : 0;
   c.plane_count = p.plane_count;
   c.iterations = p.solver_iterations;
+  c.all_pairs = p.use_uniform_grid ? 0 : 1;
   c.first_slot = first;
   c.count = count;
   for (int q = 0; q < p.plane_count; ++q) {
@@ -144,10 +145,6 @@ int validate_params(const fluid_params& p, std::string& why) {
   if (!std::isfinite(p.particle_mass)) return bad("particle_mass must be finite");
   if (p.solver_iterations < 0) return bad("solver_iterations must be >= 0");
   if (p.plane_count < 0 || p.plane_count > FLUID_MAX_PLANES) return bad("plane_count out of range");
-  if (!p.use_uniform_grid) {
-    why = "use_uniform_grid = 0 (all-pairs lists) is not implemented on the GPU";
-    return FLUID_ERR_NOT_SUPPORTED;
-  }
   return FLUID_OK;
 }
 
@@ -173,6 +170,12 @@ class Solver {
     if (device_ >= 0) cudaSetDevice(device_);
     destroy_graphs();
     destroy_events();
+    for (int k = 0; k < 2; ++k) {
+      if (frame_busy_[k]) cudaEventSynchronize(frame_done_[k]);
+      if (frame_gather_[k]) cudaEventDestroy(frame_gather_[k]);
+      if (frame_done_[k]) cudaEventDestroy(frame_done_[k]);
+    }
+    if (copy_stream_) cudaStreamDestroy(copy_stream_);
     if (status_host_) cudaFreeHost(status_host_);
     if (own_) cudaStreamDestroy(own_);
   }
@@ -617,6 +620,47 @@ class Solver {
     cudaMemcpy(gvi, cur[1], b, out);
     if (gvisc)
       for (int sc = 0; sc < S_; ++sc) gvisc[sc] = static_cast<float>(total[sc]);
+    return FLUID_OK;
+  }
+
+  // ---- Frame output -------------------------------------------------------
+
+  int frame_begin(int slot, float* hpos, float* hvel) {
+    if (slot < 0 || slot > 1 || !hpos) return fail(FLUID_ERR_INVALID_ARGUMENT, "bad frame slot or buffer");
+    if (!uploaded_) return fail(FLUID_ERR_STATE, "no state uploaded");
+    int rc = synchronize();  // a pending step may still be re-run
+    if (rc) return rc;
+    const size_t n = static_cast<size_t>(std::max(n_, 1));
+    if (!copy_stream_ && cudaStreamCreateWithFlags(&copy_stream_, cudaStreamNonBlocking) != cudaSuccess)
+      return cuda_fail("copy stream");
+    for (int k = 0; k < 2; ++k) {
+      if (!frame_gather_[k] && (cudaEventCreateWithFlags(&frame_gather_[k], cudaEventDisableTiming) ||
+                                cudaEventCreateWithFlags(&frame_done_[k], cudaEventDisableTiming)))
+        return cuda_fail("frame events");
+    }
+    if (frame_stage_[slot].n != 6 * n && frame_stage_[slot].alloc(6 * n))
+      return fail(FLUID_ERR_OUT_OF_MEMORY, "frame staging");
+    if (frame_busy_[slot] && cudaEventSynchronize(frame_done_[slot]) != cudaSuccess) return cuda_fail("frame");
+    if (n_ == 0) return FLUID_OK;
+    float* st = frame_stage_[slot].p;
+    const size_t m = static_cast<size_t>(n_);
+    if (enqueue_download(x_[parity_].p, v_[parity_].p, slot_[parity_].p, st, st + m, st + 2 * m, st + 3 * m,
+                         st + 4 * m, st + 5 * m, n_, stream_) != cudaSuccess)
+      return cuda_fail("frame gather");
+    cudaEventRecord(frame_gather_[slot], stream_);
+    cudaStreamWaitEvent(copy_stream_, frame_gather_[slot], 0);
+    cudaMemcpyAsync(hpos, st, 3 * m * sizeof(float), cudaMemcpyDeviceToHost, copy_stream_);
+    if (hvel) cudaMemcpyAsync(hvel, st + 3 * m, 3 * m * sizeof(float), cudaMemcpyDeviceToHost, copy_stream_);
+    if (cudaEventRecord(frame_done_[slot], copy_stream_) != cudaSuccess) return cuda_fail("frame copy");
+    frame_busy_[slot] = true;
+    return FLUID_OK;
+  }
+
+  int frame_wait(int slot) {
+    if (slot < 0 || slot > 1) return fail(FLUID_ERR_INVALID_ARGUMENT, "bad frame slot");
+    if (!frame_busy_[slot]) return FLUID_OK;
+    if (cudaEventSynchronize(frame_done_[slot]) != cudaSuccess) return cuda_fail("frame wait");
+    frame_busy_[slot] = false;
     return FLUID_OK;
   }
 
@@ -1135,6 +1179,11 @@ class Solver {
   Snap final_;
   int rec_steps_ = 0, rec_every_ = 1;
 
+  cudaStream_t copy_stream_ = nullptr;
+  cudaEvent_t frame_gather_[2] = {nullptr, nullptr}, frame_done_[2] = {nullptr, nullptr};
+  bool frame_busy_[2] = {false, false};
+  DBuf<float> frame_stage_[2];
+
   int device_;
   cudaStream_t own_ = nullptr, stream_ = nullptr;
   int S_ = 0, n_ = 0, warps_ = 0, tiles_ = 1;
@@ -1355,6 +1404,16 @@ int fluid_solver_backward(fluid_solver* s, const float* g_pos_final, const float
                           float* g_vel_initial, float* g_visc_c, int32_t memory) {
   FLUID_CHECK_SOLVER(s);
   return s->impl.backward(g_pos_final, g_vel_final, g_pos_initial, g_vel_initial, g_visc_c, memory);
+}
+
+int fluid_solver_frame_begin(fluid_solver* s, int32_t slot, float* host_pos, float* host_vel) {
+  FLUID_CHECK_SOLVER(s);
+  return s->impl.frame_begin(slot, host_pos, host_vel);
+}
+
+int fluid_solver_frame_wait(fluid_solver* s, int32_t slot) {
+  FLUID_CHECK_SOLVER(s);
+  return s->impl.frame_wait(slot);
 }
 
 int fluid_solver_get_time(fluid_solver* s, int32_t scene, float* time) {

@@ -258,3 +258,134 @@ def differentiable_block(n_side: int = 32, seed: int = 0, unit_mass: bool = Fals
     vel = (0.1 * normal(seed ^ 0x5E1, 3 * n).reshape(n, 3).T).astype(np.float32)
     return Scene(f"differentiable_{n}" + ("_unit_mass" if unit_mass else ""), p, pos, vel, steps=60,
                  info={"spacing": sp, "box": (2.0, 2.0, 2.0), "seed": seed, "target": (1.5, 0.3, 1.0)})
+
+
+def _fill_axis(start: np.float32, stop: np.float32, step: np.float32) -> np.ndarray:
+    """float v = start; v < stop; v += step -- accumulated in float32."""
+    out = []
+    v = np.float32(start)
+    while v < stop:
+        out.append(v)
+        v = np.float32(v + step)
+    return np.array(out, dtype=np.float32)
+
+
+def _cbrtf(x: np.float32) -> np.float32:
+    """The C library's cbrtf (what std::cbrt(float) calls), for bit-identical
+    spacing; numpy's float32 cbrt may differ in the last place."""
+    import ctypes
+    import ctypes.util
+
+    try:
+        libm = ctypes.CDLL(ctypes.util.find_library("m") or "libm.so.6")
+        fn = libm.cbrtf
+        fn.argtypes = [ctypes.c_float]
+        fn.restype = ctypes.c_float
+        return np.float32(fn(float(x)))
+    except (OSError, AttributeError):
+        return np.cbrt(np.float32(x), dtype=np.float32)
+
+
+def load_scene_json(path: str) -> Scene:
+    """Scene file in the reference's legacy format (core/src/init.cpp:158-418):
+    fluid {particle_mass, density, h, epsilon, n, k, c, shape[]} with cube
+    (origin, size) and sphere (origin, radius) fills and an optional velocity,
+    external_forces, and collisions[] of planes (point, normal). Fills
+    accumulate in float32 exactly as the reference's loops do, so the
+    particles are bit-identical to the reference loader's.
+
+    Additional keys, ignored by the reference and optional here:
+      "solver": {"dt", "iterations", "scorr_dq_coeff", "vort_epsilon",
+                 "enable_scorr", "enable_xsph", "enable_vorticity",
+                 "plane_restitution", "plane_friction"}
+      "jitter": {"amplitude", "seed"}  -- U(-a, a) per coordinate (SplitMix64)
+    """
+    import json
+
+    f32 = np.float32
+    with open(path) as fh:
+        root = json.load(fh)
+    if not isinstance(root.get("fluid"), dict):
+        raise ValueError("Scene JSON missing fluid object.")
+    fl = root["fluid"]
+    p = default_params()
+    for key, field in (("particle_mass", "particle_mass"), ("density", "density"), ("h", "h"),
+                       ("epsilon", "epsilon"), ("k", "scorr_k"), ("c", "visc_c")):
+        if key in fl:
+            setattr(p, field, float(f32(fl[key])))
+    if "n" in fl:
+        p.scorr_n = int(fl["n"])
+    if "external_forces" in root:
+        fx, fy, fz = root["external_forces"]
+        p.external_force[0], p.external_force[1], p.external_force[2] = float(f32(fx)), float(f32(fy)), float(f32(fz))
+    spacing = f32(0)
+    from_mass = False
+    if f32(p.density) > 0 and f32(p.particle_mass) > 0:
+        spacing = _cbrtf(f32(p.particle_mass) / f32(p.density))
+        from_mass = True
+    if spacing <= 0 and f32(p.particle_radius) > 0:
+        spacing = f32(p.particle_radius) * f32(2.0)
+    if spacing <= 0:
+        spacing = f32(0.02)
+    if from_mass or f32(p.particle_radius) <= 0:
+        p.particle_radius = float(spacing * f32(0.5))
+    if f32(p.h) <= 0:
+        p.h = float(f32(2.5) * spacing)
+    if not isinstance(fl.get("shape"), list):
+        raise ValueError("Fluid shape must be an array.")
+    half = spacing * f32(0.5)
+    blocks_p, blocks_v = [], []
+    for shape in fl["shape"]:
+        kind = shape.get("type")
+        vel = [f32(c) for c in shape.get("velocity", (0, 0, 0))]
+        o = [f32(c) for c in shape["origin"]]
+        if kind == "cube":
+            size = [f32(c) for c in shape["size"]]
+            ax = [_fill_axis(f32(o[d] + half), f32(o[d] + size[d]), spacing) for d in range(3)]
+            xx, yy, zz = np.meshgrid(*ax, indexing="ij")  # x outermost, z innermost
+            pts = np.stack([xx.ravel(), yy.ravel(), zz.ravel()])
+        elif kind == "sphere":
+            r = f32(shape["radius"])
+            ax = [_fill_axis(f32(f32(o[d] - r) + half), f32(o[d] + r), spacing) for d in range(3)]
+            xx, yy, zz = np.meshgrid(*ax, indexing="ij")
+            dx, dy, dz = (xx - o[0]).astype(np.float32), (yy - o[1]).astype(np.float32), (zz - o[2]).astype(np.float32)
+            keep = ((dx * dx + dy * dy) + dz * dz) < f32(r * r)
+            pts = np.stack([xx[keep], yy[keep], zz[keep]])
+        else:
+            raise ValueError(f"Unsupported shape type: {kind}")
+        blocks_p.append(pts.astype(np.float32))
+        blocks_v.append(np.repeat(np.array(vel, np.float32)[:, None], pts.shape[1], axis=1))
+    pos = np.concatenate(blocks_p, axis=1) if blocks_p else np.zeros((3, 0), np.float32)
+    vel = np.concatenate(blocks_v, axis=1) if blocks_v else np.zeros((3, 0), np.float32)
+    p.plane_count = 0
+    for entry in root.get("collisions", []):
+        if entry.get("type") != "plane":
+            raise ValueError(f"Unsupported collision type: {entry.get('type')}")
+        px_, py_, pz_ = (f32(c) for c in entry["point"])
+        nx, ny, nz = (f32(c) for c in entry["normal"])
+        len_sq = (nx * nx + ny * ny) + nz * nz
+        if len_sq <= 0:
+            raise ValueError("Collision normal must be non-zero.")
+        inv = f32(1) / np.sqrt(len_sq, dtype=np.float32)
+        nx, ny, nz = nx * inv, ny * inv, nz * inv
+        d = (nx * px_ + ny * py_) + nz * pz_
+        i = p.plane_count
+        if i >= MAX_PLANES:
+            raise ValueError("too many planes")
+        p.plane_nx[i], p.plane_ny[i], p.plane_nz[i], p.plane_d[i] = float(nx), float(ny), float(nz), float(d)
+        p.plane_count = i + 1
+    solver = root.get("solver", {})
+    for key, field in (("dt", "dt"), ("scorr_dq_coeff", "scorr_dq_coeff"), ("vort_epsilon", "vort_epsilon"),
+                       ("plane_restitution", "plane_restitution"), ("plane_friction", "plane_friction")):
+        if key in solver:
+            setattr(p, field, float(f32(solver[key])))
+    if "iterations" in solver:
+        p.solver_iterations = int(solver["iterations"])
+    for key in ("enable_scorr", "enable_xsph", "enable_vorticity"):
+        if key in solver:
+            setattr(p, key, int(bool(solver[key])))
+    if "jitter" in root:
+        pos = jitter(pos, float(root["jitter"].get("amplitude", 0.0)), int(root["jitter"].get("seed", 0)))
+    import os
+
+    return Scene(os.path.splitext(os.path.basename(path))[0], p, pos, vel, steps=1, info={"path": path})

@@ -203,6 +203,17 @@ class Solver:
                                                    gc.ctypes.data_as(c_void_p), _capi.MEMORY_HOST))
         return gpi, gvi, gc
 
+    def frame_begin(self, slot: int, host_pos, host_vel=None) -> None:
+        """Starts an asynchronous copy of the current state into host
+        buffers of shape (3, N) (pinned memory for overlap)."""
+        pr, _ = _rows(host_pos)
+        vr = _rows(host_vel)[0][0] if host_vel is not None else None
+        self._check(self.lib.fluid_solver_frame_begin(self.h, slot, c_void_p(pr[0]),
+                                                      c_void_p(vr) if vr is not None else None))
+
+    def frame_wait(self, slot: int) -> None:
+        self._check(self.lib.fluid_solver_frame_wait(self.h, slot))
+
     def read_debug(self, what: int) -> np.ndarray:
         if what == _capi.DEBUG_CELL_KEYS:
             out = np.empty((self.n, 3), np.int32)
@@ -226,3 +237,38 @@ def cuda_step(params: FluidParams, pos: np.ndarray, vel: np.ndarray, time: float
     if rc != 0:
         raise FluidError(rc, "fluid_gb300_cuda_step")
     return t.value
+
+
+def write_vtp(path: str, pos: np.ndarray, binary: bool = True) -> None:
+    """One frame of positions (3, N) as VTK PolyData (.vtp)."""
+    lib = _capi.load()
+    pos = np.ascontiguousarray(pos, np.float32)
+    rc = lib.fluid_write_vtp(path.encode(), pos[0].ctypes.data_as(c_void_p), pos[1].ctypes.data_as(c_void_p),
+                             pos[2].ctypes.data_as(c_void_p), pos.shape[1], int(binary))
+    if rc != 0:
+        raise FluidError(rc, f"write_vtp {path}")
+
+
+def write_pvd(path: str, times, files) -> None:
+    lib = _capi.load()
+    t = (c_double * len(times))(*times)
+    f = (c_char_p * len(files))(*[x.encode() for x in files])
+    rc = lib.fluid_write_pvd(path.encode(), t, f, len(files))
+    if rc != 0:
+        raise FluidError(rc, f"write_pvd {path}")
+
+
+def read_vtp(path: str) -> np.ndarray:
+    """Positions (3, N) from a .vtp written by write_vtp (either encoding)."""
+    import re
+
+    data = open(path, "rb").read()
+    n = int(re.search(rb'NumberOfPoints="(\d+)"', data).group(1))
+    if b'format="appended"' in data:
+        start = data.index(b"<AppendedData encoding=\"raw\">") + len(b"<AppendedData encoding=\"raw\">")
+        start = data.index(b"_", start) + 1
+        nbytes = int(np.frombuffer(data[start:start + 8], np.uint64)[0])
+        xyz = np.frombuffer(data[start + 8:start + 8 + nbytes], np.float32).reshape(n, 3)
+        return np.ascontiguousarray(xyz.T)
+    body = data.split(b'format="ascii">')[1].split(b"</DataArray>")[0]
+    return np.array(body.split(), dtype=np.float32).reshape(n, 3).T.copy()

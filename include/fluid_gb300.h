@@ -56,7 +56,7 @@ typedef struct fluid_params {
   float epsilon;                 /* core.h:24, lambda relaxation */
   int32_t solver_iterations;     /* core.h:25 */
   float neighbor_reserve_factor; /* core.h:26, neighbour-list growth factor */
-  int32_t use_uniform_grid;      /* core.h:27 */
+  int32_t use_uniform_grid;      /* core.h:27; 0 = all-pairs lists (O(N^2)) */
   int32_t enable_scorr;          /* core.h:28 */
   int32_t enable_xsph;           /* core.h:29 */
   int32_t enable_vorticity;      /* core.h:30 */
@@ -302,6 +302,33 @@ enum {
 /* Copies a debug record to host memory of `capacity` elements (int32/float). */
 int fluid_solver_read_debug(fluid_solver* solver, int32_t what, void* host_out,
                             int64_t capacity);
+
+/*
+ * Frame output (replaces the reference's per-frame host read of State plus
+ * VtkWriter::write_frame, app/src/main.cpp:259-274, io/src/vtk_writer.cpp).
+ *
+ * fluid_solver_frame_begin starts copying the current positions (and
+ * velocities when host_vel is not NULL) into caller-owned host buffers of
+ * 3 * particles floats (x block, y block, z block, caller order) -- pinned
+ * memory makes the copy asynchronous. It waits for steps already enqueued,
+ * then returns at once; the copy runs on its own stream and overlaps steps
+ * enqueued afterwards. Two slots (0, 1) may be in flight; reusing a slot
+ * waits for its previous copy. fluid_solver_frame_wait blocks until the
+ * slot's copy has landed.
+ */
+int fluid_solver_frame_begin(fluid_solver* solver, int32_t slot, float* host_pos,
+                             float* host_vel);
+int fluid_solver_frame_wait(fluid_solver* solver, int32_t slot);
+
+/* Writes one frame as VTK PolyData: binary == 0 reproduces the reference's
+ * ASCII .vtp byte for byte (io/src/vtk_writer.cpp:25-79); binary != 0 writes
+ * an appended raw block (20 bytes per particle). */
+int fluid_write_vtp(const char* path, const float* pos_x, const float* pos_y,
+                    const float* pos_z, int64_t count, int32_t binary);
+
+/* Writes a ParaView collection of frames (io/src/vtk_writer.cpp:107-130). */
+int fluid_write_pvd(const char* path, const double* times, const char* const* files,
+                    int64_t count);
 
 /* Last error message of this solver (static storage owned by the solver). */
 const char* fluid_solver_last_error(const fluid_solver* solver);
