@@ -322,6 +322,9 @@ def run_ours(args, world, rank, local):
         traj["kernel_ms_total"] = {k: round(v[0], 2) for k, v in tail.items() if v[1]}
     solver.close()
 
+    output = None
+    if not args.no_output and rank == 0:
+        output = run_output(sc, dev, stream, args)
     batched = None
     if not args.no_batched:
         batched = run_batched(args, dev, stream, l2_flush)
@@ -346,7 +349,7 @@ def run_ours(args, world, rank, local):
         "step_roofline": {"bytes_per_particle_step": ALGO_BYTES_PER_STEP, "frac": round(step_frac, 5)},
         "kernel_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in stage.items() if v[1]},
         "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches, "trajectory": traj,
-        "batched": batched, "differentiable": differentiable,
+        "batched": batched, "differentiable": differentiable, "output": output,
     }
     if world > 1:
         import torch.distributed as dist
@@ -514,6 +517,52 @@ def run_differentiable(args, dev, stream, with_cpu=True):
                                "note": "oracle FP64 adjoint linearised around the same FP32 trajectory"}
     s.close()
     return out
+
+
+def run_output(sc, dev, stream, args):
+    """Frame output at 1M particles, per frame: the reference's path
+    (synchronous read of the whole state, ASCII .vtp with 9 decimals) against
+    an asynchronous frame copy into pinned memory overlapped with the next
+    step, written as binary .vtp."""
+    import tempfile
+
+    import torch
+
+    from fluidsimulator_gb300.solver import Solver, write_vtp
+
+    n = sc.count
+    s = Solver(dev.index)
+    s.configure([sc.params], [n])
+    s.set_stream(stream.cuda_stream)
+    s.upload(sc.pos, sc.vel)
+    s.step(2)
+    frames = 3
+    hp = torch.empty((3, n), dtype=torch.float32, pin_memory=True).numpy()
+    with tempfile.TemporaryDirectory() as d:
+        t0 = time.perf_counter()
+        for k in range(frames):
+            s.step(1)
+            pos, _ = s.download()
+            write_vtp(os.path.join(d, f"a{k}.vtp"), pos, binary=False)
+        ascii_ms = 1e3 * (time.perf_counter() - t0) / frames
+        s.upload(sc.pos, sc.vel)
+        s.step(2)
+        t0 = time.perf_counter()
+        for k in range(frames):
+            s.frame_begin(0, hp)
+            s.step_async(1)  # the copy overlaps this step
+            s.frame_wait(0)
+            write_vtp(os.path.join(d, f"b{k}.vtp"), hp, binary=True)
+            s.synchronize()
+        binary_ms = 1e3 * (time.perf_counter() - t0) / frames
+        size_a = os.path.getsize(os.path.join(d, "a0.vtp"))
+        size_b = os.path.getsize(os.path.join(d, "b0.vtp"))
+    s.close()
+    return {"particles": n, "frames": frames,
+            "reference_path_ms_per_step_and_frame": round(ascii_ms, 2),
+            "async_binary_ms_per_step_and_frame": round(binary_ms, 2),
+            "speedup": round(ascii_ms / binary_ms, 2), "ascii_bytes": size_a, "binary_bytes": size_b,
+            "note": "one step plus one frame written per iteration, host wall clock, local disk"}
 
 
 def run_batched(args, dev, stream, l2_flush):
@@ -710,6 +759,7 @@ def main(argv=None):
     ap.add_argument("--batch-trajectory", type=int, default=30)
     ap.add_argument("--side", type=int, default=100, help="lattice side of the throughput scene (100 = 1M)")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-scene measurement")
+    ap.add_argument("--no-output", action="store_true", help="skip the frame-output measurement")
     ap.add_argument("--adj-steps", type=int, default=60)
     ap.add_argument("--fd-dirs", type=int, default=16)
     ap.add_argument("--traffic", type=float, default=None,
