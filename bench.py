@@ -210,10 +210,18 @@ def run_ours(args, world, rank, local):
     def restore():
         solver.upload(pos0, vel0)
 
-    # warm-up (also sizes the neighbour lists and captures the graphs)
+    # warm-up (also sizes the neighbour lists and captures the graphs), then
+    # the autotuner picks each kernel's launch shape on this state
     for _ in range(args.warmup):
         restore()
         solver.step(1)
+    tuning = None
+    if not args.no_autotune:
+        restore()
+        tuning = solver.autotune(2)
+        for _ in range(args.warmup):
+            restore()
+            solver.step(1)
     solver.set_profiling(True)
     solver.kernel_times(reset=True)
     launches0 = solver.stats()["kernel_launches"]
@@ -344,7 +352,8 @@ def run_ours(args, world, rank, local):
                                "4 iterations, one step over the initial batch per timed step",
                    "particles": n, "neighbors_per_particle": round(stats["neighbor_pairs"] / n, 2),
                    "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{world}",
-                   "graphs": True, "exact_fp32": True},
+                   "graphs": True, "exact_fp32": True,
+                   "tuning": ({k: [v["unroll"], v["block"]] for k, v in tuning.items()} if tuning else "default")},
         "roofline": roofline, "pair_roofline": pair_roofline,
         "step_roofline": {"bytes_per_particle_step": ALGO_BYTES_PER_STEP, "frac": round(step_frac, 5)},
         "kernel_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in stage.items() if v[1]},
@@ -760,6 +769,7 @@ def main(argv=None):
     ap.add_argument("--side", type=int, default=100, help="lattice side of the throughput scene (100 = 1M)")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-scene measurement")
     ap.add_argument("--no-output", action="store_true", help="skip the frame-output measurement")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--adj-steps", type=int, default=60)
     ap.add_argument("--fd-dirs", type=int, default=16)
     ap.add_argument("--traffic", type=float, default=None,

@@ -34,6 +34,11 @@ namespace fgb {
 namespace {
 
 constexpr int kMaxBlock = 512;  // largest block the tuner may pick
+// Minimum resident 512-thread blocks the list passes are compiled for (caps
+// their registers: 1 -> 128, 2 -> 64, 3 -> 42 per thread).
+#ifndef FGB_LIST_MIN_BLOCKS
+#define FGB_LIST_MIN_BLOCKS 2
+#endif
 constexpr int kMaxBuildBlock = 256;  // k_nbr_build: kStage ints per thread of shared memory
 constexpr int kStage = 40;           // list entries per lane staged in shared memory
 
@@ -464,29 +469,49 @@ struct Cell27 {
   int cx, cy, cz;
 };
 
+// Calls f(j, pos[j]) for j in [lo, hi) except j == self (kSkip), kFetch
+// records loaded before any is used. Lanes of a warp whose particles share a
+// cell walk the same j together, so each load is a broadcast.
+template <int kFetch, bool kSkip, typename F>
+__device__ __forceinline__ void scan_range(const float4* __restrict__ pos, int lo, int hi, int self, F& f) {
+  int j = lo;
+  for (; j + kFetch <= hi; j += kFetch) {
+    float4 q[kFetch];
+#pragma unroll
+    for (int u = 0; u < kFetch; ++u) q[u] = __ldg(pos + j + u);
+#pragma unroll
+    for (int u = 0; u < kFetch; ++u)
+      if (!kSkip || j + u != self) f(j + u, q[u]);
+  }
+  for (; j < hi; ++j)
+    if (!kSkip || j != self) f(j, __ldg(pos + j));
+}
+
 // Visits every j != i of the 27 cells around p in the reference's order
-// (core.cpp:211-243), calling f(j, q_j) for each candidate.
-template <typename F>
+// (core.cpp:211-243), calling f(j, q_j) for each candidate. Cell keys advance
+// incrementally along x; candidates are fetched kFetch at a time (issued
+// before any is tested, tested in order); only the centre cell tests j != i.
+template <int kFetch, typename F>
 __device__ __forceinline__ void for_each_candidate(const StepArgs& a, const uint32_t* ks, const GridInfo& g,
                                                    const SceneConst& c, int i, const float4 p,
                                                    const float4* __restrict__ pos, F&& f) {
   int cx, cy, cz;
   cell_of(c, p, cx, cy, cz);
+  const int xstride = g.dimy * g.dimz;
   for (int oz = -1; oz <= 1; ++oz) {
     const int z = cz + oz;
     if (z < g.minz || z >= g.minz + g.dimz) continue;
     for (int oy = -1; oy <= 1; ++oy) {
       const int y = cy + oy;
       if (y < g.miny || y >= g.miny + g.dimy) continue;
-      for (int ox = -1; ox <= 1; ++ox) {
+      uint32_t key = cell_key(g, cx - 1, y, z);
+      for (int ox = -1; ox <= 1; ++ox, key += static_cast<uint32_t>(xstride)) {
         const int xx = cx + ox;
         if (xx < g.minx || xx >= g.minx + g.dimx) continue;
         int first, end;
-        if (!cell_range(a, ks, cell_key(g, xx, y, z), first, end)) continue;
-        for (int j = first; j < end; ++j) {
-          if (j == i) continue;
-          f(j, pos[j]);
-        }
+        if (!cell_range(a, ks, key, first, end)) continue;
+        if (oz == 0 && oy == 0 && ox == 0) scan_range<kFetch, true>(pos, first, end, i, f);
+        else scan_range<kFetch, false>(pos, first, end, i, f);
       }
     }
   }
@@ -563,7 +588,7 @@ __global__ void __launch_bounds__(kMaxBuildBlock) k_nbr_build(StepArgs a) {
       }
     };
     if (c.all_pairs) for_each_pair_candidate(a, c, i, a.p[0], test);
-    else for_each_candidate(a, ks, g, c, i, p, a.p[0], test);
+    else for_each_candidate<4>(a, ks, g, c, i, p, a.p[0], test);
     a.cnt[i] = count;
   }
   const int mx = __reduce_max_sync(kFull, count);
@@ -604,7 +629,7 @@ __global__ void __launch_bounds__(kMaxBuildBlock) k_nbr_build(StepArgs a) {
 }
 
 // List entries kStage and above, for the warps k_nbr_build flagged.
-__global__ void __launch_bounds__(kMaxBlock) k_nbr_overflow(StepArgs a) {
+__global__ void __launch_bounds__(kMaxBlock, 1) k_nbr_overflow(StepArgs a) {
   if (failed(a.status)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n || !a.ovf[i >> 5]) return;
@@ -624,7 +649,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_nbr_overflow(StepArgs a) {
     }
   };
   if (c.all_pairs) for_each_pair_candidate(a, c, i, a.p[0], test);
-  else for_each_candidate(a, ks, g, c, i, p, a.p[0], test);
+  else for_each_candidate<4>(a, ks, g, c, i, p, a.p[0], test);
 }
 
 // ---------------------------------------------------------------------------
@@ -668,7 +693,7 @@ struct PosOmega {
 };
 
 template <int U>
-__global__ void __launch_bounds__(kMaxBlock) k_lambda(StepArgs a, int in) {
+__global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_lambda(StepArgs a, int in) {
   if (failed(a.status)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
@@ -706,7 +731,7 @@ __device__ __forceinline__ void commit(const StepArgs& a, const SceneConst& c, i
 }
 
 template <int U>
-__global__ void __launch_bounds__(kMaxBlock) k_delta(StepArgs a, int in, int last, int to_v2, int rest, float4* q_out) {
+__global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_delta(StepArgs a, int in, int last, int to_v2, int rest, float4* q_out) {
   if (failed(a.status)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
@@ -774,7 +799,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_commit(StepArgs a, int to_v2, int
 
 // XSPH (core.cpp:423-466): reads v2 (committed), writes v.
 template <int U>
-__global__ void __launch_bounds__(kMaxBlock) k_xsph(StepArgs a, int rest) {
+__global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_xsph(StepArgs a, int rest) {
   if (failed(a.status)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
@@ -812,7 +837,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_xsph(StepArgs a, int rest) {
 
 // Vorticity omega and |omega| (core.cpp:472-508).
 template <int U>
-__global__ void __launch_bounds__(kMaxBlock) k_omega(StepArgs a) {
+__global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_omega(StepArgs a) {
   if (failed(a.status)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
@@ -845,7 +870,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_omega(StepArgs a) {
 // Eta, confinement force, velocity update (core.cpp:512-570) and plane
 // restitution (core.cpp:573-612).
 template <int U>
-__global__ void __launch_bounds__(kMaxBlock) k_eta(StepArgs a, int rest) {
+__global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_eta(StepArgs a, int rest) {
   if (failed(a.status)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
