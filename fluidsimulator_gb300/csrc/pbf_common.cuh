@@ -9,6 +9,8 @@
 //   p0, p1        float4 predicted positions (p.w = scene), ping-pong over
 //                 the Jacobi iterations.
 //   v2            float4 velocity scratch for XSPH; omega float4 (w = |omega|).
+//   pl            float4 {p.xyz, lambda} of the current Jacobi iteration, so
+//                 the delta pass gathers one record per neighbour.
 //   lambda, rho[2] float per slot.
 //   keys/vals     radix-sort ping-pong (u32 cell key, int caller index).
 //   table         int2 (first, end) per cell of the per-scene bounding grids.
@@ -95,6 +97,7 @@ struct StepArgs {
   int* slot;
   float4* p[2];
   float4* omega;
+  float4* pl;              // {p.xyz, lambda}, written by the lambda pass
   float* lambda;
   float* rho;
   uint32_t* keys[2];

@@ -111,6 +111,19 @@ __device__ __forceinline__ float pow_n(float r, int n) {
   return powf(r, static_cast<float>(n));
 }
 
+// ratio^n with n fixed at compile time (kPow 2, 3 or 4), or read per scene
+// (kPow 0); the same operations as pow_n.
+template <int kPow>
+__device__ __forceinline__ float pow_k(float r, int n) {
+  if (kPow == 2) return r * r;
+  if (kPow == 3) return r * r * r;
+  if (kPow == 4) {
+    const float r2 = r * r;
+    return r2 * r2;
+  }
+  return pow_n(r, n);
+}
+
 // Plane restitution and friction on velocity (core.cpp:586-606).
 __device__ __forceinline__ void restitution(const SceneConst& c, float px, float py, float pz,
                                             float& vx, float& vy, float& vz) {
@@ -655,41 +668,37 @@ __global__ void __launch_bounds__(kMaxBlock, 1) k_nbr_overflow(StepArgs a) {
 // ---------------------------------------------------------------------------
 // Jacobi passes over the lists.
 
-// Walks this lane's list entries k = 0..n-1 in order. kUnroll indices and the
-// records they point at are fetched before any is used, so every warp keeps
-// several independent gathers in flight; the body still sees the entries in
-// list order, so sums accumulate in the reference's order.
+// Walks this lane's list entries k = 0..n-1 in order. kUnroll records are
+// fetched before any is used, and the next kUnroll list indices are fetched
+// while the current records are processed, so every warp keeps several
+// independent gathers in flight and the index latency stays hidden; the body
+// still sees the entries in list order, so sums accumulate in the
+// reference's order.
 template <int kUnroll, typename Load, typename Body>
 __device__ __forceinline__ void for_each_neighbor(const int* __restrict__ list, int n, Load&& load, Body&& body) {
   using Rec = decltype(load(0));
   int k = 0;
-  for (; k + kUnroll <= n; k += kUnroll) {
-    int j[kUnroll];
+  int j[kUnroll];
+  if (kUnroll <= n) {
 #pragma unroll
-    for (int u = 0; u < kUnroll; ++u) j[u] = __ldg(list + 32ll * (k + u));
+    for (int u = 0; u < kUnroll; ++u) j[u] = __ldg(list + 32ll * u);
+  }
+  for (; k + kUnroll <= n; k += kUnroll) {
     Rec r[kUnroll];
 #pragma unroll
     for (int u = 0; u < kUnroll; ++u) r[u] = load(j[u]);
+    if (k + 2 * kUnroll <= n) {
+#pragma unroll
+      for (int u = 0; u < kUnroll; ++u) j[u] = __ldg(list + 32ll * (k + kUnroll + u));
+    }
 #pragma unroll
     for (int u = 0; u < kUnroll; ++u) body(r[u]);
   }
   for (; k < n; ++k) body(load(__ldg(list + 32ll * k)));
 }
 
-struct PosLam {
-  float4 q;
-  float l;
-};
-struct PosVelRho {
-  float4 x, v;
-  float rho;
-};
 struct PosVel {
   float4 x, v;
-};
-struct PosOmega {
-  float4 x;
-  float om;
 };
 
 template <int U>
@@ -710,14 +719,22 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_lambda(StepA
     if (r2 < h2) acc.add(c, dx, dy, dz, r2);
   });
   float rho;
-  a.lambda[i] = finish_lambda(c, acc.rho, acc.gsx, acc.gsy, acc.gsz, acc.sum_g2, rho);
+  const float lam = finish_lambda(c, acc.rho, acc.gsx, acc.gsy, acc.gsz, acc.sum_g2, rho);
+  a.lambda[i] = lam;
   a.rho[i] = rho;
+  a.pl[i] = make_float4(p.x, p.y, p.z, lam);
 }
 
 // Commit v = (p - x)/dt, x = p (core.cpp:414-421); restitution when this is
-// the step's last velocity write.
+// the step's last velocity write. Ahead of XSPH (to_v2) it also writes the
+// record XSPH gathers per neighbour, {x.xyz, m / rho} into xr: the
+// per-neighbour factor of core.cpp:446-447, the same value for every i.
 __device__ __forceinline__ void commit(const StepArgs& a, const SceneConst& c, int i, float px, float py, float pz,
-                                       float scene_bits, bool to_v2, bool rest) {
+                                       float scene_bits, bool to_v2, bool rest, float4* xr) {
+  if (to_v2) {
+    const float rho = a.rho[i];
+    xr[i] = make_float4(px, py, pz, (rho > 0.0f) ? (c.mass / rho) : 0.0f);
+  }
   float4 x = a.x[i];
   float vx = (px - x.x) / c.dt;
   float vy = (py - x.y) / c.dt;
@@ -730,30 +747,31 @@ __device__ __forceinline__ void commit(const StepArgs& a, const SceneConst& c, i
   (to_v2 ? a.v2 : a.v)[i] = make_float4(vx, vy, vz, scene_bits);
 }
 
-template <int U>
+// kPow: the s_corr exponent when every scene with s_corr shares it (2, 3,
+// 4), else 0 (read per scene).
+template <int U, int kPow>
 __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_delta(StepArgs a, int in, int last, int to_v2, int rest, float4* q_out) {
   if (failed(a.status)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
-  const float4* __restrict__ pos = a.p[in];
-  const float4 p = pos[i];
+  const float4 p = a.p[in][i];
   const SceneConst& c = a.sc[__float_as_int(p.w)];
   const int n = a.cnt[i];
   const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
-  const float* __restrict__ lam = a.lambda;
-  const float li = lam[i];
+  const float4* __restrict__ pl = a.pl;  // {p_j, lambda_j} in one record
+  const float li = a.lambda[i];
   const float h2 = c.h2;
   float ax = 0.0f, ay = 0.0f, az = 0.0f;
   const bool scorr = c.scorr_on != 0;
-  for_each_neighbor<U>(list, n, [&](int j) { return PosLam{__ldg(pos + j), __ldg(lam + j)}; }, [&](const PosLam r) {
-    const float dx = p.x - r.q.x, dy = p.y - r.q.y, dz = p.z - r.q.z;
+  for_each_neighbor<U>(list, n, [&](int j) { return __ldg(pl + j); }, [&](const float4 r) {
+    const float dx = p.x - r.x, dy = p.y - r.y, dz = p.z - r.z;
     const float r2 = dist2(dx, dy, dz);
     if (r2 < h2) {
       const float gf = spiky(c, clamped_r(c, r2));
-      float s = li + r.l;
+      float s = li + r.w;
       if (scorr) {
         const float ratio = poly6(c, r2) * c.scorr_inv_wdq;
-        s += c.scorr_neg_k * pow_n(ratio, c.scorr_n);
+        s += c.scorr_neg_k * pow_k<kPow>(ratio, c.scorr_n);
       }
       ax += s * gf * dx;
       ay += s * gf * dy;
@@ -784,7 +802,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_delta(StepAr
   if (!last) {
     a.p[in ^ 1][i] = make_float4(nx, ny, nz, p.w);
   } else {
-    commit(a, c, i, nx, ny, nz, p.w, to_v2 != 0, rest != 0);
+    commit(a, c, i, nx, ny, nz, p.w, to_v2 != 0, rest != 0, a.p[in ^ 1]);
   }
 }
 
@@ -794,16 +812,17 @@ __global__ void __launch_bounds__(kMaxBlock) k_commit(StepArgs a, int to_v2, int
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   const float4 p = a.p[0][i];
-  commit(a, a.sc[__float_as_int(p.w)], i, p.x, p.y, p.z, p.w, to_v2 != 0, rest != 0);
+  commit(a, a.sc[__float_as_int(p.w)], i, p.x, p.y, p.z, p.w, to_v2 != 0, rest != 0, a.p[1]);
 }
 
-// XSPH (core.cpp:423-466): reads v2 (committed), writes v.
+// XSPH (core.cpp:423-466): reads v2 (committed) and the committing pass's
+// {x, m / rho} records xr, writes v.
 template <int U>
-__global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_xsph(StepArgs a, int rest) {
+__global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_xsph(StepArgs a, int rest, const float4* xr) {
   if (failed(a.status)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
-  const float4* __restrict__ xs = a.x;
+  const float4* __restrict__ xs = xr;
   const float4* __restrict__ vs = a.v2;
   const float4 xi = xs[i];
   const float4 vi = vs[i];
@@ -812,16 +831,15 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_xsph(StepArg
   if (c.xsph_on) {
     const int n = a.cnt[i];
     const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
-    const float* __restrict__ rho = a.rho;
     const float h2 = c.h2;
     float sx = 0.0f, sy = 0.0f, sz = 0.0f;
     for_each_neighbor<U>(
-        list, n, [&](int j) { return PosVelRho{__ldg(xs + j), __ldg(vs + j), __ldg(rho + j)}; },
-        [&](const PosVelRho r) {
+        list, n, [&](int j) { return PosVel{__ldg(xs + j), __ldg(vs + j)}; },
+        [&](const PosVel r) {
           const float r2 = dist2(xi.x - r.x.x, xi.y - r.x.y, xi.z - r.x.z);
           if (r2 < h2) {
             const float W = poly6(c, r2);
-            const float inv_rho_j = (r.rho > 0.0f) ? (c.mass / r.rho) : 0.0f;
+            const float inv_rho_j = r.x.w;
             sx += (r.v.x - vi.x) * W * inv_rho_j;
             sy += (r.v.y - vi.y) * W * inv_rho_j;
             sz += (r.v.z - vi.z) * W * inv_rho_j;
@@ -864,7 +882,9 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_omega(StepAr
       }
     });
   }
-  a.omega[i] = make_float4(ox, oy, oz, sqrtf(ox * ox + oy * oy + oz * oz));
+  const float mag = sqrtf(ox * ox + oy * oy + oz * oz);
+  a.omega[i] = make_float4(ox, oy, oz, mag);
+  a.pl[i] = make_float4(xi.x, xi.y, xi.z, mag);  // the record k_eta gathers per neighbour
 }
 
 // Eta, confinement force, velocity update (core.cpp:512-570) and plane
@@ -874,24 +894,23 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_eta(StepArgs
   if (failed(a.status)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
-  const float4* __restrict__ xs = a.x;
-  const float4* __restrict__ om = a.omega;
-  const float4 xi = xs[i];
+  const float4* __restrict__ xo = a.pl;  // {x_j, |omega_j|}, written by k_omega
+  const float4 xi = a.x[i];
   float4 v = a.v[i];
   const SceneConst& c = a.sc[__float_as_int(v.w)];
   if (c.vort_on) {
-    const float4 oi = om[i];
+    const float4 oi = a.omega[i];
     const int n = a.cnt[i];
     const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
     const float h2 = c.h2;
     float ex = 0.0f, ey = 0.0f, ez = 0.0f;
-    for_each_neighbor<U>(list, n, [&](int j) { return PosOmega{__ldg(xs + j), __ldg(&om[j].w)}; },
-                      [&](const PosOmega r) {
-                        const float dx = xi.x - r.x.x, dy = xi.y - r.x.y, dz = xi.z - r.x.z;
+    for_each_neighbor<U>(list, n, [&](int j) { return __ldg(xo + j); },
+                      [&](const float4 r) {
+                        const float dx = xi.x - r.x, dy = xi.y - r.y, dz = xi.z - r.z;
                         const float r2 = dist2(dx, dy, dz);
                         if (r2 < h2) {
                           const float gf = spiky(c, clamped_r(c, r2));
-                          const float coeff = r.om - oi.w;
+                          const float coeff = r.w - oi.w;
                           ex += coeff * (gf * dx);
                           ey += coeff * (gf * dy);
                           ez += coeff * (gf * dz);
@@ -981,6 +1000,35 @@ inline int blocks_for(long long n, int threads) { return static_cast<int>((n + t
     }                                                                   \
   } while (0)
 
+template <int kPow>
+struct DeltaPow {
+  template <int U>
+  static void launch(int grid, int block, cudaStream_t st, const StepArgs& a, int in, int last, int to_v2, int rest,
+                     float4* q_out) {
+    k_delta<U, kPow><<<grid, block, 0, st>>>(a, in, last, to_v2, rest, q_out);
+  }
+  static void dispatch(int u, int grid, int block, cudaStream_t st, const StepArgs& a, int in, int last, int to_v2,
+                       int rest, float4* q_out) {
+    switch (u) {
+      case 1: launch<1>(grid, block, st, a, in, last, to_v2, rest, q_out); break;
+      case 2: launch<2>(grid, block, st, a, in, last, to_v2, rest, q_out); break;
+      case 8: launch<8>(grid, block, st, a, in, last, to_v2, rest, q_out); break;
+      default: launch<4>(grid, block, st, a, in, last, to_v2, rest, q_out); break;
+    }
+  }
+};
+
+void launch_delta(const StepPlan& plan, int grid, int block, cudaStream_t st, const StepArgs& a, int in, int last,
+                  int to_v2, int rest, float4* q_out) {
+  const int u = plan.unroll[FLUID_KERNEL_DELTA];
+  switch (plan.scorr_pow) {
+    case 2: DeltaPow<2>::dispatch(u, grid, block, st, a, in, last, to_v2, rest, q_out); break;
+    case 3: DeltaPow<3>::dispatch(u, grid, block, st, a, in, last, to_v2, rest, q_out); break;
+    case 4: DeltaPow<4>::dispatch(u, grid, block, st, a, in, last, to_v2, rest, q_out); break;
+    default: DeltaPow<0>::dispatch(u, grid, block, st, a, in, last, to_v2, rest, q_out); break;
+  }
+}
+
 }  // namespace
 
 void LaunchMarks::start() {
@@ -1059,8 +1107,7 @@ cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t s
     const int last = (it == plan.iterations - 1) ? 1 : 0;
     const int b = plan.block[FLUID_KERNEL_DELTA];
     float4* q_out = rec ? rec->q + static_cast<size_t>(it) * a.n : nullptr;
-    FGB_DISPATCH_UNROLL(plan.unroll[FLUID_KERNEL_DELTA], k_delta, blocks_for(a.n, b), b, st, a, in, last, to_v2,
-                        last ? rest_commit : 0, q_out);
+    launch_delta(plan, blocks_for(a.n, b), b, st, a, in, last, to_v2, last ? rest_commit : 0, q_out);
     m.mark(FLUID_KERNEL_DELTA);
     if (rec)  // p^(it+1); the last iteration's lands in x (commit)
       cudaMemcpyAsync(rec->p + static_cast<size_t>(it + 1) * a.n, last ? a.x : a.p[in ^ 1], n4,
@@ -1069,8 +1116,10 @@ cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t s
   if (rec) cudaMemcpyAsync(rec->rho, a.rho, n1, cudaMemcpyDeviceToDevice, st);
   if (plan.xsph) {
     const int b = plan.block[FLUID_KERNEL_XSPH];
+    // The committing pass left {x, m / rho} in the p buffer it did not use.
+    const float4* xr = a.p[plan.iterations == 0 ? 1 : (plan.iterations & 1)];
     FGB_DISPATCH_UNROLL(plan.unroll[FLUID_KERNEL_XSPH], k_xsph, blocks_for(a.n, b), b, st, a,
-                        (!plan.vorticity && plan.restitution) ? 1 : 0);
+                        (!plan.vorticity && plan.restitution) ? 1 : 0, xr);
     m.mark(FLUID_KERNEL_XSPH);
   }
   if (plan.vorticity) {

@@ -17,6 +17,7 @@ struct StepPlan {
   bool vorticity = false; // some scene runs vorticity confinement
   bool restitution = false;
   int radix_passes = 1;   // passes launched (cover the grid capacity)
+  int scorr_pow = 0;      // s_corr exponent shared by every s_corr scene (2-4), else 0
   // Per-kernel launch shape (indexed by FLUID_KERNEL_*), chosen by the
   // autotuner: neighbour entries fetched ahead (1, 2, 4, 8) in the list
   // passes, and threads per block (128, 256, 512) for the neighbour kernels.
@@ -29,6 +30,18 @@ struct StepPlan {
     }
   }
 };
+
+// The s_corr exponent to compile into the delta pass: n when every scene with
+// s_corr on uses the same n in {2, 3, 4}, else 0 (n read per scene).
+inline int shared_scorr_pow(const SceneConst* sc, int scenes) {
+  int n = 0;
+  for (int s = 0; s < scenes; ++s) {
+    if (!sc[s].scorr_on) continue;
+    if (sc[s].scorr_n < 2 || sc[s].scorr_n > 4 || (n && n != sc[s].scorr_n)) return 0;
+    n = sc[s].scorr_n;
+  }
+  return n;
+}
 
 // Kernels whose launch shape the autotuner chooses.
 inline bool tunable_unroll(int k) {

@@ -48,7 +48,8 @@ constexpr size_t kI32 = up(sizeof(int) * kMaxN);
 // Byte offsets of every buffer inside the arena.
 constexpr size_t kX0 = 0, kX1 = kX0 + kF4, kV0 = kX1 + kF4, kV1 = kV0 + kF4;
 constexpr size_t kP0 = kV1 + kF4, kP1 = kP0 + kF4, kV2 = kP1 + kF4, kOmega = kV2 + kF4;
-constexpr size_t kSlot0 = kOmega + kF4, kSlot1 = kSlot0 + kI32, kRho0 = kSlot1 + kI32, kRho1 = kRho0 + kI32;
+constexpr size_t kPl = kOmega + kF4;
+constexpr size_t kSlot0 = kPl + kF4, kSlot1 = kSlot0 + kI32, kRho0 = kSlot1 + kI32, kRho1 = kRho0 + kI32;
 constexpr size_t kLambda = kRho1 + kI32, kKeys0 = kLambda + kI32, kKeys1 = kKeys0 + kI32;
 constexpr size_t kVals0 = kKeys1 + kI32, kVals1 = kVals0 + kI32, kCnt = kVals1 + kI32;
 constexpr size_t kDepth = kCnt + kI32, kWbase = kDepth + up(sizeof(int) * (kMaxWarps + 1));
@@ -105,6 +106,7 @@ StepArgs carve(unsigned char* b, int n) {
   a.p[0] = at<float4>(b, kP0);
   a.p[1] = at<float4>(b, kP1);
   a.omega = at<float4>(b, kOmega);
+  a.pl = at<float4>(b, kPl);
   a.lambda = at<float>(b, kLambda);
   a.rho = at<float>(b, kRho1);
   a.keys[0] = at<uint32_t>(b, kKeys0);
@@ -164,6 +166,7 @@ extern "C" int fluid_gb300_step_noalloc(const fluid_params* params, int64_t coun
   plan.vorticity = c.vort_on != 0;
   plan.restitution = c.rest_on != 0;
   plan.radix_passes = 3;  // keys < FLUID_NOALLOC_MAX_CELLS = 2^18
+  plan.scorr_pow = shared_scorr_pow(&c, 1);
   LaunchMarks marks;      // profiling off
 
   if (cudaMemcpyAsync(const_cast<SceneConst*>(a.sc), &c, sizeof(c), cudaMemcpyHostToDevice, st) != cudaSuccess)

@@ -248,6 +248,7 @@ class Solver {
     }
     ok &= v2_.alloc(np) == cudaSuccess;
     ok &= omega_.alloc(np) == cudaSuccess;
+    ok &= pl_.alloc(np) == cudaSuccess;
     ok &= lambda_.alloc(np) == cudaSuccess;
     ok &= cnt_.alloc(np) == cudaSuccess;
     ok &= depth_.alloc(static_cast<size_t>(warps_) + 1) == cudaSuccess;
@@ -295,7 +296,7 @@ class Solver {
     StepPlan old = plan_;
     make_plan();
     if (old.iterations != plan_.iterations || old.xsph != plan_.xsph || old.vorticity != plan_.vorticity ||
-        old.restitution != plan_.restitution)
+        old.restitution != plan_.restitution || old.scorr_pow != plan_.scorr_pow)
       invalidate_graphs();
     return FLUID_OK;
   }
@@ -840,6 +841,7 @@ class Solver {
       plan_.restitution |= c.rest_on != 0;
     }
     plan_.radix_passes = std::max(1, (bits_for(grid_cap_) + 7) / 8);
+    plan_.scorr_pow = shared_scorr_pow(sc_host_.data(), S_);
   }
 
   void advance_times(int steps) {
@@ -867,6 +869,7 @@ class Solver {
     a.p[0] = p_[0].p;
     a.p[1] = p_[1].p;
     a.omega = omega_.p;
+    a.pl = pl_.p;
     a.lambda = lambda_.p;
     a.rho = rho_[par ^ 1].p;
     a.keys[0] = keys_[0].p;
@@ -1196,7 +1199,7 @@ class Solver {
   long long steps_ = 0, regrows_ = 0, launches_ = 0, launches_per_step_ = 0;
   long long last_pairs_ = 0;
   int last_max_ = 0, last_cells_ = 0;
-  DBuf<float4> x_[2], v_[2], p_[2], v2_, omega_;
+  DBuf<float4> x_[2], v_[2], p_[2], v2_, omega_, pl_;
   DBuf<int> slot_[2], vals_[2], cnt_, depth_, ovf_, nbr_, bmin_, bmax_;
   DBuf<float> rho_[2], lambda_;
   DBuf<uint32_t> keys_[2], hist_, digit_total_;
