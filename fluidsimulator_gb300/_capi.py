@@ -184,6 +184,10 @@ def _declare(lib):
     lib.fluid_solver_get_tuning.restype = c_int
     lib.fluid_solver_set_tuning.argtypes = [c_void_p, POINTER(c_int32), POINTER(c_int32), c_int32]
     lib.fluid_solver_set_tuning.restype = c_int
+    lib.fluid_solver_get_sort_bits.argtypes = [c_void_p, POINTER(c_int32)]
+    lib.fluid_solver_get_sort_bits.restype = c_int
+    lib.fluid_solver_set_sort_bits.argtypes = [c_void_p, c_int32]
+    lib.fluid_solver_set_sort_bits.restype = c_int
     lib.fluid_solver_step_backward.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int32]
     lib.fluid_solver_step_backward.restype = c_int
     lib.fluid_solver_record.argtypes = [c_void_p, c_int32, c_int32]

@@ -30,6 +30,7 @@ namespace fgb {
 constexpr int kBlock = 256;
 constexpr int kRadixItems = 8;                      // keys per thread
 constexpr int kRadixTile = kBlock * kRadixItems;    // keys per CTA
+constexpr int kRadixMaxBins = 1 << 11;                // widest digit (11 bits)
 constexpr int kRadixMaxPasses = 4;                  // 8-bit digits of a u32
 constexpr unsigned kFull = 0xffffffffu;
 
@@ -102,8 +103,8 @@ struct StepArgs {
   float* rho;
   uint32_t* keys[2];
   int* vals[2];
-  uint32_t* hist;         // 256 x tiles, digit-major
-  uint32_t* digit_total;  // kRadixMaxPasses x 256
+  uint32_t* hist;         // (digits) x tiles, digit-major
+  uint32_t* digit_total;  // kRadixMaxPasses x kRadixMaxBins
   int2* table;
   int* cnt;
   int* depth;             // per warp

@@ -25,6 +25,7 @@
 // prediction use explicit round-to-nearest intrinsics as well.
 
 #include <climits>
+#include <type_traits>
 #include <cstdint>
 
 #include "pbf_common.cuh"
@@ -242,10 +243,11 @@ __global__ void __launch_bounds__(kBlock) k_bounds(StepArgs a) {
   }
 }
 
-__global__ void __launch_bounds__(kBlock) k_grid_setup(StepArgs a) {
+// radix_bits: digit width of the sort (8 or 11), which sets the pass count.
+__global__ void __launch_bounds__(kBlock) k_grid_setup(StepArgs a, int radix_bits) {
   if (failed(a.status)) return;
   DevStatus* st = a.status;
-  for (int i = threadIdx.x; i < kRadixMaxPasses * 256; i += blockDim.x) a.digit_total[i] = 0;
+  for (int i = threadIdx.x; i < kRadixMaxPasses * kRadixMaxBins; i += blockDim.x) a.digit_total[i] = 0;
   if (threadIdx.x != 0) return;
   st->step = st->started;
   st->started = st->started + 1;
@@ -283,7 +285,7 @@ __global__ void __launch_bounds__(kBlock) k_grid_setup(StepArgs a) {
     a.bmax[3 * s + 0] = a.bmax[3 * s + 1] = a.bmax[3 * s + 2] = INT_MIN;
   }
   st->total_cells = total;
-  st->npass = total <= 1ull ? 0 : (32 - __clz(static_cast<int>(total - 1ull)) + 7) / 8;
+  st->npass = total <= 1ull ? 0 : (32 - __clz(static_cast<int>(total - 1ull)) + radix_bits - 1) / radix_bits;
   if (domain) {
     set_error(st, FLUID_ERR_DOMAIN);
   } else if (static_cast<long long>(total) > a.grid_capacity) {
@@ -311,41 +313,49 @@ __global__ void __launch_bounds__(kBlock) k_keys(StepArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// Stable LSD radix sort, 8-bit digits. Pass p reads keys[p&1] (pass 0: values
-// are the caller indices themselves) and writes keys[(p+1)&1].
+// Stable LSD radix sort, kBits-bit digits (8 or 11, chosen by the autotuner).
+// Pass p reads keys[p&1] (pass 0: values are the caller indices themselves)
+// and writes keys[(p+1)&1].
 
+template <int kBits>
 __global__ void __launch_bounds__(kBlock) k_radix_hist(StepArgs a, int pass) {
   if (failed(a.status) || pass >= a.status->npass) return;
-  __shared__ uint32_t cnt[kBlock / 32][256];
-  const int warp = threadIdx.x >> 5;
-  for (int i = threadIdx.x; i < (kBlock / 32) * 256; i += kBlock) (&cnt[0][0])[i] = 0;
+  constexpr int kBins = 1 << kBits;
+  constexpr int kCopies = kBits <= 8 ? kBlock / 32 : 1;  // one histogram per warp where they fit
+  __shared__ uint32_t cnt[kCopies][kBins];
+  const int copy = kCopies > 1 ? (threadIdx.x >> 5) : 0;
+  for (int i = threadIdx.x; i < kCopies * kBins; i += kBlock) (&cnt[0][0])[i] = 0;
   __syncthreads();
   const uint32_t* kin = a.keys[pass & 1];
-  const int shift = 8 * pass;
+  const int shift = kBits * pass;
   const long long base = static_cast<long long>(blockIdx.x) * kRadixTile;
 #pragma unroll
   for (int r = 0; r < kRadixItems; ++r) {
     const long long idx = base + r * kBlock + threadIdx.x;
-    if (idx < a.n) atomicAdd(&cnt[warp][(kin[idx] >> shift) & 255u], 1u);
+    if (idx < a.n) atomicAdd(&cnt[copy][(kin[idx] >> shift) & (kBins - 1u)], 1u);
   }
   __syncthreads();
-  const int d = threadIdx.x;
-  uint32_t sum = 0;
+  for (int d = threadIdx.x; d < kBins; d += kBlock) {
+    uint32_t sum = 0;
 #pragma unroll
-  for (int w = 0; w < kBlock / 32; ++w) sum += cnt[w][d];
-  a.hist[static_cast<long long>(d) * a.tiles + blockIdx.x] = sum;
-  if (sum) atomicAdd(&a.digit_total[pass * 256 + d], sum);
+    for (int w = 0; w < kCopies; ++w) sum += cnt[w][d];
+    a.hist[static_cast<long long>(d) * a.tiles + blockIdx.x] = sum;
+    if (sum) atomicAdd(&a.digit_total[pass * kBins + d], sum);
+  }
 }
 
 // One CTA per digit: exclusive scan of that digit's tile counts plus the
 // number of keys with a smaller digit.
+template <int kBits>
 __global__ void __launch_bounds__(kBlock) k_radix_scan(StepArgs a, int pass) {
   if (failed(a.status) || pass >= a.status->npass) return;
+  constexpr int kBins = 1 << kBits;
   __shared__ uint32_t warp_sums[kBlock / 32];
   __shared__ uint32_t carry;
   const int d = blockIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint32_t below = (threadIdx.x < d) ? a.digit_total[pass * 256 + threadIdx.x] : 0u;
+  uint32_t below = 0;
+  for (int e = threadIdx.x; e < d; e += kBlock) below += a.digit_total[pass * kBins + e];
   below = __reduce_add_sync(kFull, below);
   if (lane == 0) warp_sums[warp] = below;
   __syncthreads();
@@ -382,19 +392,24 @@ __global__ void __launch_bounds__(kBlock) k_radix_scan(StepArgs a, int pass) {
   }
 }
 
+template <int kBits>
 __global__ void __launch_bounds__(kBlock) k_radix_scatter(StepArgs a, int pass) {
   if (failed(a.status) || pass >= a.status->npass) return;
-  __shared__ uint32_t wcnt[kBlock / 32][256];
-  __shared__ uint32_t goff[256];
+  constexpr int kBins = 1 << kBits;
+  // Per-warp digit counts; at most 32 * kRadixItems * (kBlock / 32) = 2048
+  // per tile, so 16 bits hold them when 32-bit counters would not fit.
+  using Count = typename std::conditional<(kBits <= 8), uint32_t, uint16_t>::type;
+  __shared__ Count wcnt[kBlock / 32][kBins];
+  __shared__ uint32_t goff[kBins];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int i = threadIdx.x; i < (kBlock / 32) * 256; i += kBlock) (&wcnt[0][0])[i] = 0;
-  goff[threadIdx.x] = a.hist[static_cast<long long>(threadIdx.x) * a.tiles + blockIdx.x];
+  for (int i = threadIdx.x; i < (kBlock / 32) * kBins; i += kBlock) (&wcnt[0][0])[i] = 0;
+  for (int d = threadIdx.x; d < kBins; d += kBlock) goff[d] = a.hist[static_cast<long long>(d) * a.tiles + blockIdx.x];
   __syncthreads();
   const uint32_t* kin = a.keys[pass & 1];
   const int* vin = a.vals[pass & 1];
   uint32_t* kout = a.keys[(pass + 1) & 1];
   int* vout = a.vals[(pass + 1) & 1];
-  const int shift = 8 * pass;
+  const int shift = kBits * pass;
   // Warp w ranks its contiguous 32*kRadixItems keys in order, 32 at a time.
   const long long base = static_cast<long long>(blockIdx.x) * kRadixTile + warp * (32 * kRadixItems);
   uint32_t key[kRadixItems];
@@ -407,24 +422,23 @@ __global__ void __launch_bounds__(kBlock) k_radix_scatter(StepArgs a, int pass) 
     const bool ok = idx < a.n;
     key[r] = ok ? kin[idx] : 0u;
     val[r] = ok ? (pass == 0 ? static_cast<int>(idx) : vin[idx]) : 0;
-    const int d = ok ? static_cast<int>((key[r] >> shift) & 255u) : 256;
+    const int d = ok ? static_cast<int>((key[r] >> shift) & (kBins - 1u)) : kBins;
     dig[r] = d;
     const unsigned peers = __match_any_sync(kFull, d);
     const uint32_t before = __popc(peers & lanemask_lt(lane));
-    const uint32_t run = (d < 256) ? wcnt[warp][d] : 0u;
+    const uint32_t run = (d < kBins) ? static_cast<uint32_t>(wcnt[warp][d]) : 0u;
     __syncwarp();
-    if (d < 256 && before == 0) wcnt[warp][d] = run + __popc(peers);
+    if (d < kBins && before == 0) wcnt[warp][d] = static_cast<Count>(run + __popc(peers));
     __syncwarp();
     rank[r] = run + before;
   }
   __syncthreads();
-  {
-    const int d = threadIdx.x;
+  for (int d = threadIdx.x; d < kBins; d += kBlock) {
     uint32_t run = 0;
 #pragma unroll
     for (int w = 0; w < kBlock / 32; ++w) {
       const uint32_t t = wcnt[w][d];
-      wcnt[w][d] = run;
+      wcnt[w][d] = static_cast<Count>(run);
       run += t;
     }
   }
@@ -432,7 +446,7 @@ __global__ void __launch_bounds__(kBlock) k_radix_scatter(StepArgs a, int pass) 
 #pragma unroll
   for (int r = 0; r < kRadixItems; ++r) {
     const int d = dig[r];
-    if (d < 256) {
+    if (d < kBins) {
       const uint32_t pos = goff[d] + wcnt[warp][d] + rank[r];
       kout[pos] = key[r];
       vout[pos] = val[r];
@@ -1061,16 +1075,24 @@ cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t s
   m.start();
   k_bounds<<<nb, kBlock, 0, st>>>(a);
   m.mark(FLUID_KERNEL_BOUNDS);
-  k_grid_setup<<<1, kBlock, 0, st>>>(a);
+  k_grid_setup<<<1, kBlock, 0, st>>>(a, plan.radix_bits);
   m.mark(FLUID_KERNEL_GRID);
   k_keys<<<nb, kBlock, 0, st>>>(a);
   m.mark(FLUID_KERNEL_KEYS);
   for (int pass = 0; pass < plan.radix_passes; ++pass) {
-    k_radix_hist<<<a.tiles, kBlock, 0, st>>>(a, pass);
-    m.mark(FLUID_KERNEL_RADIX_HIST);
-    k_radix_scan<<<256, kBlock, 0, st>>>(a, pass);
-    m.mark(FLUID_KERNEL_RADIX_SCAN);
-    k_radix_scatter<<<a.tiles, kBlock, 0, st>>>(a, pass);
+    if (plan.radix_bits == 11) {
+      k_radix_hist<11><<<a.tiles, kBlock, 0, st>>>(a, pass);
+      m.mark(FLUID_KERNEL_RADIX_HIST);
+      k_radix_scan<11><<<1 << 11, kBlock, 0, st>>>(a, pass);
+      m.mark(FLUID_KERNEL_RADIX_SCAN);
+      k_radix_scatter<11><<<a.tiles, kBlock, 0, st>>>(a, pass);
+    } else {
+      k_radix_hist<8><<<a.tiles, kBlock, 0, st>>>(a, pass);
+      m.mark(FLUID_KERNEL_RADIX_HIST);
+      k_radix_scan<8><<<1 << 8, kBlock, 0, st>>>(a, pass);
+      m.mark(FLUID_KERNEL_RADIX_SCAN);
+      k_radix_scatter<8><<<a.tiles, kBlock, 0, st>>>(a, pass);
+    }
     m.mark(FLUID_KERNEL_RADIX_SCATTER);
   }
   k_reorder<<<nb, kBlock, 0, st>>>(a);

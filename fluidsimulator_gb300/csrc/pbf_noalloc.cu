@@ -55,8 +55,8 @@ constexpr size_t kVals0 = kKeys1 + kI32, kVals1 = kVals0 + kI32, kCnt = kVals1 +
 constexpr size_t kDepth = kCnt + kI32, kWbase = kDepth + up(sizeof(int) * (kMaxWarps + 1));
 constexpr size_t kOvf = kWbase + up(sizeof(long long) * (kMaxWarps + 1));
 constexpr size_t kHist = kOvf + up(sizeof(int) * (kMaxWarps + 1));
-constexpr size_t kDigits = kHist + up(sizeof(uint32_t) * 256 * kMaxTiles);
-constexpr size_t kBmin = kDigits + up(sizeof(uint32_t) * 256 * kRadixMaxPasses);
+constexpr size_t kDigits = kHist + up(sizeof(uint32_t) * kRadixMaxBins * kMaxTiles);
+constexpr size_t kBmin = kDigits + up(sizeof(uint32_t) * kRadixMaxBins * kRadixMaxPasses);
 constexpr size_t kBmax = kBmin + up(3 * sizeof(int));
 constexpr size_t kGrid = kBmax + up(3 * sizeof(int));
 constexpr size_t kStatus = kGrid + up(sizeof(GridInfo));
@@ -165,6 +165,7 @@ extern "C" int fluid_gb300_step_noalloc(const fluid_params* params, int64_t coun
   plan.xsph = c.xsph_on != 0;
   plan.vorticity = c.vort_on != 0;
   plan.restitution = c.rest_on != 0;
+  plan.radix_bits = 8;
   plan.radix_passes = 3;  // keys < FLUID_NOALLOC_MAX_CELLS = 2^18
   plan.scorr_pow = shared_scorr_pow(&c, 1);
   LaunchMarks marks;      // profiling off

@@ -254,8 +254,8 @@ class Solver {
     ok &= depth_.alloc(static_cast<size_t>(warps_) + 1) == cudaSuccess;
     ok &= ovf_.alloc(static_cast<size_t>(warps_) + 1) == cudaSuccess;
     ok &= wbase_.alloc(static_cast<size_t>(warps_) + 1) == cudaSuccess;
-    ok &= hist_.alloc(static_cast<size_t>(tiles_) * 256) == cudaSuccess;
-    ok &= digit_total_.alloc(kRadixMaxPasses * 256) == cudaSuccess;
+    ok &= hist_.alloc(static_cast<size_t>(tiles_) * kRadixMaxBins) == cudaSuccess;
+    ok &= digit_total_.alloc(kRadixMaxPasses * kRadixMaxBins) == cudaSuccess;
     ok &= bmin_.alloc(3 * static_cast<size_t>(S_)) == cudaSuccess;
     ok &= bmax_.alloc(3 * static_cast<size_t>(S_)) == cudaSuccess;
     ok &= grid_.alloc(static_cast<size_t>(S_)) == cudaSuccess;
@@ -400,6 +400,7 @@ class Solver {
       last_pairs_ = static_cast<long long>(st.pairs);
       last_max_ = st.nbr_max;
       last_cells_ = static_cast<int>(st.total_cells);
+      last_npass_ = st.npass;
       if (enqueue_reset(status_.p, bmin_.p, bmax_.p, S_, stream_) != cudaSuccess) return cuda_fail("reset");
       if (!st.err) return FLUID_OK;
       if (st.err != FLUID_ERR_CAPACITY) {
@@ -505,9 +506,46 @@ class Solver {
       plan_.unroll[k] = best.unroll[k];
       plan_.block[k] = best.block[k];
     }
+    // Sort digit width: the three radix stages' time per step under each.
+    double best_sort = 1e300;
+    int best_bits = plan_.radix_bits;
+    for (int bits : {8, 11}) {
+      plan_.radix_bits = bits;
+      make_plan();
+      invalidate_graphs();
+      kernel_times(nullptr, nullptr, 0, 1);
+      for (int t = 0; t < trials; ++t) {
+        rc = launch_one();
+        if (!rc) rc = synchronize();
+        revert();
+        if (rc) break;
+      }
+      if (rc) break;
+      const double ms = stage_ms_[FLUID_KERNEL_RADIX_HIST] + stage_ms_[FLUID_KERNEL_RADIX_SCAN] +
+                        stage_ms_[FLUID_KERNEL_RADIX_SCATTER];
+      if (ms < best_sort) {
+        best_sort = ms;
+        best_bits = bits;
+      }
+    }
+    plan_.radix_bits = best_bits;
+    make_plan();
     kernel_times(nullptr, nullptr, 0, 1);
     invalidate_graphs();
-    return set_profiling(prof);
+    const int prof_rc = set_profiling(prof);
+    return rc ? rc : prof_rc;
+  }
+
+  int sort_bits() const { return plan_.radix_bits; }
+
+  int set_sort_bits(int bits) {
+    if (bits != 8 && bits != 11) return fail(FLUID_ERR_INVALID_ARGUMENT, "sort digit width must be 8 or 11");
+    int rc = synchronize();
+    if (rc) return rc;
+    plan_.radix_bits = bits;
+    make_plan();
+    invalidate_graphs();
+    return FLUID_OK;
   }
 
   // ---- Adjoint -----------------------------------------------------------
@@ -828,9 +866,7 @@ class Solver {
     return lo;
   }
 
-  int last_npass() const {
-    return last_cells_ <= 1 ? 0 : (bits_for(last_cells_) + 7) / 8;
-  }
+  int last_npass() const { return last_npass_; }
 
   void make_plan() {
     plan_.iterations = params_[0].solver_iterations;
@@ -840,7 +876,7 @@ class Solver {
       plan_.vorticity |= c.vort_on != 0;
       plan_.restitution |= c.rest_on != 0;
     }
-    plan_.radix_passes = std::max(1, (bits_for(grid_cap_) + 7) / 8);
+    plan_.radix_passes = std::max(1, (bits_for(grid_cap_) + plan_.radix_bits - 1) / plan_.radix_bits);
     plan_.scorr_pow = shared_scorr_pow(sc_host_.data(), S_);
   }
 
@@ -1099,6 +1135,7 @@ class Solver {
       last_pairs_ = static_cast<long long>(st.pairs);
       last_max_ = st.nbr_max;
       last_cells_ = static_cast<int>(st.total_cells);
+      last_npass_ = st.npass;
       commit_steps(1);
       return FLUID_OK;
     }
@@ -1198,7 +1235,7 @@ class Solver {
   int parity_ = 0, pending_ = 0;
   long long steps_ = 0, regrows_ = 0, launches_ = 0, launches_per_step_ = 0;
   long long last_pairs_ = 0;
-  int last_max_ = 0, last_cells_ = 0;
+  int last_max_ = 0, last_cells_ = 0, last_npass_ = 0;
   DBuf<float4> x_[2], v_[2], p_[2], v2_, omega_, pl_;
   DBuf<int> slot_[2], vals_[2], cnt_, depth_, ovf_, nbr_, bmin_, bmax_;
   DBuf<float> rho_[2], lambda_;
@@ -1390,6 +1427,18 @@ int fluid_solver_get_tuning(fluid_solver* s, int32_t* unroll, int32_t* block, in
 int fluid_solver_set_tuning(fluid_solver* s, const int32_t* unroll, const int32_t* block, int32_t kernels) {
   FLUID_CHECK_SOLVER(s);
   return s->impl.set_tuning(unroll, block, kernels);
+}
+
+int fluid_solver_get_sort_bits(fluid_solver* s, int32_t* bits) {
+  FLUID_CHECK_SOLVER(s);
+  if (!bits) return FLUID_ERR_INVALID_ARGUMENT;
+  *bits = s->impl.sort_bits();
+  return FLUID_OK;
+}
+
+int fluid_solver_set_sort_bits(fluid_solver* s, int32_t bits) {
+  FLUID_CHECK_SOLVER(s);
+  return s->impl.set_sort_bits(bits);
 }
 
 int fluid_solver_step_backward(fluid_solver* s, const float* g_pos_out, const float* g_vel_out, float* g_pos_in,

@@ -148,8 +148,9 @@ class Solver:
         return {name: (ms[k], la[k]) for k, name in enumerate(_capi.KERNEL_NAMES)}
 
     def autotune(self, trials: int = 2) -> dict:
-        """Picks the fastest launch shape per kernel on the current state
-        (state not advanced); returns the chosen shapes."""
+        """Picks the fastest launch shape per kernel and the faster sort
+        digit width on the current state (state not advanced); returns the
+        chosen shapes (`sort_bits()` gives the width)."""
         self._check(self.lib.fluid_solver_autotune(self.h, trials))
         return self.tuning()
 
@@ -171,6 +172,15 @@ class Solver:
             if shape:
                 u[k], b[k] = shape["unroll"], shape["block"]
         self._check(self.lib.fluid_solver_set_tuning(self.h, u, b, n))
+
+    def sort_bits(self) -> int:
+        """Digit width of the cell-key radix sort (8 or 11)."""
+        b = ctypes.c_int32(0)
+        self._check(self.lib.fluid_solver_get_sort_bits(self.h, ctypes.byref(b)))
+        return b.value
+
+    def set_sort_bits(self, bits: int) -> None:
+        self._check(self.lib.fluid_solver_set_sort_bits(self.h, int(bits)))
 
     def _cot(self, a):
         a = np.ascontiguousarray(a, dtype=np.float32).reshape(3, self.n)

@@ -230,8 +230,9 @@ int fluid_solver_kernel_times(fluid_solver* solver, double* ms_out,
  * neighbour-list passes and the list build) under every launch shape --
  * neighbour entries fetched ahead in {1, 2, 4, 8}, threads per block in
  * {128, 256, 512} -- over `trials` discarded steps of the current state, and
- * keeps the fastest shape per kernel. The state and time are not advanced.
- * Every shape computes identical results; only speed differs.
+ * keeps the fastest shape per kernel; then times the cell-key sort with 8-
+ * and 11-bit digits and keeps the faster width. The state and time are not
+ * advanced. Every choice computes identical results; only speed differs.
  */
 int fluid_solver_autotune(fluid_solver* solver, int32_t trials);
 
@@ -241,6 +242,11 @@ int fluid_solver_get_tuning(fluid_solver* solver, int32_t* unroll, int32_t* bloc
                             int32_t kernels);
 int fluid_solver_set_tuning(fluid_solver* solver, const int32_t* unroll,
                             const int32_t* block, int32_t kernels);
+
+/* Digit width of the cell-key radix sort: 8 (default) or 11 bits. Keys of
+ * b bits take ceil(b / width) passes; the permutation does not depend on it. */
+int fluid_solver_get_sort_bits(fluid_solver* solver, int32_t* bits);
+int fluid_solver_set_sort_bits(fluid_solver* solver, int32_t bits);
 
 /*
  * Reverse-mode derivative (no reference counterpart: the reference has no

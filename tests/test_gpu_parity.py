@@ -273,6 +273,50 @@ def test_autotune_keeps_state_and_results(cuda_lib, oracle_lib):
     s.close()
 
 
+def _two_corner_blocks():
+    """Two 6^3 blocks at opposite corners of a 9^3 box, h = 0.1: ~6e5 cells
+    in the bounding grid, 20-bit keys (three 8-bit passes, two 11-bit)."""
+    sp, h = 0.05, 0.1
+    p = scenes.base_params(sp, h)
+    scenes.init_planes(p, 9.0, 9.0, 9.0)
+    scenes.all_flags(p, h)
+    a = scenes.init_block(6, 6, 6, (0.05, 0.05, 0.05), sp)
+    b = scenes.init_block(6, 6, 6, (8.6, 8.6, 8.6), sp)
+    pos = scenes.jitter(np.concatenate([a, b], axis=1), 5e-4, 3)
+    return scenes.Scene("two_corner_blocks", p, pos, np.zeros_like(pos), steps=6)
+
+
+@pytest.mark.parametrize("case", ["small_grid", "wide_grid"])
+def test_sort_width_gives_same_permutation(cuda_lib, oracle_lib, case):
+    """8- and 11-bit digits: same cell keys, stable permutation and trajectory
+    (small_grid: keys of <= 11 bits, one 11-bit pass against two 8-bit ones;
+    wide_grid: 20-bit keys, two passes against three)."""
+    sc = scenes.dam_break(8, seed=5, flags=True) if case == "small_grid" else _two_corner_blocks()
+    ref = oracle_lib.Oracle().run(sc.params, sc.pos, sc.vel, 0.0, 6, dump=True)
+    out = {}
+    for bits in (8, 11):
+        s = Solver(0)
+        s.configure([sc.params], [sc.count])
+        s.set_sort_bits(bits)
+        assert s.sort_bits() == bits
+        s.upload(sc.pos, sc.vel)
+        s.step(6)
+        pos, vel = s.download()
+        out[bits] = (pos, vel, s.read_debug(_capi.DEBUG_SORTED_ORDER), s.read_debug(_capi.DEBUG_CELL_KEYS))
+        s.close()
+        np.testing.assert_array_equal(pos, ref["pos"])
+        np.testing.assert_array_equal(vel, ref["vel"])
+        np.testing.assert_array_equal(out[bits][2], ref["sorted_order"])
+        np.testing.assert_array_equal(out[bits][3], ref["cell_keys"])
+    for x, y in zip(out[8], out[11]):
+        np.testing.assert_array_equal(x, y)
+    s = Solver(0)
+    s.configure([sc.params], [sc.count])
+    with pytest.raises(FluidError):
+        s.set_sort_bits(9)
+    s.close()
+
+
 def test_all_pairs_lists_match_oracle(cuda_lib, oracle_lib):
     """use_uniform_grid = 0: lists in ascending caller index from all pairs
     (core/src/core.cpp:248-268), a different summation order than the grid's."""
