@@ -154,18 +154,6 @@ __device__ __forceinline__ const uint32_t* sorted_keys(const StepArgs& a, int np
   return a.keys[npass & 1];
 }
 
-// Cell range from the table; entries left from earlier steps are rejected
-// because the first slot of a live entry holds that cell's key this step.
-__device__ __forceinline__ bool cell_range(const StepArgs& a, const uint32_t* ks, uint32_t key,
-                                           int& first, int& end) {
-  const int2 e = a.table[key];
-  if (e.x < 0 || e.x >= e.y || e.y > a.n) return false;
-  if (__ldg(ks + e.x) != key) return false;
-  first = e.x;
-  end = e.y;
-  return true;
-}
-
 // ---------------------------------------------------------------------------
 // Bounds, grid, keys
 
@@ -531,14 +519,30 @@ __device__ __forceinline__ void for_each_candidate(const StepArgs& a, const uint
     for (int oy = -1; oy <= 1; ++oy) {
       const int y = cy + oy;
       if (y < g.miny || y >= g.miny + g.dimy) continue;
-      uint32_t key = cell_key(g, cx - 1, y, z);
-      for (int ox = -1; ox <= 1; ++ox, key += static_cast<uint32_t>(xstride)) {
-        const int xx = cx + ox;
-        if (xx < g.minx || xx >= g.minx + g.dimx) continue;
-        int first, end;
-        if (!cell_range(a, ks, key, first, end)) continue;
-        if (oz == 0 && oy == 0 && ox == 0) scan_range<kFetch, true>(pos, first, end, i, f);
-        else scan_range<kFetch, false>(pos, first, end, i, f);
+      // The row's three cell ranges: table entries, then their validating
+      // keys, each three loads in flight, then the scans in x order. The
+      // table is not cleared between steps; an entry left from an earlier
+      // step is rejected because the first slot of a live entry holds that
+      // cell's key this step.
+      const uint32_t key0 = cell_key(g, cx - 1, y, z);
+      int2 e[3];
+      uint32_t kk[3];
+#pragma unroll
+      for (int t = 0; t < 3; ++t) {
+        const int xx = cx - 1 + t;
+        const bool in = xx >= g.minx && xx < g.minx + g.dimx;
+        e[t] = in ? a.table[key0 + static_cast<uint32_t>(t * xstride)] : make_int2(0, 0);
+      }
+#pragma unroll
+      for (int t = 0; t < 3; ++t) {
+        if (e[t].x < 0 || e[t].x >= e[t].y || e[t].y > a.n) e[t] = make_int2(0, 0);
+        kk[t] = e[t].x < e[t].y ? __ldg(ks + e[t].x) : 0u;
+      }
+#pragma unroll
+      for (int t = 0; t < 3; ++t) {
+        if (e[t].x >= e[t].y || kk[t] != key0 + static_cast<uint32_t>(t * xstride)) continue;
+        if (oz == 0 && oy == 0 && t == 1) scan_range<kFetch, true>(pos, e[t].x, e[t].y, i, f);
+        else scan_range<kFetch, false>(pos, e[t].x, e[t].y, i, f);
       }
     }
   }
