@@ -56,6 +56,7 @@ struct SceneConst {
   int iterations;
   int all_pairs;                  // use_uniform_grid == 0: lists from all pairs
   int first_slot, count;          // particle range of the scene
+  float neg_zero;                 // -0.0f, read at run time (see pmul in the kernels)
   float4 planes[FLUID_MAX_PLANES];  // (nx, ny, nz, d)
 };
 

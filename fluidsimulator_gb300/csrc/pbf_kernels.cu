@@ -83,6 +83,23 @@ __device__ __forceinline__ float dist2(float dx, float dy, float dz) {
   return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
 }
 
+// Paired FP32 arithmetic: two IEEE round-to-nearest operations per
+// instruction (sm_100 and later); each half equals the scalar operation.
+__device__ __forceinline__ float2 f2(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float2 padd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+// a * b rounded once, written as fma(a, b, nz) with nz = -0.0 read from
+// memory (SceneConst::neg_zero). A paired multiply whose result feeds a
+// paired add is contracted into one fused multiply-add by the code generator
+// even with explicit round-to-nearest and contraction disabled (measured: the
+// sum then equals fma(x, x, y * y)), which rounds once where the reference
+// rounds twice. An fma with an addend unknown at compile time cannot be
+// contracted further, and RN(a * b + (-0)) = RN(a * b) for every a and b,
+// signed zeros included.
+__device__ __forceinline__ float2 pmul(float2 a, float2 b, float2 nz) { return __ffma2_rn(a, b, nz); }
+// a - b rounded once, as fma(b, -1, a): b * -1 is exact, and the signs of
+// zero come out as in a - b. No operand of a psub comes from a pmul.
+__device__ __forceinline__ float2 psub(float2 a, float2 b) { return __ffma2_rn(b, f2(-1.0f), a); }
+
 // W_poly6 for r2 < h2 (core.cpp:35-46): coeff * ((d*d)*d), d = h2 - r2.
 __device__ __forceinline__ float poly6(const SceneConst& c, float r2) {
   const float d = c.h2 - r2;
@@ -576,6 +593,44 @@ struct LambdaAcc {
     const float jx = ng * gx, jy = ng * gy, jz = ng * gz;
     sum_g2 += jx * jx + jy * jy + jz * jz;
   }
+  // Entries a and b (in list order) relative to p, each added only when
+  // r2 < h2: the same operations as the membership test plus add() on a,
+  // then on b, with the per-entry terms formed in paired arithmetic.
+  __device__ __forceinline__ void add_pair(const SceneConst& c, const float2 px, const float2 py, const float2 pz,
+                                           const float4 qa, const float4 qb) {
+    const float2 nz = f2(c.neg_zero);
+    const float2 dx = psub(px, make_float2(qa.x, qb.x));
+    const float2 dy = psub(py, make_float2(qa.y, qb.y));
+    const float2 dz = psub(pz, make_float2(qa.z, qb.z));
+    const float2 r2 = padd(padd(pmul(dx, dx, nz), pmul(dy, dy, nz)), pmul(dz, dz, nz));
+    const bool oka = r2.x < c.h2, okb = r2.y < c.h2;
+    if (!oka && !okb) return;
+    const float2 d = psub(f2(c.h2), r2);
+    const float2 w = pmul(f2(c.poly6_c), pmul(pmul(d, d, nz), d, nz), nz);
+    const float2 r = make_float2(clamped_r(c, r2.x), clamped_r(c, r2.y));
+    const float2 e = psub(f2(c.h), r);
+    float2 gf = pmul(pmul(f2(c.spiky_c), e, nz), e, nz);
+    if (r.x > c.h) gf.x = 0.0f;
+    if (r.y > c.h) gf.y = 0.0f;
+    const float2 gx = pmul(gf, dx, nz), gy = pmul(gf, dy, nz), gz = pmul(gf, dz, nz);
+    const float2 ng = f2(-c.grad_scale);
+    const float2 jx = pmul(ng, gx, nz), jy = pmul(ng, gy, nz), jz = pmul(ng, gz, nz);
+    const float2 t = padd(padd(pmul(jx, jx, nz), pmul(jy, jy, nz)), pmul(jz, jz, nz));
+    if (oka) {
+      rho += w.x;
+      gsx += gx.x;
+      gsy += gy.x;
+      gsz += gz.x;
+      sum_g2 += t.x;
+    }
+    if (okb) {
+      rho += w.y;
+      gsx += gx.y;
+      gsy += gy.y;
+      gsz += gz.y;
+      sum_g2 += t.y;
+    }
+  }
 };
 
 // All-pairs candidates (core.cpp:248-268, use_uniform_grid == 0): every other
@@ -715,6 +770,37 @@ __device__ __forceinline__ void for_each_neighbor(const int* __restrict__ list, 
   for (; k < n; ++k) body(load(__ldg(list + 32ll * k)));
 }
 
+// for_each_neighbor for bodies that take two consecutive entries at once
+// (a then b, in list order); an odd last entry goes to body1. kUnroll >= 2.
+template <int kUnroll, typename Load, typename Body2, typename Body1>
+__device__ __forceinline__ void for_each_neighbor_pair(const int* __restrict__ list, int n, Load&& load, Body2&& body2,
+                                                       Body1&& body1) {
+  static_assert(kUnroll % 2 == 0, "entries are consumed in pairs");
+  using Rec = decltype(load(0));
+  int k = 0;
+  int j[kUnroll];
+  if (kUnroll <= n) {
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) j[u] = __ldg(list + 32ll * u);
+  }
+  for (; k + kUnroll <= n; k += kUnroll) {
+    Rec r[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) r[u] = load(j[u]);
+    if (k + 2 * kUnroll <= n) {
+#pragma unroll
+      for (int u = 0; u < kUnroll; ++u) j[u] = __ldg(list + 32ll * (k + kUnroll + u));
+    }
+#pragma unroll
+    for (int u = 0; u < kUnroll; u += 2) body2(r[u], r[u + 1]);
+  }
+  for (; k + 2 <= n; k += 2) {
+    const Rec ra = load(__ldg(list + 32ll * k)), rb = load(__ldg(list + 32ll * (k + 1)));
+    body2(ra, rb);
+  }
+  if (k < n) body1(load(__ldg(list + 32ll * k)));
+}
+
 struct PosVel {
   float4 x, v;
 };
@@ -731,11 +817,19 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_lambda(StepA
   const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
   const float h2 = c.h2;
   LambdaAcc acc;
-  for_each_neighbor<U>(list, n, [&](int j) { return __ldg(pos + j); }, [&](const float4 q) {
+  auto one = [&](const float4 q) {
     const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
     const float r2 = dist2(dx, dy, dz);
     if (r2 < h2) acc.add(c, dx, dy, dz, r2);
-  });
+  };
+  auto load = [&](int j) { return __ldg(pos + j); };
+  if constexpr (U == 1) {
+    for_each_neighbor<1>(list, n, load, one);
+  } else {
+    const float2 px = f2(p.x), py = f2(p.y), pz = f2(p.z);
+    for_each_neighbor_pair<U>(list, n, load,
+                              [&](const float4 qa, const float4 qb) { acc.add_pair(c, px, py, pz, qa, qb); }, one);
+  }
   float rho;
   const float lam = finish_lambda(c, acc.rho, acc.gsx, acc.gsy, acc.gsz, acc.sum_g2, rho);
   a.lambda[i] = lam;

@@ -127,6 +127,7 @@ SceneConst make_scene_const(const fluid_params& p, int first, int count) {
   c.iterations = p.solver_iterations;
   c.all_pairs = p.use_uniform_grid ? 0 : 1;
   c.first_slot = first;
+  c.neg_zero = -0.0f;
   c.count = count;
   for (int q = 0; q < p.plane_count; ++q) {
     c.planes[q] = make_float4(p.plane_nx[q], p.plane_ny[q], p.plane_nz[q], p.plane_d[q]);
