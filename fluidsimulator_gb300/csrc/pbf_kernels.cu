@@ -875,7 +875,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_delta(StepAr
   const float h2 = c.h2;
   float ax = 0.0f, ay = 0.0f, az = 0.0f;
   const bool scorr = c.scorr_on != 0;
-  for_each_neighbor<U>(list, n, [&](int j) { return __ldg(pl + j); }, [&](const float4 r) {
+  auto one = [&](const float4 r) {
     const float dx = p.x - r.x, dy = p.y - r.y, dz = p.z - r.z;
     const float r2 = dist2(dx, dy, dz);
     if (r2 < h2) {
@@ -889,7 +889,59 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_delta(StepAr
       ay += s * gf * dy;
       az += s * gf * dz;
     }
-  });
+  };
+  auto load = [&](int j) { return __ldg(pl + j); };
+  if constexpr (U == 1) {
+    for_each_neighbor<1>(list, n, load, one);
+  } else {
+    // Two entries at a time: the same operations as one() on a, then on b,
+    // with the per-entry terms in paired arithmetic (pmul keeps each
+    // product rounded on its own).
+    const float2 px = f2(p.x), py = f2(p.y), pz = f2(p.z), nz = f2(c.neg_zero);
+    auto two = [&](const float4 qa, const float4 qb) {
+      const float2 dx = psub(px, make_float2(qa.x, qb.x));
+      const float2 dy = psub(py, make_float2(qa.y, qb.y));
+      const float2 dz = psub(pz, make_float2(qa.z, qb.z));
+      const float2 r2 = padd(padd(pmul(dx, dx, nz), pmul(dy, dy, nz)), pmul(dz, dz, nz));
+      const bool oka = r2.x < h2, okb = r2.y < h2;
+      if (!oka && !okb) return;
+      const float2 r = make_float2(clamped_r(c, r2.x), clamped_r(c, r2.y));
+      const float2 e = psub(f2(c.h), r);
+      float2 gf = pmul(pmul(f2(c.spiky_c), e, nz), e, nz);
+      if (r.x > c.h) gf.x = 0.0f;
+      if (r.y > c.h) gf.y = 0.0f;
+      float2 s = padd(f2(li), make_float2(qa.w, qb.w));
+      if (scorr) {
+        const float2 d = psub(f2(c.h2), r2);
+        const float2 ratio = pmul(pmul(f2(c.poly6_c), pmul(pmul(d, d, nz), d, nz), nz), f2(c.scorr_inv_wdq), nz);
+        float2 pw;
+        if (kPow == 2) {
+          pw = pmul(ratio, ratio, nz);
+        } else if (kPow == 3) {
+          pw = pmul(pmul(ratio, ratio, nz), ratio, nz);
+        } else if (kPow == 4) {
+          const float2 sq = pmul(ratio, ratio, nz);
+          pw = pmul(sq, sq, nz);
+        } else {
+          pw = make_float2(pow_n(ratio.x, c.scorr_n), pow_n(ratio.y, c.scorr_n));
+        }
+        s = padd(s, pmul(f2(c.scorr_neg_k), pw, nz));
+      }
+      const float2 sg = pmul(s, gf, nz);
+      const float2 tx = pmul(sg, dx, nz), ty = pmul(sg, dy, nz), tz = pmul(sg, dz, nz);
+      if (oka) {
+        ax += tx.x;
+        ay += ty.x;
+        az += tz.x;
+      }
+      if (okb) {
+        ax += tx.y;
+        ay += ty.y;
+        az += tz.y;
+      }
+    };
+    for_each_neighbor_pair<U>(list, n, load, two, one);
+  }
   ax *= c.inv_density;
   ay *= c.inv_density;
   az *= c.inv_density;
