@@ -5,6 +5,12 @@ Numerics flags: -fmad=false keeps every device multiply and add separately
 rounded (no FMA contraction) and -ffp-contract=off does the same for host code
 (GCC contracts by default on aarch64), so the step reproduces the reference's
 float arithmetic. Division and square root stay IEEE (nvcc defaults).
+
+The adjoint kernels (pbf_adjoint.cu) reproduce no reference arithmetic: they
+are checked against the oracle's FP64 adjoint to a relative tolerance, and the
+one test whose outcome must match the forward exactly (neighbour membership,
+r2 < h2) is written there with explicit round-to-nearest operations. That
+translation unit is built with contraction on and fast division / square root.
 """
 
 from __future__ import annotations
@@ -33,8 +39,13 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found")
 
 
-def cuda_flags() -> list[str]:
-    return ["-std=c++17", "-O3", *ARCH, "-lineinfo", "-fmad=false", "--extended-lambda",
+# Translation units free of the reference's exact float arithmetic.
+RELAXED = {"pbf_adjoint.cu"}
+
+
+def cuda_flags(src: str = "") -> list[str]:
+    fp = ["-fmad=true", "-prec-div=false", "-prec-sqrt=false"] if src in RELAXED else ["-fmad=false"]
+    return ["-std=c++17", "-O3", *ARCH, "-lineinfo", *fp, "--extended-lambda",
             "-Xcompiler", "-fPIC,-ffp-contract=off,-O3", "-I", INCLUDE, "-I", CSRC]
 
 
@@ -75,7 +86,7 @@ def build(verbose: bool = False, force: bool = False, extra: list[str] | None = 
         obj = os.path.join(BUILD_DIR, os.path.basename(src).rsplit(".", 1)[0] + ".o")
         objs.append(obj)
         if force or _stale(obj, [path, __file__] + headers):
-            jobs.append([nv, *cuda_flags(), *(extra or []), "-c", path, "-o", obj])
+            jobs.append([nv, *cuda_flags(src), *(extra or []), "-c", path, "-o", obj])
     with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 1))) as ex:
         list(ex.map(lambda c: _run(c, verbose), jobs))
     if force or jobs or _stale(LIB, objs):

@@ -36,7 +36,20 @@ __device__ __forceinline__ bool adj_failed(const DevStatus* st) {
   return *reinterpret_cast<const volatile int*>(&st->err) != 0;
 }
 
-__device__ __forceinline__ float d2(float x, float y, float z) { return x * x + y * y + z * z; }
+// (x*x + y*y) + z*z with every operation rounded on its own, as the forward's
+// membership test computes it, so the adjoint visits exactly the forward's
+// pairs (this file is compiled with contraction on).
+__device__ __forceinline__ float d2(float x, float y, float z) {
+  return __fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z));
+}
+
+// Signed distance ((nx x + ny y) + nz z) - d and the projection q += n pen,
+// each operation rounded on its own as in the forward (core.cpp:372-393,
+// 586-606): contacts decided from recorded positions come out as the
+// forward's, also for particles resting exactly on a plane.
+__device__ __forceinline__ float plane_sd(const float4 pl, float x, float y, float z) {
+  return __fsub_rn(__fadd_rn(__fadd_rn(__fmul_rn(pl.x, x), __fmul_rn(pl.y, y)), __fmul_rn(pl.z, z)), pl.w);
+}
 
 template <typename Body>
 __device__ __forceinline__ void for_list(const StepArgs& s, int i, Body&& body) {
@@ -53,6 +66,38 @@ __device__ __forceinline__ void for_list(const StepArgs& s, int i, Body&& body) 
   }
   for (; k < n; ++k) body(__ldg(list + 32ll * k));
 }
+
+// for_list with the neighbours' records fetched four ahead and the next four
+// list indices fetched while those are used; body(rec) sees list order.
+template <typename Load, typename Body>
+__device__ __forceinline__ void for_list_rec(const StepArgs& s, int i, Load&& load, Body&& body) {
+  constexpr int kAhead = 4;
+  using Rec = decltype(load(0));
+  const int n = s.cnt[i];
+  const int* __restrict__ list = s.nbr + s.wbase[i >> 5] + (i & 31);
+  int k = 0;
+  int j[kAhead];
+  if (kAhead <= n) {
+#pragma unroll
+    for (int u = 0; u < kAhead; ++u) j[u] = __ldg(list + 32ll * u);
+  }
+  for (; k + kAhead <= n; k += kAhead) {
+    Rec r[kAhead];
+#pragma unroll
+    for (int u = 0; u < kAhead; ++u) r[u] = load(j[u]);
+    if (k + 2 * kAhead <= n) {
+#pragma unroll
+      for (int u = 0; u < kAhead; ++u) j[u] = __ldg(list + 32ll * (k + kAhead + u));
+    }
+#pragma unroll
+    for (int u = 0; u < kAhead; ++u) body(r[u]);
+  }
+  for (; k < n; ++k) body(load(__ldg(list + 32ll * k)));
+}
+
+struct Rec2 {
+  float4 a, b;
+};
 
 __device__ __forceinline__ float dW(const SceneConst& c, float r2) {  // dW_poly6 / d(r^2)
   const float d = c.h2 - r2;
@@ -157,7 +202,7 @@ __global__ void __launch_bounds__(kAdjBlock) k_adj_out(AdjArgs a) {
     unsigned act = 0, neg = 0;
     for (int q = 0; q < c.plane_count; ++q) {
       const float4 pl = c.planes[q];
-      if (pl.x * xi.x + pl.y * xi.y + pl.z * xi.z - pl.w <= 0.0f) {
+      if (plane_sd(pl, xi.x, xi.y, xi.z) <= 0.0f) {
         act |= 1u << q;
         const float vn = pl.x * v[0] + pl.y * v[1] + pl.z * v[2];
         const float s = vn < 0.0f ? c.rest_neg_e : 1.0f;
@@ -356,12 +401,12 @@ __global__ void __launch_bounds__(kAdjBlock) k_adj_proj(AdjArgs a, int it) {
   unsigned act = 0;
   for (int k = 0; k < c.plane_count; ++k) {
     const float4 pl = c.planes[k];
-    const float pen = -(pl.x * q[0] + pl.y * q[1] + pl.z * q[2] - pl.w);
+    const float pen = -plane_sd(pl, q[0], q[1], q[2]);
     if (pen > 0.0f) {
       act |= 1u << k;
-      q[0] += pl.x * pen;
-      q[1] += pl.y * pen;
-      q[2] += pl.z * pen;
+      q[0] = __fadd_rn(q[0], __fmul_rn(pl.x, pen));
+      q[1] = __fadd_rn(q[1], __fmul_rn(pl.y, pen));
+      q[2] = __fadd_rn(q[2], __fmul_rn(pl.z, pen));
     }
   }
   for (int k = c.plane_count - 1; k >= 0; --k) {
@@ -372,7 +417,7 @@ __global__ void __launch_bounds__(kAdjBlock) k_adj_proj(AdjArgs a, int it) {
     g[1] -= gn * pl.y;
     g[2] -= gn * pl.z;
   }
-  a.gd[i] = make_float4(g[0], g[1], g[2], 0.0f);
+  a.gd[i] = make_float4(g[0], g[1], g[2], a.rec.lambda[static_cast<size_t>(it) * n + i]);
 }
 
 __global__ void __launch_bounds__(kAdjBlock) k_adj_delta(AdjArgs a, int it) {
@@ -381,23 +426,24 @@ __global__ void __launch_bounds__(kAdjBlock) k_adj_delta(AdjArgs a, int it) {
   const int n = a.s.n;
   if (i >= n) return;
   const float4* __restrict__ P = a.rec.p + static_cast<size_t>(it) * n;
-  const float* __restrict__ L = a.rec.lambda + static_cast<size_t>(it) * n;
+  const float4* __restrict__ GD = a.gd;  // w = lambda_j
   const float4 pi = P[i];
   const SceneConst& c = a.s.sc[__float_as_int(a.rec.p[i].w)];
-  const float4 gdi = a.gd[i];
-  const float li = L[i];
+  const float4 gdi = GD[i];
+  const float li = gdi.w;
   const bool scorr = c.scorr_on != 0;
   float gx = gdi.x, gy = gdi.y, gz = gdi.z, gl = 0.0f;
   float rs = 0.0f, Gx = 0.0f, Gy = 0.0f, Gz = 0.0f, s1 = 0.0f;
-  for_list(a.s, i, [&](int j) {
-    const float4 pj = __ldg(P + j);
+  auto load = [&](int j) { return Rec2{__ldg(P + j), __ldg(GD + j)}; };
+  for_list_rec(a.s, i, load, [&](const Rec2 rj) {
+    const float4 pj = rj.a;
     const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
     const float r2 = d2(dx, dy, dz);
     if (!(r2 < c.h2)) return;
     const bool clamp = r2 < c.min_r2;
     const float r = sqrtf(clamp ? c.min_r2 : r2);
     const float f = Fs(c, r), fpr = clamp ? 0.0f : dFs(c, r) / r;
-    float s = li + __ldg(L + j);
+    float s = li + rj.b.w;
     float alpha;
     if (scorr) {
       const float x = Wp(c, r2) * c.scorr_inv_wdq;
@@ -407,7 +453,7 @@ __global__ void __launch_bounds__(kAdjBlock) k_adj_delta(AdjArgs a, int it) {
     } else {
       alpha = s * fpr;
     }
-    const float4 gdj = __ldg(a.gd + j);
+    const float4 gdj = rj.b;
     const float ex = gdi.x - gdj.x, ey = gdi.y - gdj.y, ez = gdi.z - gdj.z;
     const float de = dx * ex + dy * ey + dz * ez;
     gx += c.inv_density * (s * f * ex + alpha * de * dx);
@@ -426,7 +472,7 @@ __global__ void __launch_bounds__(kAdjBlock) k_adj_delta(AdjArgs a, int it) {
   const float lam = -C / (S + c.epsilon);
   const float gC = -gl / (S + c.epsilon);
   const float gS = -gl * lam / (S + c.epsilon);
-  a.grt[i] = (it == a.iters - 1 ? a.grho[i] : 0.0f) + gC * c.inv_density;
+  a.pg[i] = make_float4(pi.x, pi.y, pi.z, (it == a.iters - 1 ? a.grho[i] : 0.0f) + gC * c.inv_density);
   a.aux[i] = make_float4(Gx, Gy, Gz, gS);
   a.gp[i] = make_float4(gx, gy, gz, 0.0f);
 }
@@ -436,23 +482,25 @@ __global__ void __launch_bounds__(kAdjBlock) k_adj_lambda(AdjArgs a, int it) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int n = a.s.n;
   if (i >= n) return;
-  const float4* __restrict__ P = a.rec.p + static_cast<size_t>(it) * n;
-  const float4 pi = P[i];
+  const float4* __restrict__ PG = a.pg;  // (p_j, dL/drho_j)
+  const float4* __restrict__ AUX = a.aux;
+  const float4 pgi = PG[i];
   const SceneConst& c = a.s.sc[__float_as_int(a.rec.p[i].w)];
-  const float4 ai = a.aux[i];
-  const float gri = a.grt[i];
+  const float4 ai = AUX[i];
+  const float gri = pgi.w;
   const float gs2 = c.grad_scale * c.grad_scale;
   float ax = 0.0f, ay = 0.0f, az = 0.0f;
-  for_list(a.s, i, [&](int j) {
-    const float4 pj = __ldg(P + j);
-    const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+  auto load = [&](int j) { return Rec2{__ldg(PG + j), __ldg(AUX + j)}; };
+  for_list_rec(a.s, i, load, [&](const Rec2 rj) {
+    const float4 pj = rj.a;
+    const float dx = pgi.x - pj.x, dy = pgi.y - pj.y, dz = pgi.z - pj.z;
     const float r2 = d2(dx, dy, dz);
     if (!(r2 < c.h2)) return;
     const bool clamp = r2 < c.min_r2;
     const float r = sqrtf(clamp ? c.min_r2 : r2);
     const float f = Fs(c, r), fpr = clamp ? 0.0f : dFs(c, r) / r;
-    const float4 aj = __ldg(a.aux + j);
-    const float grj = __ldg(a.grt + j);
+    const float4 aj = rj.b;
+    const float grj = pj.w;
     const float dGi = dx * ai.x + dy * ai.y + dz * ai.z;
     const float dGj = dx * aj.x + dy * aj.y + dz * aj.z;
     const float t = 2.0f * c.mass * dW(c, r2) * (gri + grj) +

@@ -17,10 +17,10 @@ struct AdjArgs {
   float4* gv;        // cotangent of the output velocity
   float4* gv3;       // ... before restitution
   float4* gp;        // cotangent of p^k
-  float4* gd;        // cotangent of the correction of iteration k
+  float4* gd;        // cotangent of the correction of iteration k; w = lambda_i^k
   float4* gx0;       // cotangent of the input positions through the commit
   float4* aux;       // (G_i, dL/dS_i) of the density constraint
-  float* grt;        // dL/drho_i (total)
+  float4* pg;        // (p_i of the iteration reversed, dL/drho_i total)
   float* grho;       // dL/drho_i from XSPH
   float* cc;         // per-particle share of dL/dc (XSPH coefficient)
   int vorticity;     // some scene runs vorticity confinement

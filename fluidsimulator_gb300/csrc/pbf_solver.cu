@@ -1173,7 +1173,7 @@ class Solver {
     aa.gd = a_gd_.p;
     aa.gx0 = a_gx0_.p;
     aa.aux = a_aux_.p;
-    aa.grt = a_grt_.p;
+    aa.pg = a_pg_.p;
     aa.grho = a_grho_.p;
     aa.cc = a_cc_.p;
     aa.g_pos_out = gpo;
@@ -1200,7 +1200,7 @@ class Solver {
     if (adj_n_ == n) return FLUID_OK;
     bool ok = a_v2_.alloc(n) == cudaSuccess && a_gx_.alloc(n) == cudaSuccess && a_gv_.alloc(n) == cudaSuccess &&
               a_gv3_.alloc(n) == cudaSuccess && a_gp_.alloc(n) == cudaSuccess && a_gd_.alloc(n) == cudaSuccess &&
-              a_gx0_.alloc(n) == cudaSuccess && a_aux_.alloc(n) == cudaSuccess && a_grt_.alloc(n) == cudaSuccess &&
+              a_gx0_.alloc(n) == cudaSuccess && a_aux_.alloc(n) == cudaSuccess && a_pg_.alloc(n) == cudaSuccess &&
               a_grho_.alloc(n) == cudaSuccess && a_cc_.alloc(n) == cudaSuccess && a_io_.alloc(12 * n) == cudaSuccess &&
               a_v3_.alloc(n) == cudaSuccess && a_dv_.alloc(n) == cudaSuccess && a_gv4_.alloc(n) == cudaSuccess &&
               a_eb_.alloc(n) == cudaSuccess && a_obd_.alloc(n) == cudaSuccess && a_ob_.alloc(n) == cudaSuccess;
@@ -1212,8 +1212,8 @@ class Solver {
     return FLUID_OK;
   }
 
-  DBuf<float4> a_v2_, a_gx_, a_gv_, a_gv3_, a_gp_, a_gd_, a_gx0_, a_aux_, a_v3_, a_dv_, a_gv4_, a_eb_, a_obd_, a_ob_;
-  DBuf<float> a_grt_, a_grho_, a_cc_, a_io_;
+  DBuf<float4> a_v2_, a_gx_, a_gv_, a_gv3_, a_gp_, a_gd_, a_gx0_, a_aux_, a_pg_, a_v3_, a_dv_, a_gv4_, a_eb_, a_obd_, a_ob_;
+  DBuf<float> a_grho_, a_cc_, a_io_;
   size_t adj_n_ = 0;
   std::vector<Tape> tapes_;
   std::vector<Snap> checkpoints_;
