@@ -98,6 +98,9 @@ __device__ __forceinline__ void for_list_rec(const StepArgs& s, int i, Load&& lo
 struct Rec2 {
   float4 a, b;
 };
+struct Rec3 {
+  float4 a, b, c;
+};
 
 __device__ __forceinline__ float dW(const SceneConst& c, float r2) {  // dW_poly6 / d(r^2)
   const float d = c.h2 - r2;
@@ -131,7 +134,10 @@ __global__ void __launch_bounds__(kAdjBlock) k_adj_prepare(AdjArgs a) {
   const float4 pk = a.rec.p[static_cast<size_t>(a.iters) * n + i];
   const float4 p0 = a.rec.p[i];
   const SceneConst& c = a.s.sc[__float_as_int(p0.w)];
-  a.v2[i] = make_float4((pk.x - x0.x) / c.dt, (pk.y - x0.y) / c.dt, (pk.z - x0.z) / c.dt, p0.w);
+  // w: m / rho_i, the XSPH weight of i as a neighbour (core.cpp:446-447).
+  const float ri = a.rec.rho[i];
+  a.v2[i] = make_float4((pk.x - x0.x) / c.dt, (pk.y - x0.y) / c.dt, (pk.z - x0.z) / c.dt,
+                        ri > 0.0f ? c.mass / ri : 0.0f);
   const int o = __float_as_int(x0.w);
   a.gx[i] = make_float4(a.g_pos_out[o], a.g_pos_out[n + o], a.g_pos_out[2 * n + o], 0.0f);
   a.gv[i] = make_float4(a.g_vel_out[o], a.g_vel_out[n + o], a.g_vel_out[2 * n + o], 0.0f);
@@ -145,16 +151,16 @@ __global__ void __launch_bounds__(kAdjBlock) k_adj_out(AdjArgs a) {
   const float4* __restrict__ x1 = a.rec.p + static_cast<size_t>(a.iters) * n;
   const float4 xi = x1[i];
   const float4 vi = a.v2[i];
-  const SceneConst& c = a.s.sc[__float_as_int(vi.w)];
+  const SceneConst& c = a.s.sc[__float_as_int(a.rec.p[i].w)];
   float sx = 0.0f, sy = 0.0f, sz = 0.0f;
   if (c.xsph_on) {
-    for_list(a.s, i, [&](int j) {
-      const float4 xj = __ldg(x1 + j);
+    auto load = [&](int j) { return Rec2{__ldg(x1 + j), __ldg(a.v2 + j)}; };
+    for_list_rec(a.s, i, load, [&](const Rec2 rj) {
+      const float4 xj = rj.a;
       const float r2 = d2(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
       if (r2 < c.h2) {
-        const float rj = __ldg(a.rec.rho + j);
-        const float aj = rj > 0.0f ? c.mass / rj : 0.0f;
-        const float4 vj = __ldg(a.v2 + j);
+        const float4 vj = rj.b;
+        const float aj = vj.w;
         const float w = Wp(c, r2) * aj;
         sx += (vj.x - vi.x) * w;
         sy += (vj.y - vi.y) * w;
@@ -164,7 +170,7 @@ __global__ void __launch_bounds__(kAdjBlock) k_adj_out(AdjArgs a) {
   }
   float v[3] = {vi.x + c.visc_c * sx, vi.y + c.visc_c * sy, vi.z + c.visc_c * sz};
   a.dv[i] = make_float4(sx, sy, sz, 0.0f);
-  a.v3[i] = make_float4(v[0], v[1], v[2], vi.w);
+  a.v3[i] = make_float4(v[0], v[1], v[2], 0.0f);
   // Vorticity confinement recomputed (core.cpp:512-570): eta from the
   // recorded |omega|, N = eta/|eta|, f = eps N x omega.
   float N[3] = {0.0f, 0.0f, 0.0f}, om[3] = {0.0f, 0.0f, 0.0f}, elen = 0.0f;
@@ -257,7 +263,7 @@ __global__ void __launch_bounds__(kAdjBlock) k_adj_eta(AdjArgs a) {
   if (i >= n) return;
   const float4* __restrict__ x1 = a.rec.p + static_cast<size_t>(a.iters) * n;
   const float4 xi = x1[i];
-  const SceneConst& c = a.s.sc[__float_as_int(a.v2[i].w)];
+  const SceneConst& c = a.s.sc[__float_as_int(a.rec.p[i].w)];
   const float4 ebi = a.eb[i];
   const float4 oi = c.vort_on ? a.rec.omega[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   float mb = 0.0f, ax = 0.0f, ay = 0.0f, az = 0.0f;
@@ -346,7 +352,7 @@ __global__ void __launch_bounds__(kAdjBlock) k_adj_xsph(AdjArgs a) {
   const float4* __restrict__ x1 = a.rec.p + static_cast<size_t>(a.iters) * n;
   const float4 xi = x1[i];
   const float4 vi = a.v2[i];
-  const SceneConst& c = a.s.sc[__float_as_int(vi.w)];
+  const SceneConst& c = a.s.sc[__float_as_int(a.rec.p[i].w)];
   const float4 g3 = a.gv3[i];
   float4 gx = a.gx[i];
   float g2x = g3.x, g2y = g3.y, g2z = g3.z, grho = 0.0f;
@@ -354,15 +360,15 @@ __global__ void __launch_bounds__(kAdjBlock) k_adj_xsph(AdjArgs a) {
     const float ri = a.rec.rho[i];
     const float ai = ri > 0.0f ? c.mass / ri : 0.0f;
     float wsum = 0.0f, vx = 0.0f, vy = 0.0f, vz = 0.0f, rsum = 0.0f;
-    for_list(a.s, i, [&](int j) {
-      const float4 xj = __ldg(x1 + j);
+    auto load = [&](int j) { return Rec3{__ldg(x1 + j), __ldg(a.v2 + j), __ldg(a.gv3 + j)}; };
+    for_list_rec(a.s, i, load, [&](const Rec3 rj) {
+      const float4 xj = rj.a;
       const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
       const float r2 = d2(dx, dy, dz);
       if (!(r2 < c.h2)) return;
-      const float rj = __ldg(a.rec.rho + j);
-      const float aj = rj > 0.0f ? c.mass / rj : 0.0f;
-      const float4 vj = __ldg(a.v2 + j);
-      const float4 gj = __ldg(a.gv3 + j);
+      const float4 vj = rj.b;
+      const float aj = vj.w;
+      const float4 gj = rj.c;
       const float w = Wp(c, r2);
       const float ux = vj.x - vi.x, uy = vj.y - vi.y, uz = vj.z - vi.z;
       const float ti = ux * g3.x + uy * g3.y + uz * g3.z;
