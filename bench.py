@@ -353,7 +353,8 @@ def run_ours(args, world, rank, local):
                    "particles": n, "neighbors_per_particle": round(stats["neighbor_pairs"] / n, 2),
                    "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{world}",
                    "graphs": True, "exact_fp32": True,
-                   "tuning": ({k: [v["unroll"], v["block"]] for k, v in tuning.items()} if tuning else "default")},
+                   "tuning": ({k: [v["unroll"], v["block"]] for k, v in tuning.items()} if tuning else "default"),
+                   "sort_bits": solver.sort_bits()},
         "roofline": roofline, "pair_roofline": pair_roofline,
         "step_roofline": {"bytes_per_particle_step": ALGO_BYTES_PER_STEP, "frac": round(step_frac, 5)},
         "kernel_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in stage.items() if v[1]},
@@ -599,6 +600,7 @@ def run_batched(args, dev, stream, l2_flush):
     big.set_stream(stream.cuda_stream)
     big.upload(pos, vel)
     shapes = big.autotune(1)
+    sort_bits = big.sort_bits()
     small = []
     for sc, pp, vv in zip(scs, parts_p, parts_v):
         s = Solver(dev.index)
@@ -606,6 +608,7 @@ def run_batched(args, dev, stream, l2_flush):
         s.set_stream(stream.cuda_stream)
         s.upload(pp, vv)
         s.set_tuning(shapes)
+        s.set_sort_bits(sort_bits)
         small.append(s)
 
     def time_batched(steps, restore):
@@ -652,7 +655,7 @@ def run_batched(args, dev, stream, l2_flush):
            "serial_scene_steps_per_s": round(len(scs) * 1e3 / statistics.mean(sr), 1),
            "speedup": round(statistics.mean(sr) / statistics.mean(b), 3),
            "workload": "one step over each scene's initial batch per timed step, L2 flushed between steps",
-           "tuning": shapes, }
+           "tuning": shapes, "sort_bits": sort_bits, }
     if args.batch_trajectory > 0:
         tb = time_batched(args.batch_trajectory, False)
         ts = time_serial(args.batch_trajectory, False)
