@@ -222,6 +222,7 @@ def run_ours(args, world, rank, local):
         for _ in range(args.warmup):
             restore()
             solver.step(1)
+    sort_bits = solver.sort_bits()
     solver.set_profiling(True)
     solver.kernel_times(reset=True)
     launches0 = solver.stats()["kernel_launches"]
@@ -354,7 +355,7 @@ def run_ours(args, world, rank, local):
                    "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{world}",
                    "graphs": True, "exact_fp32": True,
                    "tuning": ({k: [v["unroll"], v["block"]] for k, v in tuning.items()} if tuning else "default"),
-                   "sort_bits": solver.sort_bits()},
+                   "sort_bits": sort_bits},
         "roofline": roofline, "pair_roofline": pair_roofline,
         "step_roofline": {"bytes_per_particle_step": ALGO_BYTES_PER_STEP, "frac": round(step_frac, 5)},
         "kernel_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in stage.items() if v[1]},
