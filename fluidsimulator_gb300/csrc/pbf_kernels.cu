@@ -142,6 +142,36 @@ __device__ __forceinline__ float pow_k(float r, int n) {
   return pow_n(r, n);
 }
 
+// Paired forms of the per-entry geometry and kernel functions, for two list
+// entries a and b at once; every lane rounds exactly as the scalar form.
+// d = p - q per axis and r2 = dist2(d).
+struct PairGeom {
+  float2 dx, dy, dz, r2;
+};
+__device__ __forceinline__ PairGeom pair_geom(const float2 px, const float2 py, const float2 pz, const float4 qa,
+                                              const float4 qb, const float2 nz) {
+  PairGeom g;
+  g.dx = psub(px, make_float2(qa.x, qb.x));
+  g.dy = psub(py, make_float2(qa.y, qb.y));
+  g.dz = psub(pz, make_float2(qa.z, qb.z));
+  g.r2 = padd(padd(pmul(g.dx, g.dx, nz), pmul(g.dy, g.dy, nz)), pmul(g.dz, g.dz, nz));
+  return g;
+}
+// poly6 of both lanes.
+__device__ __forceinline__ float2 poly6_pair(const SceneConst& c, const float2 r2, const float2 nz) {
+  const float2 d = psub(f2(c.h2), r2);
+  return pmul(f2(c.poly6_c), pmul(pmul(d, d, nz), d, nz), nz);
+}
+// spiky(clamped_r(r2)) of both lanes.
+__device__ __forceinline__ float2 spiky_pair(const SceneConst& c, const float2 r2, const float2 nz) {
+  const float2 r = make_float2(clamped_r(c, r2.x), clamped_r(c, r2.y));
+  const float2 e = psub(f2(c.h), r);
+  float2 gf = pmul(pmul(f2(c.spiky_c), e, nz), e, nz);
+  if (r.x > c.h) gf.x = 0.0f;
+  if (r.y > c.h) gf.y = 0.0f;
+  return gf;
+}
+
 // Plane restitution and friction on velocity (core.cpp:586-606).
 __device__ __forceinline__ void restitution(const SceneConst& c, float px, float py, float pz,
                                             float& vx, float& vy, float& vz) {
@@ -599,20 +629,12 @@ struct LambdaAcc {
   __device__ __forceinline__ void add_pair(const SceneConst& c, const float2 px, const float2 py, const float2 pz,
                                            const float4 qa, const float4 qb) {
     const float2 nz = f2(c.neg_zero);
-    const float2 dx = psub(px, make_float2(qa.x, qb.x));
-    const float2 dy = psub(py, make_float2(qa.y, qb.y));
-    const float2 dz = psub(pz, make_float2(qa.z, qb.z));
-    const float2 r2 = padd(padd(pmul(dx, dx, nz), pmul(dy, dy, nz)), pmul(dz, dz, nz));
-    const bool oka = r2.x < c.h2, okb = r2.y < c.h2;
+    const PairGeom g = pair_geom(px, py, pz, qa, qb, nz);
+    const bool oka = g.r2.x < c.h2, okb = g.r2.y < c.h2;
     if (!oka && !okb) return;
-    const float2 d = psub(f2(c.h2), r2);
-    const float2 w = pmul(f2(c.poly6_c), pmul(pmul(d, d, nz), d, nz), nz);
-    const float2 r = make_float2(clamped_r(c, r2.x), clamped_r(c, r2.y));
-    const float2 e = psub(f2(c.h), r);
-    float2 gf = pmul(pmul(f2(c.spiky_c), e, nz), e, nz);
-    if (r.x > c.h) gf.x = 0.0f;
-    if (r.y > c.h) gf.y = 0.0f;
-    const float2 gx = pmul(gf, dx, nz), gy = pmul(gf, dy, nz), gz = pmul(gf, dz, nz);
+    const float2 w = poly6_pair(c, g.r2, nz);
+    const float2 gf = spiky_pair(c, g.r2, nz);
+    const float2 gx = pmul(gf, g.dx, nz), gy = pmul(gf, g.dy, nz), gz = pmul(gf, g.dz, nz);
     const float2 ng = f2(-c.grad_scale);
     const float2 jx = pmul(ng, gx, nz), jy = pmul(ng, gy, nz), jz = pmul(ng, gz, nz);
     const float2 t = padd(padd(pmul(jx, jx, nz), pmul(jy, jy, nz)), pmul(jz, jz, nz));
@@ -899,21 +921,13 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_delta(StepAr
     // product rounded on its own).
     const float2 px = f2(p.x), py = f2(p.y), pz = f2(p.z), nz = f2(c.neg_zero);
     auto two = [&](const float4 qa, const float4 qb) {
-      const float2 dx = psub(px, make_float2(qa.x, qb.x));
-      const float2 dy = psub(py, make_float2(qa.y, qb.y));
-      const float2 dz = psub(pz, make_float2(qa.z, qb.z));
-      const float2 r2 = padd(padd(pmul(dx, dx, nz), pmul(dy, dy, nz)), pmul(dz, dz, nz));
-      const bool oka = r2.x < h2, okb = r2.y < h2;
+      const PairGeom g = pair_geom(px, py, pz, qa, qb, nz);
+      const bool oka = g.r2.x < h2, okb = g.r2.y < h2;
       if (!oka && !okb) return;
-      const float2 r = make_float2(clamped_r(c, r2.x), clamped_r(c, r2.y));
-      const float2 e = psub(f2(c.h), r);
-      float2 gf = pmul(pmul(f2(c.spiky_c), e, nz), e, nz);
-      if (r.x > c.h) gf.x = 0.0f;
-      if (r.y > c.h) gf.y = 0.0f;
+      const float2 gf = spiky_pair(c, g.r2, nz);
       float2 s = padd(f2(li), make_float2(qa.w, qb.w));
       if (scorr) {
-        const float2 d = psub(f2(c.h2), r2);
-        const float2 ratio = pmul(pmul(f2(c.poly6_c), pmul(pmul(d, d, nz), d, nz), nz), f2(c.scorr_inv_wdq), nz);
+        const float2 ratio = pmul(poly6_pair(c, g.r2, nz), f2(c.scorr_inv_wdq), nz);
         float2 pw;
         if (kPow == 2) {
           pw = pmul(ratio, ratio, nz);
@@ -928,7 +942,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_delta(StepAr
         s = padd(s, pmul(f2(c.scorr_neg_k), pw, nz));
       }
       const float2 sg = pmul(s, gf, nz);
-      const float2 tx = pmul(sg, dx, nz), ty = pmul(sg, dy, nz), tz = pmul(sg, dz, nz);
+      const float2 tx = pmul(sg, g.dx, nz), ty = pmul(sg, g.dy, nz), tz = pmul(sg, g.dz, nz);
       if (oka) {
         ax += tx.x;
         ay += ty.x;
@@ -997,18 +1011,44 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_xsph(StepArg
     const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
     const float h2 = c.h2;
     float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-    for_each_neighbor<U>(
-        list, n, [&](int j) { return PosVel{__ldg(xs + j), __ldg(vs + j)}; },
-        [&](const PosVel r) {
-          const float r2 = dist2(xi.x - r.x.x, xi.y - r.x.y, xi.z - r.x.z);
-          if (r2 < h2) {
-            const float W = poly6(c, r2);
-            const float inv_rho_j = r.x.w;
-            sx += (r.v.x - vi.x) * W * inv_rho_j;
-            sy += (r.v.y - vi.y) * W * inv_rho_j;
-            sz += (r.v.z - vi.z) * W * inv_rho_j;
-          }
-        });
+    auto load = [&](int j) { return PosVel{__ldg(xs + j), __ldg(vs + j)}; };
+    auto one = [&](const PosVel r) {
+      const float r2 = dist2(xi.x - r.x.x, xi.y - r.x.y, xi.z - r.x.z);
+      if (r2 < h2) {
+        const float W = poly6(c, r2);
+        const float inv_rho_j = r.x.w;
+        sx += (r.v.x - vi.x) * W * inv_rho_j;
+        sy += (r.v.y - vi.y) * W * inv_rho_j;
+        sz += (r.v.z - vi.z) * W * inv_rho_j;
+      }
+    };
+    if constexpr (U == 1) {
+      for_each_neighbor<1>(list, n, load, one);
+    } else {
+      // Two entries at a time, as one() on a then on b (paired arithmetic).
+      const float2 px = f2(xi.x), py = f2(xi.y), pz = f2(xi.z), nz = f2(c.neg_zero);
+      auto two = [&](const PosVel ra, const PosVel rb) {
+        const PairGeom g = pair_geom(px, py, pz, ra.x, rb.x, nz);
+        const bool oka = g.r2.x < h2, okb = g.r2.y < h2;
+        if (!oka && !okb) return;
+        const float2 w = poly6_pair(c, g.r2, nz);
+        const float2 ir = make_float2(ra.x.w, rb.x.w);
+        const float2 tx = pmul(pmul(psub(make_float2(ra.v.x, rb.v.x), f2(vi.x)), w, nz), ir, nz);
+        const float2 ty = pmul(pmul(psub(make_float2(ra.v.y, rb.v.y), f2(vi.y)), w, nz), ir, nz);
+        const float2 tz = pmul(pmul(psub(make_float2(ra.v.z, rb.v.z), f2(vi.z)), w, nz), ir, nz);
+        if (oka) {
+          sx += tx.x;
+          sy += ty.x;
+          sz += tz.x;
+        }
+        if (okb) {
+          sx += tx.y;
+          sy += ty.y;
+          sz += tz.y;
+        }
+      };
+      for_each_neighbor_pair<U>(list, n, load, two, one);
+    }
     vx += c.visc_c * sx;
     vy += c.visc_c * sy;
     vz += c.visc_c * sz;
@@ -1033,7 +1073,8 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_omega(StepAr
     const int n = a.cnt[i];
     const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
     const float h2 = c.h2;
-    for_each_neighbor<U>(list, n, [&](int j) { return PosVel{__ldg(xs + j), __ldg(vs + j)}; }, [&](const PosVel r) {
+    auto load = [&](int j) { return PosVel{__ldg(xs + j), __ldg(vs + j)}; };
+    auto one = [&](const PosVel r) {
       const float dx = xi.x - r.x.x, dy = xi.y - r.x.y, dz = xi.z - r.x.z;
       const float r2 = dist2(dx, dy, dz);
       if (r2 < h2) {
@@ -1044,7 +1085,37 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_omega(StepAr
         oy += uz * gx - ux * gz;
         oz += ux * gy - uy * gx;
       }
-    });
+    };
+    if constexpr (U == 1) {
+      for_each_neighbor<1>(list, n, load, one);
+    } else {
+      // Two entries at a time, as one() on a then on b (paired arithmetic).
+      const float2 px = f2(xi.x), py = f2(xi.y), pz = f2(xi.z), nz = f2(c.neg_zero);
+      auto two = [&](const PosVel ra, const PosVel rb) {
+        const PairGeom g = pair_geom(px, py, pz, ra.x, rb.x, nz);
+        const bool oka = g.r2.x < h2, okb = g.r2.y < h2;
+        if (!oka && !okb) return;
+        const float2 gf = spiky_pair(c, g.r2, nz);
+        const float2 gx = pmul(gf, g.dx, nz), gy = pmul(gf, g.dy, nz), gz = pmul(gf, g.dz, nz);
+        const float2 ux = psub(make_float2(ra.v.x, rb.v.x), f2(vi.x));
+        const float2 uy = psub(make_float2(ra.v.y, rb.v.y), f2(vi.y));
+        const float2 uz = psub(make_float2(ra.v.z, rb.v.z), f2(vi.z));
+        const float2 cx = psub(pmul(uy, gz, nz), pmul(uz, gy, nz));
+        const float2 cy = psub(pmul(uz, gx, nz), pmul(ux, gz, nz));
+        const float2 cz = psub(pmul(ux, gy, nz), pmul(uy, gx, nz));
+        if (oka) {
+          ox += cx.x;
+          oy += cy.x;
+          oz += cz.x;
+        }
+        if (okb) {
+          ox += cx.y;
+          oy += cy.y;
+          oz += cz.y;
+        }
+      };
+      for_each_neighbor_pair<U>(list, n, load, two, one);
+    }
   }
   const float mag = sqrtf(ox * ox + oy * oy + oz * oz);
   a.omega[i] = make_float4(ox, oy, oz, mag);
@@ -1068,18 +1139,45 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_eta(StepArgs
     const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
     const float h2 = c.h2;
     float ex = 0.0f, ey = 0.0f, ez = 0.0f;
-    for_each_neighbor<U>(list, n, [&](int j) { return __ldg(xo + j); },
-                      [&](const float4 r) {
-                        const float dx = xi.x - r.x, dy = xi.y - r.y, dz = xi.z - r.z;
-                        const float r2 = dist2(dx, dy, dz);
-                        if (r2 < h2) {
-                          const float gf = spiky(c, clamped_r(c, r2));
-                          const float coeff = r.w - oi.w;
-                          ex += coeff * (gf * dx);
-                          ey += coeff * (gf * dy);
-                          ez += coeff * (gf * dz);
-                        }
-                      });
+    auto load = [&](int j) { return __ldg(xo + j); };
+    auto one = [&](const float4 r) {
+      const float dx = xi.x - r.x, dy = xi.y - r.y, dz = xi.z - r.z;
+      const float r2 = dist2(dx, dy, dz);
+      if (r2 < h2) {
+        const float gf = spiky(c, clamped_r(c, r2));
+        const float coeff = r.w - oi.w;
+        ex += coeff * (gf * dx);
+        ey += coeff * (gf * dy);
+        ez += coeff * (gf * dz);
+      }
+    };
+    if constexpr (U == 1) {
+      for_each_neighbor<1>(list, n, load, one);
+    } else {
+      // Two entries at a time, as one() on a then on b (paired arithmetic).
+      const float2 px = f2(xi.x), py = f2(xi.y), pz = f2(xi.z), nz = f2(c.neg_zero);
+      auto two = [&](const float4 ra, const float4 rb) {
+        const PairGeom g = pair_geom(px, py, pz, ra, rb, nz);
+        const bool oka = g.r2.x < h2, okb = g.r2.y < h2;
+        if (!oka && !okb) return;
+        const float2 gf = spiky_pair(c, g.r2, nz);
+        const float2 coeff = psub(make_float2(ra.w, rb.w), f2(oi.w));
+        const float2 tx = pmul(coeff, pmul(gf, g.dx, nz), nz);
+        const float2 ty = pmul(coeff, pmul(gf, g.dy, nz), nz);
+        const float2 tz = pmul(coeff, pmul(gf, g.dz, nz), nz);
+        if (oka) {
+          ex += tx.x;
+          ey += ty.x;
+          ez += tz.x;
+        }
+        if (okb) {
+          ex += tx.y;
+          ey += ty.y;
+          ez += tz.y;
+        }
+      };
+      for_each_neighbor_pair<U>(list, n, load, two, one);
+    }
     const float len = sqrtf(ex * ex + ey * ey + ez * ez);
     float nx = 0.0f, ny = 0.0f, nz = 0.0f;
     if (len > c.vort_norm_eps) {
