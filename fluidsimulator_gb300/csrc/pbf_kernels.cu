@@ -776,7 +776,7 @@ __device__ __forceinline__ void for_each_neighbor(const int* __restrict__ list, 
   int j[kUnroll];
   if (kUnroll <= n) {
 #pragma unroll
-    for (int u = 0; u < kUnroll; ++u) j[u] = __ldg(list + 32ll * u);
+    for (int u = 0; u < kUnroll; ++u) j[u] = __ldcs(list + 32ll * u);
   }
   for (; k + kUnroll <= n; k += kUnroll) {
     Rec r[kUnroll];
@@ -784,12 +784,12 @@ __device__ __forceinline__ void for_each_neighbor(const int* __restrict__ list, 
     for (int u = 0; u < kUnroll; ++u) r[u] = load(j[u]);
     if (k + 2 * kUnroll <= n) {
 #pragma unroll
-      for (int u = 0; u < kUnroll; ++u) j[u] = __ldg(list + 32ll * (k + kUnroll + u));
+      for (int u = 0; u < kUnroll; ++u) j[u] = __ldcs(list + 32ll * (k + kUnroll + u));
     }
 #pragma unroll
     for (int u = 0; u < kUnroll; ++u) body(r[u]);
   }
-  for (; k < n; ++k) body(load(__ldg(list + 32ll * k)));
+  for (; k < n; ++k) body(load(__ldcs(list + 32ll * k)));
 }
 
 // for_each_neighbor for bodies that take two consecutive entries at once
@@ -803,7 +803,7 @@ __device__ __forceinline__ void for_each_neighbor_pair(const int* __restrict__ l
   int j[kUnroll];
   if (kUnroll <= n) {
 #pragma unroll
-    for (int u = 0; u < kUnroll; ++u) j[u] = __ldg(list + 32ll * u);
+    for (int u = 0; u < kUnroll; ++u) j[u] = __ldcs(list + 32ll * u);
   }
   for (; k + kUnroll <= n; k += kUnroll) {
     Rec r[kUnroll];
@@ -811,16 +811,16 @@ __device__ __forceinline__ void for_each_neighbor_pair(const int* __restrict__ l
     for (int u = 0; u < kUnroll; ++u) r[u] = load(j[u]);
     if (k + 2 * kUnroll <= n) {
 #pragma unroll
-      for (int u = 0; u < kUnroll; ++u) j[u] = __ldg(list + 32ll * (k + kUnroll + u));
+      for (int u = 0; u < kUnroll; ++u) j[u] = __ldcs(list + 32ll * (k + kUnroll + u));
     }
 #pragma unroll
     for (int u = 0; u < kUnroll; u += 2) body2(r[u], r[u + 1]);
   }
   for (; k + 2 <= n; k += 2) {
-    const Rec ra = load(__ldg(list + 32ll * k)), rb = load(__ldg(list + 32ll * (k + 1)));
+    const Rec ra = load(__ldcs(list + 32ll * k)), rb = load(__ldcs(list + 32ll * (k + 1)));
     body2(ra, rb);
   }
-  if (k < n) body1(load(__ldg(list + 32ll * k)));
+  if (k < n) body1(load(__ldcs(list + 32ll * k)));
 }
 
 struct PosVel {
