@@ -57,14 +57,14 @@ __device__ __forceinline__ void for_list(const StepArgs& s, int i, Body&& body) 
   const int* __restrict__ list = s.nbr + s.wbase[i >> 5] + (i & 31);
   int k = 0;
   for (; k + 4 <= n; k += 4) {
-    const int j0 = __ldg(list + 32ll * k), j1 = __ldg(list + 32ll * (k + 1));
-    const int j2 = __ldg(list + 32ll * (k + 2)), j3 = __ldg(list + 32ll * (k + 3));
+    const int j0 = __ldcs(list + 32ll * k), j1 = __ldcs(list + 32ll * (k + 1));
+    const int j2 = __ldcs(list + 32ll * (k + 2)), j3 = __ldcs(list + 32ll * (k + 3));
     body(j0);
     body(j1);
     body(j2);
     body(j3);
   }
-  for (; k < n; ++k) body(__ldg(list + 32ll * k));
+  for (; k < n; ++k) body(__ldcs(list + 32ll * k));
 }
 
 // for_list with the neighbours' records fetched four ahead and the next four
@@ -79,7 +79,7 @@ __device__ __forceinline__ void for_list_rec(const StepArgs& s, int i, Load&& lo
   int j[kAhead];
   if (kAhead <= n) {
 #pragma unroll
-    for (int u = 0; u < kAhead; ++u) j[u] = __ldg(list + 32ll * u);
+    for (int u = 0; u < kAhead; ++u) j[u] = __ldcs(list + 32ll * u);
   }
   for (; k + kAhead <= n; k += kAhead) {
     Rec r[kAhead];
@@ -87,12 +87,12 @@ __device__ __forceinline__ void for_list_rec(const StepArgs& s, int i, Load&& lo
     for (int u = 0; u < kAhead; ++u) r[u] = load(j[u]);
     if (k + 2 * kAhead <= n) {
 #pragma unroll
-      for (int u = 0; u < kAhead; ++u) j[u] = __ldg(list + 32ll * (k + kAhead + u));
+      for (int u = 0; u < kAhead; ++u) j[u] = __ldcs(list + 32ll * (k + kAhead + u));
     }
 #pragma unroll
     for (int u = 0; u < kAhead; ++u) body(r[u]);
   }
-  for (; k < n; ++k) body(load(__ldg(list + 32ll * k)));
+  for (; k < n; ++k) body(load(__ldcs(list + 32ll * k)));
 }
 
 struct Rec2 {
