@@ -317,6 +317,64 @@ def test_sort_width_gives_same_permutation(cuda_lib, oracle_lib, case):
     s.close()
 
 
+@pytest.mark.parametrize("n", [2, 3, 4])
+def test_scorr_exponent_variants_match_oracle(cuda_lib, oracle_lib, n):
+    """s_corr with n = 2, 3, 4: the delta pass compiled for that exponent
+    (every s_corr scene shares it) stays bit-exact with the oracle."""
+    sc = scenes.dam_break(8, seed=31 + n, flags=True)
+    sc.params.scorr_n = n
+    ref = oracle_lib.Oracle().run(sc.params, sc.pos, sc.vel, 0.0, 20)
+    got = run_gpu(sc, 20)
+    np.testing.assert_array_equal(got["pos"], ref["pos"])
+    np.testing.assert_array_equal(got["vel"], ref["vel"])
+
+
+def test_scorr_exponent_read_per_scene(cuda_lib, oracle_lib):
+    """Scenes with different s_corr exponents in one solver take the delta
+    pass that reads n per scene; n = 5 goes through powf, whose last ulp may
+    differ from glibc's pow, so that scene is held to the floating-point bar
+    (max |dx| <= 1e-5 h after one step) instead of exact equality."""
+    scs = []
+    for k, n in enumerate((2, 3, 5)):
+        sc = scenes.dam_break(6, seed=40 + k, flags=True)
+        sc.params.scorr_n = n
+        scs.append(sc)
+    s = Solver(0)
+    s.configure([sc.params for sc in scs], [sc.count for sc in scs])
+    s.upload(np.concatenate([sc.pos for sc in scs], axis=1), np.concatenate([sc.vel for sc in scs], axis=1))
+    s.step(1)
+    pos, vel = s.download()
+    s.close()
+    off = 0
+    for sc in scs:
+        ref = oracle_lib.Oracle().run(sc.params, sc.pos, sc.vel, 0.0, 1)
+        got = pos[:, off:off + sc.count]
+        if sc.params.scorr_n <= 4:
+            np.testing.assert_array_equal(got, ref["pos"])
+            np.testing.assert_array_equal(vel[:, off:off + sc.count], ref["vel"])
+        else:
+            assert np.max(np.abs(got - ref["pos"])) <= 1e-5 * sc.params.h
+        off += sc.count
+
+
+@pytest.mark.parametrize("unroll", [1, 2, 4, 8])
+def test_every_unroll_matches_oracle(cuda_lib, oracle_lib, unroll):
+    """Each list-pass variant (scalar at 1, two entries per step in paired
+    arithmetic from 2 up, odd tails included) gives the oracle's bits, with
+    s_corr, XSPH, vorticity and planes on."""
+    sc = scenes.dam_break(9, seed=17, flags=True)
+    ref = oracle_lib.Oracle().run(sc.params, sc.pos, sc.vel, 0.0, 15)
+    s = Solver(0)
+    s.configure([sc.params], [sc.count])
+    s.set_tuning({k: {"unroll": unroll, "block": 128} for k in _capi.TUNABLE})
+    s.upload(sc.pos, sc.vel)
+    s.step(15)
+    pos, vel = s.download()
+    s.close()
+    np.testing.assert_array_equal(pos, ref["pos"])
+    np.testing.assert_array_equal(vel, ref["vel"])
+
+
 def test_all_pairs_lists_match_oracle(cuda_lib, oracle_lib):
     """use_uniform_grid = 0: lists in ascending caller index from all pairs
     (core/src/core.cpp:248-268), a different summation order than the grid's."""
