@@ -164,6 +164,21 @@ int bits_for(long long cap) {
 
 }  // namespace
 
+// Device address of a page-locked host buffer mapped for `device` (pinned
+// by cudaHostAlloc / cudaMallocHost or registered with cudaHostRegister), or
+// nullptr for any other pointer. The upload and download kernels read and
+// write such buffers in place over the host link, without staging copies;
+// pageable memory keeps the copy path.
+const void* mapped_host(const void* p, int device) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (at.type != cudaMemoryTypeHost || !at.devicePointer || at.device != device) return nullptr;
+  return at.devicePointer;
+}
+
 class Solver {
  public:
   explicit Solver(int device) : device_(device) {}
@@ -279,6 +294,9 @@ class Solver {
 
   int set_params(const fluid_params* params) {
     if (!S_) return fail(FLUID_ERR_STATE, "configure first");
+    // Unchanged parameters (the usual case of a caller stepping one scene
+    // repeatedly) need no validation, upload or synchronisation.
+    if (params && std::memcmp(params, params_.data(), sizeof(fluid_params) * S_) == 0) return FLUID_OK;
     for (int s = 0; s < S_; ++s) {
       std::string why;
       int rc = validate_params(params[s], why);
@@ -302,8 +320,10 @@ class Solver {
     return FLUID_OK;
   }
 
+  // wait = false leaves the copies in flight on the solver's stream, for a
+  // caller whose next work on that stream consumes them (the stateless step).
   int upload(const float* px, const float* py, const float* pz, const float* vx, const float* vy,
-             const float* vz, int memory) {
+             const float* vz, int memory, bool wait = true) {
     if (!S_) return fail(FLUID_ERR_STATE, "configure first");
     if (n_ > 0 && (!px || !py || !pz || !vx || !vy || !vz)) return fail(FLUID_ERR_INVALID_ARGUMENT, "null array");
     int rc = synchronize();
@@ -311,7 +331,9 @@ class Solver {
     if (n_ > 0) {
       const float* src[6] = {px, py, pz, vx, vy, vz};
       const float* dev[6];
-      if (memory == FLUID_MEMORY_HOST) {
+      if (memory == FLUID_MEMORY_HOST && all_mapped(src, dev)) {
+        // page-locked: the upload kernel reads the caller's arrays in place
+      } else if (memory == FLUID_MEMORY_HOST) {
         float* stage = reinterpret_cast<float*>(p_[0].p);  // 4n floats
         float* stage2 = reinterpret_cast<float*>(p_[1].p);
         for (int k = 0; k < 6; ++k) {
@@ -326,7 +348,7 @@ class Solver {
       if (enqueue_upload(dev[0], dev[1], dev[2], dev[3], dev[4], dev[5], x_[parity_].p, v_[parity_].p,
                          slot_[parity_].p, rho_[parity_].p, sc_.p, S_, n_, stream_) != cudaSuccess)
         return cuda_fail("upload kernel");
-      if (cudaStreamSynchronize(stream_) != cudaSuccess) return cuda_fail("upload");
+      if (wait && cudaStreamSynchronize(stream_) != cudaSuccess) return cuda_fail("upload");
     }
     uploaded_ = true;
     return FLUID_OK;
@@ -340,17 +362,21 @@ class Solver {
     if (n_ == 0) return FLUID_OK;
     float* dst[6] = {px, py, pz, vx, vy, vz};
     float* dev[6];
-    if (memory == FLUID_MEMORY_HOST) {
+    bool staged = false;
+    if (memory == FLUID_MEMORY_HOST && all_mapped(dst, dev)) {
+      // page-locked: the download kernel writes the caller's arrays in place
+    } else if (memory == FLUID_MEMORY_HOST) {
       float* stage = reinterpret_cast<float*>(p_[0].p);
       float* stage2 = reinterpret_cast<float*>(p_[1].p);
       for (int k = 0; k < 6; ++k) dev[k] = (k < 4 ? stage : stage2) + static_cast<size_t>(k % 4) * n_;
+      staged = true;
     } else {
       for (int k = 0; k < 6; ++k) dev[k] = dst[k];
     }
     if (enqueue_download(x_[parity_].p, v_[parity_].p, slot_[parity_].p, dev[0], dev[1], dev[2], dev[3], dev[4],
                          dev[5], n_, stream_) != cudaSuccess)
       return cuda_fail("download kernel");
-    if (memory == FLUID_MEMORY_HOST) {
+    if (staged) {
       for (int k = 0; k < 6; ++k) {
         if (cudaMemcpyAsync(dst[k], dev[k], sizeof(float) * n_, cudaMemcpyDeviceToHost, stream_) != cudaSuccess)
           return cuda_fail("download copy");
@@ -358,6 +384,18 @@ class Solver {
     }
     if (cudaStreamSynchronize(stream_) != cudaSuccess) return cuda_fail("download");
     return FLUID_OK;
+  }
+
+  // Device addresses of six host arrays when every one is page-locked and
+  // mapped for this solver's device.
+  template <typename T>
+  bool all_mapped(T* const (&host)[6], T* (&dev)[6]) const {
+    for (int k = 0; k < 6; ++k) {
+      const void* d = mapped_host(host[k], device_);
+      if (!d) return false;
+      dev[k] = static_cast<T*>(const_cast<void*>(d));
+    }
+    return true;
   }
 
   int step_async(int nsteps) {
@@ -1527,7 +1565,9 @@ int fluid_gb300_cuda_step(const fluid_params* params, int64_t count, float* px, 
     if (rc) return rc;
   }
   fgb::Solver& s = cache.s->impl;
-  if ((rc = s.upload(px, py, pz, vx, vy, vz, FLUID_MEMORY_HOST))) return rc;
+  // The host arrays are read by copies left in flight: the step and the
+  // download that follow on the same stream finish before this returns.
+  if ((rc = s.upload(px, py, pz, vx, vy, vz, FLUID_MEMORY_HOST, false))) return rc;
   if ((rc = s.set_time(0, *time))) return rc;
   if ((rc = s.step(1))) return rc;
   if ((rc = s.download(px, py, pz, vx, vy, vz, FLUID_MEMORY_HOST))) return rc;

@@ -175,6 +175,46 @@ def test_stateless_cuda_step_matches_golden(cuda_lib):
     np.testing.assert_array_equal(pos, d["s10_pos"])
 
 
+def _pinned_copy(a):
+    """A page-locked host copy of a float32 array (numpy view of pinned memory)."""
+    import torch
+
+    t = torch.empty(a.shape, dtype=torch.float32).pin_memory()
+    out = t.numpy()
+    out[...] = a
+    return out, t
+
+
+def test_page_locked_host_arrays_are_read_in_place(cuda_lib, oracle_lib):
+    """Page-locked caller arrays go straight to the upload / download kernels
+    (no staging copies): same bits as pageable arrays and as the oracle,
+    through the stateless step and through a solver."""
+    p, d = load_golden("dam_break_4096.npz")
+    sc = golden_scene("dam_break_4096.npz")
+    pos, keep_p = _pinned_copy(sc.pos)
+    vel, keep_v = _pinned_copy(sc.vel)
+    t = 0.0
+    for _ in range(10):
+        t = cuda_step(p, pos, vel, t)
+    np.testing.assert_array_equal(pos, d["s10_pos"])
+    np.testing.assert_array_equal(vel, d["s10_vel"])
+    flags = scenes.dam_break(8, seed=3, flags=True)
+    ref = oracle_lib.Oracle().run(flags.params, flags.pos, flags.vel, 0.0, 12)
+    ip, keep_ip = _pinned_copy(flags.pos)
+    iv, keep_iv = _pinned_copy(flags.vel)
+    op, keep_op = _pinned_copy(np.zeros_like(flags.pos))
+    ov, keep_ov = _pinned_copy(np.zeros_like(flags.vel))
+    s = Solver(0)
+    s.configure([flags.params], [flags.count])
+    s.upload(ip, iv)
+    s.step(12)
+    s.download(op, ov)
+    s.close()
+    np.testing.assert_array_equal(op, ref["pos"])
+    np.testing.assert_array_equal(ov, ref["vel"])
+    del keep_p, keep_v, keep_ip, keep_iv, keep_op, keep_ov
+
+
 def test_capacity_regrow_keeps_results(cuda_lib, oracle_lib):
     # The flags scene collapses from ~25 to ~500 neighbours: the lists grow
     # several times and every re-run step must still match the oracle.
