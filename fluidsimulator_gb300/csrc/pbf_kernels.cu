@@ -1233,6 +1233,19 @@ __global__ void __launch_bounds__(kBlock) k_download(const float4* x, const floa
   vz[o] = vs.z;
 }
 
+// One float4 field (x or v) of the step's output, caller order, into three
+// arrays, targets[0..2]; nothing is written when the step failed.
+__global__ void __launch_bounds__(kBlock) k_download_field(const float4* src, const int* slot,
+                                                           float* const* targets, int n, const DevStatus* status) {
+  if (failed(status)) return;
+  const int o = blockIdx.x * kBlock + threadIdx.x;
+  if (o >= n) return;
+  const float4 f = src[slot[o]];
+  targets[0][o] = f.x;
+  targets[1][o] = f.y;
+  targets[2][o] = f.z;
+}
+
 __global__ void k_reset(DevStatus* st, int* bmin, int* bmax, int scenes) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t == 0) {
@@ -1318,7 +1331,7 @@ void LaunchMarks::mark(int stage) {
 }
 
 cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t st, LaunchMarks& m,
-                         const StepRecord* rec) {
+                         const StepRecord* rec, const StepDownload* dl) {
   const int nb = blocks_for(a.n, kBlock);
   m.start();
   k_bounds<<<nb, kBlock, 0, st>>>(a);
@@ -1384,6 +1397,12 @@ cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t s
                       cudaMemcpyDeviceToDevice, st);
   }
   if (rec) cudaMemcpyAsync(rec->rho, a.rho, n1, cudaMemcpyDeviceToDevice, st);
+  if (dl) {  // positions are final: write them out beside the velocity passes
+    cudaEventRecord(dl->committed, st);
+    cudaStreamWaitEvent(dl->aux, dl->committed, 0);
+    k_download_field<<<nb, kBlock, 0, dl->aux>>>(a.x, a.slot, dl->targets, a.n, a.status);
+    cudaEventRecord(dl->positions_done, dl->aux);
+  }
   if (plan.xsph) {
     const int b = plan.block[FLUID_KERNEL_XSPH];
     // The committing pass left {x, m / rho} in the p buffer it did not use.
@@ -1401,6 +1420,10 @@ cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t s
     FGB_DISPATCH_UNROLL(plan.unroll[FLUID_KERNEL_ETA], k_eta, blocks_for(a.n, be), be, st, a,
                         plan.restitution ? 1 : 0);
     m.mark(FLUID_KERNEL_ETA);
+  }
+  if (dl) {
+    k_download_field<<<nb, kBlock, 0, st>>>(a.v, a.slot, dl->targets + 3, a.n, a.status);
+    cudaStreamWaitEvent(st, dl->positions_done, 0);
   }
   return cudaGetLastError();
 }

@@ -79,11 +79,26 @@ struct StepRecord {
   float4* omega = nullptr;  // omega and |omega| (when vorticity runs)
 };
 
+// The step's result written out while the step finishes (the stateless
+// step on page-locked caller arrays): the positions, final once the last
+// Jacobi iteration commits them, on `aux` while the velocity passes run; the
+// velocities after the last pass. Both writes are skipped when the step
+// failed, so a step that is re-run never exposes stale values.
+// The six destination arrays (x, y, z positions, then velocities) are read
+// from device memory, so a captured graph serves every call.
+struct StepDownload {
+  cudaStream_t aux = nullptr;
+  cudaEvent_t committed = nullptr;       // recorded on the step's stream
+  cudaEvent_t positions_done = nullptr;  // recorded on aux
+  float* const* targets = nullptr;       // device array of 6 pointers
+};
+
 // Enqueues one full timestep on `stream`; with `rec`, also records the
-// internals the adjoint needs (device-to-device copies after the kernels).
+// internals the adjoint needs (device-to-device copies after the kernels);
+// with `dl`, also writes the result out (see StepDownload).
 cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan,
                          cudaStream_t stream, LaunchMarks& marks,
-                         const StepRecord* rec = nullptr);
+                         const StepRecord* rec = nullptr, const StepDownload* dl = nullptr);
 
 // Packs caller-order SoA arrays (device) into slot-order x/v of one parity.
 cudaError_t enqueue_upload(const float* px, const float* py, const float* pz,

@@ -193,6 +193,10 @@ class Solver {
     }
     if (copy_stream_) cudaStreamDestroy(copy_stream_);
     if (status_host_) cudaFreeHost(status_host_);
+    if (split_.committed) cudaEventDestroy(split_.committed);
+    if (split_.positions_done) cudaEventDestroy(split_.positions_done);
+    if (aux_) cudaStreamDestroy(aux_);
+    if (targets_host_) cudaFreeHost(targets_host_);
     if (own_) cudaStreamDestroy(own_);
   }
 
@@ -398,6 +402,39 @@ class Solver {
     return true;
   }
 
+  // One step whose result goes straight into the caller's page-locked host
+  // arrays while the step finishes (StepDownload: positions beside the
+  // velocity passes, velocities at the end), launched without the graph;
+  // any other memory takes step + download.
+  int step_download_host(float* px, float* py, float* pz, float* vx, float* vy, float* vz) {
+    float* host[6] = {px, py, pz, vx, vy, vz};
+    float* dev[6];
+    if (n_ == 0 || profiling_ || !all_mapped(host, dev)) {
+      int rc = step(1);
+      return rc ? rc : download(px, py, pz, vx, vy, vz, FLUID_MEMORY_HOST);
+    }
+    if (!aux_) {
+      if (cudaStreamCreateWithFlags(&aux_, cudaStreamNonBlocking) != cudaSuccess ||
+          cudaEventCreateWithFlags(&split_.committed, cudaEventDisableTiming) != cudaSuccess ||
+          cudaEventCreateWithFlags(&split_.positions_done, cudaEventDisableTiming) != cudaSuccess ||
+          targets_.alloc(6) != cudaSuccess ||
+          cudaMallocHost(reinterpret_cast<void**>(&targets_host_), 6 * sizeof(float*)) != cudaSuccess)
+        return cuda_fail("download stream");
+      split_.aux = aux_;
+      split_.targets = targets_.p;
+    }
+    int rc = synchronize();  // targets_host_ may still feed an earlier copy
+    if (rc) return rc;
+    for (int k = 0; k < 6; ++k) targets_host_[k] = dev[k];
+    if (cudaMemcpyAsync(targets_.p, targets_host_, 6 * sizeof(float*), cudaMemcpyHostToDevice, stream_) !=
+        cudaSuccess)
+      return cuda_fail("download targets");
+    split_on_ = true;
+    rc = step(1);  // a step re-run after regrowth writes out again
+    split_on_ = false;
+    return rc;
+  }
+
   int step_async(int nsteps) {
     if (!uploaded_) return fail(FLUID_ERR_STATE, "no state uploaded");
     if (nsteps < 0) return fail(FLUID_ERR_INVALID_ARGUMENT, "negative step count");
@@ -424,9 +461,10 @@ class Solver {
   int synchronize() {
     for (;;) {
       if (pending_ == 0) return FLUID_OK;
-      if (cudaStreamSynchronize(stream_) != cudaSuccess) return cuda_fail("step");
-      if (cudaMemcpy(status_host_, status_.p, sizeof(DevStatus), cudaMemcpyDeviceToHost) != cudaSuccess)
+      if (cudaMemcpyAsync(status_host_, status_.p, sizeof(DevStatus), cudaMemcpyDeviceToHost, stream_) !=
+          cudaSuccess)
         return cuda_fail("status read");
+      if (cudaStreamSynchronize(stream_) != cudaSuccess) return cuda_fail("step");
       const DevStatus st = *status_host_;
       const int done = st.err ? st.fail_step : pending_;
       const int remaining = pending_ - done;
@@ -990,11 +1028,17 @@ class Solver {
         int rc = build_graphs();
         if (rc) return rc;
       }
-      if (cudaGraphLaunch(exec_[par], stream_) != cudaSuccess) return cuda_fail("graph launch");
+      if (split_on_ && !split_exec_[par]) {
+        int rc = capture(par, &split_, &split_exec_[par]);
+        if (rc) return rc;
+      }
+      if (cudaGraphLaunch(split_on_ ? split_exec_[par] : exec_[par], stream_) != cudaSuccess)
+        return cuda_fail("graph launch");
       launches_ += launches_per_step_;
     } else {
       LaunchMarks m = marks(par, false);
-      if (enqueue_step(args(par), plan_, stream_, m) != cudaSuccess) return cuda_fail("launch");
+      if (enqueue_step(args(par), plan_, stream_, m, nullptr, split_on_ ? &split_ : nullptr) != cudaSuccess)
+        return cuda_fail("launch");
       launches_ += m.launches;
       launches_per_step_ = m.launches;
       marks_used_[par] = m.next;
@@ -1003,33 +1047,43 @@ class Solver {
     return FLUID_OK;
   }
 
+  // Captures one step of parity `par` (with the result write-out when dl).
+  int capture(int par, const StepDownload* dl, cudaGraphExec_t* out) {
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+      return cuda_fail("begin capture");
+    LaunchMarks m = marks(par, true);
+    cudaError_t e = enqueue_step(args(par), plan_, stream_, m, nullptr, dl);
+    cudaError_t e2 = cudaStreamEndCapture(stream_, &g);
+    if (e != cudaSuccess || e2 != cudaSuccess || !g) return cuda_fail("capture");
+    if (cudaGraphInstantiate(out, g, 0) != cudaSuccess) {
+      cudaGraphDestroy(g);
+      return cuda_fail("graph instantiate");
+    }
+    cudaGraphDestroy(g);
+    if (!dl) {
+      launches_per_step_ = m.launches;
+      marks_used_[par] = m.next;
+    }
+    return FLUID_OK;
+  }
+
   int build_graphs() {
     destroy_graphs();
     for (int par = 0; par < 2; ++par) {
-      cudaGraph_t g = nullptr;
-      if (cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
-        return cuda_fail("begin capture");
-      LaunchMarks m = marks(par, true);
-      cudaError_t e = enqueue_step(args(par), plan_, stream_, m);
-      cudaError_t e2 = cudaStreamEndCapture(stream_, &g);
-      if (e != cudaSuccess || e2 != cudaSuccess || !g) return cuda_fail("capture");
-      if (cudaGraphInstantiate(&exec_[par], g, 0) != cudaSuccess) {
-        cudaGraphDestroy(g);
-        return cuda_fail("graph instantiate");
-      }
-      cudaGraphDestroy(g);
-      launches_per_step_ = m.launches;
-      marks_used_[par] = m.next;
+      int rc = capture(par, nullptr, &exec_[par]);
+      if (rc) return rc;
     }
     graphs_valid_ = true;
     return FLUID_OK;
   }
 
   void destroy_graphs() {
-    for (auto& e : exec_) {
-      if (e) cudaGraphExecDestroy(e);
-      e = nullptr;
-    }
+    for (auto* set : {&exec_, &split_exec_})
+      for (auto& e : *set) {
+        if (e) cudaGraphExecDestroy(e);
+        e = nullptr;
+      }
     graphs_valid_ = false;
   }
   void invalidate_graphs() { destroy_graphs(); }
@@ -1285,6 +1339,12 @@ class Solver {
   DBuf<DevStatus> status_;
   DBuf<SceneConst> sc_;
   DevStatus* status_host_ = nullptr;
+  cudaStream_t aux_ = nullptr;  // stateless step: positions written out beside the velocity passes
+  StepDownload split_;
+  bool split_on_ = false;
+  DBuf<float*> targets_;          // the write-out's six destination arrays
+  float** targets_host_ = nullptr;
+  cudaGraphExec_t split_exec_[2] = {nullptr, nullptr};
   long long grid_cap_ = 0, nbr_cap_ = 0;
   StepPlan plan_;
   bool use_graphs_ = true, graphs_valid_ = false, profiling_ = false;
@@ -1569,8 +1629,7 @@ int fluid_gb300_cuda_step(const fluid_params* params, int64_t count, float* px, 
   // download that follow on the same stream finish before this returns.
   if ((rc = s.upload(px, py, pz, vx, vy, vz, FLUID_MEMORY_HOST, false))) return rc;
   if ((rc = s.set_time(0, *time))) return rc;
-  if ((rc = s.step(1))) return rc;
-  if ((rc = s.download(px, py, pz, vx, vy, vz, FLUID_MEMORY_HOST))) return rc;
+  if ((rc = s.step_download_host(px, py, pz, vx, vy, vz))) return rc;
   return s.get_time(0, time);
 }
 

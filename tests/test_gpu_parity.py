@@ -212,7 +212,19 @@ def test_page_locked_host_arrays_are_read_in_place(cuda_lib, oracle_lib):
     s.close()
     np.testing.assert_array_equal(op, ref["pos"])
     np.testing.assert_array_equal(ov, ref["vel"])
-    del keep_p, keep_v, keep_ip, keep_iv, keep_op, keep_ov
+    # a collapsing scene through the stateless step: the lists regrow and the
+    # failed steps are re-run while the result is written out beside them
+    grow = scenes.dam_break(12, seed=9, flags=True)
+    ref = oracle_lib.Oracle().run(grow.params, grow.pos, grow.vel, 0.0, 30)
+    gp, keep_gp = _pinned_copy(grow.pos)
+    gv, keep_gv = _pinned_copy(grow.vel)
+    t = 0.0
+    for _ in range(30):
+        t = cuda_step(grow.params, gp, gv, t)
+    np.testing.assert_array_equal(gp, ref["pos"])
+    np.testing.assert_array_equal(gv, ref["vel"])
+    assert np.float32(t) == np.float32(ref["time"])
+    del keep_p, keep_v, keep_ip, keep_iv, keep_op, keep_ov, keep_gp, keep_gv
 
 
 def test_capacity_regrow_keeps_results(cuda_lib, oracle_lib):
