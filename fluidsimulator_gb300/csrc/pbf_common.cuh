@@ -31,7 +31,7 @@ constexpr int kBlock = 256;
 constexpr int kRadixItems = 8;                      // keys per thread
 constexpr int kRadixTile = kBlock * kRadixItems;    // keys per CTA
 constexpr int kRadixMaxBins = 1 << 11;                // widest digit (11 bits)
-constexpr int kRadixMaxPasses = 4;                  // 8-bit digits of a u32
+constexpr int kRadixMaxPasses = 4;                  // passes of a u32 key at 8-bit digits
 constexpr unsigned kFull = 0xffffffffu;
 
 // Per-scene constants, each computed on the host with the same float

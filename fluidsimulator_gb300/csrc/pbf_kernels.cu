@@ -4,7 +4,8 @@
 //   k_bounds        predicted cell of every particle, per-scene bounding box
 //   k_grid_setup    per-scene dense grid over that box, key base, radix passes
 //   k_keys          x-major linear cell key per particle, in caller order
-//   k_radix_*       stable LSD radix sort of (key, caller index), 8-bit digits
+//   k_radix_*       stable LSD radix sort of (key, caller index), 8- or 11-bit
+//                   digits
 //   k_reorder       gather into cell order, predict again (bit-identical),
 //                   cell (first, end) table by warp-shuffle boundary detection
 //   k_nbr_build     27-cell scan: lists in scan order staged in shared memory,
@@ -22,7 +23,9 @@
 // square root, and each neighbour sum runs in the reference's order (cells
 // dz, dy, dx; ascending caller index inside a cell), so on the same input the
 // results equal the reference CPU path bit for bit. Membership tests and the
-// prediction use explicit round-to-nearest intrinsics as well.
+// prediction use explicit round-to-nearest intrinsics as well; the list
+// passes form each neighbour's terms two at a time in paired FP32
+// instructions whose lanes round as the scalar operations do (see pmul).
 
 #include <climits>
 #include <type_traits>
@@ -526,10 +529,6 @@ __global__ void __launch_bounds__(kBlock) k_reorder(StepArgs a) {
 
 // ---------------------------------------------------------------------------
 // Neighbour lists.
-
-struct Cell27 {
-  int cx, cy, cz;
-};
 
 // Calls f(j, pos[j]) for j in [lo, hi) except j == self (kSkip), kFetch
 // records loaded before any is used. Lanes of a warp whose particles share a
