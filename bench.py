@@ -339,7 +339,7 @@ def run_ours(args, world, rank, local):
         batched = run_batched(args, dev, stream, l2_flush)
     differentiable = None
     if not args.no_adjoint:
-        differentiable = run_differentiable(args, dev, stream, with_cpu=(rank == 0 and world == 1))
+        differentiable = run_differentiable(args, dev, stream)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -370,13 +370,15 @@ def run_ours(args, world, rank, local):
         print(json.dumps(_finite(out)), flush=True)
 
 
-def run_differentiable(args, dev, stream, with_cpu=True):
+def run_differentiable(args, dev, stream):
     """Differentiable PBF: 32^3 block (32,768 particles), XSPH c = 0.01 and
     s_corr on, initial velocity N(0, 0.1^2), 60 steps, loss |COM - (1.5, 0.3,
     1.0)|^2. Times the forward run and forward + adjoint (checkpoints every 10
     steps, recomputation in between), and checks dL/dv0 and dL/dc against
     central finite differences of the GPU forward (16 random directions, step
-    1e-3) and against the oracle's FP64 adjoint of the same FP32 trajectory."""
+    1e-3). The FP64 checks of these gradients (the oracle's FP64 adjoint and
+    central differences of its FP64 forward) are tests:
+    tests/test_adjoint.py::test_differentiable_scene_gradients_match_fp64."""
     import numpy as np
     import torch
 
@@ -473,59 +475,6 @@ def run_differentiable(args, dev, stream, with_cpu=True):
     out["fd"] = {"as_specified": fd_check(sc),
                  "unit_mass": fd_check(scenes.differentiable_block(32, seed=0, unit_mass=True)),
                  "directions": args.fd_dirs, "step": 1e-3}
-    if with_cpu:
-        from oracle import pyoracle
-
-        pyoracle.build(ref=False)
-        horizon = 5
-        states = [(sc.pos, sc.vel)]
-        for _ in range(horizon):
-            r = pyoracle.Oracle().run(sc.params, *states[-1], 0.0, 1)
-            states.append((r["pos"], r["vel"]))
-        com = states[-1][0].astype(np.float64).mean(axis=1)
-        g = np.repeat((2.0 * (com - target) / n)[:, None], n, axis=1)
-        gv = np.zeros((3, n))
-        gct = 0.0
-        for t in reversed(range(horizon)):
-            g, gv, c, _, _ = pyoracle.vjp(sc.params, *states[t], g, gv, fwd32=True)
-            gct += c
-        gx0, gv0, gc = grad(horizon)
-        # central differences of the FP64 forward (step 1e-6) on the unit-mass
-        # scene against the GPU adjoint: FP32 rounding noise of a COM loss
-        # (~1e-9) swamps a 1e-3 step's signal, FP64 does not.
-        um = scenes.differentiable_block(32, seed=0, unit_mass=True)
-        s.set_params([um.params])
-        fd64 = {}
-        for hz in (1, 5):
-            s.upload(um.pos, um.vel)
-            s.record(hz, every)
-            x, _ = s.download()
-            com = x.astype(np.float64).mean(axis=1)
-            gxf = np.repeat((2.0 * (com - target) / n)[:, None], n, axis=1).astype(np.float32)
-            _, gv_um, _ = s.backward(gxf, np.zeros((3, n), np.float32))
-            rng = np.random.default_rng(7)
-            rels = []
-            for _ in range(4):
-                d = rng.standard_normal((3, n))
-                d /= np.sqrt(np.mean(d * d))
-
-                def l64(v0):
-                    r = pyoracle.Oracle(np.float64).run(um.params, um.pos.astype(np.float64), v0, 0.0, hz)
-                    return float(np.sum((r["pos"].mean(axis=1) - target) ** 2))
-
-                e6 = 1e-6
-                fd = (l64(um.vel.astype(np.float64) + e6 * d) - l64(um.vel.astype(np.float64) - e6 * d)) / (2 * e6)
-                ad = float(np.sum(gv_um.astype(np.float64) * d))
-                rels.append(abs(fd - ad) / max(abs(fd), abs(ad), 1e-30))
-            fd64[str(hz)] = {"rel_err_median": float(np.median(rels)), "rel_err_max": float(np.max(rels)),
-                             "within_1e-3": int(sum(r <= 1e-3 for r in rels)), "directions": 4}
-        s.set_params([sc.params])
-        out["fd_fp64_unit_mass"] = fd64
-        out["fp64_adjoint"] = {"horizon": horizon,
-                               "dL_dv0_rel_err": float(np.linalg.norm(gv0 - gv) / np.linalg.norm(gv)),
-                               "dL_dx0_rel_err": float(np.linalg.norm(gx0 - g) / np.linalg.norm(g)),
-                               "dL_dc_rel_err": float(abs(gc[0] - gct) / abs(gct)),
-                               "note": "oracle FP64 adjoint linearised around the same FP32 trajectory"}
     s.close()
     return out
 
