@@ -251,6 +251,7 @@ class Solver {
     checkpoints_.clear();
     tapes_.clear();
     rec_steps_ = 0;
+    tail_taped_ = false;
     adj_n_ = 0;
     warps_ = (n_ + 31) / 32;
     tiles_ = std::max(1, (n_ + kRadixTile - 1) / kRadixTile);
@@ -311,6 +312,7 @@ class Solver {
     int rc = synchronize();
     if (rc) return rc;
     params_.assign(params, params + S_);
+    tail_taped_ = false;
     build_scene_consts();
     if (cudaMemcpyAsync(sc_.p, sc_host_.data(), S_ * sizeof(SceneConst), cudaMemcpyHostToDevice, stream_) !=
             cudaSuccess ||
@@ -638,6 +640,7 @@ class Solver {
     if (n_ == 0) return FLUID_OK;
     if ((rc = ensure_adjoint_buffers())) return rc;
     if (tapes_.empty()) tapes_.resize(1);
+    tail_taped_ = false;  // tapes_[0] is overwritten below
     const int parity0 = parity_;
     const long long steps0 = steps_;
     const std::vector<float> times0 = times_;
@@ -686,14 +689,26 @@ class Solver {
     int rc = synchronize();
     if (rc) return rc;
     checkpoints_.clear();
-    checkpoints_.resize((nsteps + every - 1) / every);
-    for (int t = 0; t < nsteps; ++t) {
-      if (t % every == 0 && (rc = snap_save(checkpoints_[t / every]))) return rc;
-      if ((rc = step(1))) return rc;
+    const int segs = (nsteps + every - 1) / every;
+    checkpoints_.resize(segs);
+    tail_taped_ = false;
+    if (static_cast<int>(tapes_.size()) < every) tapes_.resize(every);
+    for (int seg = 0; seg < segs; ++seg) {
+      const int t0 = seg * every, t1 = std::min(nsteps, t0 + every);
+      if ((rc = snap_save(checkpoints_[seg]))) return rc;
+      if (seg + 1 < segs) {
+        if ((rc = step(t1 - t0))) return rc;  // one synchronisation per segment
+      } else {
+        // The last segment is taped as it runs: backward() reverses it first
+        // and needs no recomputation for it.
+        for (int t = t0; t < t1; ++t)
+          if ((rc = taped_step(tapes_[t - t0]))) return rc;
+      }
     }
     if ((rc = snap_save(final_))) return rc;
     rec_steps_ = nsteps;
     rec_every_ = every;
+    tail_taped_ = true;
     return FLUID_OK;
   }
 
@@ -720,9 +735,13 @@ class Solver {
     for (int seg = segs - 1; seg >= 0; --seg) {
       const int t0 = seg * rec_every_;
       const int t1 = std::min(rec_steps_, t0 + rec_every_);
-      if ((rc = snap_load(checkpoints_[seg]))) return rc;
-      for (int t = t0; t < t1; ++t)  // recompute the segment once, taping every step
-        if ((rc = taped_step(tapes_[t - t0]))) return rc;
+      if (seg == segs - 1 && tail_taped_) {
+        tail_taped_ = false;  // taped by record(); the tapes are reused below
+      } else {
+        if ((rc = snap_load(checkpoints_[seg]))) return rc;
+        for (int t = t0; t < t1; ++t)  // recompute the segment once, taping every step
+          if ((rc = taped_step(tapes_[t - t0]))) return rc;
+      }
       for (int t = t1 - 1; t >= t0; --t) {
         if ((rc = tape_adjoint(tapes_[t - t0], cur[0], cur[1], nxt[0], nxt[1], gc))) return rc;
         for (int sc = 0; sc < S_; ++sc) total[sc] += gc[sc];
@@ -1311,6 +1330,7 @@ class Solver {
   std::vector<Snap> checkpoints_;
   Snap final_;
   int rec_steps_ = 0, rec_every_ = 1;
+  bool tail_taped_ = false;  // tapes_ hold record()'s last segment
 
   cudaStream_t copy_stream_ = nullptr;
   cudaEvent_t frame_gather_[2] = {nullptr, nullptr}, frame_done_[2] = {nullptr, nullptr};

@@ -127,6 +127,16 @@ def test_gpu_trajectory_backward_with_checkpoints(cuda_lib, oracle_lib):
     gvf = np.zeros((3, n), np.float32)
     gx0, gv0, gc = s.backward(gxf, gvf)
     np.testing.assert_array_equal(s.download()[0], xf)  # left at the final state
+    # record() tapes its last segment for the first backward(); a second
+    # backward(), or one after step_backward() reused the tapes, recomputes it
+    for between in (None, "step_backward"):
+        if between:
+            s.upload(sc.pos, sc.vel)
+            s.record(steps, every)
+            s.step_backward(gxf, gvf)
+        again = s.backward(gxf, gvf)
+        np.testing.assert_array_equal(again[0], gx0)
+        np.testing.assert_array_equal(again[1], gv0)
     s.close()
     # oracle: chain of single-step VJPs around the float32 trajectory
     states = [(sc.pos, sc.vel)]
