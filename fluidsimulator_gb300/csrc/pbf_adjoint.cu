@@ -30,7 +30,6 @@ namespace fgb {
 namespace {
 
 constexpr int kAdjBlock = 256;
-constexpr unsigned kAll = 0xffffffffu;
 
 __device__ __forceinline__ bool adj_failed(const DevStatus* st) {
   return *reinterpret_cast<const volatile int*>(&st->err) != 0;

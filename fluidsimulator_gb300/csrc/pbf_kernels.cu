@@ -676,7 +676,15 @@ __device__ __forceinline__ void for_each_pair_candidate(const StepArgs& a, const
 // k_nbr_overflow writes their remaining entries.
 __global__ void __launch_bounds__(kMaxBuildBlock) k_nbr_build(StepArgs a) {
   extern __shared__ int stage[];
-  if (failed(a.status)) return;
+  // Other blocks of this launch may set the status (capacity) while this
+  // one starts: read it once for the whole block, so either every warp
+  // returns here or every warp reaches the barriers and the slice claim
+  // below (a warp left behind by an early return of thread 0's warp would
+  // read an unset block_base).
+  __shared__ int block_failed;
+  if (threadIdx.x == 0) block_failed = failed(a.status) ? 1 : 0;
+  __syncthreads();
+  if (block_failed) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int* mine = stage + warp * (kStage * 32) + lane;  // entry k at mine[32 k]

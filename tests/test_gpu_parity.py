@@ -238,6 +238,29 @@ def test_capacity_regrow_keeps_results(cuda_lib, oracle_lib):
     np.testing.assert_array_equal(b["vel"], a["vel"])
 
 
+@pytest.mark.parametrize("block", [128, 256, 512])
+def test_batched_regrow_matches_oracle(cuda_lib, oracle_lib, block):
+    """Several collapsing scenes in one solver: the lists outgrow their
+    capacity mid-run (blocks of the list build fail while others proceed) and
+    the failed steps are re-run, at every list-pass block size; each scene
+    stays bit-exact with the oracle."""
+    scs = [scenes.dam_break(n, seed=50 + n, flags=True) for n in (10, 12, 12)]
+    refs = [oracle_lib.Oracle().run(sc.params, sc.pos, sc.vel, 0.0, 50) for sc in scs]
+    s = Solver(0)
+    s.configure([sc.params for sc in scs], [sc.count for sc in scs])
+    s.set_tuning({k: {"unroll": 4, "block": block} for k in _capi.TUNABLE})
+    s.upload(np.concatenate([sc.pos for sc in scs], axis=1), np.concatenate([sc.vel for sc in scs], axis=1))
+    s.step(50)
+    pos, vel = s.download()
+    assert s.stats()["regrows"] >= 1
+    s.close()
+    off = 0
+    for sc, ref in zip(scs, refs):
+        np.testing.assert_array_equal(pos[:, off:off + sc.count], ref["pos"])
+        np.testing.assert_array_equal(vel[:, off:off + sc.count], ref["vel"])
+        off += sc.count
+
+
 def test_nonfinite_input_reports_error_and_keeps_state(cuda_lib):
     sc = scenes.dam_break(6, seed=1)
     pos = sc.pos.copy()
