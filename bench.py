@@ -321,6 +321,7 @@ def run_ours(args, world, rank, local):
     traj = None
     if args.trajectory > 0:
         restore()
+        solver.set_profiling(True)  # per-kernel totals; ~0.1 ms a step against 10-200 ms steps
         solver.kernel_times(reset=True)
         t_ms, t_pairs = [], []
         for _ in range(args.trajectory):
