@@ -77,6 +77,8 @@ class FluidParams(ctypes.Structure):
         ("plane_ny", c_float * MAX_PLANES),
         ("plane_nz", c_float * MAX_PLANES),
         ("plane_d", c_float * MAX_PLANES),
+        ("plane_friction_per_plane", c_int32),
+        ("plane_friction_each", c_float * MAX_PLANES),
     ]
 
     def planes(self):

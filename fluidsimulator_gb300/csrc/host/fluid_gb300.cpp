@@ -48,6 +48,12 @@ fluid_params Params::to_c() const {
     p.plane_nz[q] = planes.nz[q];
     p.plane_d[q] = planes.d[q];
   }
+  if (!plane_friction_each.empty()) {
+    if (plane_friction_each.size() != planes.size())
+      throw_status(FLUID_ERR_INVALID_ARGUMENT, "plane_friction_each needs one value per plane");
+    p.plane_friction_per_plane = 1;
+    for (std::size_t q = 0; q < planes.size(); ++q) p.plane_friction_each[q] = plane_friction_each[q];
+  }
   return p;
 }
 

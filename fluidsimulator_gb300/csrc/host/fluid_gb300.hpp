@@ -91,7 +91,12 @@ struct Params {
     }
   } planes;
 
-  // The C-ABI form (throws Error if there are more than FLUID_MAX_PLANES planes).
+  // Extension: each plane's own friction, in plane order. Empty (the
+  // default) applies plane_friction to every plane, as the reference does.
+  std::vector<float> plane_friction_each;
+
+  // The C-ABI form (throws Error if there are more than FLUID_MAX_PLANES
+  // planes, or if plane_friction_each is neither empty nor one per plane).
   fluid_params to_c() const;
 };
 

@@ -212,9 +212,10 @@ __global__ void __launch_bounds__(kAdjBlock) k_adj_out(AdjArgs a) {
         const float vn = pl.x * v[0] + pl.y * v[1] + pl.z * v[2];
         const float s = vn < 0.0f ? c.rest_neg_e : 1.0f;
         if (vn < 0.0f) neg |= 1u << q;
-        v[0] = (v[0] - vn * pl.x) * c.rest_scale + s * vn * pl.x;
-        v[1] = (v[1] - vn * pl.y) * c.rest_scale + s * vn * pl.y;
-        v[2] = (v[2] - vn * pl.z) * c.rest_scale + s * vn * pl.z;
+        const float keep = c.rest_scale[q];
+        v[0] = (v[0] - vn * pl.x) * keep + s * vn * pl.x;
+        v[1] = (v[1] - vn * pl.y) * keep + s * vn * pl.y;
+        v[2] = (v[2] - vn * pl.z) * keep + s * vn * pl.z;
       }
     }
     for (int q = c.plane_count - 1; q >= 0; --q) {
@@ -222,10 +223,11 @@ __global__ void __launch_bounds__(kAdjBlock) k_adj_out(AdjArgs a) {
       const float4 pl = c.planes[q];
       const float s = (neg >> q & 1u) ? c.rest_neg_e : 1.0f;
       const float gn = pl.x * g[0] + pl.y * g[1] + pl.z * g[2];
-      const float k = (s - c.rest_scale) * gn;
-      g[0] = c.rest_scale * g[0] + k * pl.x;
-      g[1] = c.rest_scale * g[1] + k * pl.y;
-      g[2] = c.rest_scale * g[2] + k * pl.z;
+      const float keep = c.rest_scale[q];
+      const float k = (s - keep) * gn;
+      g[0] = keep * g[0] + k * pl.x;
+      g[1] = keep * g[1] + k * pl.y;
+      g[2] = keep * g[2] + k * pl.z;
     }
   }
   if (!a.vorticity) {

@@ -50,7 +50,7 @@ struct SceneConst {
   int xsph_on;
   float vort_eps, vort_norm_eps;
   int vort_on;
-  float rest_neg_e, rest_scale;   // -restitution, 1 - friction
+  float rest_neg_e;               // -restitution
   int rest_on;
   int plane_count;
   int iterations;
@@ -58,6 +58,7 @@ struct SceneConst {
   int first_slot, count;          // particle range of the scene
   float neg_zero;                 // -0.0f, read at run time (see pmul in the kernels)
   float4 planes[FLUID_MAX_PLANES];  // (nx, ny, nz, d)
+  float rest_scale[FLUID_MAX_PLANES];  // 1 - friction of each plane
 };
 
 // Bounding grid of one scene for the current step.

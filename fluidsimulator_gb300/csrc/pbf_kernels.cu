@@ -175,7 +175,8 @@ __device__ __forceinline__ float2 spiky_pair(const SceneConst& c, const float2 r
   return gf;
 }
 
-// Plane restitution and friction on velocity (core.cpp:586-606).
+// Plane restitution and friction on velocity (core.cpp:586-606); each plane
+// has its own tangential scale 1 - friction.
 __device__ __forceinline__ void restitution(const SceneConst& c, float px, float py, float pz,
                                             float& vx, float& vy, float& vz) {
   for (int q = 0; q < c.plane_count; ++q) {
@@ -188,9 +189,10 @@ __device__ __forceinline__ void restitution(const SceneConst& c, float px, float
       const float tx = vx - vn * pl.x;
       const float ty = vy - vn * pl.y;
       const float tz = vz - vn * pl.z;
-      vx = tx * c.rest_scale + vn_new * pl.x;
-      vy = ty * c.rest_scale + vn_new * pl.y;
-      vz = tz * c.rest_scale + vn_new * pl.z;
+      const float keep = c.rest_scale[q];
+      vx = tx * keep + vn_new * pl.x;
+      vy = ty * keep + vn_new * pl.y;
+      vz = tz * keep + vn_new * pl.z;
     }
   }
 }

@@ -120,9 +120,16 @@ SceneConst make_scene_const(const fluid_params& p, int first, int count) {
   c.vort_eps = p.vort_epsilon;
   c.vort_norm_eps = p.vort_norm_eps;
   c.vort_on = (p.enable_vorticity && p.vort_epsilon != 0.0f) ? 1 : 0;
+  // core.cpp:573-612 with one friction for every plane, or each plane's own
+  // when plane_friction_per_plane is set.
   c.rest_neg_e = -p.plane_restitution;
-  c.rest_scale = 1.0f - p.plane_friction;
-  c.rest_on = ((p.plane_restitution > 0.0f || p.plane_friction > 0.0f) && p.plane_count > 0) ? 1 : 0;
+  bool friction = false;
+  for (int q = 0; q < p.plane_count; ++q) {
+    const float mu = p.plane_friction_per_plane ? p.plane_friction_each[q] : p.plane_friction;
+    c.rest_scale[q] = 1.0f - mu;
+    friction |= mu > 0.0f;
+  }
+  c.rest_on = ((p.plane_restitution > 0.0f || friction) && p.plane_count > 0) ? 1 : 0;
   c.plane_count = p.plane_count;
   c.iterations = p.solver_iterations;
   c.all_pairs = p.use_uniform_grid ? 0 : 1;

@@ -121,6 +121,16 @@ def init_planes(p: FluidParams, bx: float, by: float, bz: float) -> None:
     add_plane_normalized(p, 0.0, 0.0, -1.0, -bz)
 
 
+def set_plane_friction(p: FluidParams, frictions) -> None:
+    """Gives each plane its own friction, in plane order (an extension: the
+    reference applies one plane_friction to all planes, core/src/core.cpp:575)."""
+    if len(frictions) != p.plane_count:
+        raise ValueError(f"{len(frictions)} frictions for {p.plane_count} planes")
+    p.plane_friction_per_plane = 1
+    for q, mu in enumerate(frictions):
+        p.plane_friction_each[q] = float(np.float32(mu))
+
+
 def jitter(pos: np.ndarray, amplitude: float, seed: int, offset: int = 0) -> np.ndarray:
     """pos + U(-a, a) per coordinate; draw k = 3*i + axis, added in float32."""
     n = pos.shape[1]
@@ -297,8 +307,12 @@ def load_scene_json(path: str) -> Scene:
     Additional keys, ignored by the reference and optional here:
       "solver": {"dt", "iterations", "scorr_dq_coeff", "vort_epsilon",
                  "enable_scorr", "enable_xsph", "enable_vorticity",
-                 "plane_restitution", "plane_friction"}
+                 "plane_restitution", "plane_friction", "per_plane_friction"}
       "jitter": {"amplitude", "seed"}  -- U(-a, a) per coordinate (SplitMix64)
+    With "per_plane_friction": true, each collision's own "friction" (the key
+    the reference scene files carry and the reference loader drops) applies
+    to its plane; a collision without one takes "plane_friction". Without
+    that switch the per-collision values are ignored, as in the reference.
     """
     import json
 
@@ -358,6 +372,7 @@ def load_scene_json(path: str) -> Scene:
     pos = np.concatenate(blocks_p, axis=1) if blocks_p else np.zeros((3, 0), np.float32)
     vel = np.concatenate(blocks_v, axis=1) if blocks_v else np.zeros((3, 0), np.float32)
     p.plane_count = 0
+    plane_mu = []
     for entry in root.get("collisions", []):
         if entry.get("type") != "plane":
             raise ValueError(f"Unsupported collision type: {entry.get('type')}")
@@ -374,6 +389,7 @@ def load_scene_json(path: str) -> Scene:
             raise ValueError("too many planes")
         p.plane_nx[i], p.plane_ny[i], p.plane_nz[i], p.plane_d[i] = float(nx), float(ny), float(nz), float(d)
         p.plane_count = i + 1
+        plane_mu.append(entry.get("friction"))
     solver = root.get("solver", {})
     for key, field in (("dt", "dt"), ("scorr_dq_coeff", "scorr_dq_coeff"), ("vort_epsilon", "vort_epsilon"),
                        ("plane_restitution", "plane_restitution"), ("plane_friction", "plane_friction")):
@@ -384,6 +400,8 @@ def load_scene_json(path: str) -> Scene:
     for key in ("enable_scorr", "enable_xsph", "enable_vorticity"):
         if key in solver:
             setattr(p, key, int(bool(solver[key])))
+    if solver.get("per_plane_friction", False):
+        set_plane_friction(p, [p.plane_friction if mu is None else mu for mu in plane_mu])
     if "jitter" in root:
         pos = jitter(pos, float(root["jitter"].get("amplitude", 0.0)), int(root["jitter"].get("seed", 0)))
     import os

@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define FLUID_GB300_ABI_VERSION 1
+#define FLUID_GB300_ABI_VERSION 2
 /* Planes per scene. The reference keeps an unbounded std::vector SoA
  * (core/include/fluid/core.h:44-78); every reference scene uses 6. */
 #define FLUID_MAX_PLANES 32
@@ -45,7 +45,8 @@ typedef enum fluid_status {
  * Mirrors fluid::Params (core/include/fluid/core.h:11-79) field for field, same
  * meaning and units. The plane SoA (core.h:44-78) becomes fixed arrays plus a
  * count so the struct holds no pointers. Params::backend (core.h:13-17) is not
- * carried: neither reference step function reads it.
+ * carried: neither reference step function reads it. The last two fields
+ * (per-plane friction) extend it; left zero they change nothing.
  */
 typedef struct fluid_params {
   float dt;                      /* core.h:12 */
@@ -74,6 +75,15 @@ typedef struct fluid_params {
   float plane_ny[FLUID_MAX_PLANES];
   float plane_nz[FLUID_MAX_PLANES];
   float plane_d[FLUID_MAX_PLANES]; /* signed distance = n.x - d */
+  /* Per-plane friction, an extension with no fluid::Params counterpart: the
+   * reference scene files give each collision plane a "friction" value that
+   * its loader drops (core/src/init.cpp:371-414). When nonzero, plane q scales
+   * the tangential velocity by 1 - plane_friction_each[q] in place of
+   * 1 - plane_friction, and the contact pass runs when plane_restitution > 0
+   * or any plane's friction > 0. Zero (the default) keeps the reference's
+   * single friction. */
+  int32_t plane_friction_per_plane;
+  float plane_friction_each[FLUID_MAX_PLANES];
 } fluid_params;
 
 /* Fills *p with the defaults of core/include/fluid/core.h:12-43 (no planes). */
@@ -115,7 +125,7 @@ int fluid_gb300_cuda_step(const fluid_params* params, int64_t count,
  * and the call returns when it is done.
  *
  * All scratch lives in one fixed device array inside this library (about
- * 7.3 MiB, held on every GPU that loads the library until the process
+ * 7.5 MiB, held on every GPU that loads the library until the process
  * exits). Limits: count <= FLUID_NOALLOC_MAX_PARTICLES, at most
  * FLUID_NOALLOC_MAX_NEIGHBOR_SLOTS neighbour-list entries (32-wide slices)
  * and FLUID_NOALLOC_MAX_CELLS grid cells per step; beyond any of them the

@@ -73,6 +73,19 @@ T pow_n(T ratio, int n) {
   return std::pow(ratio, static_cast<T>(n));
 }
 
+// Friction of plane q: the scene's single value (core.cpp:575), or the
+// plane's own under the per-plane extension of fluid_params.
+inline float plane_mu(const fluid_params& p, int q) {
+  return p.plane_friction_per_plane ? p.plane_friction_each[q] : p.plane_friction;
+}
+
+// core.cpp:573-574: the contact pass runs when restitution or friction is on.
+inline bool contacts_on(const fluid_params& p) {
+  bool friction = false;
+  for (int q = 0; q < p.plane_count; ++q) friction |= plane_mu(p, q) > 0.0f;
+  return (p.plane_restitution > 0.0f || friction) && p.plane_count > 0;
+}
+
 struct Cell {
   int x, y, z;
 };
@@ -537,10 +550,10 @@ int step(Workspace<T>& w, const fluid_params& p, std::size_t n, T* X, T* Y,
   }
 
   // Plane restitution and friction (core.cpp:573-612).
-  if ((p.plane_restitution > 0.0f || p.plane_friction > 0.0f) &&
-      p.plane_count > 0) {
+  if (contacts_on(p)) {
     const T e = T(p.plane_restitution);
-    const T scale = T(1) - T(p.plane_friction);
+    T scale[FLUID_MAX_PLANES];
+    for (int q = 0; q < p.plane_count; ++q) scale[q] = T(1) - T(plane_mu(p, q));
 #pragma omp parallel for
     for (long long i = 0; i < N; ++i) {
       T vx = VX[i], vy = VY[i], vz = VZ[i];
@@ -556,9 +569,9 @@ int step(Workspace<T>& w, const fluid_params& p, std::size_t n, T* X, T* Y,
           const T tx = vx - vn * nx;
           const T ty = vy - vn * ny;
           const T tz = vz - vn * nz;
-          vx = tx * scale + vn_new * nx;
-          vy = ty * scale + vn_new * ny;
-          vz = tz * scale + vn_new * nz;
+          vx = tx * scale[q] + vn_new * nx;
+          vy = ty * scale[q] + vn_new * ny;
+          vz = tz * scale[q] + vn_new * nz;
         }
       }
       VX[i] = vx;
@@ -640,8 +653,10 @@ int adjoint(const Record<T>& R, const fluid_params& p, const T* gxo, const T* gv
   const int sn = c.scorr_n;
   const bool xsph = p.enable_xsph && p.visc_c != 0.0f;
   const T cv = T(p.visc_c);
-  const bool rest = (p.plane_restitution > 0.0f || p.plane_friction > 0.0f) && p.plane_count > 0;
-  const T e = T(p.plane_restitution), mu_s = T(1) - T(p.plane_friction);
+  const bool rest = contacts_on(p);
+  const T e = T(p.plane_restitution);
+  T mu_s[FLUID_MAX_PLANES];
+  for (int q = 0; q < p.plane_count; ++q) mu_s[q] = T(1) - T(plane_mu(p, q));
   auto W = [&](T r2) { const T d = h2 - r2; return c6 * d * d * d; };
   auto dW = [&](T r2) { const T d = h2 - r2; return T(-3) * c6 * d * d; };
   auto F = [&](T r) { const T d = h - r; return csp * d * d; };
@@ -705,14 +720,14 @@ int adjoint(const Record<T>& R, const fluid_params& p, const T* gxo, const T* gv
         if (act[q]) {
           const T vn = nq[0] * v[0] + nq[1] * v[1] + nq[2] * v[2];
           sc[q] = (vn < T(0)) ? -e : T(1);
-          for (int a = 0; a < 3; ++a) v[a] = (v[a] - vn * nq[a]) * mu_s + sc[q] * vn * nq[a];
+          for (int a = 0; a < 3; ++a) v[a] = (v[a] - vn * nq[a]) * mu_s[q] + sc[q] * vn * nq[a];
         }
       }
       for (int q = p.plane_count - 1; q >= 0; --q) {
         if (!act[q]) continue;
         const T nq[3] = {T(p.plane_nx[q]), T(p.plane_ny[q]), T(p.plane_nz[q])};
         const T gn = nq[0] * g[0] + nq[1] * g[1] + nq[2] * g[2];
-        for (int a = 0; a < 3; ++a) g[a] = mu_s * g[a] + (sc[q] - mu_s) * gn * nq[a];
+        for (int a = 0; a < 3; ++a) g[a] = mu_s[q] * g[a] + (sc[q] - mu_s[q]) * gn * nq[a];
       }
     }
     for (int a = 0; a < 3; ++a) gv4[a * n + i] = g[a];

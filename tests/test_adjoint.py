@@ -10,10 +10,14 @@ from fluidsimulator_gb300 import scenes
 
 
 def _scene(side=6, seed=1, floor=False):
+    """floor: start just above the floor, moving down (plane contacts in
+    step 1); "per_plane" also gives each plane its own friction."""
     sc = scenes.differentiable_block(side, seed=seed)
-    if floor:  # start just above the floor, moving down: plane contacts in step 1
+    if floor:
         sc.pos[1] -= np.float32(0.045)
         sc.vel[1] -= np.float32(3.0)
+    if floor == "per_plane":
+        scenes.set_plane_friction(sc.params, [0.3, 0.0, 0.6, 0.2, 0.9, 0.1])
     return sc
 
 
@@ -22,7 +26,7 @@ def _run64(oracle_lib, params, pos, vel, steps):
     return r["pos"], r["vel"]
 
 
-@pytest.mark.parametrize("floor", [False, True])
+@pytest.mark.parametrize("floor", [False, True, "per_plane"])
 def test_cpu_adjoint_matches_central_differences(oracle_lib, floor):
     sc = _scene(floor=floor)
     rng = np.random.default_rng(3)
@@ -83,7 +87,7 @@ def _rel(a, b):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("floor", [False, True])
+@pytest.mark.parametrize("floor", [False, True, "per_plane"])
 def test_gpu_vjp_matches_oracle(cuda_lib, oracle_lib, floor):
     """FP32 GPU adjoint vs the oracle's FP64 adjoint of the same FP32 forward."""
     from fluidsimulator_gb300.solver import Solver

@@ -455,10 +455,12 @@ def _corners():
     base = scenes.dam_break(8, seed=11, flags=True)
     out = []
 
-    def variant(name, **kw):
+    def variant(name, frictions=None, **kw):
         v = base.copy()
         for k, val in kw.items():
             setattr(v.params, k, val)
+        if frictions is not None:
+            scenes.set_plane_friction(v.params, frictions)
         out.append((name, v))
 
     variant("all_flags")
@@ -474,6 +476,12 @@ def _corners():
     variant("no_flags", enable_xsph=0, enable_vorticity=0, enable_scorr=0)
     variant("no_iterations_flags", solver_iterations=0)
     variant("no_iterations_vorticity_only", solver_iterations=0, enable_xsph=0)
+    mus = [0.0, 0.7, 0.5, 0.2, 0.05, 1.0]  # x-, x+, floor, ceiling, z-, z+ walls
+    variant("per_plane_all_flags", frictions=mus)
+    variant("per_plane_xsph_only", frictions=mus, enable_vorticity=0)
+    variant("per_plane_no_flags", frictions=mus, enable_xsph=0, enable_vorticity=0, enable_scorr=0)
+    variant("per_plane_friction_only", frictions=mus, plane_restitution=0.0, plane_friction=0.0)
+    variant("per_plane_all_zero", frictions=[0.0] * 6, plane_restitution=0.0)
     return out
 
 
@@ -508,6 +516,29 @@ def test_parameter_corners_match_oracle(cuda_lib, oracle_lib, name, sc):
     for k in ("pos", "vel", "neighbor_counts", "rho"):
         np.testing.assert_array_equal(got[k], ref[k], err_msg=k)
     assert np.float32(got["time"]) == np.float32(ref["time"])
+
+
+def test_per_plane_friction_read_per_scene(cuda_lib, oracle_lib):
+    """Scenes with a single friction and with per-plane frictions in one
+    solver: each takes its own planes' scales, bit-exact with the oracle."""
+    scs = []
+    for k, mus in enumerate((None, [0.9, 0.0, 0.4, 0.0, 0.1, 0.6], [0.0] * 6)):
+        sc = scenes.dam_break(7, seed=50 + k, flags=k != 1)
+        if mus is not None:
+            scenes.set_plane_friction(sc.params, mus)
+        scs.append(sc)
+    s = Solver(0)
+    s.configure([sc.params for sc in scs], [sc.count for sc in scs])
+    s.upload(np.concatenate([sc.pos for sc in scs], axis=1), np.concatenate([sc.vel for sc in scs], axis=1))
+    s.step(30)
+    pos, vel = s.download()
+    s.close()
+    off = 0
+    for sc in scs:
+        ref = oracle_lib.Oracle().run(sc.params, sc.pos, sc.vel, 0.0, 30)
+        np.testing.assert_array_equal(pos[:, off:off + sc.count], ref["pos"])
+        np.testing.assert_array_equal(vel[:, off:off + sc.count], ref["vel"])
+        off += sc.count
 
 
 def test_all_pairs_lists_match_oracle(cuda_lib, oracle_lib):

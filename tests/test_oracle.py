@@ -144,3 +144,50 @@ def test_default_params_match_reference(oracle_lib):
     if not oracle_lib.ref_available():
         pytest.skip("reference tree not present")
     assert bytes(default_params()) == bytes(oracle_lib.ref_default_params())
+
+
+def _floor(p):
+    return next(q for q in range(p.plane_count) if p.plane_ny[q] == 1.0 and p.plane_d[q] == 0.0)
+
+
+def test_per_plane_friction_with_equal_values_is_single_friction(oracle_lib):
+    """Per-plane friction set to the scene's single value changes no bit;
+    the reference pin refuses a per-plane scene (fluid::Params cannot hold it)."""
+    base = scenes.dam_break(8, seed=11, flags=True)
+    same = base.copy()
+    scenes.set_plane_friction(same.params, [base.params.plane_friction] * base.params.plane_count)
+    a = oracle_lib.Oracle().run(base.params, base.pos, base.vel, 0.0, 12)
+    b = oracle_lib.Oracle().run(same.params, same.pos, same.vel, 0.0, 12)
+    np.testing.assert_array_equal(a["pos"], b["pos"])
+    np.testing.assert_array_equal(a["vel"], b["vel"])
+    mus = [0.0] * base.params.plane_count
+    mus[_floor(base.params)] = 0.6
+    floor_only = base.copy()
+    scenes.set_plane_friction(floor_only.params, mus)
+    c = oracle_lib.Oracle().run(floor_only.params, floor_only.pos, floor_only.vel, 0.0, 12)
+    assert not np.array_equal(a["vel"], c["vel"])
+    if oracle_lib.ref_available():
+        with pytest.raises(RuntimeError):
+            oracle_lib.Reference().run(same.params, same.pos, same.vel, 0.0, 1)
+
+
+@pytest.mark.parametrize("restitution,mu_floor,mu_wall", [(0.05, 0.5, 0.0), (0.0, 0.3, 0.9), (0.0, 0.0, 0.0)])
+def test_per_plane_friction_scales_tangential_velocity_of_touching_plane(oracle_lib, restitution, mu_floor, mu_wall):
+    """One particle (no neighbours) crossing the floor of the unit box with
+    velocity (1, -1, 0): the floor's friction alone scales its tangential x
+    velocity; a wall it does not touch has no effect. With restitution and
+    every friction zero the contact pass does not run at all."""
+    p = scenes.dam_break(2).params
+    p.plane_restitution = restitution
+    p.plane_friction = 0.25  # overridden by the per-plane values
+    mus = [mu_wall] * p.plane_count
+    mus[_floor(p)] = mu_floor
+    scenes.set_plane_friction(p, mus)
+    pos = np.array([[0.5], [0.001], [0.5]], np.float32)
+    vel = np.array([[1.0], [-1.0], [0.0]], np.float32)
+    r = oracle_lib.Oracle().run(p, pos, vel, 0.0, 1)
+    vx = float(r["vel"][0, 0])
+    assert abs(vx - (1.0 - mu_floor)) <= 1e-5
+    assert float(r["vel"][2, 0]) == 0.0
+    d = oracle_lib.Oracle(np.float64).run(p, pos.astype(np.float64), vel.astype(np.float64), 0.0, 1)
+    assert abs(float(d["vel"][0, 0]) - (1.0 - mu_floor)) <= 1e-5

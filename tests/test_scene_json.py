@@ -50,3 +50,28 @@ def test_additional_keys(tmp_path):
     path.write_text(json.dumps(plain))
     base = scenes.load_scene_json(str(path))
     assert 0 < np.max(np.abs(sc.pos - base.pos)) <= 5e-4 * 1.0001
+
+
+def test_per_plane_friction_key(tmp_path):
+    """Per-collision "friction" is read only under "per_plane_friction";
+    a collision without one takes the scene's plane_friction."""
+    scene = {
+        "fluid": {"particle_mass": 0.125, "density": 1000, "h": 0.1, "epsilon": 100,
+                  "shape": [{"type": "cube", "origin": [0.1, 0.1, 0.1], "size": [0.2, 0.2, 0.2]}]},
+        "collisions": [{"type": "plane", "point": [0, 0, 0], "normal": [0, 1, 0], "friction": 0.5},
+                       {"type": "plane", "point": [0, 0, 0], "normal": [1, 0, 0]},
+                       {"type": "plane", "point": [1, 1, 1], "normal": [0, -1, 0], "friction": 0.0}],
+        "solver": {"plane_restitution": 0.05, "plane_friction": 0.1},
+    }
+    path = tmp_path / "s.json"
+    path.write_text(json.dumps(scene))
+    off = scenes.load_scene_json(str(path))
+    assert off.params.plane_friction_per_plane == 0
+    assert list(off.params.plane_friction_each[:3]) == [0.0, 0.0, 0.0]
+    scene["solver"]["per_plane_friction"] = True
+    path.write_text(json.dumps(scene))
+    on = scenes.load_scene_json(str(path))
+    assert on.params.plane_friction_per_plane == 1
+    mu = [np.float32(x) for x in on.params.plane_friction_each[:3]]
+    assert mu == [np.float32(0.5), np.float32(0.1), np.float32(0.0)]
+    np.testing.assert_array_equal(on.pos, off.pos)
