@@ -1243,16 +1243,18 @@ __global__ void __launch_bounds__(kBlock) k_download(const float4* x, const floa
 }
 
 // One float4 field (x or v) of the step's output, caller order, into three
-// arrays, targets[0..2]; nothing is written when the step failed.
+// arrays, targets[0..2]; nothing is written when the step failed. Any grid
+// covers all n (grid-stride), so the write-out that runs beside the velocity
+// passes can take a few blocks and leave the SMs to those passes.
 __global__ void __launch_bounds__(kBlock) k_download_field(const float4* src, const int* slot,
                                                            float* const* targets, int n, const DevStatus* status) {
   if (failed(status)) return;
-  const int o = blockIdx.x * kBlock + threadIdx.x;
-  if (o >= n) return;
-  const float4 f = src[slot[o]];
-  targets[0][o] = f.x;
-  targets[1][o] = f.y;
-  targets[2][o] = f.z;
+  for (int o = blockIdx.x * kBlock + threadIdx.x; o < n; o += gridDim.x * kBlock) {
+    const float4 f = src[slot[o]];
+    targets[0][o] = f.x;
+    targets[1][o] = f.y;
+    targets[2][o] = f.z;
+  }
 }
 
 __global__ void k_reset(DevStatus* st, int* bmin, int* bmax, int scenes) {
@@ -1409,7 +1411,8 @@ cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t s
   if (dl) {  // positions are final: write them out beside the velocity passes
     cudaEventRecord(dl->committed, st);
     cudaStreamWaitEvent(dl->aux, dl->committed, 0);
-    k_download_field<<<nb, kBlock, 0, dl->aux>>>(a.x, a.slot, dl->targets, a.n, a.status);
+    const int bx = (dl->blocks > 0 && dl->blocks < nb) ? dl->blocks : nb;
+    k_download_field<<<bx, kBlock, 0, dl->aux>>>(a.x, a.slot, dl->targets, a.n, a.status);
     cudaEventRecord(dl->positions_done, dl->aux);
   }
   if (plan.xsph) {

@@ -91,6 +91,11 @@ struct StepDownload {
   cudaEvent_t committed = nullptr;       // recorded on the step's stream
   cudaEvent_t positions_done = nullptr;  // recorded on aux
   float* const* targets = nullptr;       // device array of 6 pointers
+  // Blocks of the position write-out. The host link, not the SMs, bounds
+  // it: a quarter of the SMs' worth of blocks keeps it at the link's rate
+  // while leaving the rest to the velocity passes beside it (a full grid
+  // slowed those passes by as much as the overlap saved).
+  int blocks = 0;
 };
 
 // Enqueues one full timestep on `stream`; with `rec`, also records the

@@ -431,6 +431,9 @@ class Solver {
         return cuda_fail("download stream");
       split_.aux = aux_;
       split_.targets = targets_.p;
+      int sms = 0;
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_);
+      split_.blocks = sms > 4 ? sms / 4 : 1;
     }
     int rc = synchronize();  // targets_host_ may still feed an earlier copy
     if (rc) return rc;
