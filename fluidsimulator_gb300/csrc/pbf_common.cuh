@@ -32,6 +32,7 @@ constexpr int kRadixItems = 8;                      // keys per thread
 constexpr int kRadixTile = kBlock * kRadixItems;    // keys per CTA
 constexpr int kRadixMaxBins = 1 << 11;                // widest digit (11 bits)
 constexpr int kRadixMaxPasses = 4;                  // passes of a u32 key at 8-bit digits
+constexpr int kRadixDigitBlocks = 304;              // k_radix_digits grid (stride over tiles)
 constexpr unsigned kFull = 0xffffffffu;
 
 // Per-scene constants, each computed on the host with the same float
@@ -78,7 +79,7 @@ struct DevStatus {
   int step;       // index within the batch of the step in progress
   int fail_step;  // step index within the batch that failed
   int npass;      // radix passes needed this step
-  int pad0;
+  unsigned epoch; // steps started on this status word (never reset): tags the sort's look-back words
   unsigned long long total_cells;
   unsigned long long need_grid;
   unsigned long long need_nbr;
@@ -105,8 +106,9 @@ struct StepArgs {
   float* rho;
   uint32_t* keys[2];
   int* vals[2];
-  uint32_t* hist;         // (digits) x tiles, digit-major
-  uint32_t* digit_total;  // kRadixMaxPasses x kRadixMaxBins
+  unsigned long long* look;  // tiles x (1 << radix bits) look-back words of the sort pass
+  int* radix_next;           // kRadixMaxPasses tile counters of the sort passes
+  uint32_t* digit_total;     // kRadixMaxPasses x kRadixMaxBins: counts, then starts
   int2* table;
   int* cnt;
   int* depth;             // per warp

@@ -288,7 +288,9 @@ __global__ void __launch_bounds__(kBlock) k_grid_setup(StepArgs a, int radix_bit
   if (failed(a.status)) return;
   DevStatus* st = a.status;
   for (int i = threadIdx.x; i < kRadixMaxPasses * kRadixMaxBins; i += blockDim.x) a.digit_total[i] = 0;
+  if (threadIdx.x < kRadixMaxPasses) a.radix_next[threadIdx.x] = 0;
   if (threadIdx.x != 0) return;
+  st->epoch = st->epoch + 1u;  // look-back words of earlier steps no longer match
   st->step = st->started;
   st->started = st->started + 1;
   st->pairs = 0ull;
@@ -353,105 +355,130 @@ __global__ void __launch_bounds__(kBlock) k_keys(StepArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// Stable LSD radix sort, kBits-bit digits (8 or 11, chosen by the autotuner).
-// Pass p reads keys[p&1] (pass 0: values are the caller indices themselves)
-// and writes keys[(p+1)&1].
+// Stable LSD radix sort, kBits-bit digits (8 or 11, chosen by the autotuner),
+// one kernel per pass. Pass p reads keys[p&1] (pass 0: values are the caller
+// indices themselves) and writes keys[(p+1)&1]. The digit counts of every
+// pass come from one read of the keys (k_radix_digits); each
+// pass then ranks a tile of keys in shared memory and finds where its digits
+// go by a decoupled look-back over the tiles before it: the single-pass
+// prefix scan of Merrill and Garland (2016) applied per digit, as in the
+// "onesweep" radix sort of Adinets and Merrill (2022).
 
+// Look-back words, one per (tile, digit): tag (step epoch and pass) in the
+// high half, then a 2-bit flag and a 30-bit count. A word whose tag is not
+// the current one is not ready.
+constexpr uint32_t kLookAggregate = 1u;  // count = this tile's keys of the digit
+constexpr uint32_t kLookPrefix = 2u;     // count = keys of the digit in tiles 0..this
+constexpr int kLookSpinLimit = 1 << 22;  // then the step fails (FLUID_ERR_CUDA)
+
+__device__ __forceinline__ unsigned long long look_word(uint32_t tag, uint32_t flag, uint32_t count) {
+  return (static_cast<unsigned long long>(tag) << 32) | (static_cast<unsigned long long>(flag) << 30) | count;
+}
+
+__device__ __forceinline__ uint32_t look_tag(const DevStatus* st, int pass) {
+  return (static_cast<uint32_t>(st->epoch) << 2) | static_cast<uint32_t>(pass);
+}
+
+// Digit counts of every pass (digit_total[pass * kBins + d]) from one read
+// of the keys; grid-stride over the radix tiles. At 8-bit digits each warp
+// counts into its own copy (fewer collisions on one counter).
 template <int kBits>
-__global__ void __launch_bounds__(kBlock) k_radix_hist(StepArgs a, int pass) {
-  if (failed(a.status) || pass >= a.status->npass) return;
+__global__ void __launch_bounds__(kBlock) k_radix_digits(StepArgs a) {
+  if (failed(a.status)) return;
   constexpr int kBins = 1 << kBits;
-  constexpr int kCopies = kBits <= 8 ? kBlock / 32 : 1;  // one histogram per warp where they fit
-  __shared__ uint32_t cnt[kCopies][kBins];
+  constexpr int kPasses = (32 + kBits - 1) / kBits < kRadixMaxPasses ? (32 + kBits - 1) / kBits : kRadixMaxPasses;
+  constexpr int kCopies = kBits <= 8 ? kBlock / 32 : 1;
+  const int npass = a.status->npass;
+  if (npass == 0) return;
+  __shared__ uint32_t cnt[kCopies][kPasses][kBins];
+  for (int i = threadIdx.x; i < kCopies * kPasses * kBins; i += kBlock) (&cnt[0][0][0])[i] = 0;
+  __syncthreads();
   const int copy = kCopies > 1 ? (threadIdx.x >> 5) : 0;
-  for (int i = threadIdx.x; i < kCopies * kBins; i += kBlock) (&cnt[0][0])[i] = 0;
-  __syncthreads();
-  const uint32_t* kin = a.keys[pass & 1];
-  const int shift = kBits * pass;
-  const long long base = static_cast<long long>(blockIdx.x) * kRadixTile;
+  const uint32_t* keys = a.keys[0];
+  for (long long base = static_cast<long long>(blockIdx.x) * kRadixTile; base < a.n;
+       base += static_cast<long long>(gridDim.x) * kRadixTile) {
 #pragma unroll
-  for (int r = 0; r < kRadixItems; ++r) {
-    const long long idx = base + r * kBlock + threadIdx.x;
-    if (idx < a.n) atomicAdd(&cnt[copy][(kin[idx] >> shift) & (kBins - 1u)], 1u);
+    for (int r = 0; r < kRadixItems; ++r) {
+      const long long idx = base + r * kBlock + threadIdx.x;
+      if (idx >= a.n) continue;
+      const uint32_t key = keys[idx];
+      for (int p = 0; p < npass && p < kPasses; ++p)
+        atomicAdd(&cnt[copy][p][(key >> (kBits * p)) & (kBins - 1u)], 1u);
+    }
   }
   __syncthreads();
-  for (int d = threadIdx.x; d < kBins; d += kBlock) {
-    uint32_t sum = 0;
+  for (int i = threadIdx.x; i < npass * kBins && i < kPasses * kBins; i += kBlock) {
+    uint32_t v = 0;
 #pragma unroll
-    for (int w = 0; w < kCopies; ++w) sum += cnt[w][d];
-    a.hist[static_cast<long long>(d) * a.tiles + blockIdx.x] = sum;
-    if (sum) atomicAdd(&a.digit_total[pass * kBins + d], sum);
+    for (int c = 0; c < kCopies; ++c) v += (&cnt[c][0][0])[i];
+    if (v) atomicAdd(&a.digit_total[i], v);
   }
 }
 
-// One CTA per digit: exclusive scan of that digit's tile counts plus the
-// number of keys with a smaller digit.
+// Exclusive prefix over the kBins digit counts `tot` into starts[] (shared),
+// by the whole block; ends with a barrier.
 template <int kBits>
-__global__ void __launch_bounds__(kBlock) k_radix_scan(StepArgs a, int pass) {
-  if (failed(a.status) || pass >= a.status->npass) return;
+__device__ __forceinline__ void digit_starts(const uint32_t* __restrict__ tot, uint32_t* starts) {
   constexpr int kBins = 1 << kBits;
+  constexpr int kPer = (kBins + kBlock - 1) / kBlock;  // contiguous digits per thread
   __shared__ uint32_t warp_sums[kBlock / 32];
-  __shared__ uint32_t carry;
-  const int d = blockIdx.x;
+  uint32_t v[kPer];
+  uint32_t sum = 0;
+#pragma unroll
+  for (int k = 0; k < kPer; ++k) {
+    const int d = threadIdx.x * kPer + k;
+    v[k] = d < kBins ? tot[d] : 0u;
+    sum += v[k];
+  }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint32_t below = 0;
-  for (int e = threadIdx.x; e < d; e += kBlock) below += a.digit_total[pass * kBins + e];
-  below = __reduce_add_sync(kFull, below);
-  if (lane == 0) warp_sums[warp] = below;
+  uint32_t inc = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(kFull, inc, o);
+    if (lane >= o) inc += y;
+  }
+  if (lane == 31) warp_sums[warp] = inc;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    uint32_t s = 0;
-    for (int w = 0; w < kBlock / 32; ++w) s += warp_sums[w];
-    carry = s;
+  uint32_t before = inc - sum;
+  for (int w = 0; w < warp; ++w) before += warp_sums[w];
+#pragma unroll
+  for (int k = 0; k < kPer; ++k) {
+    const int d = threadIdx.x * kPer + k;
+    if (d < kBins) starts[d] = before;
+    before += v[k];
   }
   __syncthreads();
-  uint32_t* row = a.hist + static_cast<long long>(d) * a.tiles;
-  for (int chunk = 0; chunk < a.tiles; chunk += kBlock) {
-    const int t = chunk + threadIdx.x;
-    const uint32_t v = (t < a.tiles) ? row[t] : 0u;
-    uint32_t inc = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(kFull, inc, o);
-      if (lane >= o) inc += y;
-    }
-    __syncthreads();
-    if (lane == 31) warp_sums[warp] = inc;
-    __syncthreads();
-    uint32_t wpre = 0, all = 0;
-#pragma unroll
-    for (int w = 0; w < kBlock / 32; ++w) {
-      const uint32_t ws = warp_sums[w];
-      if (w < warp) wpre += ws;
-      all += ws;
-    }
-    const uint32_t c0 = carry;
-    if (t < a.tiles) row[t] = c0 + wpre + inc - v;
-    __syncthreads();
-    if (threadIdx.x == 0) carry = c0 + all;
-  }
 }
 
+// One pass: tiles are taken in launch order from a counter (so every tile a
+// tile waits for has started, and the waits always end), ranked in shared
+// memory, placed by the look-back, and scattered.
 template <int kBits>
-__global__ void __launch_bounds__(kBlock) k_radix_scatter(StepArgs a, int pass) {
-  if (failed(a.status) || pass >= a.status->npass) return;
+__global__ void __launch_bounds__(kBlock) k_radix_onesweep(StepArgs a, int pass) {
   constexpr int kBins = 1 << kBits;
   // Per-warp digit counts; at most 32 * kRadixItems * (kBlock / 32) = 2048
   // per tile, so 16 bits hold them when 32-bit counters would not fit.
   using Count = typename std::conditional<(kBits <= 8), uint32_t, uint16_t>::type;
   __shared__ Count wcnt[kBlock / 32][kBins];
-  __shared__ uint32_t goff[kBins];
+  __shared__ uint32_t goff[kBins];  // digit starts, then this tile's first slot per digit
+  __shared__ int s_tile, s_skip;
+  if (threadIdx.x == 0) {
+    s_skip = (failed(a.status) || pass >= a.status->npass) ? 1 : 0;
+    s_tile = s_skip ? 0 : atomicAdd(&a.radix_next[pass], 1);
+  }
+  __syncthreads();
+  if (s_skip) return;
+  const int tile = s_tile;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int i = threadIdx.x; i < (kBlock / 32) * kBins; i += kBlock) (&wcnt[0][0])[i] = 0;
-  for (int d = threadIdx.x; d < kBins; d += kBlock) goff[d] = a.hist[static_cast<long long>(d) * a.tiles + blockIdx.x];
-  __syncthreads();
+  digit_starts<kBits>(a.digit_total + pass * kBins, goff);
   const uint32_t* kin = a.keys[pass & 1];
   const int* vin = a.vals[pass & 1];
   uint32_t* kout = a.keys[(pass + 1) & 1];
   int* vout = a.vals[(pass + 1) & 1];
   const int shift = kBits * pass;
   // Warp w ranks its contiguous 32*kRadixItems keys in order, 32 at a time.
-  const long long base = static_cast<long long>(blockIdx.x) * kRadixTile + warp * (32 * kRadixItems);
+  const long long base = static_cast<long long>(tile) * kRadixTile + warp * (32 * kRadixItems);
   uint32_t key[kRadixItems];
   int val[kRadixItems];
   int dig[kRadixItems];
@@ -473,7 +500,18 @@ __global__ void __launch_bounds__(kBlock) k_radix_scatter(StepArgs a, int pass) 
     rank[r] = run + before;
   }
   __syncthreads();
-  for (int d = threadIdx.x; d < kBins; d += kBlock) {
+  // Every digit's count goes out first (tile 0's as a prefix), so a tile
+  // behind this one never waits on this tile's own look-back. Thread t owns
+  // digits t, t + kBlock, ... in both loops.
+  constexpr int kOwn = (kBins + kBlock - 1) / kBlock;
+  const uint32_t tag = look_tag(a.status, pass);
+  unsigned long long* look = a.look + static_cast<long long>(tile) * kBins;
+  uint32_t runs[kOwn];
+#pragma unroll
+  for (int k = 0; k < kOwn; ++k) {
+    const int d = threadIdx.x + k * kBlock;
+    runs[k] = 0;
+    if (d >= kBins) continue;
     uint32_t run = 0;
 #pragma unroll
     for (int w = 0; w < kBlock / 32; ++w) {
@@ -481,15 +519,51 @@ __global__ void __launch_bounds__(kBlock) k_radix_scatter(StepArgs a, int pass) 
       wcnt[w][d] = static_cast<Count>(run);
       run += t;
     }
+    runs[k] = run;
+    *(volatile unsigned long long*)(look + d) = look_word(tag, tile == 0 ? kLookPrefix : kLookAggregate, run);
   }
+  bool timed_out = false;
+#pragma unroll
+  for (int k = 0; k < kOwn; ++k) {
+    const int d = threadIdx.x + k * kBlock;
+    if (d >= kBins) continue;
+    uint32_t excl = 0;
+    if (tile > 0) {
+      int j = tile - 1;
+      int spins = 0;
+      for (;;) {
+        const unsigned long long w =
+            *(volatile const unsigned long long*)(a.look + static_cast<long long>(j) * kBins + d);
+        const uint32_t flag = static_cast<uint32_t>(w >> 30) & 3u;
+        if (static_cast<uint32_t>(w >> 32) != tag || flag == 0u) {
+          if (++spins > kLookSpinLimit) {
+            timed_out = true;
+            break;
+          }
+          if (spins > 64) __nanosleep(64);
+          continue;
+        }
+        excl += static_cast<uint32_t>(w) & 0x3fffffffu;
+        if (flag == kLookPrefix) break;
+        --j;  // tile 0 always ends the walk with a prefix
+      }
+      *(volatile unsigned long long*)(look + d) = look_word(tag, kLookPrefix, excl + runs[k]);
+    }
+    goff[d] += excl;
+  }
+  if (timed_out) set_error(a.status, FLUID_ERR_CUDA);
   __syncthreads();
 #pragma unroll
   for (int r = 0; r < kRadixItems; ++r) {
     const int d = dig[r];
     if (d < kBins) {
       const uint32_t pos = goff[d] + wcnt[warp][d] + rank[r];
-      kout[pos] = key[r];
-      vout[pos] = val[r];
+      if (pos < static_cast<uint32_t>(a.n)) {
+        kout[pos] = key[r];
+        vout[pos] = val[r];
+      } else {
+        set_error(a.status, FLUID_ERR_CUDA);
+      }
     }
   }
 }
@@ -1351,21 +1425,21 @@ cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t s
   m.mark(FLUID_KERNEL_GRID);
   k_keys<<<nb, kBlock, 0, st>>>(a);
   m.mark(FLUID_KERNEL_KEYS);
-  for (int pass = 0; pass < plan.radix_passes; ++pass) {
-    if (plan.radix_bits == 11) {
-      k_radix_hist<11><<<a.tiles, kBlock, 0, st>>>(a, pass);
-      m.mark(FLUID_KERNEL_RADIX_HIST);
-      k_radix_scan<11><<<1 << 11, kBlock, 0, st>>>(a, pass);
-      m.mark(FLUID_KERNEL_RADIX_SCAN);
-      k_radix_scatter<11><<<a.tiles, kBlock, 0, st>>>(a, pass);
-    } else {
-      k_radix_hist<8><<<a.tiles, kBlock, 0, st>>>(a, pass);
-      m.mark(FLUID_KERNEL_RADIX_HIST);
-      k_radix_scan<8><<<1 << 8, kBlock, 0, st>>>(a, pass);
-      m.mark(FLUID_KERNEL_RADIX_SCAN);
-      k_radix_scatter<8><<<a.tiles, kBlock, 0, st>>>(a, pass);
+  const int digit_blocks = a.tiles < kRadixDigitBlocks ? a.tiles : kRadixDigitBlocks;
+  if (plan.radix_bits == 11) {
+    k_radix_digits<11><<<digit_blocks, kBlock, 0, st>>>(a);
+    m.mark(FLUID_KERNEL_RADIX_HIST);
+    for (int pass = 0; pass < plan.radix_passes; ++pass) {
+      k_radix_onesweep<11><<<a.tiles, kBlock, 0, st>>>(a, pass);
+      m.mark(FLUID_KERNEL_RADIX_SCATTER);
     }
-    m.mark(FLUID_KERNEL_RADIX_SCATTER);
+  } else {
+    k_radix_digits<8><<<digit_blocks, kBlock, 0, st>>>(a);
+    m.mark(FLUID_KERNEL_RADIX_HIST);
+    for (int pass = 0; pass < plan.radix_passes; ++pass) {
+      k_radix_onesweep<8><<<a.tiles, kBlock, 0, st>>>(a, pass);
+      m.mark(FLUID_KERNEL_RADIX_SCATTER);
+    }
   }
   k_reorder<<<nb, kBlock, 0, st>>>(a);
   m.mark(FLUID_KERNEL_REORDER);

@@ -54,8 +54,9 @@ constexpr size_t kLambda = kRho1 + kI32, kKeys0 = kLambda + kI32, kKeys1 = kKeys
 constexpr size_t kVals0 = kKeys1 + kI32, kVals1 = kVals0 + kI32, kCnt = kVals1 + kI32;
 constexpr size_t kDepth = kCnt + kI32, kWbase = kDepth + up(sizeof(int) * (kMaxWarps + 1));
 constexpr size_t kOvf = kWbase + up(sizeof(long long) * (kMaxWarps + 1));
-constexpr size_t kHist = kOvf + up(sizeof(int) * (kMaxWarps + 1));
-constexpr size_t kDigits = kHist + up(sizeof(uint32_t) * kRadixMaxBins * kMaxTiles);
+constexpr size_t kLook = kOvf + up(sizeof(int) * (kMaxWarps + 1));
+constexpr size_t kRadixNext = kLook + up(sizeof(unsigned long long) * kRadixMaxBins * kMaxTiles);
+constexpr size_t kDigits = kRadixNext + up(sizeof(int) * kRadixMaxPasses);
 constexpr size_t kBmin = kDigits + up(sizeof(uint32_t) * kRadixMaxBins * kRadixMaxPasses);
 constexpr size_t kBmax = kBmin + up(3 * sizeof(int));
 constexpr size_t kGrid = kBmax + up(3 * sizeof(int));
@@ -113,7 +114,8 @@ StepArgs carve(unsigned char* b, int n) {
   a.keys[1] = at<uint32_t>(b, kKeys1);
   a.vals[0] = at<int>(b, kVals0);
   a.vals[1] = at<int>(b, kVals1);
-  a.hist = at<uint32_t>(b, kHist);
+  a.look = at<unsigned long long>(b, kLook);
+  a.radix_next = at<int>(b, kRadixNext);
   a.digit_total = at<uint32_t>(b, kDigits);
   a.table = at<int2>(b, kTable);
   a.cnt = at<int>(b, kCnt);

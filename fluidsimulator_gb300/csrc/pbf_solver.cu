@@ -238,7 +238,7 @@ class Solver {
         return fail(FLUID_ERR_NOT_SUPPORTED, "all scenes must share solver_iterations");
       total += counts[s];
     }
-    if (total > (1ll << 30)) return fail(FLUID_ERR_INVALID_ARGUMENT, "more than 2^30 particles");
+    if (total >= (1ll << 30)) return fail(FLUID_ERR_INVALID_ARGUMENT, "2^30 or more particles");
     cudaSetDevice(device_);
     int rc = synchronize_quiet();
     (void)rc;
@@ -282,7 +282,8 @@ class Solver {
     ok &= depth_.alloc(static_cast<size_t>(warps_) + 1) == cudaSuccess;
     ok &= ovf_.alloc(static_cast<size_t>(warps_) + 1) == cudaSuccess;
     ok &= wbase_.alloc(static_cast<size_t>(warps_) + 1) == cudaSuccess;
-    ok &= hist_.alloc(static_cast<size_t>(tiles_) * kRadixMaxBins) == cudaSuccess;
+    ok &= look_.alloc(static_cast<size_t>(tiles_) * kRadixMaxBins) == cudaSuccess;
+    ok &= radix_next_.alloc(kRadixMaxPasses) == cudaSuccess;
     ok &= digit_total_.alloc(kRadixMaxPasses * kRadixMaxBins) == cudaSuccess;
     ok &= bmin_.alloc(3 * static_cast<size_t>(S_)) == cudaSuccess;
     ok &= bmax_.alloc(3 * static_cast<size_t>(S_)) == cudaSuccess;
@@ -295,6 +296,7 @@ class Solver {
         nbr_.alloc(static_cast<size_t>(nbr_cap_)) != cudaSuccess)
       return fail(FLUID_ERR_OUT_OF_MEMORY, "device allocation failed");
     cudaMemsetAsync(table_.p, 0, table_.n * sizeof(int2), stream_);
+    cudaMemsetAsync(look_.p, 0, look_.n * sizeof(unsigned long long), stream_);  // tag 0: never current
     if (cudaMemcpyAsync(sc_.p, sc_host_.data(), S_ * sizeof(SceneConst), cudaMemcpyHostToDevice, stream_) !=
         cudaSuccess)
       return cuda_fail("upload scene constants");
@@ -495,6 +497,7 @@ class Solver {
       if (st.err != FLUID_ERR_CAPACITY) {
         cudaStreamSynchronize(stream_);
         return fail(st.err, st.err == FLUID_ERR_NONFINITE ? "non-finite predicted position"
+                            : st.err == FLUID_ERR_CUDA    ? "sort look-back did not complete"
                                                           : "particle cells span too large a grid");
       }
       int rc = grow(st.need_grid, st.cursor);
@@ -1018,7 +1021,8 @@ class Solver {
     a.keys[1] = keys_[1].p;
     a.vals[0] = vals_[0].p;
     a.vals[1] = vals_[1].p;
-    a.hist = hist_.p;
+    a.look = look_.p;
+    a.radix_next = radix_next_.p;
     a.digit_total = digit_total_.p;
     a.table = table_.p;
     a.cnt = cnt_.p;
@@ -1144,6 +1148,7 @@ class Solver {
       cap = std::min<long long>(cap, (1ll << 31) - 1);
       if (table_.alloc(static_cast<size_t>(cap)) != cudaSuccess) return fail(FLUID_ERR_OUT_OF_MEMORY, "cell table");
       cudaMemsetAsync(table_.p, 0, table_.n * sizeof(int2), stream_);
+    cudaMemsetAsync(look_.p, 0, look_.n * sizeof(unsigned long long), stream_);  // tag 0: never current
       grid_cap_ = cap;
       changed = true;
     }
@@ -1362,7 +1367,9 @@ class Solver {
   DBuf<float4> x_[2], v_[2], p_[2], v2_, omega_, pl_;
   DBuf<int> slot_[2], vals_[2], cnt_, depth_, ovf_, nbr_, bmin_, bmax_;
   DBuf<float> rho_[2], lambda_;
-  DBuf<uint32_t> keys_[2], hist_, digit_total_;
+  DBuf<uint32_t> keys_[2], digit_total_;
+  DBuf<unsigned long long> look_;
+  DBuf<int> radix_next_;
   DBuf<long long> wbase_;
   DBuf<int2> table_;
   DBuf<GridInfo> grid_;
@@ -1537,7 +1544,7 @@ int fluid_solver_kernel_times(fluid_solver* s, double* ms, int64_t* launches, in
 
 const char* fluid_kernel_name(int kernel) {
   static const char* const names[FLUID_KERNEL_COUNT] = {
-      "k_bounds", "k_grid_setup", "k_keys", "k_radix_hist", "k_radix_scan", "k_radix_scatter",
+      "k_bounds", "k_grid_setup", "k_keys", "k_radix_digits", "k_radix_starts", "k_radix_onesweep",
       "k_reorder", "k_nbr_build", "k_nbr_overflow", "k_lambda", "k_delta",
       "k_commit", "k_xsph", "k_omega", "k_eta"};
   return (kernel >= 0 && kernel < FLUID_KERNEL_COUNT) ? names[kernel] : nullptr;
