@@ -370,6 +370,7 @@ __global__ void __launch_bounds__(kBlock) k_keys(StepArgs a) {
 constexpr uint32_t kLookAggregate = 1u;  // count = this tile's keys of the digit
 constexpr uint32_t kLookPrefix = 2u;     // count = keys of the digit in tiles 0..this
 constexpr int kLookSpinLimit = 1 << 22;  // then the step fails (FLUID_ERR_CUDA)
+constexpr int kLookWindow = 4;           // earlier tiles read per look-back step
 
 __device__ __forceinline__ unsigned long long look_word(uint32_t tag, uint32_t flag, uint32_t count) {
   return (static_cast<unsigned long long>(tag) << 32) | (static_cast<unsigned long long>(flag) << 30) | count;
@@ -529,23 +530,36 @@ __global__ void __launch_bounds__(kBlock) k_radix_onesweep(StepArgs a, int pass)
     if (d >= kBins) continue;
     uint32_t excl = 0;
     if (tile > 0) {
+      // kLookWindow earlier tiles' words read at once, used nearest first
+      // up to the first one not ready yet (polled again) or a prefix.
       int j = tile - 1;
       int spins = 0;
       for (;;) {
-        const unsigned long long w =
-            *(volatile const unsigned long long*)(a.look + static_cast<long long>(j) * kBins + d);
-        const uint32_t flag = static_cast<uint32_t>(w >> 30) & 3u;
-        if (static_cast<uint32_t>(w >> 32) != tag || flag == 0u) {
+        unsigned long long w[kLookWindow];
+#pragma unroll
+        for (int u = 0; u < kLookWindow; ++u)
+          w[u] = (j - u >= 0) ? *(volatile const unsigned long long*)(a.look + static_cast<long long>(j - u) * kBins + d)
+                              : 0ull;
+        int used = 0;
+        bool done = false;
+#pragma unroll
+        for (int u = 0; u < kLookWindow; ++u) {
+          if (used != u || done) break;
+          const uint32_t flag = static_cast<uint32_t>(w[u] >> 30) & 3u;
+          if (static_cast<uint32_t>(w[u] >> 32) != tag || flag == 0u) break;
+          excl += static_cast<uint32_t>(w[u]) & 0x3fffffffu;
+          used = u + 1;
+          done = flag == kLookPrefix;  // tile 0 always ends the walk with a prefix
+        }
+        if (done) break;
+        if (used == 0) {
           if (++spins > kLookSpinLimit) {
             timed_out = true;
             break;
           }
           if (spins > 64) __nanosleep(64);
-          continue;
         }
-        excl += static_cast<uint32_t>(w) & 0x3fffffffu;
-        if (flag == kLookPrefix) break;
-        --j;  // tile 0 always ends the walk with a prefix
+        j -= used;
       }
       *(volatile unsigned long long*)(look + d) = look_word(tag, kLookPrefix, excl + runs[k]);
     }
