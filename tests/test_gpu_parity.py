@@ -392,6 +392,28 @@ def test_sort_width_gives_same_permutation(cuda_lib, oracle_lib, case):
     s.close()
 
 
+@pytest.mark.parametrize("bits", [8, 11])
+def test_sort_across_many_tiles(cuda_lib, oracle_lib, bits):
+    """216,000 particles (106 sort tiles, so every pass chains its look-back
+    across tiles): the permutation of step 1 and the state after three steps
+    (look-back words reused from step to step) equal the oracle's."""
+    sc = scenes.falling_block(60, seed=2)
+    one = oracle_lib.Oracle().run(sc.params, sc.pos, sc.vel, 0.0, 1, dump=True)
+    three = oracle_lib.Oracle().run(sc.params, sc.pos, sc.vel, 0.0, 3)
+    s = Solver(0)
+    s.configure([sc.params], [sc.count])
+    s.set_sort_bits(bits)
+    s.upload(sc.pos, sc.vel)
+    s.step(1)
+    np.testing.assert_array_equal(s.read_debug(_capi.DEBUG_SORTED_ORDER), one["sorted_order"])
+    np.testing.assert_array_equal(s.read_debug(_capi.DEBUG_CELL_KEYS), one["cell_keys"])
+    s.step(2)
+    pos, vel = s.download()
+    s.close()
+    np.testing.assert_array_equal(pos, three["pos"])
+    np.testing.assert_array_equal(vel, three["vel"])
+
+
 @pytest.mark.parametrize("n", [2, 3, 4])
 def test_scorr_exponent_variants_match_oracle(cuda_lib, oracle_lib, n):
     """s_corr with n = 2, 3, 4: the delta pass compiled for that exponent
