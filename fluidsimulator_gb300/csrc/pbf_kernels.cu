@@ -209,21 +209,11 @@ __device__ __forceinline__ const uint32_t* sorted_keys(const StepArgs& a, int np
 // ---------------------------------------------------------------------------
 // Bounds, grid, keys
 
-__global__ void __launch_bounds__(kBlock) k_bounds(StepArgs a) {
-  if (failed(a.status)) return;
-  const int s = blockIdx.x * kBlock + threadIdx.x;
-  int scene = -1;
-  int cx = 0, cy = 0, cz = 0;
-  bool ok = false;
-  if (s < a.n) {
-    const float4 x = a.x_old[s];
-    float4 v = a.v_old[s];
-    scene = __float_as_int(v.w);
-    const SceneConst& c = a.sc[scene];
-    ok = cell_of(c, predict(c, x, v), cx, cy, cz);
-  }
-  // Warp, then block reduction when the block is one scene; mixed blocks
-  // (scene boundaries) fall back to per-warp or per-lane atomics.
+// Adds each thread's predicted cell (ok) of `scene` (< 0: none) to the
+// per-scene bounding box: warp, then block reduction when the block is one
+// scene; mixed blocks (scene boundaries) fall back to per-warp or per-lane
+// atomics. Called by every thread of a kBlock-thread block.
+__device__ __forceinline__ void add_bounds(int* bmin, int* bmax, int scene, bool ok, int cx, int cy, int cz) {
   __shared__ int wmin[kBlock / 32][3], wmax[kBlock / 32][3], wscene[kBlock / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int s0 = __shfl_sync(kFull, scene, 0);
@@ -237,12 +227,12 @@ __global__ void __launch_bounds__(kBlock) k_bounds(StepArgs a) {
     mx[1] = __reduce_max_sync(kFull, ok ? cy : INT_MIN);
     mx[2] = __reduce_max_sync(kFull, ok ? cz : INT_MIN);
   } else if (ok) {
-    atomicMin(&a.bmin[3 * scene + 0], cx);
-    atomicMin(&a.bmin[3 * scene + 1], cy);
-    atomicMin(&a.bmin[3 * scene + 2], cz);
-    atomicMax(&a.bmax[3 * scene + 0], cx);
-    atomicMax(&a.bmax[3 * scene + 1], cy);
-    atomicMax(&a.bmax[3 * scene + 2], cz);
+    atomicMin(&bmin[3 * scene + 0], cx);
+    atomicMin(&bmin[3 * scene + 1], cy);
+    atomicMin(&bmin[3 * scene + 2], cz);
+    atomicMax(&bmax[3 * scene + 0], cx);
+    atomicMax(&bmax[3 * scene + 1], cy);
+    atomicMax(&bmax[3 * scene + 2], cz);
   }
   if (lane == 0) {
     wscene[warp] = (uniform && mn[0] != INT_MAX) ? s0 : -1;
@@ -269,18 +259,34 @@ __global__ void __launch_bounds__(kBlock) k_bounds(StepArgs a) {
         lo = min(lo, wmin[w][d]);
         hi = max(hi, wmax[w][d]);
       }
-      atomicMin(&a.bmin[3 * bs + d], lo);
-      atomicMax(&a.bmax[3 * bs + d], hi);
+      atomicMin(&bmin[3 * bs + d], lo);
+      atomicMax(&bmax[3 * bs + d], hi);
     }
   } else {
     for (int w = 0; w < kBlock / 32; ++w) {
       if (wscene[w] < 0) continue;
       for (int d = 0; d < 3; ++d) {
-        atomicMin(&a.bmin[3 * wscene[w] + d], wmin[w][d]);
-        atomicMax(&a.bmax[3 * wscene[w] + d], wmax[w][d]);
+        atomicMin(&bmin[3 * wscene[w] + d], wmin[w][d]);
+        atomicMax(&bmax[3 * wscene[w] + d], wmax[w][d]);
       }
     }
   }
+}
+
+__global__ void __launch_bounds__(kBlock) k_bounds(StepArgs a) {
+  if (failed(a.status)) return;
+  const int s = blockIdx.x * kBlock + threadIdx.x;
+  int scene = -1;
+  int cx = 0, cy = 0, cz = 0;
+  bool ok = false;
+  if (s < a.n) {
+    const float4 x = a.x_old[s];
+    float4 v = a.v_old[s];
+    scene = __float_as_int(v.w);
+    const SceneConst& c = a.sc[scene];
+    ok = cell_of(c, predict(c, x, v), cx, cy, cz);
+  }
+  add_bounds(a.bmin, a.bmax, scene, ok, cx, cy, cz);
 }
 
 // radix_bits: digit width of the sort (8 or 11), which sets the pass count.
@@ -1297,21 +1303,37 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_eta(StepArgs
 // ---------------------------------------------------------------------------
 // Upload / download / reset.
 
+// Caller-order SoA arrays into slot-order x/v. With bmin (the stateless
+// step over page-locked arrays, whose read of the host link bounds this
+// kernel) it also adds each particle's predicted cell to the bounding box,
+// the work of k_bounds, which that step's graph then leaves out.
 __global__ void __launch_bounds__(kBlock) k_upload(const float* px, const float* py, const float* pz,
                                                    const float* vx, const float* vy, const float* vz,
                                                    float4* x, float4* v, int* slot, float* rho,
-                                                   const SceneConst* sc, int scenes, int n) {
+                                                   const SceneConst* sc, int scenes, int n, int* bmin, int* bmax) {
   const int o = blockIdx.x * kBlock + threadIdx.x;
-  if (o >= n) return;
-  int lo = 0, hi = scenes - 1;  // last scene whose first slot <= o
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (sc[mid].first_slot <= o) lo = mid; else hi = mid - 1;
+  int scene = -1;
+  int cx = 0, cy = 0, cz = 0;
+  bool ok = false;
+  if (o < n) {
+    int lo = 0, hi = scenes - 1;  // last scene whose first slot <= o
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (sc[mid].first_slot <= o) lo = mid; else hi = mid - 1;
+    }
+    const float4 xo = make_float4(px[o], py[o], pz[o], __int_as_float(o));
+    const float4 vo = make_float4(vx[o], vy[o], vz[o], __int_as_float(lo));
+    x[o] = xo;
+    v[o] = vo;
+    slot[o] = o;
+    rho[o] = 0.0f;
+    if (bmin) {
+      float4 vp = vo;
+      scene = lo;
+      ok = cell_of(sc[lo], predict(sc[lo], xo, vp), cx, cy, cz);
+    }
   }
-  x[o] = make_float4(px[o], py[o], pz[o], __int_as_float(o));
-  v[o] = make_float4(vx[o], vy[o], vz[o], __int_as_float(lo));
-  slot[o] = o;
-  rho[o] = 0.0f;
+  if (bmin) add_bounds(bmin, bmax, scene, ok, cx, cy, cz);
 }
 
 __global__ void __launch_bounds__(kBlock) k_download(const float4* x, const float4* v, const int* slot,
@@ -1433,8 +1455,10 @@ cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t s
                          const StepRecord* rec, const StepDownload* dl) {
   const int nb = blocks_for(a.n, kBlock);
   m.start();
-  k_bounds<<<nb, kBlock, 0, st>>>(a);
-  m.mark(FLUID_KERNEL_BOUNDS);
+  if (!(dl && dl->bounds_done)) {
+    k_bounds<<<nb, kBlock, 0, st>>>(a);
+    m.mark(FLUID_KERNEL_BOUNDS);
+  }
   k_grid_setup<<<1, kBlock, 0, st>>>(a, plan.radix_bits);
   m.mark(FLUID_KERNEL_GRID);
   k_keys<<<nb, kBlock, 0, st>>>(a);
@@ -1530,8 +1554,10 @@ cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t s
 
 cudaError_t enqueue_upload(const float* px, const float* py, const float* pz, const float* vx, const float* vy,
                            const float* vz, float4* x, float4* v, int* slot, float* rho, const SceneConst* sc,
-                           int scenes, int n, cudaStream_t st) {
-  if (n > 0) k_upload<<<blocks_for(n, kBlock), kBlock, 0, st>>>(px, py, pz, vx, vy, vz, x, v, slot, rho, sc, scenes, n);
+                           int scenes, int n, cudaStream_t st, int* bmin, int* bmax) {
+  if (n > 0)
+    k_upload<<<blocks_for(n, kBlock), kBlock, 0, st>>>(px, py, pz, vx, vy, vz, x, v, slot, rho, sc, scenes, n, bmin,
+                                                       bmax);
   return cudaGetLastError();
 }
 

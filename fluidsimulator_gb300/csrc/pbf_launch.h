@@ -96,6 +96,9 @@ struct StepDownload {
   // while leaving the rest to the velocity passes beside it (a full grid
   // slowed those passes by as much as the overlap saved).
   int blocks = 0;
+  // The upload already added the predicted cells to the bounding box, so
+  // the step starts at k_grid_setup.
+  bool bounds_done = false;
 };
 
 // Enqueues one full timestep on `stream`; with `rec`, also records the
@@ -105,12 +108,14 @@ cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan,
                          cudaStream_t stream, LaunchMarks& marks,
                          const StepRecord* rec = nullptr, const StepDownload* dl = nullptr);
 
-// Packs caller-order SoA arrays (device) into slot-order x/v of one parity.
+// Packs caller-order SoA arrays (device) into slot-order x/v of one parity;
+// with bmin/bmax it also accumulates the predicted cells' bounding box (what
+// k_bounds does), for a step launched with StepDownload::bounds_done.
 cudaError_t enqueue_upload(const float* px, const float* py, const float* pz,
                            const float* vx, const float* vy, const float* vz,
                            float4* x, float4* v, int* slot, float* rho,
                            const SceneConst* sc, int scenes, int n,
-                           cudaStream_t stream);
+                           cudaStream_t stream, int* bmin = nullptr, int* bmax = nullptr);
 
 // Gathers slot-order x/v of one parity into caller-order SoA arrays (device).
 cudaError_t enqueue_download(const float4* x, const float4* v, const int* slot,

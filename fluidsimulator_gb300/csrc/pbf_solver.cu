@@ -337,17 +337,22 @@ class Solver {
 
   // wait = false leaves the copies in flight on the solver's stream, for a
   // caller whose next work on that stream consumes them (the stateless step).
+  // bounds: for page-locked arrays, the upload kernel also adds the
+  // predicted cells to the bounding box and the next step_download_host
+  // skips k_bounds (the stateless step).
   int upload(const float* px, const float* py, const float* pz, const float* vx, const float* vy,
-             const float* vz, int memory, bool wait = true) {
+             const float* vz, int memory, bool wait = true, bool bounds = false) {
     if (!S_) return fail(FLUID_ERR_STATE, "configure first");
     if (n_ > 0 && (!px || !py || !pz || !vx || !vy || !vz)) return fail(FLUID_ERR_INVALID_ARGUMENT, "null array");
     int rc = synchronize();
     if (rc) return rc;
+    bounds_ready_ = false;
     if (n_ > 0) {
       const float* src[6] = {px, py, pz, vx, vy, vz};
       const float* dev[6];
       if (memory == FLUID_MEMORY_HOST && all_mapped(src, dev)) {
         // page-locked: the upload kernel reads the caller's arrays in place
+        bounds_ready_ = bounds;
       } else if (memory == FLUID_MEMORY_HOST) {
         float* stage = reinterpret_cast<float*>(p_[0].p);  // 4n floats
         float* stage2 = reinterpret_cast<float*>(p_[1].p);
@@ -361,7 +366,8 @@ class Solver {
         for (int k = 0; k < 6; ++k) dev[k] = src[k];
       }
       if (enqueue_upload(dev[0], dev[1], dev[2], dev[3], dev[4], dev[5], x_[parity_].p, v_[parity_].p,
-                         slot_[parity_].p, rho_[parity_].p, sc_.p, S_, n_, stream_) != cudaSuccess)
+                         slot_[parity_].p, rho_[parity_].p, sc_.p, S_, n_, stream_,
+                         bounds_ready_ ? bmin_.p : nullptr, bounds_ready_ ? bmax_.p : nullptr) != cudaSuccess)
         return cuda_fail("upload kernel");
       if (wait && cudaStreamSynchronize(stream_) != cudaSuccess) return cuda_fail("upload");
     }
@@ -1061,21 +1067,29 @@ class Solver {
         int rc = build_graphs();
         if (rc) return rc;
       }
-      if (split_on_ && !split_exec_[par]) {
-        int rc = capture(par, &split_, &split_exec_[par]);
+      // The box from the upload serves only the step right after it; a
+      // step re-run after regrowth recomputes it.
+      cudaGraphExec_t& split = split_exec_[2 * par + (bounds_ready_ ? 1 : 0)];
+      if (split_on_ && !split) {
+        split_.bounds_done = bounds_ready_;
+        int rc = capture(par, &split_, &split);
+        split_.bounds_done = false;
         if (rc) return rc;
       }
-      if (cudaGraphLaunch(split_on_ ? split_exec_[par] : exec_[par], stream_) != cudaSuccess)
+      if (cudaGraphLaunch(split_on_ ? split : exec_[par], stream_) != cudaSuccess)
         return cuda_fail("graph launch");
-      launches_ += launches_per_step_;
+      launches_ += launches_per_step_ - ((split_on_ && bounds_ready_) ? 1 : 0);
     } else {
       LaunchMarks m = marks(par, false);
-      if (enqueue_step(args(par), plan_, stream_, m, nullptr, split_on_ ? &split_ : nullptr) != cudaSuccess)
-        return cuda_fail("launch");
+      split_.bounds_done = split_on_ && bounds_ready_;
+      const cudaError_t e = enqueue_step(args(par), plan_, stream_, m, nullptr, split_on_ ? &split_ : nullptr);
+      split_.bounds_done = false;
+      if (e != cudaSuccess) return cuda_fail("launch");
       launches_ += m.launches;
       launches_per_step_ = m.launches;
       marks_used_[par] = m.next;
     }
+    bounds_ready_ = false;
     ++pending_;
     return FLUID_OK;
   }
@@ -1112,11 +1126,14 @@ class Solver {
   }
 
   void destroy_graphs() {
-    for (auto* set : {&exec_, &split_exec_})
-      for (auto& e : *set) {
-        if (e) cudaGraphExecDestroy(e);
-        e = nullptr;
-      }
+    for (auto& e : exec_) {
+      if (e) cudaGraphExecDestroy(e);
+      e = nullptr;
+    }
+    for (auto& e : split_exec_) {
+      if (e) cudaGraphExecDestroy(e);
+      e = nullptr;
+    }
     graphs_valid_ = false;
   }
   void invalidate_graphs() { destroy_graphs(); }
@@ -1381,7 +1398,8 @@ class Solver {
   bool split_on_ = false;
   DBuf<float*> targets_;          // the write-out's six destination arrays
   float** targets_host_ = nullptr;
-  cudaGraphExec_t split_exec_[2] = {nullptr, nullptr};
+  cudaGraphExec_t split_exec_[4] = {nullptr, nullptr, nullptr, nullptr};  // [2 * parity + box from upload]
+  bool bounds_ready_ = false;  // the last upload added the predicted cells to the bounding box
   long long grid_cap_ = 0, nbr_cap_ = 0;
   StepPlan plan_;
   bool use_graphs_ = true, graphs_valid_ = false, profiling_ = false;
@@ -1664,7 +1682,7 @@ int fluid_gb300_cuda_step(const fluid_params* params, int64_t count, float* px, 
   fgb::Solver& s = cache.s->impl;
   // The host arrays are read by copies left in flight: the step and the
   // download that follow on the same stream finish before this returns.
-  if ((rc = s.upload(px, py, pz, vx, vy, vz, FLUID_MEMORY_HOST, false))) return rc;
+  if ((rc = s.upload(px, py, pz, vx, vy, vz, FLUID_MEMORY_HOST, false, true))) return rc;
   if ((rc = s.set_time(0, *time))) return rc;
   if ((rc = s.step_download_host(px, py, pz, vx, vy, vz))) return rc;
   return s.get_time(0, time);
