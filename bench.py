@@ -19,6 +19,9 @@ steps; `trajectory` reports that regime separately.
           against the FP32 issue rate, from per-launch CUDA events.
   cpu_baseline  the oracle (a CPU restatement of the reference step) on the
           host cores on a bounded sample, rank 0 at N = 1.
+  parity_step1  that sample's first step on the GPU against the oracle
+          (untimed): per-particle neighbour counts and their histogram,
+          positions and velocities, bit for bit.
 
 `--impl reference` times the reference's CPU step (the oracle restatement;
 the reference binary is not buildable on the GPU host) on the host cores.
@@ -352,9 +355,9 @@ def run_ours(args, world, rank, local):
     if not args.no_adjoint:
         differentiable = run_differentiable(args, dev, stream)
 
-    cpu = None
+    cpu = parity = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(sc, budget_s=args.cpu_budget)
+        cpu, parity = cpu_baseline(sc, budget_s=args.cpu_budget)
 
     out = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -373,7 +376,8 @@ def run_ours(args, world, rank, local):
         "roofline": roofline, "pair_roofline": pair_roofline,
         "step_roofline": {"bytes_per_particle_step": ALGO_BYTES_PER_STEP, "frac": round(step_frac, 5)},
         "kernel_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in stage.items() if v[1]},
-        "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches, "trajectory": traj,
+        "cpu_baseline": cpu, "parity_step1": parity, "e2e": e2e, "clocks": clk, "gpu_launches": launches,
+        "trajectory": traj,
         "batched": batched, "differentiable": differentiable, "output": output,
     }
     if world > 1:
@@ -675,10 +679,39 @@ def cpu_baseline(sc, budget_s=20.0, steps=None):
     for _ in range(reps):
         pyoracle.Oracle().run(sample.params, sample.pos, sample.vel, 0.0, 1)
     dt = time.perf_counter() - t0
-    return {"value": round(sample.count * reps / dt, 1), "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{reps} x step 1 of the first {sample.count} particles (whole z-layers) of the 1M scene, "
-                      f"oracle/pbf_oracle.cpp (restatement of core/src/core.cpp:119-615), OpenMP {threads} threads, "
-                      f"{os.uname().machine}"}
+    out = {"value": round(sample.count * reps / dt, 1), "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"{reps} x step 1 of the first {sample.count} particles (whole z-layers) of the 1M scene, "
+                     f"oracle/pbf_oracle.cpp (restatement of core/src/core.cpp:119-615), OpenMP {threads} threads, "
+                     f"{os.uname().machine}"}
+    return out, step1_parity(sample)
+
+
+def step1_parity(sample):
+    """The sample's first step on the GPU against the oracle as checker (an
+    untimed run): neighbour counts per particle and their histogram, and the
+    positions and velocities, bit for bit."""
+    import numpy as np
+
+    from fluidsimulator_gb300 import _capi
+    from fluidsimulator_gb300.solver import Solver
+    from oracle import pyoracle
+
+    ref = pyoracle.Oracle().run(sample.params, sample.pos, sample.vel, 0.0, 1, dump=True)
+    s = Solver(0)
+    s.configure([sample.params], [sample.count])
+    s.upload(sample.pos, sample.vel)
+    s.step(1)
+    counts = s.read_debug(_capi.DEBUG_NEIGHBOR_COUNTS)
+    pos, vel = s.download()
+    s.close()
+    hist_gpu = np.bincount(counts)
+    hist_ref = np.bincount(ref["neighbor_counts"])
+    return {"particles": sample.count, "neighbor_counts_equal": bool(np.array_equal(counts, ref["neighbor_counts"])),
+            "histogram_equal": bool(np.array_equal(hist_gpu, hist_ref)),
+            "neighbors_mean": round(float(counts.mean()), 2), "neighbors_max": int(counts.max()),
+            "positions_equal": bool(np.array_equal(pos, ref["pos"])),
+            "velocities_equal": bool(np.array_equal(vel, ref["vel"])),
+            "max_abs_dx_over_h": float(np.max(np.abs(pos - ref["pos"]))) / float(sample.params.h)}
 
 
 def run_reference(args, world, rank):
