@@ -689,7 +689,8 @@ def cpu_baseline(sc, budget_s=20.0, steps=None):
 def step1_parity(sample):
     """The sample's first step on the GPU against the oracle as checker (an
     untimed run): neighbour counts per particle and their histogram, and the
-    positions and velocities, bit for bit."""
+    positions and velocities, bit for bit; and the GPU's and the CPU FP32
+    step's distance from an FP64 run of the oracle."""
     import numpy as np
 
     from fluidsimulator_gb300 import _capi
@@ -706,7 +707,13 @@ def step1_parity(sample):
     s.close()
     hist_gpu = np.bincount(counts)
     hist_ref = np.bincount(ref["neighbor_counts"])
+    # Error of each FP32 result against an FP64 run of the same step.
+    ref64 = pyoracle.Oracle(np.float64).run(sample.params, sample.pos.astype(np.float64),
+                                            sample.vel.astype(np.float64), 0.0, 1)
+    h = float(sample.params.h)
     return {"particles": sample.count, "neighbor_counts_equal": bool(np.array_equal(counts, ref["neighbor_counts"])),
+            "gpu_max_abs_dx_vs_fp64_over_h": float(np.max(np.abs(pos - ref64["pos"]))) / h,
+            "cpu_fp32_max_abs_dx_vs_fp64_over_h": float(np.max(np.abs(ref["pos"] - ref64["pos"]))) / h,
             "histogram_equal": bool(np.array_equal(hist_gpu, hist_ref)),
             "neighbors_mean": round(float(counts.mean()), 2), "neighbors_max": int(counts.max()),
             "positions_equal": bool(np.array_equal(pos, ref["pos"])),

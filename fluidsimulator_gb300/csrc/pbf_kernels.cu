@@ -930,6 +930,79 @@ struct PosVel {
   float4 x, v;
 };
 
+// Live bits of a list's first kLiveEntries entries at one set of positions
+// (the committed ones): bit k is 1 unless entry k is out of range (r2 >= h2)
+// there. XSPH, which tests every entry at those positions, records them
+// (for_each_neighbor_pair_rec); the vorticity passes at the same positions
+// gather and evaluate only the live ones among those entries
+// (for_each_live_then), the rest as usual.
+constexpr int kLiveEntries = 64;
+
+__device__ __forceinline__ void store_live(uint32_t* live, int n, int i, unsigned long long bits) {
+  live[i] = static_cast<uint32_t>(bits);
+  live[n + i] = static_cast<uint32_t>(bits >> 32);
+}
+
+// for_each_neighbor_pair whose bodies return which entries were within h
+// (body2: bit 0 for a, bit 1 for b; body1: a bool); returns the live bits of
+// the first kLiveEntries entries. Entries past those go through the plain
+// walker.
+template <int kUnroll, typename Load, typename Body2, typename Body1>
+__device__ __forceinline__ unsigned long long for_each_neighbor_pair_rec(const int* __restrict__ list, int n,
+                                                                         Load&& load, Body2&& body2,
+                                                                         Body1&& body1) {
+  static_assert(kUnroll % 2 == 0 && kLiveEntries % kUnroll == 0, "entries are consumed in pairs");
+  using Rec = decltype(load(0));
+  const int head = n < kLiveEntries ? n : kLiveEntries;
+  unsigned long long bits = 0ull;
+  int k = 0;
+  int j[kUnroll];
+  if (kUnroll <= head) {
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) j[u] = __ldcs(list + 32ll * u);
+  }
+  for (; k + kUnroll <= head; k += kUnroll) {
+    Rec r[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) r[u] = load(j[u]);
+    if (k + 2 * kUnroll <= head) {
+#pragma unroll
+      for (int u = 0; u < kUnroll; ++u) j[u] = __ldcs(list + 32ll * (k + kUnroll + u));
+    }
+    unsigned long long got = 0ull;
+#pragma unroll
+    for (int u = 0; u < kUnroll; u += 2) got |= static_cast<unsigned long long>(body2(r[u], r[u + 1])) << u;
+    bits |= got << k;
+  }
+  for (; k + 2 <= head; k += 2) {
+    const Rec ra = load(__ldcs(list + 32ll * k)), rb = load(__ldcs(list + 32ll * (k + 1)));
+    bits |= static_cast<unsigned long long>(body2(ra, rb)) << k;
+  }
+  if (k < head && body1(load(__ldcs(list + 32ll * k)))) bits |= 1ull << k;
+  if (n > kLiveEntries) for_each_neighbor_pair<kUnroll>(list + 32ll * kLiveEntries, n - kLiveEntries, load, body2, body1);
+  return bits;
+}
+
+// The first kLiveEntries entries one at a time, each read from the list and
+// gathered only where its live bit is set; a dead entry reaches the body as
+// `dead`, a record no
+// particle is within h of, which the body rejects exactly as it would the
+// real one (r2 < h2 fails). The remaining entries by for_each_neighbor_pair.
+// Sums accumulate in list order either way.
+template <int kUnroll, typename Load, typename Rec, typename Body2, typename Body1>
+__device__ __forceinline__ void for_each_live_then(const int* __restrict__ list, int n, unsigned long long bits,
+                                                   Load&& load, const Rec dead, Body2&& body2, Body1&& body1) {
+  const int head = n < kLiveEntries ? n : kLiveEntries;
+  for (int k = 0; k < head; ++k) body1(((bits >> k) & 1ull) ? load(__ldcs(list + 32ll * k)) : dead);
+  if (n > kLiveEntries) {
+    if constexpr (kUnroll == 1) {
+      for_each_neighbor<1>(list + 32ll * kLiveEntries, n - kLiveEntries, load, body1);
+    } else {
+      for_each_neighbor_pair<kUnroll>(list + 32ll * kLiveEntries, n - kLiveEntries, load, body2, body1);
+    }
+  }
+}
+
 template <int U>
 __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_lambda(StepArgs a, int in) {
   if (failed(a.status)) return;
@@ -1098,7 +1171,9 @@ __global__ void __launch_bounds__(kMaxBlock) k_commit(StepArgs a, int to_v2, int
 
 // XSPH (core.cpp:423-466): reads v2 (committed) and the committing pass's
 // {x, m / rho} records xr, writes v.
-template <int U>
+// kLiveOut: record the live bits of the committed positions for the
+// vorticity passes (all ones where this scene skips XSPH).
+template <int U, bool kLiveOut>
 __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_xsph(StepArgs a, int rest, const float4* xr) {
   if (failed(a.status)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1109,6 +1184,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_xsph(StepArg
   const float4 vi = vs[i];
   const SceneConst& c = a.sc[__float_as_int(vi.w)];
   float vx = vi.x, vy = vi.y, vz = vi.z;
+  unsigned long long bits = ~0ull;
   if (c.xsph_on) {
     const int n = a.cnt[i];
     const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
@@ -1124,16 +1200,26 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_xsph(StepArg
         sy += (r.v.y - vi.y) * W * inv_rho_j;
         sz += (r.v.z - vi.z) * W * inv_rho_j;
       }
+      return r2 < h2;
     };
     if constexpr (U == 1) {
-      for_each_neighbor<1>(list, n, load, one);
+      if constexpr (kLiveOut) {
+        bits = 0ull;
+        int k = 0;
+        for_each_neighbor<1>(list, n, load, [&](const PosVel r) {
+          if (one(r) && k < kLiveEntries) bits |= 1ull << k;
+          ++k;
+        });
+      } else {
+        for_each_neighbor<1>(list, n, load, one);
+      }
     } else {
       // Two entries at a time, as one() on a then on b (paired arithmetic).
       const float2 px = f2(xi.x), py = f2(xi.y), pz = f2(xi.z), nz = f2(c.neg_zero);
-      auto two = [&](const PosVel ra, const PosVel rb) {
+      auto two = [&](const PosVel ra, const PosVel rb) -> unsigned {
         const PairGeom g = pair_geom(px, py, pz, ra.x, rb.x, nz);
         const bool oka = g.r2.x < h2, okb = g.r2.y < h2;
-        if (!oka && !okb) return;
+        if (!oka && !okb) return 0u;
         const float2 w = poly6_pair(c, g.r2, nz);
         const float2 ir = make_float2(ra.x.w, rb.x.w);
         const float2 tx = pmul(pmul(psub(make_float2(ra.v.x, rb.v.x), f2(vi.x)), w, nz), ir, nz);
@@ -1149,19 +1235,24 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_xsph(StepArg
           sy += ty.y;
           sz += tz.y;
         }
+        return (oka ? 1u : 0u) | (okb ? 2u : 0u);
       };
-      for_each_neighbor_pair<U>(list, n, load, two, one);
+      if constexpr (kLiveOut) bits = for_each_neighbor_pair_rec<U>(list, n, load, two, one);
+      else for_each_neighbor_pair<U>(list, n, load, two, one);
     }
     vx += c.visc_c * sx;
     vy += c.visc_c * sy;
     vz += c.visc_c * sz;
   }
+  if (kLiveOut) store_live(a.live, a.n, i, bits);
   if (rest && c.rest_on) restitution(c, xi.x, xi.y, xi.z, vx, vy, vz);
   a.v[i] = make_float4(vx, vy, vz, vi.w);
 }
 
-// Vorticity omega and |omega| (core.cpp:472-508).
-template <int U>
+// Vorticity omega and |omega| (core.cpp:472-508). kLive: 1 = only the live
+// ones among the first entries (live bits from XSPH, same positions); 2 =
+// record the live bits for the eta pass (no XSPH this step).
+template <int U, int kLive>
 __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_omega(StepArgs a) {
   if (failed(a.status)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1172,6 +1263,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_omega(StepAr
   const float4 vi = vs[i];
   const SceneConst& c = a.sc[__float_as_int(vi.w)];
   float ox = 0.0f, oy = 0.0f, oz = 0.0f;
+  unsigned long long bits = ~0ull;
   if (c.vort_on) {
     const int n = a.cnt[i];
     const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
@@ -1188,45 +1280,59 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_omega(StepAr
         oy += uz * gx - ux * gz;
         oz += ux * gy - uy * gx;
       }
+      return r2 < h2;
     };
-    if constexpr (U == 1) {
-      for_each_neighbor<1>(list, n, load, one);
+    // Two entries at a time, as one() on a then on b (paired arithmetic).
+    const float2 px = f2(xi.x), py = f2(xi.y), pz = f2(xi.z), nz = f2(c.neg_zero);
+    auto two = [&](const PosVel ra, const PosVel rb) -> unsigned {
+      const PairGeom g = pair_geom(px, py, pz, ra.x, rb.x, nz);
+      const bool oka = g.r2.x < h2, okb = g.r2.y < h2;
+      if (!oka && !okb) return 0u;
+      const float2 gf = spiky_pair(c, g.r2, nz);
+      const float2 gx = pmul(gf, g.dx, nz), gy = pmul(gf, g.dy, nz), gz = pmul(gf, g.dz, nz);
+      const float2 ux = psub(make_float2(ra.v.x, rb.v.x), f2(vi.x));
+      const float2 uy = psub(make_float2(ra.v.y, rb.v.y), f2(vi.y));
+      const float2 uz = psub(make_float2(ra.v.z, rb.v.z), f2(vi.z));
+      const float2 cx = psub(pmul(uy, gz, nz), pmul(uz, gy, nz));
+      const float2 cy = psub(pmul(uz, gx, nz), pmul(ux, gz, nz));
+      const float2 cz = psub(pmul(ux, gy, nz), pmul(uy, gx, nz));
+      if (oka) {
+        ox += cx.x;
+        oy += cy.x;
+        oz += cz.x;
+      }
+      if (okb) {
+        ox += cx.y;
+        oy += cy.y;
+        oz += cz.y;
+      }
+      return (oka ? 1u : 0u) | (okb ? 2u : 0u);
+    };
+    if constexpr (kLive == 1) {
+      const PosVel dead{make_float4(INFINITY, xi.y, xi.z, 0.0f), make_float4(0.0f, 0.0f, 0.0f, 0.0f)};
+      for_each_live_then<U>(list, n, static_cast<unsigned long long>(a.live[i]) |
+                                         (static_cast<unsigned long long>(a.live[a.n + i]) << 32),
+                            load, dead, two, one);
+    } else if constexpr (U == 1) {
+      bits = 0ull;
+      int k = 0;
+      for_each_neighbor<1>(list, n, load, [&](const PosVel r) {
+        if (one(r) && k < kLiveEntries) bits |= 1ull << k;
+        ++k;
+      });
     } else {
-      // Two entries at a time, as one() on a then on b (paired arithmetic).
-      const float2 px = f2(xi.x), py = f2(xi.y), pz = f2(xi.z), nz = f2(c.neg_zero);
-      auto two = [&](const PosVel ra, const PosVel rb) {
-        const PairGeom g = pair_geom(px, py, pz, ra.x, rb.x, nz);
-        const bool oka = g.r2.x < h2, okb = g.r2.y < h2;
-        if (!oka && !okb) return;
-        const float2 gf = spiky_pair(c, g.r2, nz);
-        const float2 gx = pmul(gf, g.dx, nz), gy = pmul(gf, g.dy, nz), gz = pmul(gf, g.dz, nz);
-        const float2 ux = psub(make_float2(ra.v.x, rb.v.x), f2(vi.x));
-        const float2 uy = psub(make_float2(ra.v.y, rb.v.y), f2(vi.y));
-        const float2 uz = psub(make_float2(ra.v.z, rb.v.z), f2(vi.z));
-        const float2 cx = psub(pmul(uy, gz, nz), pmul(uz, gy, nz));
-        const float2 cy = psub(pmul(uz, gx, nz), pmul(ux, gz, nz));
-        const float2 cz = psub(pmul(ux, gy, nz), pmul(uy, gx, nz));
-        if (oka) {
-          ox += cx.x;
-          oy += cy.x;
-          oz += cz.x;
-        }
-        if (okb) {
-          ox += cx.y;
-          oy += cy.y;
-          oz += cz.y;
-        }
-      };
-      for_each_neighbor_pair<U>(list, n, load, two, one);
+      bits = for_each_neighbor_pair_rec<U>(list, n, load, two, one);
     }
   }
+  if (kLive == 2) store_live(a.live, a.n, i, bits);
   const float mag = sqrtf(ox * ox + oy * oy + oz * oz);
   a.omega[i] = make_float4(ox, oy, oz, mag);
   a.pl[i] = make_float4(xi.x, xi.y, xi.z, mag);  // the record k_eta gathers per neighbour
 }
 
 // Eta, confinement force, velocity update (core.cpp:512-570) and plane
-// restitution (core.cpp:573-612).
+// restitution (core.cpp:573-612); only the live ones among the first
+// entries (live bits of these positions from XSPH or omega).
 template <int U>
 __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_eta(StepArgs a, int rest) {
   if (failed(a.status)) return;
@@ -1254,43 +1360,42 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_eta(StepArgs
         ez += coeff * (gf * dz);
       }
     };
-    if constexpr (U == 1) {
-      for_each_neighbor<1>(list, n, load, one);
-    } else {
-      // Two entries at a time, as one() on a then on b (paired arithmetic).
-      const float2 px = f2(xi.x), py = f2(xi.y), pz = f2(xi.z), nz = f2(c.neg_zero);
-      auto two = [&](const float4 ra, const float4 rb) {
-        const PairGeom g = pair_geom(px, py, pz, ra, rb, nz);
-        const bool oka = g.r2.x < h2, okb = g.r2.y < h2;
-        if (!oka && !okb) return;
-        const float2 gf = spiky_pair(c, g.r2, nz);
-        const float2 coeff = psub(make_float2(ra.w, rb.w), f2(oi.w));
-        const float2 tx = pmul(coeff, pmul(gf, g.dx, nz), nz);
-        const float2 ty = pmul(coeff, pmul(gf, g.dy, nz), nz);
-        const float2 tz = pmul(coeff, pmul(gf, g.dz, nz), nz);
-        if (oka) {
-          ex += tx.x;
-          ey += ty.x;
-          ez += tz.x;
-        }
-        if (okb) {
-          ex += tx.y;
-          ey += ty.y;
-          ez += tz.y;
-        }
-      };
-      for_each_neighbor_pair<U>(list, n, load, two, one);
-    }
+    // Two entries at a time, as one() on a then on b (paired arithmetic).
+    const float2 px = f2(xi.x), py = f2(xi.y), pz = f2(xi.z), nz = f2(c.neg_zero);
+    auto two = [&](const float4 ra, const float4 rb) {
+      const PairGeom g = pair_geom(px, py, pz, ra, rb, nz);
+      const bool oka = g.r2.x < h2, okb = g.r2.y < h2;
+      if (!oka && !okb) return;
+      const float2 gf = spiky_pair(c, g.r2, nz);
+      const float2 coeff = psub(make_float2(ra.w, rb.w), f2(oi.w));
+      const float2 tx = pmul(coeff, pmul(gf, g.dx, nz), nz);
+      const float2 ty = pmul(coeff, pmul(gf, g.dy, nz), nz);
+      const float2 tz = pmul(coeff, pmul(gf, g.dz, nz), nz);
+      if (oka) {
+        ex += tx.x;
+        ey += ty.x;
+        ez += tz.x;
+      }
+      if (okb) {
+        ex += tx.y;
+        ey += ty.y;
+        ez += tz.y;
+      }
+    };
+    const float4 dead = make_float4(INFINITY, xi.y, xi.z, 0.0f);
+    for_each_live_then<U>(list, n, static_cast<unsigned long long>(a.live[i]) |
+                                       (static_cast<unsigned long long>(a.live[a.n + i]) << 32),
+                          load, dead, two, one);
     const float len = sqrtf(ex * ex + ey * ey + ez * ez);
-    float nx = 0.0f, ny = 0.0f, nz = 0.0f;
+    float nx = 0.0f, ny = 0.0f, nz2 = 0.0f;
     if (len > c.vort_norm_eps) {
       const float inv = 1.0f / len;
       nx = ex * inv;
       ny = ey * inv;
-      nz = ez * inv;
+      nz2 = ez * inv;
     }
-    const float fx = c.vort_eps * (ny * oi.z - nz * oi.y);
-    const float fy = c.vort_eps * (nz * oi.x - nx * oi.z);
+    const float fx = c.vort_eps * (ny * oi.z - nz2 * oi.y);
+    const float fy = c.vort_eps * (nz2 * oi.x - nx * oi.z);
     const float fz = c.vort_eps * (nx * oi.y - ny * oi.x);
     v.x += c.dt * fx;
     v.y += c.dt * fy;
@@ -1425,6 +1530,26 @@ void launch_delta(const StepPlan& plan, int grid, int block, cudaStream_t st, co
   }
 }
 
+template <bool kLiveOut>
+void launch_xsph(int u, int grid, int block, cudaStream_t st, const StepArgs& a, int rest, const float4* xr) {
+  switch (u) {
+    case 1: k_xsph<1, kLiveOut><<<grid, block, 0, st>>>(a, rest, xr); break;
+    case 2: k_xsph<2, kLiveOut><<<grid, block, 0, st>>>(a, rest, xr); break;
+    case 8: k_xsph<8, kLiveOut><<<grid, block, 0, st>>>(a, rest, xr); break;
+    default: k_xsph<4, kLiveOut><<<grid, block, 0, st>>>(a, rest, xr); break;
+  }
+}
+
+template <int kLive>
+void launch_omega(int u, int grid, int block, cudaStream_t st, const StepArgs& a) {
+  switch (u) {
+    case 1: k_omega<1, kLive><<<grid, block, 0, st>>>(a); break;
+    case 2: k_omega<2, kLive><<<grid, block, 0, st>>>(a); break;
+    case 8: k_omega<8, kLive><<<grid, block, 0, st>>>(a); break;
+    default: k_omega<4, kLive><<<grid, block, 0, st>>>(a); break;
+  }
+}
+
 }  // namespace
 
 void LaunchMarks::start() {
@@ -1531,13 +1656,17 @@ cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t s
     const int b = plan.block[FLUID_KERNEL_XSPH];
     // The committing pass left {x, m / rho} in the p buffer it did not use.
     const float4* xr = a.p[plan.iterations == 0 ? 1 : (plan.iterations & 1)];
-    FGB_DISPATCH_UNROLL(plan.unroll[FLUID_KERNEL_XSPH], k_xsph, blocks_for(a.n, b), b, st, a,
-                        (!plan.vorticity && plan.restitution) ? 1 : 0, xr);
+    const int rest = (!plan.vorticity && plan.restitution) ? 1 : 0;
+    if (plan.vorticity) launch_xsph<true>(plan.unroll[FLUID_KERNEL_XSPH], blocks_for(a.n, b), b, st, a, rest, xr);
+    else launch_xsph<false>(plan.unroll[FLUID_KERNEL_XSPH], blocks_for(a.n, b), b, st, a, rest, xr);
     m.mark(FLUID_KERNEL_XSPH);
   }
   if (plan.vorticity) {
     const int bo = plan.block[FLUID_KERNEL_OMEGA];
-    FGB_DISPATCH_UNROLL(plan.unroll[FLUID_KERNEL_OMEGA], k_omega, blocks_for(a.n, bo), bo, st, a);
+    // Live bits of the committed positions: from XSPH when it ran, else
+    // recorded here; the eta pass reads them.
+    if (plan.xsph) launch_omega<1>(plan.unroll[FLUID_KERNEL_OMEGA], blocks_for(a.n, bo), bo, st, a);
+    else launch_omega<2>(plan.unroll[FLUID_KERNEL_OMEGA], blocks_for(a.n, bo), bo, st, a);
     m.mark(FLUID_KERNEL_OMEGA);
     if (rec && rec->omega) cudaMemcpyAsync(rec->omega, a.omega, n4, cudaMemcpyDeviceToDevice, st);
     const int be = plan.block[FLUID_KERNEL_ETA];

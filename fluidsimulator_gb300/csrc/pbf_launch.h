@@ -20,8 +20,9 @@ struct StepPlan {
   int radix_bits = 8;     // digit width of the sort: 8 or 11
   int scorr_pow = 0;      // s_corr exponent shared by every s_corr scene (2-4), else 0
   // Per-kernel launch shape (indexed by FLUID_KERNEL_*), chosen by the
-  // autotuner: neighbour entries fetched ahead (1, 2, 4, 8) in the list
-  // passes, and threads per block (128, 256, 512) for the neighbour kernels.
+  // autotuner: neighbour entries fetched ahead (2, 4, 8; 1 when set
+  // explicitly) in the list passes, and threads per block (128, 256, 512)
+  // for the neighbour kernels.
   int unroll[FLUID_KERNEL_COUNT];
   int block[FLUID_KERNEL_COUNT];
   StepPlan() {

@@ -49,7 +49,8 @@ constexpr size_t kI32 = up(sizeof(int) * kMaxN);
 constexpr size_t kX0 = 0, kX1 = kX0 + kF4, kV0 = kX1 + kF4, kV1 = kV0 + kF4;
 constexpr size_t kP0 = kV1 + kF4, kP1 = kP0 + kF4, kV2 = kP1 + kF4, kOmega = kV2 + kF4;
 constexpr size_t kPl = kOmega + kF4;
-constexpr size_t kSlot0 = kPl + kF4, kSlot1 = kSlot0 + kI32, kRho0 = kSlot1 + kI32, kRho1 = kRho0 + kI32;
+constexpr size_t kLive = kPl + kF4;
+constexpr size_t kSlot0 = kLive + up(2 * sizeof(uint32_t) * kMaxN), kSlot1 = kSlot0 + kI32, kRho0 = kSlot1 + kI32, kRho1 = kRho0 + kI32;
 constexpr size_t kLambda = kRho1 + kI32, kKeys0 = kLambda + kI32, kKeys1 = kKeys0 + kI32;
 constexpr size_t kVals0 = kKeys1 + kI32, kVals1 = kVals0 + kI32, kCnt = kVals1 + kI32;
 constexpr size_t kDepth = kCnt + kI32, kWbase = kDepth + up(sizeof(int) * (kMaxWarps + 1));
@@ -108,6 +109,7 @@ StepArgs carve(unsigned char* b, int n) {
   a.p[1] = at<float4>(b, kP1);
   a.omega = at<float4>(b, kOmega);
   a.pl = at<float4>(b, kPl);
+  a.live = at<uint32_t>(b, kLive);
   a.lambda = at<float>(b, kLambda);
   a.rho = at<float>(b, kRho1);
   a.keys[0] = at<uint32_t>(b, kKeys0);

@@ -238,11 +238,15 @@ int fluid_solver_kernel_times(fluid_solver* solver, double* ms_out,
 /*
  * Autotuner (no reference counterpart). Times each tunable kernel (the
  * neighbour-list passes and the list build) under every launch shape --
- * neighbour entries fetched ahead in {1, 2, 4, 8}, threads per block in
- * {128, 256, 512} -- over `trials` discarded steps of the current state, and
- * keeps the fastest shape per kernel; then times the cell-key sort with 8-
- * and 11-bit digits and keeps the faster width. The state and time are not
- * advanced. Every choice computes identical results; only speed differs.
+ * neighbour entries fetched ahead in {2, 4, 8}, threads per block in
+ * {128, 256, 512} -- over `trials` discarded steps of the current state. It
+ * keeps the default shape (4, 256) unless another is at least 2 % faster,
+ * and else the fastest, per kernel. It then times the cell-key sort with 8-
+ * and 11-bit digits and keeps the faster width. One entry ahead (the
+ * single-entry walker) is left out of the sweep: where all lists are short
+ * it can win narrowly and then lose by far once they grow; set it with
+ * fluid_solver_set_tuning. The state and time are not advanced. Every choice
+ * computes identical results; only speed differs.
  */
 int fluid_solver_autotune(fluid_solver* solver, int32_t trials);
 

@@ -334,6 +334,7 @@ def test_autotune_keeps_state_and_results(cuda_lib, oracle_lib):
     np.testing.assert_array_equal(before[1], after[1])
     assert s.time() == t0 and s.stats()["steps"] == steps0
     assert set(shapes) >= {"k_delta", "k_lambda"}
+    assert all(v["unroll"] in (2, 4, 8) for v in shapes.values())  # one ahead only when set
     s.step(10)
     ref = oracle_lib.Oracle().run(sc.params, sc.pos, sc.vel, 0.0, 30)
     got = s.download()
@@ -561,6 +562,52 @@ def test_per_plane_friction_read_per_scene(cuda_lib, oracle_lib):
         np.testing.assert_array_equal(pos[:, off:off + sc.count], ref["pos"])
         np.testing.assert_array_equal(vel[:, off:off + sc.count], ref["vel"])
         off += sc.count
+
+
+def test_live_bits_with_mixed_scene_flags(cuda_lib, oracle_lib):
+    """Scenes with XSPH and vorticity, vorticity only, and XSPH only in one
+    solver: the vorticity passes skip the entries XSPH found out of range
+    only where XSPH ran (the others' live bits are all set), bit-exact."""
+    scs = []
+    for k, (xs, vo) in enumerate(((1, 1), (0, 1), (1, 0))):
+        sc = scenes.dam_break(7, seed=60 + k, flags=True)
+        sc.params.enable_xsph, sc.params.enable_vorticity = xs, vo
+        scs.append(sc)
+    s = Solver(0)
+    s.configure([sc.params for sc in scs], [sc.count for sc in scs])
+    s.upload(np.concatenate([sc.pos for sc in scs], axis=1), np.concatenate([sc.vel for sc in scs], axis=1))
+    s.step(25)
+    pos, vel = s.download()
+    s.close()
+    off = 0
+    for sc in scs:
+        ref = oracle_lib.Oracle().run(sc.params, sc.pos, sc.vel, 0.0, 25)
+        np.testing.assert_array_equal(pos[:, off:off + sc.count], ref["pos"])
+        np.testing.assert_array_equal(vel[:, off:off + sc.count], ref["vel"])
+        off += sc.count
+
+
+@pytest.mark.parametrize("unroll", [1, 2, 4, 8])
+def test_lists_longer_than_the_live_bit_head(cuda_lib, oracle_lib, unroll):
+    """A dense lattice (spacing 0.03 at h = 0.1, ~150 neighbours): every
+    list runs past the 64 entries that carry live bits, so the XSPH and
+    vorticity passes go through both halves of their walkers."""
+    p = scenes.base_params(0.03, 0.1)
+    scenes.init_planes(p, 1.0, 1.0, 1.0)
+    scenes.all_flags(p, 0.1)
+    pos = scenes.jitter(scenes.init_block(10, 10, 10, (0.2, 0.2, 0.2), 0.03), 5e-4, 8)
+    sc = scenes.Scene("dense_block", p, pos, np.zeros_like(pos), steps=1)
+    ref = oracle_lib.Oracle().run(sc.params, sc.pos, sc.vel, 0.0, 1, dump=True)
+    assert ref["neighbor_counts"].mean() > 100
+    s = Solver(0)
+    s.configure([sc.params], [sc.count])
+    s.set_tuning({k: {"unroll": unroll, "block": 128} for k in _capi.TUNABLE})
+    s.upload(sc.pos, sc.vel)
+    s.step(1)
+    got_pos, got_vel = s.download()
+    s.close()
+    np.testing.assert_array_equal(got_pos, ref["pos"])
+    np.testing.assert_array_equal(got_vel, ref["vel"])
 
 
 def test_all_pairs_lists_match_oracle(cuda_lib, oracle_lib):
