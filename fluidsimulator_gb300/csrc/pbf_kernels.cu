@@ -984,10 +984,10 @@ __device__ __forceinline__ unsigned long long for_each_neighbor_pair_rec(const i
 }
 
 // The first kLiveEntries entries one at a time, each read from the list and
-// gathered only where its live bit is set; a dead entry reaches the body as
-// `dead`, a record no
-// particle is within h of, which the body rejects exactly as it would the
-// real one (r2 < h2 fails). The remaining entries by for_each_neighbor_pair.
+// gathered only where its live bit is set (a dead entry costs no memory
+// access); a dead entry reaches the body as `dead`, a record no particle is
+// within h of, which the body rejects exactly as it would the real one
+// (r2 < h2 fails). The remaining entries go through for_each_neighbor_pair.
 // Sums accumulate in list order either way.
 template <int kUnroll, typename Load, typename Rec, typename Body2, typename Body1>
 __device__ __forceinline__ void for_each_live_then(const int* __restrict__ list, int n, unsigned long long bits,
