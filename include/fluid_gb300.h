@@ -125,7 +125,7 @@ int fluid_gb300_cuda_step(const fluid_params* params, int64_t count,
  * and the call returns when it is done.
  *
  * All scratch lives in one fixed device array inside this library (about
- * 7.5 MiB, held on every GPU that loads the library until the process
+ * 7.6 MiB, held on every GPU that loads the library until the process
  * exits). Limits: count <= FLUID_NOALLOC_MAX_PARTICLES, at most
  * FLUID_NOALLOC_MAX_NEIGHBOR_SLOTS neighbour-list entries (32-wide slices)
  * and FLUID_NOALLOC_MAX_CELLS grid cells per step; beyond any of them the
