@@ -47,6 +47,7 @@ int main(int argc, char** argv) {
   p.external_forces.y = cp.external_force[1];
   p.external_forces.z = cp.external_force[2];
   for (int q = 0; q < cp.plane_count; ++q) p.planes.add(cp.plane_nx[q], cp.plane_ny[q], cp.plane_nz[q], cp.plane_d[q]);
+  if (cp.plane_friction_per_plane) p.plane_friction_each.assign(cp.plane_friction_each, cp.plane_friction_each + cp.plane_count);
 
   int count = 0;
   const char* err = nullptr;

@@ -57,6 +57,16 @@ def test_host_interface_builds(cuda_lib, tmp_path):
     assert os.path.exists(exe)
 
 
+def test_params_per_plane_friction_to_c(cuda_lib, tmp_path):
+    """Params::plane_friction_each maps to the C struct's per-plane fields;
+    a list that does not match the planes is rejected."""
+    exe = str(tmp_path / "params_to_c_main")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"), "-I", HOST,
+                    os.path.join(ROOT, "tests", "cpp", "params_to_c_main.cpp"), "-L", LIB_DIR, "-lfluid_gb300",
+                    f"-Wl,-rpath,{LIB_DIR}", "-o", exe], check=True)
+    assert subprocess.run([exe]).returncode == 0
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("mode", ["cuda_step", "solver"])
 def test_host_interface_matches_golden(cuda_lib, tmp_path, mode):
