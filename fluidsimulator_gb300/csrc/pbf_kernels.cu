@@ -993,7 +993,22 @@ template <int kUnroll, typename Load, typename Rec, typename Body2, typename Bod
 __device__ __forceinline__ void for_each_live_then(const int* __restrict__ list, int n, unsigned long long bits,
                                                    Load&& load, const Rec dead, Body2&& body2, Body1&& body1) {
   const int head = n < kLiveEntries ? n : kLiveEntries;
-  for (int k = 0; k < head; ++k) body1(((bits >> k) & 1ull) ? load(__ldcs(list + 32ll * k)) : dead);
+  unsigned long long m = head < kLiveEntries ? bits & ((1ull << head) - 1ull) : bits;
+  if (m) {
+    // Live entries only, in order, the next one's record loaded while the
+    // current one is used.
+    int k = __ffsll(static_cast<long long>(m)) - 1;
+    m &= m - 1ull;
+    auto r = load(__ldcs(list + 32ll * k));
+    while (m) {
+      const int kn = __ffsll(static_cast<long long>(m)) - 1;
+      m &= m - 1ull;
+      const auto rn = load(__ldcs(list + 32ll * kn));
+      body1(r);
+      r = rn;
+    }
+    body1(r);
+  }
   if (n > kLiveEntries) {
     if constexpr (kUnroll == 1) {
       for_each_neighbor<1>(list + 32ll * kLiveEntries, n - kLiveEntries, load, body1);
