@@ -102,7 +102,7 @@ struct StepArgs {
   float4* p[2];
   float4* omega;
   float4* pl;              // {p.xyz, lambda}, written by the lambda pass
-  uint32_t* live;          // 2 x n: live bits of each list's first 64 entries at the committed positions
+  uint32_t* live;          // 2 x n: live bits of each list's first 64 entries at one set of positions
   float* lambda;
   float* rho;
   uint32_t* keys[2];

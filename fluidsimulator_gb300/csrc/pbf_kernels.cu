@@ -721,12 +721,13 @@ struct LambdaAcc {
   // Entries a and b (in list order) relative to p, each added only when
   // r2 < h2: the same operations as the membership test plus add() on a,
   // then on b, with the per-entry terms formed in paired arithmetic.
-  __device__ __forceinline__ void add_pair(const SceneConst& c, const float2 px, const float2 py, const float2 pz,
-                                           const float4 qa, const float4 qb) {
+  // Returns which of a (bit 0) and b (bit 1) were within h.
+  __device__ __forceinline__ unsigned add_pair(const SceneConst& c, const float2 px, const float2 py,
+                                               const float2 pz, const float4 qa, const float4 qb) {
     const float2 nz = f2(c.neg_zero);
     const PairGeom g = pair_geom(px, py, pz, qa, qb, nz);
     const bool oka = g.r2.x < c.h2, okb = g.r2.y < c.h2;
-    if (!oka && !okb) return;
+    if (!oka && !okb) return 0u;
     const float2 w = poly6_pair(c, g.r2, nz);
     const float2 gf = spiky_pair(c, g.r2, nz);
     const float2 gx = pmul(gf, g.dx, nz), gy = pmul(gf, g.dy, nz), gz = pmul(gf, g.dz, nz);
@@ -747,6 +748,7 @@ struct LambdaAcc {
       gsz += gz.y;
       sum_g2 += t.y;
     }
+    return (oka ? 1u : 0u) | (okb ? 2u : 0u);
   }
 };
 
@@ -1018,7 +1020,10 @@ __device__ __forceinline__ void for_each_live_then(const int* __restrict__ list,
   }
 }
 
-template <int U>
+// kLiveOut: record the live bits of these positions for the delta pass
+// (iterations after the first; the first runs at the positions the lists
+// were built from, where every entry is live).
+template <int U, bool kLiveOut>
 __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_lambda(StepArgs a, int in) {
   if (failed(a.status)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1034,14 +1039,26 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_lambda(StepA
     const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
     const float r2 = dist2(dx, dy, dz);
     if (r2 < h2) acc.add(c, dx, dy, dz, r2);
+    return r2 < h2;
   };
   auto load = [&](int j) { return __ldg(pos + j); };
   if constexpr (U == 1) {
-    for_each_neighbor<1>(list, n, load, one);
+    if constexpr (kLiveOut) {
+      unsigned long long bits = 0ull;
+      int k = 0;
+      for_each_neighbor<1>(list, n, load, [&](const float4 q) {
+        if (one(q) && k < kLiveEntries) bits |= 1ull << k;
+        ++k;
+      });
+      store_live(a.live, a.n, i, bits);
+    } else {
+      for_each_neighbor<1>(list, n, load, one);
+    }
   } else {
     const float2 px = f2(p.x), py = f2(p.y), pz = f2(p.z);
-    for_each_neighbor_pair<U>(list, n, load,
-                              [&](const float4 qa, const float4 qb) { acc.add_pair(c, px, py, pz, qa, qb); }, one);
+    auto two = [&](const float4 qa, const float4 qb) { return acc.add_pair(c, px, py, pz, qa, qb); };
+    if constexpr (kLiveOut) store_live(a.live, a.n, i, for_each_neighbor_pair_rec<U>(list, n, load, two, one));
+    else for_each_neighbor_pair<U>(list, n, load, two, one);
   }
   float rho;
   const float lam = finish_lambda(c, acc.rho, acc.gsx, acc.gsy, acc.gsz, acc.sum_g2, rho);
@@ -1074,7 +1091,9 @@ __device__ __forceinline__ void commit(const StepArgs& a, const SceneConst& c, i
 
 // kPow: the s_corr exponent when every scene with s_corr shares it (2, 3,
 // 4), else 0 (read per scene).
-template <int U, int kPow>
+// kLiveIn: only the live ones among the first entries (live bits from the
+// lambda pass of this iteration, same positions).
+template <int U, int kPow, bool kLiveIn>
 __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_delta(StepArgs a, int in, int last, int to_v2, int rest, float4* q_out) {
   if (failed(a.status)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1104,8 +1123,13 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_delta(StepAr
     }
   };
   auto load = [&](int j) { return __ldg(pl + j); };
+  const unsigned long long live =
+      kLiveIn ? (static_cast<unsigned long long>(a.live[i]) | (static_cast<unsigned long long>(a.live[a.n + i]) << 32))
+              : 0ull;
+  const float4 dead = make_float4(INFINITY, p.y, p.z, 0.0f);
   if constexpr (U == 1) {
-    for_each_neighbor<1>(list, n, load, one);
+    if constexpr (kLiveIn) for_each_live_then<1>(list, n, live, load, dead, one, one);
+    else for_each_neighbor<1>(list, n, load, one);
   } else {
     // Two entries at a time: the same operations as one() on a, then on b,
     // with the per-entry terms in paired arithmetic (pmul keeps each
@@ -1145,7 +1169,8 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_delta(StepAr
         az += tz.y;
       }
     };
-    for_each_neighbor_pair<U>(list, n, load, two, one);
+    if constexpr (kLiveIn) for_each_live_then<U>(list, n, live, load, dead, two, one);
+    else for_each_neighbor_pair<U>(list, n, load, two, one);
   }
   ax *= c.inv_density;
   ay *= c.inv_density;
@@ -1516,12 +1541,12 @@ inline int blocks_for(long long n, int threads) { return static_cast<int>((n + t
     }                                                                   \
   } while (0)
 
-template <int kPow>
+template <int kPow, bool kLiveIn>
 struct DeltaPow {
   template <int U>
   static void launch(int grid, int block, cudaStream_t st, const StepArgs& a, int in, int last, int to_v2, int rest,
                      float4* q_out) {
-    k_delta<U, kPow><<<grid, block, 0, st>>>(a, in, last, to_v2, rest, q_out);
+    k_delta<U, kPow, kLiveIn><<<grid, block, 0, st>>>(a, in, last, to_v2, rest, q_out);
   }
   static void dispatch(int u, int grid, int block, cudaStream_t st, const StepArgs& a, int in, int last, int to_v2,
                        int rest, float4* q_out) {
@@ -1534,14 +1559,33 @@ struct DeltaPow {
   }
 };
 
-void launch_delta(const StepPlan& plan, int grid, int block, cudaStream_t st, const StepArgs& a, int in, int last,
-                  int to_v2, int rest, float4* q_out) {
+template <bool kLiveIn>
+void launch_delta_pow(const StepPlan& plan, int grid, int block, cudaStream_t st, const StepArgs& a, int in, int last,
+                      int to_v2, int rest, float4* q_out) {
   const int u = plan.unroll[FLUID_KERNEL_DELTA];
   switch (plan.scorr_pow) {
-    case 2: DeltaPow<2>::dispatch(u, grid, block, st, a, in, last, to_v2, rest, q_out); break;
-    case 3: DeltaPow<3>::dispatch(u, grid, block, st, a, in, last, to_v2, rest, q_out); break;
-    case 4: DeltaPow<4>::dispatch(u, grid, block, st, a, in, last, to_v2, rest, q_out); break;
-    default: DeltaPow<0>::dispatch(u, grid, block, st, a, in, last, to_v2, rest, q_out); break;
+    case 2: DeltaPow<2, kLiveIn>::dispatch(u, grid, block, st, a, in, last, to_v2, rest, q_out); break;
+    case 3: DeltaPow<3, kLiveIn>::dispatch(u, grid, block, st, a, in, last, to_v2, rest, q_out); break;
+    case 4: DeltaPow<4, kLiveIn>::dispatch(u, grid, block, st, a, in, last, to_v2, rest, q_out); break;
+    default: DeltaPow<0, kLiveIn>::dispatch(u, grid, block, st, a, in, last, to_v2, rest, q_out); break;
+  }
+}
+
+// live: the lambda pass of this iteration recorded live bits (iterations
+// after the first).
+void launch_delta(const StepPlan& plan, int grid, int block, cudaStream_t st, const StepArgs& a, int in, int last,
+                  int to_v2, int rest, float4* q_out, bool live) {
+  if (live) launch_delta_pow<true>(plan, grid, block, st, a, in, last, to_v2, rest, q_out);
+  else launch_delta_pow<false>(plan, grid, block, st, a, in, last, to_v2, rest, q_out);
+}
+
+template <bool kLiveOut>
+void launch_lambda(int u, int grid, int block, cudaStream_t st, const StepArgs& a, int in) {
+  switch (u) {
+    case 1: k_lambda<1, kLiveOut><<<grid, block, 0, st>>>(a, in); break;
+    case 2: k_lambda<2, kLiveOut><<<grid, block, 0, st>>>(a, in); break;
+    case 8: k_lambda<8, kLiveOut><<<grid, block, 0, st>>>(a, in); break;
+    default: k_lambda<4, kLiveOut><<<grid, block, 0, st>>>(a, in); break;
   }
 }
 
@@ -1645,7 +1689,8 @@ cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t s
     const int in = it & 1;
     {
       const int b = plan.block[FLUID_KERNEL_LAMBDA];
-      FGB_DISPATCH_UNROLL(plan.unroll[FLUID_KERNEL_LAMBDA], k_lambda, blocks_for(a.n, b), b, st, a, in);
+      if (it == 0) launch_lambda<false>(plan.unroll[FLUID_KERNEL_LAMBDA], blocks_for(a.n, b), b, st, a, in);
+      else launch_lambda<true>(plan.unroll[FLUID_KERNEL_LAMBDA], blocks_for(a.n, b), b, st, a, in);
       m.mark(FLUID_KERNEL_LAMBDA);
       if (rec)
         cudaMemcpyAsync(rec->lambda + static_cast<size_t>(it) * a.n, a.lambda, n1, cudaMemcpyDeviceToDevice, st);
@@ -1653,7 +1698,7 @@ cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t s
     const int last = (it == plan.iterations - 1) ? 1 : 0;
     const int b = plan.block[FLUID_KERNEL_DELTA];
     float4* q_out = rec ? rec->q + static_cast<size_t>(it) * a.n : nullptr;
-    launch_delta(plan, blocks_for(a.n, b), b, st, a, in, last, to_v2, last ? rest_commit : 0, q_out);
+    launch_delta(plan, blocks_for(a.n, b), b, st, a, in, last, to_v2, last ? rest_commit : 0, q_out, it > 0);
     m.mark(FLUID_KERNEL_DELTA);
     if (rec)  // p^(it+1); the last iteration's lands in x (commit)
       cudaMemcpyAsync(rec->p + static_cast<size_t>(it + 1) * a.n, last ? a.x : a.p[in ^ 1], n4,
