@@ -4,19 +4,24 @@
 //   k_bounds        predicted cell of every particle, per-scene bounding box
 //   k_grid_setup    per-scene dense grid over that box, key base, radix passes
 //   k_keys          x-major linear cell key per particle, in caller order
-//   k_radix_*       stable LSD radix sort of (key, caller index), 8- or 11-bit
-//                   digits
+//   k_radix_digits  digit counts of every sort pass, one read of the keys
+//   k_radix_onesweep  one stable LSD pass of (key, caller index), 8- or 11-bit
+//                   digits: tile ranking, decoupled look-back, scatter
 //   k_reorder       gather into cell order, predict again (bit-identical),
 //                   cell (first, end) table by warp-shuffle boundary detection
 //   k_nbr_build     27-cell scan: lists in scan order staged in shared memory,
 //                   slices claimed by one atomic per block, coalesced copy-out;
 //                   capacity check
 //   k_nbr_overflow  re-scan for warps whose lists outgrew the staging
-//   k_lambda        density / lambda
+//   k_lambda        density / lambda (iterations 1-3 also record which of
+//                   each list's first 64 entries are within h: live bits)
 //   k_delta         position correction, s_corr, plane projection (last
-//                   iteration also commits v = (p - x)/dt, x = p)
-//   k_xsph          XSPH viscosity over the step's lists
-//   k_omega, k_eta  vorticity confinement (+ plane restitution / friction)
+//                   iteration also commits v = (p - x)/dt, x = p); iterations
+//                   1-3 walk only the live ones of those entries
+//   k_xsph          XSPH viscosity over the step's lists (records live bits
+//                   at the committed positions)
+//   k_omega, k_eta  vorticity confinement (+ plane restitution / friction),
+//                   walking only the live ones of the first 64 entries
 //
 // Arithmetic follows the reference's float operations one for one: the
 // library is compiled with -fmad=false (no contraction), IEEE division and
