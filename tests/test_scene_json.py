@@ -75,3 +75,11 @@ def test_per_plane_friction_key(tmp_path):
     mu = [np.float32(x) for x in on.params.plane_friction_each[:3]]
     assert mu == [np.float32(0.5), np.float32(0.1), np.float32(0.0)]
     np.testing.assert_array_equal(on.pos, off.pos)
+
+
+def test_set_plane_friction_needs_one_value_per_plane():
+    p = scenes.dam_break(2).params
+    with pytest.raises(ValueError):
+        scenes.set_plane_friction(p, [0.1] * (p.plane_count - 1))
+    scenes.set_plane_friction(p, [0.1] * p.plane_count)
+    assert p.plane_friction_per_plane == 1
