@@ -212,7 +212,9 @@ enum {
   FLUID_KERNEL_GRID = 1,     /* per-scene grid over the box */
   FLUID_KERNEL_KEYS = 2,     /* linear cell keys */
   FLUID_KERNEL_RADIX_HIST = 3,    /* sort: digit counts of every pass, one read */
-  FLUID_KERNEL_RADIX_SCAN = 4,    /* sort: digit starts */
+  FLUID_KERNEL_RADIX_SCAN = 4,    /* no launches: the digit starts are found by
+                                     each pass's look-back; id kept so the
+                                     others keep their values */
   FLUID_KERNEL_RADIX_SCATTER = 5, /* sort: one pass per digit (rank, look-back, scatter) */
   FLUID_KERNEL_REORDER = 6,  /* gather into cell order + cell table */
   FLUID_KERNEL_NBR_BUILD = 7, /* lists (one scan) + slices */
