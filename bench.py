@@ -8,7 +8,9 @@ scene's initial batch: before every step the initial state is restored
 device-to-device (outside the timed region), so every step does the same
 work (the lattice phase, ~28 neighbours per particle). The reference's own
 run of this scene collapses to ~10^4 neighbours per particle within ~30
-steps; `trajectory` reports that regime separately.
+steps; `trajectory` reports that regime separately: step times and the
+HBM fraction of steps 1-5 (the lattice, collapsing from step 2 on) and of
+the last 5, and neighbour-count histograms at steps 1, 5 and the last.
 
   value   particle-steps/s, inputs resident in HBM, L2 flushed between steps,
           per-step CUDA events on the solver's stream, max over ranks.
@@ -69,6 +71,18 @@ ALGO_BYTES_PER_STEP = 452
 # r^2 5, sqrt 1, spiky factor 3, lambda sum 1, s_corr 9, accumulate 7.
 DELTA_OPS_PER_PAIR = 29
 FP32_LANES_PER_SM = 128
+# Bin edges of the per-step neighbour-count histograms: [0, 8), [8, 16),
+# [16, 32), ... [16384, 32768), [32768, inf). The lattice phase fills the
+# bins below 64; the collapsed phase spreads over the thousands.
+HIST_EDGES = [0, 8] + [16 << k for k in range(12)]
+
+
+def neighbor_histogram(counts):
+    """Particles per bin of HIST_EDGES (the last bin is open-ended)."""
+    import numpy as np
+
+    idx = np.searchsorted(np.asarray(HIST_EDGES), np.asarray(counts), side="right") - 1
+    return np.bincount(idx, minlength=len(HIST_EDGES)).tolist()
 
 
 def log(*a):
@@ -326,19 +340,27 @@ def run_ours(args, world, rank, local):
         restore()
         solver.set_profiling(True)  # per-kernel totals; ~0.1 ms a step against 10-200 ms steps
         solver.kernel_times(reset=True)
-        t_ms, t_pairs = [], []
-        for _ in range(args.trajectory):
+        t_ms, t_pairs, hists = [], [], {}
+        hist_steps = {1, min(5, args.trajectory), args.trajectory}
+        for k in range(1, args.trajectory + 1):
             ev0.record(stream)
             solver.step(1)
             ev1.record(stream)
             ev1.synchronize()
             t_ms.append(ev0.elapsed_time(ev1))
             t_pairs.append(solver.stats()["neighbor_pairs"])
+            if k in hist_steps:  # outside the events; the step has completed
+                hists[f"step{k}"] = neighbor_histogram(solver.read_debug(_capi.DEBUG_NEIGHBOR_COUNTS))
         st = solver.stats()
-        traj = {"steps": args.trajectory, "ms_per_step_first5": round(statistics.mean(t_ms[:5]), 3),
-                "ms_per_step_last5": round(statistics.mean(t_ms[-5:]), 3),
+        first5, last5 = statistics.mean(t_ms[:5]), statistics.mean(t_ms[-5:])
+        peak_gbs = measured_peaks()[0]
+        traj = {"steps": args.trajectory, "ms_per_step_first5": round(first5, 3),
+                "ms_per_step_last5": round(last5, 3),
+                "hbm_frac_first5": round(ALGO_BYTES_PER_STEP * n / (first5 / 1e3) / 1e9 / peak_gbs, 5),
+                "hbm_frac_last5": round(ALGO_BYTES_PER_STEP * n / (last5 / 1e3) / 1e9 / peak_gbs, 7),
                 "neighbors_per_particle_step1": round(t_pairs[0] / n, 2),
                 "neighbors_per_particle_last": round(t_pairs[-1] / n, 2), "neighbor_max_last": st["neighbor_max"],
+                "neighbor_histogram": {"edges": HIST_EDGES, **hists},
                 "particle_steps_per_s": round(n * len(t_ms) / (sum(t_ms) / 1e3), 1),
                 "regrows": st["regrows"]}
         tail = solver.kernel_times(reset=True)
