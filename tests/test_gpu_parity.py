@@ -161,6 +161,47 @@ def test_full_size_first_step_1m(cuda_lib, oracle_lib):
     np.testing.assert_array_equal(hist_a, hist_b)
 
 
+def test_full_size_double_dam_break_two_steps(cuda_lib, oracle_lib):
+    """The 250,000-particle double dam break (two 50^3 blocks, all three
+    flags) at full size: after two steps (the collapse has begun: up to ~200
+    neighbours) keys, order, counts, rho, lambda, positions and velocities
+    equal the oracle's."""
+    sc = scenes.double_dam_break(50, seed=0)
+    assert sc.count == 250_000
+    a = oracle_lib.Oracle().run(sc.params, sc.pos, sc.vel, 0.0, 2, dump=True)
+    b = run_gpu(sc, 2, records=True)
+    for k in ("cell_keys", "sorted_order", "neighbor_counts", "rho", "lambda", "pos", "vel"):
+        np.testing.assert_array_equal(b[k], a[k], err_msg=k)
+    assert np.float32(b["time"]) == np.float32(a["time"])
+
+
+def test_full_size_batch_first_step(cuda_lib, oracle_lib):
+    """The 64 batched dam breaks (particle counts U[2k, 64k] from seed 0,
+    about 2.1M particles) stepped together in one solver: every scene's
+    step-1 keys, order, counts, rho, lambda, positions, velocities and time
+    equal the oracle run on that scene alone."""
+    scs = scenes.batched_scenes(64, seed=0)
+    s = Solver(0)
+    s.configure([sc.params for sc in scs], [sc.count for sc in scs])
+    s.upload(np.concatenate([sc.pos for sc in scs], axis=1), np.concatenate([sc.vel for sc in scs], axis=1))
+    s.step(1)
+    rec = {k: s.read_debug(w) for k, w in DEBUG.items()}
+    pos, vel = s.download()
+    times = [s.time(k) for k in range(len(scs))]
+    s.close()
+    off = 0
+    for k, sc in enumerate(scs):
+        a = oracle_lib.Oracle().run(sc.params, sc.pos, sc.vel, 0.0, 1, dump=True)
+        part = slice(off, off + sc.count)
+        for name in DEBUG:
+            np.testing.assert_array_equal(rec[name][part], a[name], err_msg=f"scene {k}: {name}")
+        np.testing.assert_array_equal(pos[:, part], a["pos"], err_msg=f"scene {k}: pos")
+        np.testing.assert_array_equal(vel[:, part], a["vel"], err_msg=f"scene {k}: vel")
+        assert np.float32(times[k]) == np.float32(a["time"])
+        off += sc.count
+    assert off == sum(sc.count for sc in scs) > 2_000_000
+
+
 def test_stateless_cuda_step_matches_golden(cuda_lib):
     p, d = load_golden("dam_break_4096.npz")
     sc = golden_scene("dam_break_4096.npz")
