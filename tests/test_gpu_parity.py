@@ -175,6 +175,22 @@ def test_full_size_double_dam_break_two_steps(cuda_lib, oracle_lib):
     assert np.float32(b["time"]) == np.float32(a["time"])
 
 
+def test_full_size_differentiable_scene_20_steps(cuda_lib, oracle_lib):
+    """The 32,768-particle differentiable scene (XSPH and s_corr, initial
+    velocities N(0, 0.1^2)) at full size over 20 steps, by which it has
+    collapsed to ~380 neighbours per particle (max ~1,700: lists regrow and
+    run past the staged and live-bit heads): the last step's records and the
+    state equal the oracle's."""
+    sc = scenes.differentiable_block(32, seed=0)
+    assert sc.count == 32_768
+    a = oracle_lib.Oracle().run(sc.params, sc.pos, sc.vel, 0.0, 20, dump=True)
+    b = run_gpu(sc, 20, records=True)
+    assert b["stats"]["regrows"] >= 1 and b["stats"]["neighbor_max"] > 64
+    for k in ("cell_keys", "sorted_order", "neighbor_counts", "rho", "lambda", "pos", "vel"):
+        np.testing.assert_array_equal(b[k], a[k], err_msg=k)
+    assert np.float32(b["time"]) == np.float32(a["time"])
+
+
 def test_full_size_batch_first_step(cuda_lib, oracle_lib):
     """The 64 batched dam breaks (particle counts U[2k, 64k] from seed 0,
     about 2.1M particles) stepped together in one solver: every scene's
