@@ -1173,7 +1173,7 @@ class Solver {
       cap = std::min<long long>(cap, (1ll << 31) - 1);
       if (table_.alloc(static_cast<size_t>(cap)) != cudaSuccess) return fail(FLUID_ERR_OUT_OF_MEMORY, "cell table");
       cudaMemsetAsync(table_.p, 0, table_.n * sizeof(int2), stream_);
-    cudaMemsetAsync(look_.p, 0, look_.n * sizeof(unsigned long long), stream_);  // tag 0: never current
+      cudaMemsetAsync(look_.p, 0, look_.n * sizeof(unsigned long long), stream_);  // tag 0: never current
       grid_cap_ = cap;
       changed = true;
     }
