@@ -5,7 +5,7 @@
 //   k_grid_setup    per-scene dense grid over that box, key base, radix passes
 //   k_keys          x-major linear cell key per particle, in caller order
 //   k_radix_digits  digit counts of every sort pass, one read of the keys
-//   k_radix_onesweep  one stable LSD pass of (key, caller index), 8- or 11-bit
+//   k_radix_onesweep  one stable LSD pass of (key, caller index), 8-, 9- or 11-bit
 //                   digits: tile ranking, decoupled look-back, scatter
 //   k_reorder       gather into cell order, predict again (bit-identical),
 //                   cell (first, end) table by warp-shuffle boundary detection
@@ -294,7 +294,7 @@ __global__ void __launch_bounds__(kBlock) k_bounds(StepArgs a) {
   add_bounds(a.bmin, a.bmax, scene, ok, cx, cy, cz);
 }
 
-// radix_bits: digit width of the sort (8 or 11), which sets the pass count.
+// radix_bits: digit width of the sort (8, 9 or 11), which sets the pass count.
 __global__ void __launch_bounds__(kBlock) k_grid_setup(StepArgs a, int radix_bits) {
   if (failed(a.status)) return;
   DevStatus* st = a.status;
@@ -366,7 +366,7 @@ __global__ void __launch_bounds__(kBlock) k_keys(StepArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// Stable LSD radix sort, kBits-bit digits (8 or 11, chosen by the autotuner),
+// Stable LSD radix sort, kBits-bit digits (8, 9 or 11, chosen by the autotuner),
 // one kernel per pass. Pass p reads keys[p&1] (pass 0: values are the caller
 // indices themselves) and writes keys[(p+1)&1]. The digit counts of every
 // pass come from one read of the keys (k_radix_digits); each
@@ -1614,6 +1614,19 @@ void launch_omega(int u, int grid, int block, cudaStream_t st, const StepArgs& a
   }
 }
 
+// The cell-key sort at one digit width: digit counts, then `passes` passes
+// (those beyond the step's own pass count return at entry).
+template <int kBits>
+void launch_sort(const StepArgs& a, int passes, cudaStream_t st, LaunchMarks& m) {
+  const int digit_blocks = a.tiles < kRadixDigitBlocks ? a.tiles : kRadixDigitBlocks;
+  k_radix_digits<kBits><<<digit_blocks, kBlock, 0, st>>>(a);
+  m.mark(FLUID_KERNEL_RADIX_HIST);
+  for (int pass = 0; pass < passes; ++pass) {
+    k_radix_onesweep<kBits><<<a.tiles, kBlock, 0, st>>>(a, pass);
+    m.mark(FLUID_KERNEL_RADIX_SCATTER);
+  }
+}
+
 }  // namespace
 
 void LaunchMarks::start() {
@@ -1652,21 +1665,10 @@ cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t s
   m.mark(FLUID_KERNEL_GRID);
   k_keys<<<nb, kBlock, 0, st>>>(a);
   m.mark(FLUID_KERNEL_KEYS);
-  const int digit_blocks = a.tiles < kRadixDigitBlocks ? a.tiles : kRadixDigitBlocks;
-  if (plan.radix_bits == 11) {
-    k_radix_digits<11><<<digit_blocks, kBlock, 0, st>>>(a);
-    m.mark(FLUID_KERNEL_RADIX_HIST);
-    for (int pass = 0; pass < plan.radix_passes; ++pass) {
-      k_radix_onesweep<11><<<a.tiles, kBlock, 0, st>>>(a, pass);
-      m.mark(FLUID_KERNEL_RADIX_SCATTER);
-    }
-  } else {
-    k_radix_digits<8><<<digit_blocks, kBlock, 0, st>>>(a);
-    m.mark(FLUID_KERNEL_RADIX_HIST);
-    for (int pass = 0; pass < plan.radix_passes; ++pass) {
-      k_radix_onesweep<8><<<a.tiles, kBlock, 0, st>>>(a, pass);
-      m.mark(FLUID_KERNEL_RADIX_SCATTER);
-    }
+  switch (plan.radix_bits) {
+    case 11: launch_sort<11>(a, plan.radix_passes, st, m); break;
+    case 9: launch_sort<9>(a, plan.radix_passes, st, m); break;
+    default: launch_sort<8>(a, plan.radix_passes, st, m); break;
   }
   k_reorder<<<nb, kBlock, 0, st>>>(a);
   m.mark(FLUID_KERNEL_REORDER);

@@ -17,7 +17,7 @@ struct StepPlan {
   bool vorticity = false; // some scene runs vorticity confinement
   bool restitution = false;
   int radix_passes = 1;   // passes launched (cover the grid capacity)
-  int radix_bits = 8;     // digit width of the sort: 8 or 11
+  int radix_bits = 8;     // digit width of the sort: 8, 9 or 11
   int scorr_pow = 0;      // s_corr exponent shared by every s_corr scene (2-4), else 0
   // Per-kernel launch shape (indexed by FLUID_KERNEL_*), chosen by the
   // autotuner: neighbour entries fetched ahead (2, 4, 8; 1 when set

@@ -614,7 +614,7 @@ class Solver {
     // Sort digit width: the three radix stages' time per step under each.
     double best_sort = 1e300;
     int best_bits = plan_.radix_bits;
-    for (int bits : {8, 11}) {
+    for (int bits : {8, 9, 11}) {
       plan_.radix_bits = bits;
       make_plan();
       invalidate_graphs();
@@ -644,7 +644,8 @@ class Solver {
   int sort_bits() const { return plan_.radix_bits; }
 
   int set_sort_bits(int bits) {
-    if (bits != 8 && bits != 11) return fail(FLUID_ERR_INVALID_ARGUMENT, "sort digit width must be 8 or 11");
+    if (bits != 8 && bits != 9 && bits != 11)
+      return fail(FLUID_ERR_INVALID_ARGUMENT, "sort digit width must be 8, 9 or 11");
     int rc = synchronize();
     if (rc) return rc;
     plan_.radix_bits = bits;

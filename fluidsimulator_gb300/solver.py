@@ -174,7 +174,7 @@ class Solver:
         self._check(self.lib.fluid_solver_set_tuning(self.h, u, b, n))
 
     def sort_bits(self) -> int:
-        """Digit width of the cell-key radix sort (8 or 11)."""
+        """Digit width of the cell-key radix sort (8, 9 or 11)."""
         b = ctypes.c_int32(0)
         self._check(self.lib.fluid_solver_get_sort_bits(self.h, ctypes.byref(b)))
         return b.value

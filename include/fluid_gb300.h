@@ -243,8 +243,8 @@ int fluid_solver_kernel_times(fluid_solver* solver, double* ms_out,
  * neighbour entries fetched ahead in {2, 4, 8}, threads per block in
  * {128, 256, 512} -- over `trials` discarded steps of the current state. It
  * keeps the default shape (4, 256) unless another is at least 2 % faster,
- * and else the fastest, per kernel. It then times the cell-key sort with 8-
- * and 11-bit digits and keeps the faster width. One entry ahead (the
+ * and else the fastest, per kernel. It then times the cell-key sort with 8-,
+ * 9- and 11-bit digits and keeps the fastest width. One entry ahead (the
  * single-entry walker) is left out of the sweep: where all lists are short
  * it can win narrowly and then lose by far once they grow; set it with
  * fluid_solver_set_tuning. The state and time are not advanced. Every choice
@@ -259,7 +259,7 @@ int fluid_solver_get_tuning(fluid_solver* solver, int32_t* unroll, int32_t* bloc
 int fluid_solver_set_tuning(fluid_solver* solver, const int32_t* unroll,
                             const int32_t* block, int32_t kernels);
 
-/* Digit width of the cell-key radix sort: 8 (default) or 11 bits. Keys of
+/* Digit width of the cell-key radix sort: 8 (default), 9 or 11 bits. Keys of
  * b bits take ceil(b / width) passes; the permutation does not depend on it. */
 int fluid_solver_get_sort_bits(fluid_solver* solver, int32_t* bits);
 int fluid_solver_set_sort_bits(fluid_solver* solver, int32_t bits);

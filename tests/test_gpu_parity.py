@@ -421,13 +421,14 @@ def _two_corner_blocks():
 
 @pytest.mark.parametrize("case", ["small_grid", "wide_grid"])
 def test_sort_width_gives_same_permutation(cuda_lib, oracle_lib, case):
-    """8- and 11-bit digits: same cell keys, stable permutation and trajectory
-    (small_grid: keys of <= 11 bits, one 11-bit pass against two 8-bit ones;
-    wide_grid: 20-bit keys, two passes against three)."""
+    """8-, 9- and 11-bit digits: same cell keys, stable permutation and
+    trajectory (small_grid: keys of <= 11 bits, one 11-bit pass against two
+    8- or 9-bit ones; wide_grid: 20-bit keys, two 11-bit passes against
+    three)."""
     sc = scenes.dam_break(8, seed=5, flags=True) if case == "small_grid" else _two_corner_blocks()
     ref = oracle_lib.Oracle().run(sc.params, sc.pos, sc.vel, 0.0, 6, dump=True)
     out = {}
-    for bits in (8, 11):
+    for bits in (8, 9, 11):
         s = Solver(0)
         s.configure([sc.params], [sc.count])
         s.set_sort_bits(bits)
@@ -441,16 +442,18 @@ def test_sort_width_gives_same_permutation(cuda_lib, oracle_lib, case):
         np.testing.assert_array_equal(vel, ref["vel"])
         np.testing.assert_array_equal(out[bits][2], ref["sorted_order"])
         np.testing.assert_array_equal(out[bits][3], ref["cell_keys"])
-    for x, y in zip(out[8], out[11]):
-        np.testing.assert_array_equal(x, y)
+    for bits in (9, 11):
+        for x, y in zip(out[8], out[bits]):
+            np.testing.assert_array_equal(x, y)
     s = Solver(0)
     s.configure([sc.params], [sc.count])
-    with pytest.raises(FluidError):
-        s.set_sort_bits(9)
+    for bad in (7, 10, 12):
+        with pytest.raises(FluidError):
+            s.set_sort_bits(bad)
     s.close()
 
 
-@pytest.mark.parametrize("bits", [8, 11])
+@pytest.mark.parametrize("bits", [8, 9, 11])
 def test_sort_across_many_tiles(cuda_lib, oracle_lib, bits):
     """216,000 particles (106 sort tiles, so every pass chains its look-back
     across tiles): the permutation of step 1 and the state after three steps
