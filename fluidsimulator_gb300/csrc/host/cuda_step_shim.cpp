@@ -4,6 +4,17 @@
 // functions of cuda/include/fluid/cuda.h:7-9 on top of the C ABI, so
 // app/src/main.cpp (:171-184 device check, :250-251 per-step call) runs the
 // GB300 step unchanged. Includes the reference's own headers.
+//
+// Failure behaviour (a stated difference from the reference, whose
+// cuda_step checks no CUDA error and carries on): a step that fails -- the
+// library's status is not FLUID_OK, for example non-finite input positions
+// -- throws std::runtime_error("cuda_step: <status>") and leaves `state`
+// unchanged. The reference's application calls cuda_step outside any try
+// block (app/src/main.cpp:251), so there the exception ends the run through
+// std::terminate; GCC's default terminate handler prints the exception's
+// what() string to stderr before aborting. A failed step therefore stops the
+// simulation loudly instead of writing frames of an unadvanced or corrupt
+// state. A caller that wants to continue catches the exception.
 
 #include <stdexcept>
 #include <string>

@@ -378,6 +378,15 @@ __global__ void __launch_bounds__(kBlock) k_keys(StepArgs a) {
 // Look-back words, one per (tile, digit): tag (step epoch and pass) in the
 // high half, then a 2-bit flag and a 30-bit count. A word whose tag is not
 // the current one is not ready.
+//
+// The tag keeps the low 30 bits of the epoch, so tags repeat every 2^30 steps
+// of one status word. Every step that runs a pass rewrites the words of all
+// of that pass's tiles and digits, so a word left from an earlier step can
+// carry the current tag only if it was last written exactly a multiple of
+// 2^30 steps ago and no step since ran that pass over that tile (a grid that
+// needed fewer passes, or a smaller particle count, for all of 2^30 steps).
+// That bound -- about 12 days of back-to-back 1 ms steps -- is an accepted
+// limit of a solver handle; a new handle or configure starts its own words.
 constexpr uint32_t kLookAggregate = 1u;  // count = this tile's keys of the digit
 constexpr uint32_t kLookPrefix = 2u;     // count = keys of the digit in tiles 0..this
 constexpr int kLookSpinLimit = 1 << 22;  // then the step fails (FLUID_ERR_CUDA)

@@ -182,9 +182,12 @@ extern "C" int fluid_gb300_step_noalloc(const fluid_params* params, int64_t coun
                      a.sc, 1, n, st) != cudaSuccess)
     return FLUID_ERR_CUDA;
   if (enqueue_step(a, plan, st, marks) != cudaSuccess) return FLUID_ERR_CUDA;
-  if (cudaStreamSynchronize(st) != cudaSuccess) return FLUID_ERR_CUDA;
+  // The status word is read on the caller's stream, behind the step, so the
+  // call waits on that stream only (not on other streams of the device).
   DevStatus status;
-  if (cudaMemcpy(&status, a.status, sizeof(status), cudaMemcpyDeviceToHost) != cudaSuccess) return FLUID_ERR_CUDA;
+  if (cudaMemcpyAsync(&status, a.status, sizeof(status), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+    return FLUID_ERR_CUDA;
+  if (cudaStreamSynchronize(st) != cudaSuccess) return FLUID_ERR_CUDA;
   if (status.err) return status.err;  // caller's arrays untouched
   if (enqueue_download(a.x, a.v, a.slot, pos_x, pos_y, pos_z, vel_x, vel_y, vel_z, n, st) != cudaSuccess)
     return FLUID_ERR_CUDA;

@@ -171,19 +171,29 @@ int bits_for(long long cap) {
 
 }  // namespace
 
-// Device address of a page-locked host buffer mapped for `device` (pinned
-// by cudaHostAlloc / cudaMallocHost or registered with cudaHostRegister), or
-// nullptr for any other pointer. The upload and download kernels read and
-// write such buffers in place over the host link, without staging copies;
-// pageable memory keeps the copy path.
-const void* mapped_host(const void* p, int device) {
-  cudaPointerAttributes at;
-  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
-    cudaGetLastError();
-    return nullptr;
-  }
-  if (at.type != cudaMemoryTypeHost || !at.devicePointer || at.device != device) return nullptr;
-  return at.devicePointer;
+// Device address of a page-locked host buffer of `bytes` bytes mapped for
+// `device` (pinned by cudaHostAlloc / cudaMallocHost or registered with
+// cudaHostRegister), or nullptr for any other memory. Both the first and the
+// last byte must lie in the same mapping (a registered range shorter than
+// the array would otherwise let the kernels run past it over the host link).
+// The upload and download kernels read and write such buffers in place,
+// without staging copies; any other memory keeps the copy path.
+const void* mapped_host(const void* p, size_t bytes, int device) {
+  auto lookup = [device](const void* q) -> const char* {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, q) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    if (at.type != cudaMemoryTypeHost || !at.devicePointer || at.device != device) return nullptr;
+    return static_cast<const char*>(at.devicePointer);
+  };
+  const char* first = lookup(p);
+  if (!first || bytes == 0) return first;
+  const char* last_host = static_cast<const char*>(p) + (bytes - 1);
+  const char* last = lookup(last_host);
+  if (!last || last != first + (bytes - 1)) return nullptr;
+  return first;
 }
 
 class Solver {
@@ -413,7 +423,7 @@ class Solver {
   template <typename T>
   bool all_mapped(T* const (&host)[6], T* (&dev)[6]) const {
     for (int k = 0; k < 6; ++k) {
-      const void* d = mapped_host(host[k], device_);
+      const void* d = mapped_host(host[k], sizeof(T) * static_cast<size_t>(n_), device_);
       if (!d) return false;
       dev[k] = static_cast<T*>(const_cast<void*>(d));
     }

@@ -122,7 +122,8 @@ int fluid_gb300_cuda_step(const fluid_params* params, int64_t count,
  * grow the process's footprint). The six arrays are the caller's DEVICE
  * arrays of `count` particles in caller order, advanced in place; *time +=
  * dt. Work is enqueued on `stream` (a cudaStream_t, NULL = legacy default)
- * and the call returns when it is done.
+ * and the call blocks until it is done: it synchronises `stream` once to
+ * read the step's status and once after writing the arrays.
  *
  * All scratch lives in one fixed device array inside this library (about
  * 7.6 MiB, held on every GPU that loads the library until the process

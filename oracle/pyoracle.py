@@ -20,7 +20,10 @@ from fluidsimulator_gb300._capi import FluidParams
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libpbf_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libfluid_ref.so")
-REF_TREE = "/root/reference"
+# The reference source tree (only the pin and a few tests read it): the
+# FLUIDSIM_REFERENCE_TREE environment variable, else the default location of
+# the read-only checkout. The GPU host has no such tree; the pin is then skipped.
+REF_TREE = os.environ.get("FLUIDSIM_REFERENCE_TREE", "/root/reference")
 
 
 class _Dump(ctypes.Structure):
@@ -38,7 +41,7 @@ def build(ref: bool | None = None) -> None:
     if ref is None:
         ref = os.path.isdir(REF_TREE)
     targets = ["all"] + (["ref"] if ref else [])
-    subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
+    subprocess.run(["make", "-s", "-C", HERE, f"REF={REF_TREE}"] + targets, check=True)
 
 
 _LIBS: dict[str, ctypes.CDLL] = {}

@@ -10,7 +10,7 @@ import pytest
 
 from conftest import ROOT, golden_scene, load_golden
 
-REF = "/root/reference"
+from oracle.pyoracle import REF_TREE as REF  # noqa: E402  (FLUIDSIM_REFERENCE_TREE)
 LIB_DIR = os.path.join(ROOT, "fluidsimulator_gb300", "_lib")
 HOST = os.path.join(ROOT, "fluidsimulator_gb300", "csrc", "host")
 
@@ -87,3 +87,75 @@ def test_host_interface_matches_golden(cuda_lib, tmp_path, mode):
     np.testing.assert_array_equal(pos, d["s20_pos"])
     np.testing.assert_array_equal(vel, d["s20_vel"])
     assert np.float32(raw[6 * n]) == d["s20_time"]
+
+
+def _build_shim_app(tmp_path):
+    """The shim compiled against the reference-interface stand-in
+    (tests/cpp/ref_iface) and driven as the reference's app drives it."""
+    exe = str(tmp_path / "shim_app_main")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "tests", "cpp", "ref_iface"), "-I",
+                    os.path.join(ROOT, "include"), os.path.join(ROOT, "tests", "cpp", "shim_app_main.cpp"),
+                    os.path.join(HOST, "cuda_step_shim.cpp"), "-L", LIB_DIR, "-lfluid_gb300",
+                    f"-Wl,-rpath,{LIB_DIR}", "-o", exe], check=True)
+    return exe
+
+
+def _write_scene(path, p, pos, vel):
+    with open(path, "wb") as f:
+        f.write(bytes(p))
+        f.write(np.int64(pos.shape[1]).tobytes())
+        f.write(np.ascontiguousarray(pos, np.float32).tobytes())
+        f.write(np.ascontiguousarray(vel, np.float32).tobytes())
+
+
+def test_shim_app_builds_and_checks_the_device(cuda_lib, tmp_path):
+    exe = _build_shim_app(tmp_path)
+    try:
+        import torch
+
+        has_gpu = torch.cuda.is_available()
+    except ImportError:
+        has_gpu = False
+    if not has_gpu:  # the reference app's own exit path without a device
+        r = subprocess.run([exe, "in.bin", "out.bin", "1"], capture_output=True, text=True)
+        assert r.returncode == 1 and "CUDA backend unavailable" in r.stderr
+
+
+@pytest.mark.gpu
+def test_shim_drives_the_gpu_step_like_the_reference_app(cuda_lib, tmp_path):
+    """fluid::cuda_step of the drop-in shim, called once per step as
+    app/src/main.cpp:250-251 calls it, gives the reference's 20-step result
+    (golden fixture) bit for bit."""
+    exe = _build_shim_app(tmp_path)
+    p, d = load_golden("dam_break_flags_4096.npz")
+    sc = golden_scene("dam_break_flags_4096.npz")
+    inp, out = tmp_path / "in.bin", tmp_path / "out.bin"
+    _write_scene(inp, p, sc.pos, sc.vel)
+    r = subprocess.run([exe, str(inp), str(out), "20"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert "backend=cuda" in r.stdout and f"particle_count={sc.count}" in r.stdout
+    raw = np.fromfile(out, np.float32)
+    n = sc.count
+    np.testing.assert_array_equal(raw[: 3 * n].reshape(3, n), d["s20_pos"])
+    np.testing.assert_array_equal(raw[3 * n: 6 * n].reshape(3, n), d["s20_vel"])
+    assert np.float32(raw[6 * n]) == d["s20_time"]
+
+
+@pytest.mark.gpu
+def test_shim_failure_stops_an_app_without_try(cuda_lib, tmp_path):
+    """A failed step (a non-finite input position, which the step's own key
+    kernel reports as FLUID_ERR_NONFINITE) throws from fluid::cuda_step; in
+    an application that, like the reference's, calls it outside any try
+    block, the run ends through std::terminate with the status on stderr and
+    no output written."""
+    exe = _build_shim_app(tmp_path)
+    p, _ = load_golden("dam_break_flags_4096.npz")
+    sc = golden_scene("dam_break_flags_4096.npz")
+    pos = sc.pos.copy()
+    pos[1, 17] = np.nan
+    inp, out = tmp_path / "in.bin", tmp_path / "out.bin"
+    _write_scene(inp, p, pos, sc.vel)
+    r = subprocess.run([exe, str(inp), str(out), "3"], capture_output=True, text=True)
+    assert r.returncode != 0
+    assert "cuda_step: " in r.stderr and "non-finite" in r.stderr.lower(), r.stderr
+    assert not out.exists()

@@ -11,7 +11,7 @@ from conftest import ROOT
 from fluidsimulator_gb300 import scenes
 from fluidsimulator_gb300.solver import read_vtp, write_pvd, write_vtp
 
-REF = "/root/reference"
+from oracle.pyoracle import REF_TREE as REF  # noqa: E402  (FLUIDSIM_REFERENCE_TREE)
 
 
 def _positions(n=777, seed=3):

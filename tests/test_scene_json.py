@@ -11,7 +11,9 @@ import pytest
 
 from fluidsimulator_gb300 import scenes
 
-REF_SCENES = sorted(glob.glob("/root/reference/scene/*.json"))
+from oracle.pyoracle import REF_TREE  # noqa: E402  (FLUIDSIM_REFERENCE_TREE)
+
+REF_SCENES = sorted(glob.glob(os.path.join(REF_TREE, "scene", "*.json")))
 
 
 @pytest.mark.parametrize("path", REF_SCENES, ids=[os.path.basename(p) for p in REF_SCENES])
