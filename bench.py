@@ -376,10 +376,20 @@ def run_ours(args, world, rank, local):
     differentiable = None
     if not args.no_adjoint:
         differentiable = run_differentiable(args, dev, stream)
+    configs = collapsed = None
+    if not args.no_configs:
+        configs = run_configs(args, dev, stream)
+        collapsed = run_collapsed(args, dev, stream)
 
     cpu = parity = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu, parity = cpu_baseline(sc, budget_s=args.cpu_budget)
+        if configs:
+            cpu_configs(configs, args)
+        if collapsed:
+            cpu_collapsed(collapsed)
+        if differentiable:
+            differentiable["fp64_checks"] = gradient_checks(args)
 
     out = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -399,7 +409,7 @@ def run_ours(args, world, rank, local):
         "step_roofline": {"bytes_per_particle_step": ALGO_BYTES_PER_STEP, "frac": round(step_frac, 5)},
         "kernel_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in stage.items() if v[1]},
         "cpu_baseline": cpu, "parity_step1": parity, "e2e": e2e, "clocks": clk, "gpu_launches": launches,
-        "trajectory": traj,
+        "trajectory": traj, "configs": configs, "collapsed": collapsed,
         "batched": batched, "differentiable": differentiable, "output": output,
     }
     if world > 1:
@@ -410,15 +420,116 @@ def run_ours(args, world, rank, local):
         print(json.dumps(_finite(out)), flush=True)
 
 
+def _gpu_run(sc, steps, dev, stream, phases=5):
+    """Runs `steps` steps of a scene from its initial state on a fresh solver
+    (graphs on, default shapes), each step bracketed by CUDA events on the
+    solver's stream. Returns per-step ms, neighbours per particle per step and
+    the final state."""
+    import torch
+
+    from fluidsimulator_gb300.solver import Solver
+
+    s = Solver(dev.index)
+    s.configure([sc.params], [sc.count])
+    s.set_stream(stream.cuda_stream)
+    s.upload(sc.pos, sc.vel)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ms, nbr = [], []
+    for _ in range(steps):
+        ev[0].record(stream)
+        s.step_async(1)
+        ev[1].record(stream)
+        s.synchronize()
+        ms.append(ev[0].elapsed_time(ev[1]))
+        nbr.append(s.stats()["neighbor_pairs"] / sc.count)
+    pos, vel = s.download()
+    st = s.stats()
+    s.close()
+    return ms, nbr, pos, vel, st
+
+
+def run_configs(args, dev, stream):
+    """The two single-scene configurations besides the 1M throughput scene,
+    each run over its full length on the GPU: c1, the plain dam break (4,096
+    particles, 16^3 lattice, spacing 0.05, h 0.1, flags off, 240 steps), and
+    c2, the double dam break (two 50^3 blocks, 250,000 particles, spacing
+    0.025, h 0.05, all three flags, 480 steps). The CPU side (cpu_configs)
+    times the oracle over the whole of c1 and a stated prefix of c2 on the
+    host cores and checks the GPU's state after that prefix bit for bit."""
+    from fluidsimulator_gb300 import scenes
+
+    out = {}
+    for key, sc, steps in (("c1_dam_break_4096", scenes.dam_break(16, seed=0), args.c1_steps),
+                           ("c2_double_dam_break_250k", scenes.double_dam_break(50, seed=0), args.c2_steps)):
+        if steps <= 0:
+            continue
+        _gpu_run(sc, min(steps, 3), dev, stream)  # warm-up: kernels loaded, graphs captured once
+        ms, nbr, pos, vel, st = _gpu_run(sc, steps, dev, stream)
+        total = sum(ms)
+        out[key] = {"particles": sc.count, "steps": steps,
+                    "gpu": {"ms_total": round(total, 3), "ms_per_step": round(total / steps, 4),
+                            "particle_steps_per_s": round(sc.count * steps / (total / 1e3), 1),
+                            "ms_per_step_first5": round(statistics.mean(ms[:5]), 4),
+                            "ms_per_step_last5": round(statistics.mean(ms[-5:]), 4),
+                            "neighbors_per_particle_step1": round(nbr[0], 2),
+                            "neighbors_per_particle_last": round(nbr[-1], 2), "neighbor_max_last": st["neighbor_max"],
+                            "regrows": st["regrows"],
+                            "timing": "per-step CUDA events on the solver's stream, graphs on, default shapes, "
+                                      "whole run from the initial state"},
+                    "_scene": sc}
+    return out
+
+
+def run_collapsed(args, dev, stream):
+    """One step of the collapsed phase on the GPU, for a CPU comparison on the
+    same state: the 125,000-particle falling block (50^3, the 1M scene's
+    spacing, h and flags) stepped `collapsed_at - 1` steps on the GPU, its
+    state downloaded, then step `collapsed_at` timed from that state (re-
+    uploaded before each of a few repetitions; median)."""
+    import torch
+
+    from fluidsimulator_gb300 import scenes
+    from fluidsimulator_gb300.solver import Solver
+
+    if args.collapsed_at <= 1:
+        return None
+    sc = scenes.falling_block(args.collapsed_side, seed=0)
+    s = Solver(dev.index)
+    s.configure([sc.params], [sc.count])
+    s.set_stream(stream.cuda_stream)
+    s.upload(sc.pos, sc.vel)
+    s.step(args.collapsed_at - 1)
+    pos, vel = s.download()
+    t0 = s.time()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ms = []
+    for _ in range(4):
+        s.upload(pos, vel)
+        s.set_time(t0)
+        ev[0].record(stream)
+        s.step_async(1)
+        ev[1].record(stream)
+        s.synchronize()
+        ms.append(ev[0].elapsed_time(ev[1]))
+    st = s.stats()
+    after = s.download()
+    s.close()
+    gms = statistics.median(ms[1:])
+    return {"scene": f"falling_block_{sc.count}", "particles": sc.count, "step": args.collapsed_at,
+            "neighbors_per_particle": round(st["neighbor_pairs"] / sc.count, 2), "neighbor_max": st["neighbor_max"],
+            "gpu": {"ms_per_step": round(gms, 4), "particle_steps_per_s": round(sc.count / (gms / 1e3), 1),
+                    "timing": "CUDA events around one step from the uploaded state; median of 3 after one warm-up"},
+            "_state": (sc, pos, vel, t0, after)}
+
+
 def run_differentiable(args, dev, stream):
     """Differentiable PBF: 32^3 block (32,768 particles), XSPH c = 0.01 and
     s_corr on, initial velocity N(0, 0.1^2), 60 steps, loss |COM - (1.5, 0.3,
     1.0)|^2. Times the forward run and forward + adjoint (checkpoints every 10
-    steps, recomputation in between), and checks dL/dv0 and dL/dc against
-    central finite differences of the GPU forward (16 random directions, step
-    1e-3). The FP64 checks of these gradients (the oracle's FP64 adjoint and
-    central differences of its FP64 forward) are tests:
-    tests/test_adjoint.py::test_differentiable_scene_gradients_match_fp64."""
+    steps, recomputation in between) and reports the gradient's size per
+    horizon. The checks of these gradients against the oracle (its FP64
+    adjoint, central differences of its FP64 forward) run in the CPU leg
+    (gradient_checks) and in tests/test_adjoint.py."""
     import numpy as np
     import torch
 
@@ -469,24 +580,11 @@ def run_differentiable(args, dev, stream):
            "timing": "forward: CUDA events around the 60 steps; forward+adjoint: host wall clock around record(60, 10) "
                      "+ final-state read + backward"}
 
-    def fd_check(scene):
-        """dL/dv0 and dL/dc against central differences (step 1e-3) of the
-        GPU forward, per horizon."""
-        s.set_params([scene.params])
+    def norms(scene):
+        """|dL/dv0| and dL/dc of the GPU adjoint per horizon (null where the
+        FP32 gradient overflows)."""
         res = {}
-        rng = np.random.default_rng(2024)
-        dirs = [rng.standard_normal((3, n)) for _ in range(args.fd_dirs)]
-        dirs = [d / np.sqrt(np.mean(d * d)) for d in dirs]  # unit RMS per component
-        eps = 1e-3
-
-        def loss(v0, params, horizon):
-            s.set_params([params])
-            s.upload(scene.pos, np.ascontiguousarray(v0, np.float32))
-            s.step(horizon)
-            x, _ = s.download()
-            return float(np.sum((x.astype(np.float64).mean(axis=1) - target) ** 2))
-
-        for horizon in sorted({1, 5, 10, steps}):
+        for horizon in sorted({1, 5, 10, 20, steps}):
             s.set_params([scene.params])
             s.upload(scene.pos, scene.vel)
             s.record(horizon, every)
@@ -494,27 +592,13 @@ def run_differentiable(args, dev, stream):
             com = x.astype(np.float64).mean(axis=1)
             gxf = np.repeat((2.0 * (com - target) / n)[:, None], n, axis=1).astype(np.float32)
             _, gv0, gc = s.backward(gxf, np.zeros((3, n), np.float32))
-            rel = []
-            for d in dirs:
-                fd = (loss(scene.vel + eps * d, scene.params, horizon) -
-                      loss(scene.vel - eps * d, scene.params, horizon)) / (2 * eps)
-                ad = float(np.sum(gv0.astype(np.float64) * d))
-                rel.append(abs(fd - ad) / max(abs(fd), abs(ad), 1e-30))
-            c0 = np.float32(scene.params.visc_c)
-            pp, pm = scene.params.copy(), scene.params.copy()
-            pp.visc_c, pm.visc_c = float(np.float32(c0 * 1.001)), float(np.float32(c0 * 0.999))
-            fdc = (loss(scene.vel, pp, horizon) - loss(scene.vel, pm, horizon)) / (pp.visc_c - pm.visc_c)
-            res[str(horizon)] = {
-                "grad_v0_norm": float(np.linalg.norm(gv0)), "fd_rel_err_median": float(np.median(rel)),
-                "fd_rel_err_max": float(np.max(rel)), "fd_within_1e-3": int(sum(r <= 1e-3 for r in rel)),
-                "dL_dc": float(gc[0]), "dL_dc_fd": float(fdc),
-                "dL_dc_rel_err": float(abs(fdc - gc[0]) / max(abs(fdc), abs(gc[0]), 1e-30))}
+            res[str(horizon)] = {"grad_v0_norm": float(np.linalg.norm(gv0.astype(np.float64))),
+                                 "dL_dc": float(gc[0])}
         s.set_params([sc.params])
         return res
 
-    out["fd"] = {"as_specified": fd_check(sc),
-                 "unit_mass": fd_check(scenes.differentiable_block(32, seed=0, unit_mass=True)),
-                 "directions": args.fd_dirs, "step": 1e-3}
+    out["gradient_norms"] = {"as_specified": norms(sc),
+                             "unit_mass": norms(scenes.differentiable_block(32, seed=0, unit_mass=True))}
     s.close()
     return out
 
@@ -747,6 +831,141 @@ def step1_parity(sample):
             "max_abs_dx_over_h": float(np.max(np.abs(pos - ref["pos"]))) / float(sample.params.h)}
 
 
+def cpu_configs(configs, args):
+    """The oracle on the host cores over c1 (all steps) and a prefix of c2;
+    the GPU's state after the same steps must equal the oracle's bit for bit.
+    Fills configs[key]["cpu"] and drops the scene objects."""
+    import numpy as np
+    import torch
+
+    from fluidsimulator_gb300.solver import Solver
+    from oracle import pyoracle
+
+    threads = os.cpu_count() or 1
+    pyoracle.set_threads(threads)
+    for key, c in configs.items():
+        sc = c.pop("_scene")
+        steps = c["steps"] if key.startswith("c1") else min(c["steps"], args.c2_cpu_steps)
+        o = pyoracle.Oracle()
+        t0 = time.perf_counter()
+        r = o.run(sc.params, sc.pos, sc.vel, 0.0, steps, records=True)
+        dt = time.perf_counter() - t0
+        s = Solver(torch.cuda.current_device())
+        s.configure([sc.params], [sc.count])
+        s.upload(sc.pos, sc.vel)
+        s.step(steps)
+        pos, vel = s.download()
+        s.close()
+        c["cpu"] = {"steps": steps, "ms_per_step": round(1e3 * dt / steps, 3),
+                    "particle_steps_per_s": round(sc.count * steps / dt, 1), "cores": threads, "kind": "port",
+                    "neighbors_per_particle_last": round(float(r["neighbor_pairs"][-1]) / sc.count, 2),
+                    "what": f"oracle/pbf_oracle.cpp (restatement of core/src/core.cpp:119-615), steps 1-{steps} "
+                            f"from the initial state, OpenMP {threads} threads, {os.uname().machine}"}
+        c["gpu_equals_cpu_after_cpu_steps"] = bool(np.array_equal(pos, r["pos"]) and np.array_equal(vel, r["vel"]))
+        c["gpu_over_cpu"] = round(c["gpu"]["particle_steps_per_s"] / c["cpu"]["particle_steps_per_s"], 1)
+        if steps < c["steps"]:
+            # like for like: the GPU's time over the same prefix
+            g = c["gpu"]
+            c["cpu"]["note"] = (f"prefix: steps 1-{steps} of {c['steps']}; the GPU's first-5-step time "
+                                f"{g['ms_per_step_first5']} ms/step is its figure for the same phase")
+            c["gpu_over_cpu_same_prefix"] = round(c["cpu"]["ms_per_step"] / g["ms_per_step_first5"], 1)
+
+
+def cpu_collapsed(col):
+    """The oracle timed on the collapsed state the GPU step started from; the
+    GPU's step must equal the oracle's bit for bit."""
+    import numpy as np
+
+    from oracle import pyoracle
+
+    sc, pos, vel, t0, after = col.pop("_state")
+    threads = os.cpu_count() or 1
+    pyoracle.set_threads(threads)
+    o = pyoracle.Oracle()
+    t = time.perf_counter()
+    r = o.run(sc.params, pos, vel, t0, 1, dump=True)
+    dt = time.perf_counter() - t
+    col["cpu"] = {"ms_per_step": round(1e3 * dt, 2), "particle_steps_per_s": round(sc.count / dt, 1),
+                  "cores": threads, "kind": "port",
+                  "what": f"oracle/pbf_oracle.cpp, one step from the GPU's state after step {col['step'] - 1}, "
+                          f"OpenMP {threads} threads, {os.uname().machine}"}
+    col["cpu_neighbors_per_particle"] = round(float(r["neighbor_counts"].mean()), 2)
+    col["gpu_equals_cpu"] = bool(np.array_equal(after[0], r["pos"]) and np.array_equal(after[1], r["vel"]))
+    col["gpu_over_cpu"] = round(col["gpu"]["particle_steps_per_s"] / col["cpu"]["particle_steps_per_s"], 1)
+
+
+def gradient_checks(args):
+    """The oracle as checker of the differentiable scene's gradients (unit-mass
+    variant, where the GPU's FP32 adjoint stays in range): the GPU's dL/dv0,
+    dL/dx0 and dL/dc over 60 steps (checkpoints every 10) against the
+    oracle's FP64 adjoint of the same FP32 trajectory, and dL/dv0 at horizon
+    10 against central differences of the FP64 forward (step 1e-8, 4 random
+    directions). The full set (16 directions, horizons 10 and 20, dL/dc) is
+    tests/test_adjoint.py."""
+    import numpy as np
+    import torch
+
+    from fluidsimulator_gb300 import scenes
+    from fluidsimulator_gb300.solver import Solver
+    from oracle import pyoracle
+
+    threads = os.cpu_count() or 1
+    pyoracle.set_threads(threads)
+    target = np.array([1.5, 0.3, 1.0])
+    um = scenes.differentiable_block(32, seed=0, unit_mass=True)
+    n = um.count
+
+    def cot(x):
+        com = np.asarray(x, np.float64).mean(axis=1)
+        return np.repeat((2.0 * (com - target) / n)[:, None], n, axis=1)
+
+    s = Solver(torch.cuda.current_device())
+    s.configure([um.params], [n])
+    out = {}
+    for horizon in (10, args.adj_steps):
+        s.upload(um.pos, um.vel)
+        s.record(horizon, 10)
+        x, _ = s.download()
+        gx0, gv0, gc = s.backward(cot(x).astype(np.float32), np.zeros((3, n), np.float32))
+        o = pyoracle.Oracle()
+        states = [(um.pos, um.vel)]
+        for _ in range(horizon):
+            r = o.run(um.params, *states[-1], 0.0, 1)
+            states.append((r["pos"], r["vel"]))
+        g, gv, gcr = cot(states[-1][0]), np.zeros((3, n)), 0.0
+        for t in reversed(range(horizon)):
+            g, gv, c, _, _ = pyoracle.vjp(um.params, *states[t], g, gv, fwd32=True)
+            gcr += c
+        rel = lambda a, b: float(np.linalg.norm(np.ravel(a) - np.ravel(b)) / np.linalg.norm(np.ravel(b)))  # noqa: E731
+        e = {"grad_v0_norm": float(np.linalg.norm(gv0)),
+             "rel_err_vs_fp64_adjoint": {"dL_dv0": rel(gv0, gv), "dL_dx0": rel(gx0, g),
+                                         "dL_dc": abs(float(gc[0]) - gcr) / abs(gcr)}}
+        if horizon == 10:
+            o64 = pyoracle.Oracle(np.float64)
+            x64, v64 = um.pos.astype(np.float64), um.vel.astype(np.float64)
+
+            def loss(v0):
+                r = o64.run(um.params, x64, v0, 0.0, horizon)
+                return float(np.sum((r["pos"].mean(axis=1) - target) ** 2))
+
+            rng = np.random.default_rng(7)
+            rels = []
+            for _ in range(4):
+                d = rng.standard_normal((3, n))
+                d /= np.sqrt(np.mean(d * d))
+                fd = (loss(v64 + 1e-8 * d) - loss(v64 - 1e-8 * d)) / 2e-8
+                ad = float(np.sum(gv0.astype(np.float64) * d))
+                rels.append(abs(fd - ad) / max(abs(fd), abs(ad), 1e-30))
+            e["fd_fp64_step1e-8_rel_err_max"] = max(rels)
+            e["fd_directions"] = len(rels)
+        out[f"unit_mass_h{horizon}"] = e
+    s.close()
+    out["note"] = ("unit-mass variant (m = 1, rho0 = 1/sp^3); the scene as specified leaves the FP32 range after "
+                   "~10 steps (its gradient grows ~10^3 per step); FP64 adjoint = oracle reverse mode chained "
+                   "over the same FP32 trajectory")
+    return out
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return
@@ -804,7 +1023,12 @@ def main(argv=None):
     ap.add_argument("--no-output", action="store_true", help="skip the frame-output measurement")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--adj-steps", type=int, default=60)
-    ap.add_argument("--fd-dirs", type=int, default=16)
+    ap.add_argument("--no-configs", action="store_true", help="skip c1 / c2 and the collapsed-phase comparison")
+    ap.add_argument("--c1-steps", type=int, default=240)
+    ap.add_argument("--c2-steps", type=int, default=480)
+    ap.add_argument("--c2-cpu-steps", type=int, default=3, help="prefix of c2 the oracle runs on the host")
+    ap.add_argument("--collapsed-side", type=int, default=50)
+    ap.add_argument("--collapsed-at", type=int, default=21)
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per launch of the dominant kernel from an ncu capture")
     args = ap.parse_args(argv)

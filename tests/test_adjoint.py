@@ -347,7 +347,16 @@ def test_unit_mass_gradients_match_central_differences(cuda_lib, oracle_lib, hor
     16 float32 ulps of c), within 1e-3. A step sweep on this scene (1e-7,
     1e-8, 1e-9) agrees with the FP64 adjoint to 1e-5 at 1e-8 for both
     horizons; 1e-3 or 1e-4 already crosses neighbour cut-offs and plane
-    contacts."""
+    contacts.
+
+    The GPU linearises around the FP32 trajectory and the differences around
+    the FP64 one, so each directional derivative differs by the trajectories'
+    divergence as well (median ~1e-4). Its error is measured against the
+    gradient's RMS directional derivative |dL/dv0| (for directions of unit
+    RMS, E[(g . d)^2] = |g|^2): a direction nearly orthogonal to the gradient
+    has a small derivative whose own relative error says nothing about the
+    gradient's. The median of the per-direction relative errors is held to
+    1e-3 as well."""
     from fluidsimulator_gb300.solver import Solver
 
     um = scenes.differentiable_block(32, seed=0, unit_mass=True)
@@ -364,21 +373,26 @@ def test_unit_mass_gradients_match_central_differences(cuda_lib, oracle_lib, hor
         return float(np.sum((r["pos"].mean(axis=1) - _TARGET) ** 2))
 
     rng = np.random.default_rng(7)
-    rels = []
+    g64 = gv0.astype(np.float64)
+    gnorm = float(np.linalg.norm(g64))
+    rels, errs = [], []
     for _ in range(16):
         d = rng.standard_normal((3, n))
         d /= np.sqrt(np.mean(d * d))
         eps = 1e-8
         fd = (loss(v64 + eps * d) - loss(v64 - eps * d)) / (2 * eps)
-        ad = float(np.sum(gv0.astype(np.float64) * d))
+        ad = float(np.sum(g64 * d))
         rels.append(abs(fd - ad) / max(abs(fd), abs(ad), 1e-30))
+        errs.append(abs(fd - ad) / gnorm)
     c0 = np.float32(um.params.visc_c)
     ulp = np.nextafter(c0, np.float32(1.0), dtype=np.float32) - c0
     pp, pm = um.params.copy(), um.params.copy()
     pp.visc_c, pm.visc_c = float(np.float32(c0 + 16 * ulp)), float(np.float32(c0 - 16 * ulp))
     fd_c = (loss(v64, pp) - loss(v64, pm)) / (pp.visc_c - pm.visc_c)
     rel_c = abs(fd_c - gc[0]) / abs(fd_c)
-    print(f"unit mass, horizon {horizon}: dL/dv0 against FP64 central differences, 16 directions, "
-          f"max rel {max(rels):.2e}, median {np.median(rels):.2e}; dL/dc rel {rel_c:.2e}")
-    assert max(rels) < 1e-3
+    print(f"unit mass, horizon {horizon}: dL/dv0 against FP64 central differences, 16 directions: error "
+          f"/ |dL/dv0| max {max(errs):.2e}; per-direction relative max {max(rels):.2e}, median "
+          f"{np.median(rels):.2e}; dL/dc rel {rel_c:.2e}")
+    assert max(errs) < 1e-3
+    assert np.median(rels) < 1e-3
     assert rel_c < 1e-3

@@ -175,6 +175,47 @@ def test_full_size_double_dam_break_two_steps(cuda_lib, oracle_lib):
     assert np.float32(b["time"]) == np.float32(a["time"])
 
 
+def test_full_size_double_dam_break_into_the_collapse(cuda_lib, oracle_lib):
+    """The 250,000-particle double dam break over its first 10 steps, by which
+    it has collapsed to ~1,700 neighbours per particle (max ~6,300; the lists
+    regrow several times): every step's neighbour-pair total and maximum
+    equal the oracle's, the final keys, order, counts, rho, lambda, positions
+    and velocities equal the oracle's, and the run's mean and maximum density
+    error (rho/rho0 - 1, per step) are within 0.5 % of the CPU run's (they
+    are equal here, since every rho is)."""
+    sc = scenes.double_dam_break(50, seed=0)
+    steps = 10
+    a = oracle_lib.Oracle().run(sc.params, sc.pos, sc.vel, 0.0, steps, dump=True, records=True)
+    s = Solver(0)
+    s.configure([sc.params], [sc.count])
+    s.upload(sc.pos, sc.vel)
+    pairs, mx, dmean, dmax = [], [], [], []
+    for _ in range(steps):
+        s.step(1)
+        st = s.stats()
+        pairs.append(st["neighbor_pairs"])
+        mx.append(st["neighbor_max"])
+        e = s.read_debug(_capi.DEBUG_RHO).astype(np.float64) / np.float64(sc.params.density) - 1.0
+        dmean.append(e.mean())
+        dmax.append(e.max())
+    rec = {k: s.read_debug(w) for k, w in DEBUG.items()}
+    pos, vel = s.download()
+    regrows = s.stats()["regrows"]
+    s.close()
+    assert regrows >= 1 and mx[-1] > 1000
+    np.testing.assert_array_equal(pairs, a["neighbor_pairs"])
+    np.testing.assert_array_equal(mx, a["neighbor_max"])
+    for k in DEBUG:
+        np.testing.assert_array_equal(rec[k], a[k], err_msg=k)
+    np.testing.assert_array_equal(pos, a["pos"])
+    np.testing.assert_array_equal(vel, a["vel"])
+    # the stated floating-point bar, asserted beside the exact equality
+    np.testing.assert_allclose(dmean, a["density_mean"], rtol=5e-3)
+    np.testing.assert_allclose(dmax, a["density_max"], rtol=5e-3)
+    np.testing.assert_allclose(np.mean(dmean), np.mean(a["density_mean"]), rtol=5e-3)
+    assert max(dmax) <= 1.005 * max(a["density_max"])
+
+
 def test_full_size_differentiable_scene_20_steps(cuda_lib, oracle_lib):
     """The 32,768-particle differentiable scene (XSPH and s_corr, initial
     velocities N(0, 0.1^2)) at full size over 20 steps, by which it has
