@@ -420,11 +420,13 @@ def run_ours(args, world, rank, local):
         print(json.dumps(_finite(out)), flush=True)
 
 
-def _gpu_run(sc, steps, dev, stream, phases=5):
-    """Runs `steps` steps of a scene from its initial state on a fresh solver
-    (graphs on, default shapes), each step bracketed by CUDA events on the
-    solver's stream. Returns per-step ms, neighbours per particle per step and
-    the final state."""
+def _gpu_run(sc, steps, dev, stream, pair_budget=None):
+    """Runs up to `steps` steps of a scene from its initial state on a fresh
+    solver (graphs on, default shapes), each step bracketed by CUDA events on
+    the solver's stream; stops early once a step's lists hold more than
+    `pair_budget` entries (the next steps of a collapse grow them further).
+    Returns per-step ms, neighbours per particle per step, the final state and
+    the stats."""
     import torch
 
     from fluidsimulator_gb300.solver import Solver
@@ -441,7 +443,10 @@ def _gpu_run(sc, steps, dev, stream, phases=5):
         ev[1].record(stream)
         s.synchronize()
         ms.append(ev[0].elapsed_time(ev[1]))
-        nbr.append(s.stats()["neighbor_pairs"] / sc.count)
+        pairs = s.stats()["neighbor_pairs"]
+        nbr.append(pairs / sc.count)
+        if pair_budget and pairs > pair_budget:
+            break
     pos, vel = s.download()
     st = s.stats()
     s.close()
@@ -453,22 +458,30 @@ def run_configs(args, dev, stream):
     each run over its full length on the GPU: c1, the plain dam break (4,096
     particles, 16^3 lattice, spacing 0.05, h 0.1, flags off, 240 steps), and
     c2, the double dam break (two 50^3 blocks, 250,000 particles, spacing
-    0.025, h 0.05, all three flags, 480 steps). The CPU side (cpu_configs)
-    times the oracle over the whole of c1 and a stated prefix of c2 on the
-    host cores and checks the GPU's state after that prefix bit for bit."""
+    0.025, h 0.05, all three flags, 480 steps). c2 collapses completely
+    (with m = rho0 sp^3 the Jacobi update scales by 1/m = 64, SURVEY-style
+    collapse): each block's particles end up within h of nearly all others,
+    ~125,000 neighbours each, so its lists would grow past 87e9 entries
+    (~350 GB, the reference's CSR alike). Its GPU run stops once a step's
+    lists pass `--c2-pair-budget` entries and reports the steps it covered.
+    The CPU side (cpu_configs) times the oracle over the whole of c1 and a
+    stated prefix of c2 on the host cores and checks the GPU's state after
+    that prefix bit for bit."""
     from fluidsimulator_gb300 import scenes
 
     out = {}
-    for key, sc, steps in (("c1_dam_break_4096", scenes.dam_break(16, seed=0), args.c1_steps),
-                           ("c2_double_dam_break_250k", scenes.double_dam_break(50, seed=0), args.c2_steps)):
+    for key, sc, steps, budget in (
+            ("c1_dam_break_4096", scenes.dam_break(16, seed=0), args.c1_steps, None),
+            ("c2_double_dam_break_250k", scenes.double_dam_break(50, seed=0), args.c2_steps, args.c2_pair_budget)):
         if steps <= 0:
             continue
         _gpu_run(sc, min(steps, 3), dev, stream)  # warm-up: kernels loaded, graphs captured once
-        ms, nbr, pos, vel, st = _gpu_run(sc, steps, dev, stream)
+        ms, nbr, pos, vel, st = _gpu_run(sc, steps, dev, stream, budget)
+        ran = len(ms)
         total = sum(ms)
-        out[key] = {"particles": sc.count, "steps": steps,
-                    "gpu": {"ms_total": round(total, 3), "ms_per_step": round(total / steps, 4),
-                            "particle_steps_per_s": round(sc.count * steps / (total / 1e3), 1),
+        out[key] = {"particles": sc.count, "steps": ran, "steps_of_config": steps,
+                    "gpu": {"ms_total": round(total, 3), "ms_per_step": round(total / ran, 4),
+                            "particle_steps_per_s": round(sc.count * ran / (total / 1e3), 1),
                             "ms_per_step_first5": round(statistics.mean(ms[:5]), 4),
                             "ms_per_step_last5": round(statistics.mean(ms[-5:]), 4),
                             "neighbors_per_particle_step1": round(nbr[0], 2),
@@ -476,7 +489,10 @@ def run_configs(args, dev, stream):
                             "regrows": st["regrows"],
                             "timing": "per-step CUDA events on the solver's stream, graphs on, default shapes, "
                                       "whole run from the initial state"},
-                    "_scene": sc}
+                    "_scene": sc, "_ms": ms}
+        if ran < steps:
+            out[key]["stopped"] = (f"after step {ran}: {nbr[-1]:.0f} neighbours per particle, lists past the "
+                                   f"{budget:.3g}-entry budget (a complete collapse needs ~87e9)")
     return out
 
 
@@ -845,7 +861,9 @@ def cpu_configs(configs, args):
     pyoracle.set_threads(threads)
     for key, c in configs.items():
         sc = c.pop("_scene")
+        gms = c.pop("_ms")
         steps = c["steps"] if key.startswith("c1") else min(c["steps"], args.c2_cpu_steps)
+        steps = min(steps, c["steps"])
         o = pyoracle.Oracle()
         t0 = time.perf_counter()
         r = o.run(sc.params, sc.pos, sc.vel, 0.0, steps, records=True)
@@ -862,13 +880,12 @@ def cpu_configs(configs, args):
                     "what": f"oracle/pbf_oracle.cpp (restatement of core/src/core.cpp:119-615), steps 1-{steps} "
                             f"from the initial state, OpenMP {threads} threads, {os.uname().machine}"}
         c["gpu_equals_cpu_after_cpu_steps"] = bool(np.array_equal(pos, r["pos"]) and np.array_equal(vel, r["vel"]))
-        c["gpu_over_cpu"] = round(c["gpu"]["particle_steps_per_s"] / c["cpu"]["particle_steps_per_s"], 1)
-        if steps < c["steps"]:
-            # like for like: the GPU's time over the same prefix
-            g = c["gpu"]
-            c["cpu"]["note"] = (f"prefix: steps 1-{steps} of {c['steps']}; the GPU's first-5-step time "
-                                f"{g['ms_per_step_first5']} ms/step is its figure for the same phase")
-            c["gpu_over_cpu_same_prefix"] = round(c["cpu"]["ms_per_step"] / g["ms_per_step_first5"], 1)
+        # like for like: the GPU's own time over the steps the CPU ran
+        same = statistics.mean(gms[:steps])
+        c["gpu_ms_per_step_same_steps"] = round(same, 4)
+        c["gpu_over_cpu_same_steps"] = round(c["cpu"]["ms_per_step"] / same, 1)
+        if steps < c["steps_of_config"]:
+            c["cpu"]["note"] = f"prefix: steps 1-{steps} of {c['steps_of_config']}"
 
 
 def cpu_collapsed(col):
@@ -1027,6 +1044,8 @@ def main(argv=None):
     ap.add_argument("--c1-steps", type=int, default=240)
     ap.add_argument("--c2-steps", type=int, default=480)
     ap.add_argument("--c2-cpu-steps", type=int, default=3, help="prefix of c2 the oracle runs on the host")
+    ap.add_argument("--c2-pair-budget", type=float, default=3e9,
+                    help="stop c2 once a step's lists hold more entries than this")
     ap.add_argument("--collapsed-side", type=int, default=50)
     ap.add_argument("--collapsed-at", type=int, default=21)
     ap.add_argument("--traffic", type=float, default=None,

@@ -202,6 +202,65 @@ __device__ __forceinline__ void restitution(const SceneConst& c, float px, float
   }
 }
 
+// Displacement bound of the list passes (the "skin" argument of molecular
+// dynamics neighbour lists). If every list entry of particle i was at least
+// `reach` away at the positions of the last lambda pass, i has moved at most
+// d_self since and every particle of its scene at most d_scene, then no entry
+// is closer than reach - d_self - d_scene now; when that exceeds h, no entry
+// can pass the pass's r2 < h2 test and its walk adds nothing (the reference's
+// own loop adds only within-h terms, or poly6 = 0 beyond h), so the walk is
+// skipped and the result is the same bits. Every quantity is rounded the
+// conservative way: reach is the square root of the smallest r2 seen rounded
+// down and shrunk by 2^-20 (an r2 computed with round-to-nearest operations is
+// within ~3e-7 of the exact squared distance of the float positions),
+// displacements are rounded up and grown by 2^-20, the subtractions round
+// down, and the bound must reach h grown by 2^-20, above which every
+// round-to-nearest r2 exceeds h2 = RN(h * h).
+constexpr float kReachShrink = 1.0f - 9.5367431640625e-07f;  // 1 - 2^-20
+constexpr float kReachGrow = 1.0f + 9.5367431640625e-07f;    // 1 + 2^-20
+
+__device__ __forceinline__ float reach_from_r2(float r2min) {  // +inf for an empty list
+  return __fmul_rd(__fsqrt_rd(r2min), kReachShrink);
+}
+
+__device__ __forceinline__ float moved_by(float dx, float dy, float dz) {
+  return __fmul_ru(__fsqrt_ru(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz))),
+                   kReachGrow);
+}
+
+// True when no list entry of a particle with this reach, own displacement and
+// scene displacement can be within h; `bound` is then a lower bound on its
+// distance to every entry now (NaN anywhere gives false).
+__device__ __forceinline__ bool beyond_reach(const SceneConst& c, float reach, float d_self, float d_scene,
+                                             float& bound) {
+  bound = __fsub_rd(__fsub_rd(reach, d_self), d_scene);
+  return bound >= __fmul_ru(c.h, kReachGrow);
+}
+
+// Counts the warp's skipped walks into the status word (statistics only).
+__device__ __forceinline__ void count_skipped(DevStatus* st, bool skip) {
+  const unsigned mask = __activemask();
+  const unsigned b = __ballot_sync(mask, skip);
+  if (b && (threadIdx.x & 31) == __ffs(mask) - 1) atomicAdd(&st->skipped, static_cast<unsigned long long>(__popc(b)));
+}
+
+// Largest displacement of each scene in one delta pass: a warp maximum and
+// one atomic when the warp's lanes share a scene, else one atomic per lane.
+// Called by the lanes of a warp that are still running (after their list
+// walks have reconverged). Non-negative float bits order as unsigned ints.
+__device__ __forceinline__ void record_moved(unsigned* moved, int scene, float d) {
+  const unsigned mask = __activemask();
+  const unsigned bits = __float_as_uint(d);
+  const int leader = __ffs(mask) - 1;
+  const int s0 = __shfl_sync(mask, scene, leader);
+  if (__all_sync(mask, scene == s0)) {
+    const unsigned m = __reduce_max_sync(mask, bits);
+    if ((threadIdx.x & 31) == leader) atomicMax(moved + s0, m);
+  } else {
+    atomicMax(moved + scene, bits);
+  }
+}
+
 __device__ __forceinline__ uint32_t cell_key(const GridInfo& g, int cx, int cy, int cz) {
   const long long l = (static_cast<long long>(cx - g.minx) * g.dimy + (cy - g.miny)) * g.dimz + (cz - g.minz);
   return g.base + static_cast<uint32_t>(l);
@@ -306,6 +365,7 @@ __global__ void __launch_bounds__(kBlock) k_grid_setup(StepArgs a, int radix_bit
   st->started = st->started + 1;
   st->pairs = 0ull;
   st->cursor = 0ull;
+  st->skipped = 0ull;
   st->nbr_max = 0;
   unsigned long long total = 0;
   bool domain = false;
@@ -721,6 +781,7 @@ __device__ __forceinline__ float finish_lambda(const SceneConst& c, float rho, f
 // Per-neighbour density / gradient terms (core.cpp:300-316).
 struct LambdaAcc {
   float rho = 0.0f, gsx = 0.0f, gsy = 0.0f, gsz = 0.0f, sum_g2 = 0.0f;
+  float r2min = INFINITY;  // smallest r2 of the walk (the displacement bound's reach)
   __device__ __forceinline__ void add(const SceneConst& c, float dx, float dy, float dz, float r2) {
     rho += poly6(c, r2);
     const float gf = spiky(c, clamped_r(c, r2));
@@ -740,6 +801,7 @@ struct LambdaAcc {
                                                const float2 pz, const float4 qa, const float4 qb) {
     const float2 nz = f2(c.neg_zero);
     const PairGeom g = pair_geom(px, py, pz, qa, qb, nz);
+    r2min = fminf(r2min, fminf(g.r2.x, g.r2.y));
     const bool oka = g.r2.x < c.h2, okb = g.r2.y < c.h2;
     if (!oka && !okb) return 0u;
     const float2 w = poly6_pair(c, g.r2, nz);
@@ -1037,26 +1099,47 @@ __device__ __forceinline__ void for_each_live_then(const int* __restrict__ list,
 // kLiveOut: record the live bits of these positions for the delta pass
 // (iterations after the first; the first runs at the positions the lists
 // were built from, where every entry is live).
+//
+// Every iteration's pass also leaves reach[i] (the displacement bound's lower
+// bound on the distance to the nearest list entry at these positions) and
+// clears the scene displacement words its delta pass will fill. Iterations
+// after the first (kLiveOut) first try the bound against the previous
+// iteration's positions (p[in ^ 1], which the previous delta pass read) and
+// skip the walk when it proves every entry beyond h.
 template <int U, bool kLiveOut>
 __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_lambda(StepArgs a, int in) {
   if (failed(a.status)) return;
+  if (blockIdx.x == 0)
+    for (int t = threadIdx.x; t < a.scenes; t += blockDim.x) a.moved[in * a.scenes + t] = 0u;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   const float4* __restrict__ pos = a.p[in];
   const float4 p = pos[i];
-  const SceneConst& c = a.sc[__float_as_int(p.w)];
+  const int scene = __float_as_int(p.w);
+  const SceneConst& c = a.sc[scene];
   const int n = a.cnt[i];
   const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
   const float h2 = c.h2;
   LambdaAcc acc;
+  bool skip = false;
+  float bound = 0.0f;
+  if constexpr (kLiveOut) {
+    const float4 q = a.p[in ^ 1][i];
+    skip = beyond_reach(c, a.reach[i], moved_by(p.x - q.x, p.y - q.y, p.z - q.z),
+                        __uint_as_float(a.moved[(in ^ 1) * a.scenes + scene]), bound);
+    count_skipped(a.status, skip);
+  }
   auto one = [&](const float4 q) {
     const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
     const float r2 = dist2(dx, dy, dz);
+    acc.r2min = fminf(acc.r2min, r2);
     if (r2 < h2) acc.add(c, dx, dy, dz, r2);
     return r2 < h2;
   };
   auto load = [&](int j) { return __ldg(pos + j); };
-  if constexpr (U == 1) {
+  if (skip) {
+    if constexpr (kLiveOut) store_live(a.live, a.n, i, 0ull);
+  } else if constexpr (U == 1) {
     if constexpr (kLiveOut) {
       unsigned long long bits = 0ull;
       int k = 0;
@@ -1079,6 +1162,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_lambda(StepA
   a.lambda[i] = lam;
   a.rho[i] = rho;
   a.pl[i] = make_float4(p.x, p.y, p.z, lam);
+  a.reach[i] = skip ? bound : reach_from_r2(acc.r2min);
 }
 
 // Commit v = (p - x)/dt, x = p (core.cpp:414-421); restitution when this is
@@ -1141,7 +1225,12 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_delta(StepAr
       kLiveIn ? (static_cast<unsigned long long>(a.live[i]) | (static_cast<unsigned long long>(a.live[a.n + i]) << 32))
               : 0ull;
   const float4 dead = make_float4(INFINITY, p.y, p.z, 0.0f);
-  if constexpr (U == 1) {
+  // The lambda pass of this iteration (same positions) left reach[i]: at or
+  // beyond h (grown as in beyond_reach) no entry is within h, so nothing past
+  // the live-bit head can add either.
+  const bool none = kLiveIn && a.reach[i] >= __fmul_ru(c.h, kReachGrow);
+  if (none) {
+  } else if constexpr (U == 1) {
     if constexpr (kLiveIn) for_each_live_then<1>(list, n, live, load, dead, one, one);
     else for_each_neighbor<1>(list, n, load, one);
   } else {
@@ -1207,6 +1296,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_delta(StepAr
     az = qz - p.z;
   }
   const float nx = p.x + ax, ny = p.y + ay, nz = p.z + az;  // core.cpp:404-406
+  record_moved(a.moved + in * a.scenes, __float_as_int(p.w), moved_by(nx - p.x, ny - p.y, nz - p.z));
   if (!last) {
     a.p[in ^ 1][i] = make_float4(nx, ny, nz, p.w);
   } else {
@@ -1227,8 +1317,13 @@ __global__ void __launch_bounds__(kMaxBlock) k_commit(StepArgs a, int to_v2, int
 // {x, m / rho} records xr, writes v.
 // kLiveOut: record the live bits of the committed positions for the
 // vorticity passes (all ones where this scene skips XSPH).
+// bound_par: parity of the step's last Jacobi iteration (-1 without
+// iterations): its lambda pass left reach[] at the positions p[bound_par],
+// and its delta pass the scene displacements, so the displacement bound can
+// skip walks whose entries are all beyond h at the committed positions.
 template <int U, bool kLiveOut>
-__global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_xsph(StepArgs a, int rest, const float4* xr) {
+__global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_xsph(StepArgs a, int rest, const float4* xr,
+                                                                          int bound_par) {
   if (failed(a.status)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
@@ -1236,10 +1331,20 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_xsph(StepArg
   const float4* __restrict__ vs = a.v2;
   const float4 xi = xs[i];
   const float4 vi = vs[i];
-  const SceneConst& c = a.sc[__float_as_int(vi.w)];
+  const int scene = __float_as_int(vi.w);
+  const SceneConst& c = a.sc[scene];
   float vx = vi.x, vy = vi.y, vz = vi.z;
   unsigned long long bits = ~0ull;
-  if (c.xsph_on) {
+  bool skip = false;
+  if (c.xsph_on && bound_par >= 0) {
+    const float4 q = a.p[bound_par][i];
+    float bound;
+    skip = beyond_reach(c, a.reach[i], moved_by(xi.x - q.x, xi.y - q.y, xi.z - q.z),
+                        __uint_as_float(a.moved[bound_par * a.scenes + scene]), bound);
+    if (skip) bits = 0ull;
+  }
+  if (bound_par >= 0) count_skipped(a.status, skip);
+  if (c.xsph_on && !skip) {
     const int n = a.cnt[i];
     const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
     const float h2 = c.h2;
@@ -1604,12 +1709,13 @@ void launch_lambda(int u, int grid, int block, cudaStream_t st, const StepArgs& 
 }
 
 template <bool kLiveOut>
-void launch_xsph(int u, int grid, int block, cudaStream_t st, const StepArgs& a, int rest, const float4* xr) {
+void launch_xsph(int u, int grid, int block, cudaStream_t st, const StepArgs& a, int rest, const float4* xr,
+                 int bound_par) {
   switch (u) {
-    case 1: k_xsph<1, kLiveOut><<<grid, block, 0, st>>>(a, rest, xr); break;
-    case 2: k_xsph<2, kLiveOut><<<grid, block, 0, st>>>(a, rest, xr); break;
-    case 8: k_xsph<8, kLiveOut><<<grid, block, 0, st>>>(a, rest, xr); break;
-    default: k_xsph<4, kLiveOut><<<grid, block, 0, st>>>(a, rest, xr); break;
+    case 1: k_xsph<1, kLiveOut><<<grid, block, 0, st>>>(a, rest, xr, bound_par); break;
+    case 2: k_xsph<2, kLiveOut><<<grid, block, 0, st>>>(a, rest, xr, bound_par); break;
+    case 8: k_xsph<8, kLiveOut><<<grid, block, 0, st>>>(a, rest, xr, bound_par); break;
+    default: k_xsph<4, kLiveOut><<<grid, block, 0, st>>>(a, rest, xr, bound_par); break;
   }
 }
 
@@ -1733,8 +1839,11 @@ cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t s
     // The committing pass left {x, m / rho} in the p buffer it did not use.
     const float4* xr = a.p[plan.iterations == 0 ? 1 : (plan.iterations & 1)];
     const int rest = (!plan.vorticity && plan.restitution) ? 1 : 0;
-    if (plan.vorticity) launch_xsph<true>(plan.unroll[FLUID_KERNEL_XSPH], blocks_for(a.n, b), b, st, a, rest, xr);
-    else launch_xsph<false>(plan.unroll[FLUID_KERNEL_XSPH], blocks_for(a.n, b), b, st, a, rest, xr);
+    const int bound_par = plan.iterations > 0 ? ((plan.iterations - 1) & 1) : -1;
+    if (plan.vorticity)
+      launch_xsph<true>(plan.unroll[FLUID_KERNEL_XSPH], blocks_for(a.n, b), b, st, a, rest, xr, bound_par);
+    else
+      launch_xsph<false>(plan.unroll[FLUID_KERNEL_XSPH], blocks_for(a.n, b), b, st, a, rest, xr, bound_par);
     m.mark(FLUID_KERNEL_XSPH);
   }
   if (plan.vorticity) {

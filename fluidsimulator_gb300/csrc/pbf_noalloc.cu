@@ -50,7 +50,9 @@ constexpr size_t kX0 = 0, kX1 = kX0 + kF4, kV0 = kX1 + kF4, kV1 = kV0 + kF4;
 constexpr size_t kP0 = kV1 + kF4, kP1 = kP0 + kF4, kV2 = kP1 + kF4, kOmega = kV2 + kF4;
 constexpr size_t kPl = kOmega + kF4;
 constexpr size_t kLive = kPl + kF4;
-constexpr size_t kSlot0 = kLive + up(2 * sizeof(uint32_t) * kMaxN), kSlot1 = kSlot0 + kI32, kRho0 = kSlot1 + kI32, kRho1 = kRho0 + kI32;
+constexpr size_t kReach = kLive + up(2 * sizeof(uint32_t) * kMaxN);
+constexpr size_t kMoved = kReach + up(sizeof(float) * kMaxN);
+constexpr size_t kSlot0 = kMoved + up(2 * sizeof(unsigned)), kSlot1 = kSlot0 + kI32, kRho0 = kSlot1 + kI32, kRho1 = kRho0 + kI32;
 constexpr size_t kLambda = kRho1 + kI32, kKeys0 = kLambda + kI32, kKeys1 = kKeys0 + kI32;
 constexpr size_t kVals0 = kKeys1 + kI32, kVals1 = kVals0 + kI32, kCnt = kVals1 + kI32;
 constexpr size_t kDepth = kCnt + kI32, kWbase = kDepth + up(sizeof(int) * (kMaxWarps + 1));
@@ -110,6 +112,8 @@ StepArgs carve(unsigned char* b, int n) {
   a.omega = at<float4>(b, kOmega);
   a.pl = at<float4>(b, kPl);
   a.live = at<uint32_t>(b, kLive);
+  a.reach = at<float>(b, kReach);
+  a.moved = at<unsigned>(b, kMoved);
   a.lambda = at<float>(b, kLambda);
   a.rho = at<float>(b, kRho1);
   a.keys[0] = at<uint32_t>(b, kKeys0);

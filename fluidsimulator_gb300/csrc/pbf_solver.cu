@@ -288,6 +288,8 @@ class Solver {
     ok &= omega_.alloc(np) == cudaSuccess;
     ok &= pl_.alloc(np) == cudaSuccess;
     ok &= live_.alloc(2 * np) == cudaSuccess;
+    ok &= reach_.alloc(np) == cudaSuccess;
+    ok &= moved_.alloc(2 * static_cast<size_t>(S_)) == cudaSuccess;
     ok &= lambda_.alloc(np) == cudaSuccess;
     ok &= cnt_.alloc(np) == cudaSuccess;
     ok &= depth_.alloc(static_cast<size_t>(warps_) + 1) == cudaSuccess;
@@ -308,6 +310,7 @@ class Solver {
       return fail(FLUID_ERR_OUT_OF_MEMORY, "device allocation failed");
     cudaMemsetAsync(table_.p, 0, table_.n * sizeof(int2), stream_);
     cudaMemsetAsync(look_.p, 0, look_.n * sizeof(unsigned long long), stream_);  // tag 0: never current
+    cudaMemsetAsync(moved_.p, 0, moved_.n * sizeof(unsigned), stream_);
     if (cudaMemcpyAsync(sc_.p, sc_host_.data(), S_ * sizeof(SceneConst), cudaMemcpyHostToDevice, stream_) !=
         cudaSuccess)
       return cuda_fail("upload scene constants");
@@ -507,6 +510,7 @@ class Solver {
       pending_ = 0;
       last_pairs_ = static_cast<long long>(st.pairs);
       last_max_ = st.nbr_max;
+      last_skipped_ = static_cast<long long>(st.skipped);
       last_cells_ = static_cast<int>(st.total_cells);
       last_npass_ = st.npass;
       if (enqueue_reset(status_.p, bmin_.p, bmax_.p, S_, stream_) != cudaSuccess) return cuda_fail("reset");
@@ -902,6 +906,7 @@ class Solver {
     out->grid_capacity = grid_cap_;
     out->regrows = regrows_;
     out->kernel_launches = launches_;
+    out->skipped_walks = last_skipped_;
     return FLUID_OK;
   }
 
@@ -1047,6 +1052,8 @@ class Solver {
     a.vals[1] = vals_[1].p;
     a.look = look_.p;
     a.live = live_.p;
+    a.reach = reach_.p;
+    a.moved = moved_.p;
     a.radix_next = radix_next_.p;
     a.digit_total = digit_total_.p;
     a.table = table_.p;
@@ -1297,6 +1304,7 @@ class Solver {
                       cudaMemcpyDeviceToDevice, stream_);
       last_pairs_ = static_cast<long long>(st.pairs);
       last_max_ = st.nbr_max;
+      last_skipped_ = static_cast<long long>(st.skipped);
       last_cells_ = static_cast<int>(st.total_cells);
       last_npass_ = st.npass;
       commit_steps(1);
@@ -1399,6 +1407,7 @@ class Solver {
   int parity_ = 0, pending_ = 0;
   long long steps_ = 0, regrows_ = 0, launches_ = 0, launches_per_step_ = 0;
   long long last_pairs_ = 0;
+  long long last_skipped_ = 0;
   int last_max_ = 0, last_cells_ = 0, last_npass_ = 0;
   DBuf<float4> x_[2], v_[2], p_[2], v2_, omega_, pl_;
   DBuf<int> slot_[2], vals_[2], cnt_, depth_, ovf_, nbr_, bmin_, bmax_;
@@ -1406,6 +1415,8 @@ class Solver {
   DBuf<uint32_t> keys_[2], digit_total_;
   DBuf<unsigned long long> look_;
   DBuf<uint32_t> live_;
+  DBuf<float> reach_;
+  DBuf<unsigned> moved_;
   DBuf<int> radix_next_;
   DBuf<long long> wbase_;
   DBuf<int2> table_;

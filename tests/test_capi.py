@@ -38,7 +38,7 @@ def test_params_default_matches_mirror(cuda_lib):
 
 
 def test_version(cuda_lib):
-    assert cuda_lib.fluid_gb300_version() == 2
+    assert cuda_lib.fluid_gb300_version() == 3
 
 
 def test_struct_layout_matches_header(tmp_path):
