@@ -45,6 +45,7 @@ KERNEL_NAMES = ["k_bounds", "k_grid_setup", "k_keys", "k_radix_digits", "k_radix
                 "k_reorder", "k_nbr_build", "k_nbr_overflow", "k_lambda", "k_delta", "k_commit",
                 "k_xsph", "k_omega", "k_eta"]
 TUNABLE = ("k_nbr_build", "k_nbr_overflow", "k_lambda", "k_delta", "k_xsph", "k_omega", "k_eta")
+LIST_PASSES = ("k_lambda", "k_delta", "k_xsph", "k_omega", "k_eta")  # may take several lanes per particle
 
 
 class FluidParams(ctypes.Structure):
@@ -187,6 +188,10 @@ def _declare(lib):
     lib.fluid_solver_get_tuning.restype = c_int
     lib.fluid_solver_set_tuning.argtypes = [c_void_p, POINTER(c_int32), POINTER(c_int32), c_int32]
     lib.fluid_solver_set_tuning.restype = c_int
+    lib.fluid_solver_get_lanes.argtypes = [c_void_p, POINTER(c_int32), c_int32]
+    lib.fluid_solver_get_lanes.restype = c_int
+    lib.fluid_solver_set_lanes.argtypes = [c_void_p, POINTER(c_int32), c_int32]
+    lib.fluid_solver_set_lanes.restype = c_int
     lib.fluid_solver_get_sort_bits.argtypes = [c_void_p, POINTER(c_int32)]
     lib.fluid_solver_get_sort_bits.restype = c_int
     lib.fluid_solver_set_sort_bits.argtypes = [c_void_p, c_int32]

@@ -109,11 +109,12 @@ struct StepArgs {
   // Displacement bound of the Jacobi passes (a pass may skip a list it can
   // prove holds no entry within h): reach[i] is a lower bound on the
   // distance from particle i to its nearest list entry at the positions of
-  // the last lambda pass; moved[(k & 1) * scenes + s] the largest distance
-  // (rounded up) any particle of scene s moved in the delta pass of
-  // iteration k, as float bits.
+  // the last lambda pass; moved holds two parities (iteration k uses k & 1)
+  // of moved_mask + 1 slots: the largest distance (rounded up, float bits)
+  // any particle of a bin of build cells moved in that iteration's delta pass.
   float* reach;
   unsigned* moved;
+  unsigned moved_mask;
   float* lambda;
   float* rho;
   uint32_t* keys[2];

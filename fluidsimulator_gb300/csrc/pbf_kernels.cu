@@ -202,13 +202,17 @@ __device__ __forceinline__ void restitution(const SceneConst& c, float px, float
   }
 }
 
+__device__ __forceinline__ const uint32_t* sorted_keys(const StepArgs& a, int npass) {
+  return a.keys[npass & 1];
+}
+
 // Displacement bound of the list passes (the "skin" argument of molecular
 // dynamics neighbour lists). If every list entry of particle i was at least
 // `reach` away at the positions of the last lambda pass, i has moved at most
-// d_self since and every particle of its scene at most d_scene, then no entry
-// is closer than reach - d_self - d_scene now; when that exceeds h, no entry
-// can pass the pass's r2 < h2 test and its walk adds nothing (the reference's
-// own loop adds only within-h terms, or poly6 = 0 beyond h), so the walk is
+// d_self since and every listed neighbour at most d_nb, then no entry is
+// closer than reach - d_self - d_nb now; when that exceeds h, no entry can
+// pass the pass's r2 < h2 test and its walk adds nothing (the reference's own
+// loop adds only within-h terms, or poly6 = 0 beyond h), so the walk is
 // skipped and the result is the same bits. Every quantity is rounded the
 // conservative way: reach is the square root of the smallest r2 seen rounded
 // down and shrunk by 2^-20 (an r2 computed with round-to-nearest operations is
@@ -216,6 +220,16 @@ __device__ __forceinline__ void restitution(const SceneConst& c, float px, float
 // displacements are rounded up and grown by 2^-20, the subtractions round
 // down, and the bound must reach h grown by 2^-20, above which every
 // round-to-nearest r2 exceeds h2 = RN(h * h).
+//
+// d_nb comes from a table the delta pass fills: each particle adds its
+// displacement (atomic max) to the slot of its bin, the 2x2x2 block of grid
+// cells around the cell it was listed in (the step's build cell, decoded from
+// its sorted key), slots addressed by a hash of (scene, bin). A listed
+// neighbour's build cell is within one cell of the particle's on every axis,
+// so its bin is one of the 8 bins those 3x3x3 cells touch, and the largest of
+// their slots bounds every neighbour's displacement; two bins sharing a slot
+// only raise it. Lists from all pairs (use_uniform_grid = 0) span the scene
+// and take no bound.
 constexpr float kReachShrink = 1.0f - 9.5367431640625e-07f;  // 1 - 2^-20
 constexpr float kReachGrow = 1.0f + 9.5367431640625e-07f;    // 1 + 2^-20
 
@@ -229,12 +243,66 @@ __device__ __forceinline__ float moved_by(float dx, float dy, float dz) {
 }
 
 // True when no list entry of a particle with this reach, own displacement and
-// scene displacement can be within h; `bound` is then a lower bound on its
-// distance to every entry now (NaN anywhere gives false).
-__device__ __forceinline__ bool beyond_reach(const SceneConst& c, float reach, float d_self, float d_scene,
+// neighbours' displacement can be within h; `bound` is then a lower bound on
+// its distance to every entry now (NaN anywhere gives false).
+__device__ __forceinline__ bool beyond_reach(const SceneConst& c, float reach, float d_self, float d_nb,
                                              float& bound) {
-  bound = __fsub_rd(__fsub_rd(reach, d_self), d_scene);
+  bound = __fsub_rd(__fsub_rd(reach, d_self), d_nb);
   return bound >= __fmul_ru(c.h, kReachGrow);
+}
+
+// Build cell (the cell whose 27-cell neighbourhood the step's lists were built
+// from) of the particle at sorted slot i, decoded from its sorted key.
+__device__ __forceinline__ void build_cell(const uint32_t* ks, const GridInfo& g, int i, int& cx, int& cy, int& cz) {
+  const uint32_t l = ks[i] - g.base;
+  const uint32_t yz = static_cast<uint32_t>(g.dimy) * static_cast<uint32_t>(g.dimz);
+  cx = g.minx + static_cast<int>(l / yz);
+  const uint32_t r = l % yz;
+  cy = g.miny + static_cast<int>(r / static_cast<uint32_t>(g.dimz));
+  cz = g.minz + static_cast<int>(r % static_cast<uint32_t>(g.dimz));
+}
+
+// Slot of bin (bx, by, bz) of a scene in the displacement table (mask + 1
+// slots, a power of two).
+__device__ __forceinline__ uint32_t moved_slot(int scene, int bx, int by, int bz, uint32_t mask) {
+  uint32_t h = static_cast<uint32_t>(scene) * 0x9E3779B1u ^ static_cast<uint32_t>(bx) * 0x85EBCA77u ^
+               static_cast<uint32_t>(by) * 0xC2B2AE3Du ^ static_cast<uint32_t>(bz) * 0x27D4EB2Fu;
+  h ^= h >> 15;
+  h *= 0x2C1B3C6Du;
+  h ^= h >> 12;
+  return h & mask;
+}
+
+// Largest displacement recorded in the 8 bins around build cell (cx, cy, cz).
+__device__ __forceinline__ float moved_near(const unsigned* table, uint32_t mask, int scene, int cx, int cy,
+                                            int cz) {
+  unsigned m = 0u;
+  const int bx = (cx - 1) >> 1, by = (cy - 1) >> 1, bz = (cz - 1) >> 1;
+#pragma unroll
+  for (int t = 0; t < 8; ++t)
+    m = max(m, table[moved_slot(scene, bx + (t & 1), by + ((t >> 1) & 1), bz + (t >> 2), mask)]);
+  return __uint_as_float(m);
+}
+
+// Adds displacement d of a particle in build cell (cx, cy, cz) to its bin's
+// slot: one atomic max per distinct slot of the warp's running lanes (after
+// their list walks have reconverged). Non-negative float bits order as
+// unsigned ints.
+__device__ __forceinline__ void record_moved(unsigned* table, uint32_t mask, int scene, int cx, int cy, int cz,
+                                             float d) {
+  const unsigned active = __activemask();
+  const uint32_t slot = moved_slot(scene, cx >> 1, cy >> 1, cz >> 1, mask);
+  const unsigned bits = __float_as_uint(d);
+  unsigned todo = active;
+  while (todo) {
+    const int leader = __ffs(todo) - 1;
+    const uint32_t s0 = __shfl_sync(active, slot, leader);
+    const bool mine = slot == s0;
+    const unsigned peers = __ballot_sync(active, mine);
+    const unsigned m = __reduce_max_sync(active, mine ? bits : 0u);
+    if ((threadIdx.x & 31) == leader) atomicMax(table + s0, m);
+    todo &= ~peers;
+  }
 }
 
 // Counts the warp's skipped walks into the status word (statistics only).
@@ -244,30 +312,33 @@ __device__ __forceinline__ void count_skipped(DevStatus* st, bool skip) {
   if (b && (threadIdx.x & 31) == __ffs(mask) - 1) atomicAdd(&st->skipped, static_cast<unsigned long long>(__popc(b)));
 }
 
-// Largest displacement of each scene in one delta pass: a warp maximum and
-// one atomic when the warp's lanes share a scene, else one atomic per lane.
-// Called by the lanes of a warp that are still running (after their list
-// walks have reconverged). Non-negative float bits order as unsigned ints.
-__device__ __forceinline__ void record_moved(unsigned* moved, int scene, float d) {
-  const unsigned mask = __activemask();
-  const unsigned bits = __float_as_uint(d);
-  const int leader = __ffs(mask) - 1;
-  const int s0 = __shfl_sync(mask, scene, leader);
-  if (__all_sync(mask, scene == s0)) {
-    const unsigned m = __reduce_max_sync(mask, bits);
-    if ((threadIdx.x & 31) == leader) atomicMax(moved + s0, m);
-  } else {
-    atomicMax(moved + scene, bits);
-  }
+// Clears one parity of the displacement table: every thread of a list-pass
+// launch takes a grid-stride share.
+__device__ __forceinline__ void clear_moved(unsigned* table, uint32_t mask) {
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; t <= mask; t += stride)
+    table[t] = 0u;
+}
+
+// d_nb of particle i (sorted slot) from the table of one parity; +inf (no
+// bound) for lists from all pairs.
+__device__ __forceinline__ float moved_around(const StepArgs& a, const SceneConst& c, int scene, int i, int par) {
+  if (c.all_pairs) return INFINITY;
+  int cx, cy, cz;
+  build_cell(sorted_keys(a, a.status->npass), a.grid[scene], i, cx, cy, cz);
+  return moved_near(a.moved + static_cast<size_t>(par) * (a.moved_mask + 1u), a.moved_mask, scene, cx, cy, cz);
+}
+
+// Records particle i's displacement d in the table of one parity.
+__device__ __forceinline__ void record_moved_at(const StepArgs& a, int scene, int i, int par, float d) {
+  int cx, cy, cz;
+  build_cell(sorted_keys(a, a.status->npass), a.grid[scene], i, cx, cy, cz);
+  record_moved(a.moved + static_cast<size_t>(par) * (a.moved_mask + 1u), a.moved_mask, scene, cx, cy, cz, d);
 }
 
 __device__ __forceinline__ uint32_t cell_key(const GridInfo& g, int cx, int cy, int cz) {
   const long long l = (static_cast<long long>(cx - g.minx) * g.dimy + (cy - g.miny)) * g.dimz + (cz - g.minz);
   return g.base + static_cast<uint32_t>(l);
-}
-
-__device__ __forceinline__ const uint32_t* sorted_keys(const StepArgs& a, int npass) {
-  return a.keys[npass & 1];
 }
 
 // ---------------------------------------------------------------------------
@@ -1109,8 +1180,7 @@ __device__ __forceinline__ void for_each_live_then(const int* __restrict__ list,
 template <int U, bool kLiveOut>
 __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_lambda(StepArgs a, int in) {
   if (failed(a.status)) return;
-  if (blockIdx.x == 0)
-    for (int t = threadIdx.x; t < a.scenes; t += blockDim.x) a.moved[in * a.scenes + t] = 0u;
+  clear_moved(a.moved + static_cast<size_t>(in) * (a.moved_mask + 1u), a.moved_mask);
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   const float4* __restrict__ pos = a.p[in];
@@ -1126,7 +1196,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_lambda(StepA
   if constexpr (kLiveOut) {
     const float4 q = a.p[in ^ 1][i];
     skip = beyond_reach(c, a.reach[i], moved_by(p.x - q.x, p.y - q.y, p.z - q.z),
-                        __uint_as_float(a.moved[(in ^ 1) * a.scenes + scene]), bound);
+                        moved_around(a, c, scene, i, in ^ 1), bound);
     count_skipped(a.status, skip);
   }
   auto one = [&](const float4 q) {
@@ -1185,6 +1255,41 @@ __device__ __forceinline__ void commit(const StepArgs& a, const SceneConst& c, i
   a.x[i] = x;
   if (rest && c.rest_on) restitution(c, px, py, pz, vx, vy, vz);
   (to_v2 ? a.v2 : a.v)[i] = make_float4(vx, vy, vz, scene_bits);
+}
+
+// The rest of a delta pass once the sums (ax, ay, az) of particle i are
+// complete: scale by 1/rho0, plane projection (core.cpp:368-393), the scene's
+// displacement word, then the next iteration's p* or the commit.
+__device__ __forceinline__ void delta_out(const StepArgs& a, const SceneConst& c, int i, const float4 p, float ax,
+                                          float ay, float az, int in, int last, int to_v2, int rest,
+                                          float4* q_out) {
+  ax *= c.inv_density;
+  ay *= c.inv_density;
+  az *= c.inv_density;
+  if (q_out) q_out[i] = make_float4(p.x + ax, p.y + ay, p.z + az, 0.0f);  // recorded for the adjoint
+  if (c.plane_count > 0) {  // core.cpp:372-393
+    float qx = p.x + ax, qy = p.y + ay, qz = p.z + az;
+    for (int q = 0; q < c.plane_count; ++q) {
+      const float4 pl = c.planes[q];
+      const float sd = pl.x * qx + pl.y * qy + pl.z * qz - pl.w;
+      const float pen = -sd;
+      if (pen > 0.0f) {
+        qx += pl.x * pen;
+        qy += pl.y * pen;
+        qz += pl.z * pen;
+      }
+    }
+    ax = qx - p.x;
+    ay = qy - p.y;
+    az = qz - p.z;
+  }
+  const float nx = p.x + ax, ny = p.y + ay, nz = p.z + az;  // core.cpp:404-406
+  record_moved_at(a, __float_as_int(p.w), i, in, moved_by(nx - p.x, ny - p.y, nz - p.z));
+  if (!last) {
+    a.p[in ^ 1][i] = make_float4(nx, ny, nz, p.w);
+  } else {
+    commit(a, c, i, nx, ny, nz, p.w, to_v2 != 0, rest != 0, a.p[in ^ 1]);
+  }
 }
 
 // kPow: the s_corr exponent when every scene with s_corr shares it (2, 3,
@@ -1275,33 +1380,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_delta(StepAr
     if constexpr (kLiveIn) for_each_live_then<U>(list, n, live, load, dead, two, one);
     else for_each_neighbor_pair<U>(list, n, load, two, one);
   }
-  ax *= c.inv_density;
-  ay *= c.inv_density;
-  az *= c.inv_density;
-  if (q_out) q_out[i] = make_float4(p.x + ax, p.y + ay, p.z + az, 0.0f);  // recorded for the adjoint
-  if (c.plane_count > 0) {  // core.cpp:372-393
-    float qx = p.x + ax, qy = p.y + ay, qz = p.z + az;
-    for (int q = 0; q < c.plane_count; ++q) {
-      const float4 pl = c.planes[q];
-      const float sd = pl.x * qx + pl.y * qy + pl.z * qz - pl.w;
-      const float pen = -sd;
-      if (pen > 0.0f) {
-        qx += pl.x * pen;
-        qy += pl.y * pen;
-        qz += pl.z * pen;
-      }
-    }
-    ax = qx - p.x;
-    ay = qy - p.y;
-    az = qz - p.z;
-  }
-  const float nx = p.x + ax, ny = p.y + ay, nz = p.z + az;  // core.cpp:404-406
-  record_moved(a.moved + in * a.scenes, __float_as_int(p.w), moved_by(nx - p.x, ny - p.y, nz - p.z));
-  if (!last) {
-    a.p[in ^ 1][i] = make_float4(nx, ny, nz, p.w);
-  } else {
-    commit(a, c, i, nx, ny, nz, p.w, to_v2 != 0, rest != 0, a.p[in ^ 1]);
-  }
+  delta_out(a, c, i, p, ax, ay, az, in, last, to_v2, rest, q_out);
 }
 
 // Commit without Jacobi iterations (solver_iterations == 0).
@@ -1340,7 +1419,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_xsph(StepArg
     const float4 q = a.p[bound_par][i];
     float bound;
     skip = beyond_reach(c, a.reach[i], moved_by(xi.x - q.x, xi.y - q.y, xi.z - q.z),
-                        __uint_as_float(a.moved[bound_par * a.scenes + scene]), bound);
+                        moved_around(a, c, scene, i, bound_par), bound);
     if (skip) bits = 0ull;
   }
   if (bound_par >= 0) count_skipped(a.status, skip);
@@ -1489,6 +1568,25 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_omega(StepAr
   a.pl[i] = make_float4(xi.x, xi.y, xi.z, mag);  // the record k_eta gathers per neighbour
 }
 
+// Confinement force from eta = (ex, ey, ez) and omega oi, added to v
+// (core.cpp:551-570).
+__device__ __forceinline__ void confine(const SceneConst& c, const float4 oi, float ex, float ey, float ez, float4& v) {
+  const float len = sqrtf(ex * ex + ey * ey + ez * ez);
+  float nx = 0.0f, ny = 0.0f, nz2 = 0.0f;
+  if (len > c.vort_norm_eps) {
+    const float inv = 1.0f / len;
+    nx = ex * inv;
+    ny = ey * inv;
+    nz2 = ez * inv;
+  }
+  const float fx = c.vort_eps * (ny * oi.z - nz2 * oi.y);
+  const float fy = c.vort_eps * (nz2 * oi.x - nx * oi.z);
+  const float fz = c.vort_eps * (nx * oi.y - ny * oi.x);
+  v.x += c.dt * fx;
+  v.y += c.dt * fy;
+  v.z += c.dt * fz;
+}
+
 // Eta, confinement force, velocity update (core.cpp:512-570) and plane
 // restitution (core.cpp:573-612); only the live ones among the first
 // entries (live bits of these positions from XSPH or omega).
@@ -1545,21 +1643,369 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_eta(StepArgs
     for_each_live_then<U>(list, n, static_cast<unsigned long long>(a.live[i]) |
                                        (static_cast<unsigned long long>(a.live[a.n + i]) << 32),
                           load, dead, two, one);
-    const float len = sqrtf(ex * ex + ey * ey + ez * ez);
-    float nx = 0.0f, ny = 0.0f, nz2 = 0.0f;
-    if (len > c.vort_norm_eps) {
-      const float inv = 1.0f / len;
-      nx = ex * inv;
-      ny = ey * inv;
-      nz2 = ez * inv;
-    }
-    const float fx = c.vort_eps * (ny * oi.z - nz2 * oi.y);
-    const float fy = c.vort_eps * (nz2 * oi.x - nx * oi.z);
-    const float fz = c.vort_eps * (nx * oi.y - ny * oi.x);
-    v.x += c.dt * fx;
-    v.y += c.dt * fy;
-    v.z += c.dt * fz;
+    confine(c, oi, ex, ey, ez, v);
   }
+  if (rest && c.rest_on) restitution(c, xi.x, xi.y, xi.z, v.x, v.y, v.z);
+  a.v[i] = v;
+}
+
+// ---------------------------------------------------------------------------
+// Several lanes per particle.
+//
+// With G lanes per particle (G = 2, 4 or 8: a group of consecutive lanes of
+// one warp, so a warp serves 32/G particles and a launch has G threads per
+// particle), the lanes of a group split the particle's list into rounds: in
+// round r lane u of the group takes entry rG + u, loads its index and record
+// (the next round's record is loaded while this one is used) and computes the
+// entry's terms with the same float operations as the one-lane walk. Then
+// every lane of the group adds the round's G terms in list order, each moved
+// by shuffle from the lane that computed it, so the sums are bit-identical to
+// the one-lane walk's (an entry out of range or past the list's end adds
+// nothing) and every lane of the group ends with them; the group's first
+// lane writes the results.
+//
+// This takes a long list's dependent loads and term arithmetic off a single
+// lane at the cost of the shuffles: it pays where a launch is short of warps
+// (small scenes, or a collapsed scene whose launch fills less than a wave and
+// lasts as long as its deepest lists) and loses in a launch that fills every
+// SM, so the autotuner chooses G per kernel on the live state. Live bits are
+// assembled from each round's ballot; passes that would read live bits walk
+// every entry instead (a dead entry adds nothing), and keep the displacement
+// bound's skips.
+
+// Thread -> (particle slot, lane within its group, group's first warp lane).
+template <int G>
+struct LaneGroup {
+  int i, sub, lead;
+  unsigned mask;
+  __device__ __forceinline__ LaneGroup() {
+    const long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    i = static_cast<int>(t / G);
+    const int lane = threadIdx.x & 31;
+    sub = lane & (G - 1);
+    lead = lane & ~(G - 1);
+    mask = ((1u << G) - 1u) << lead;
+  }
+  __device__ __forceinline__ float min_over(float v) const {
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(mask, v, o));
+    return v;
+  }
+};
+
+// Terms of one list entry: K floats and whether the entry is within h.
+template <int K>
+struct Terms {
+  float f[K];
+  bool live;
+  __device__ __forceinline__ Terms shfl(unsigned mask, int src) const {
+    Terms o;
+#pragma unroll
+    for (int q = 0; q < K; ++q) o.f[q] = __shfl_sync(mask, f[q], src);
+    o.live = false;
+    return o;
+  }
+};
+
+// Walks entries rG + sub (rounds r = 0, 1, ...) of a list of n entries:
+// term(record, in_list) gives an entry's Terms, add(Terms) accumulates, and
+// each lane of the group adds the round's G terms in list order. Returns the
+// live bits of entries 0..63 (the same on every lane of the group).
+template <int G, int K, typename Load, typename Term, typename Add>
+__device__ __forceinline__ unsigned long long walk_lanes(const int* __restrict__ list, int n, const LaneGroup<G>& L,
+                                                         Load&& load, Term&& term, Add&& add) {
+  using Rec = decltype(load(0));
+  unsigned long long bits = 0ull;
+  const int rounds = (n + G - 1) / G;
+  int k = L.sub;
+  int j1 = (k + G < n) ? __ldcs(list + 32ll * (k + G)) : 0;
+  Rec cur = (k < n) ? load(__ldcs(list + 32ll * k)) : Rec{};
+  for (int r = 0; r < rounds; ++r, k += G) {
+    const int j2 = (k + 2 * G < n) ? __ldcs(list + 32ll * (k + 2 * G)) : 0;
+    const Rec nxt = (k + G < n) ? load(j1) : Rec{};
+    const Terms<K> t = term(cur, k < n);
+    const unsigned lb = (__ballot_sync(L.mask, t.live) >> L.lead) & ((1u << G) - 1u);
+#pragma unroll
+    for (int u = 0; u < G; ++u) {
+      const Terms<K> tu = t.shfl(L.mask, L.lead + u);
+      if ((lb >> u) & 1u) add(tu);
+    }
+    if (r * G < kLiveEntries) bits |= static_cast<unsigned long long>(lb) << (r * G);
+    cur = nxt;
+    j1 = j2;
+  }
+  return bits;
+}
+
+template <int G, bool kLiveOut>
+__global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_lambda_lanes(StepArgs a, int in) {
+  if (failed(a.status)) return;
+  clear_moved(a.moved + static_cast<size_t>(in) * (a.moved_mask + 1u), a.moved_mask);
+  const LaneGroup<G> L;
+  const int i = L.i;
+  if (i >= a.n) return;
+  const float4* __restrict__ pos = a.p[in];
+  const float4 p = pos[i];
+  const int scene = __float_as_int(p.w);
+  const SceneConst& c = a.sc[scene];
+  const int n = a.cnt[i];
+  const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (i & 31);
+  const float h2 = c.h2;
+  LambdaAcc acc;
+  bool skip = false;
+  float bound = 0.0f;
+  if constexpr (kLiveOut) {
+    const float4 q = a.p[in ^ 1][i];
+    skip = beyond_reach(c, a.reach[i], moved_by(p.x - q.x, p.y - q.y, p.z - q.z),
+                        moved_around(a, c, scene, i, in ^ 1), bound);
+    count_skipped(a.status, skip && L.sub == 0);
+  }
+  unsigned long long bits = 0ull;
+  if (!skip) {
+    auto load = [&](int j) { return __ldg(pos + j); };
+    auto term = [&](const float4 q, bool in_list) {  // LambdaAcc::add, term by term
+      Terms<5> t;
+      const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+      const float r2 = dist2(dx, dy, dz);
+      if (in_list) acc.r2min = fminf(acc.r2min, r2);
+      t.live = in_list && r2 < h2;
+      if (t.live) {
+        t.f[0] = poly6(c, r2);
+        const float gf = spiky(c, clamped_r(c, r2));
+        t.f[1] = gf * dx;
+        t.f[2] = gf * dy;
+        t.f[3] = gf * dz;
+        const float ng = -c.grad_scale;
+        const float jx = ng * t.f[1], jy = ng * t.f[2], jz = ng * t.f[3];
+        t.f[4] = jx * jx + jy * jy + jz * jz;
+      } else {
+        t.f[0] = t.f[1] = t.f[2] = t.f[3] = t.f[4] = 0.0f;
+      }
+      return t;
+    };
+    auto add = [&](const Terms<5>& t) {
+      acc.rho += t.f[0];
+      acc.gsx += t.f[1];
+      acc.gsy += t.f[2];
+      acc.gsz += t.f[3];
+      acc.sum_g2 += t.f[4];
+    };
+    bits = walk_lanes<G, 5>(list, n, L, load, term, add);
+    acc.r2min = L.min_over(acc.r2min);
+  }
+  if (L.sub != 0) return;
+  if constexpr (kLiveOut) store_live(a.live, a.n, i, bits);
+  float rho;
+  const float lam = finish_lambda(c, acc.rho, acc.gsx, acc.gsy, acc.gsz, acc.sum_g2, rho);
+  a.lambda[i] = lam;
+  a.rho[i] = rho;
+  a.pl[i] = make_float4(p.x, p.y, p.z, lam);
+  a.reach[i] = skip ? bound : reach_from_r2(acc.r2min);
+}
+
+template <int G, int kPow, bool kLiveIn>
+__global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS)
+    k_delta_lanes(StepArgs a, int in, int last, int to_v2, int rest, float4* q_out) {
+  if (failed(a.status)) return;
+  const LaneGroup<G> L;
+  const int i = L.i;
+  if (i >= a.n) return;
+  const float4 p = a.p[in][i];
+  const SceneConst& c = a.sc[__float_as_int(p.w)];
+  const int n = a.cnt[i];
+  const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (i & 31);
+  const float4* __restrict__ pl = a.pl;
+  const float li = a.lambda[i];
+  const float h2 = c.h2;
+  float ax = 0.0f, ay = 0.0f, az = 0.0f;
+  const bool scorr = c.scorr_on != 0;
+  const bool none = kLiveIn && a.reach[i] >= __fmul_ru(c.h, kReachGrow);
+  if (!none) {
+    auto load = [&](int j) { return __ldg(pl + j); };
+    auto term = [&](const float4 r, bool in_list) {  // k_delta's one(), term by term
+      Terms<3> t;
+      const float dx = p.x - r.x, dy = p.y - r.y, dz = p.z - r.z;
+      const float r2 = dist2(dx, dy, dz);
+      t.live = in_list && r2 < h2;
+      if (t.live) {
+        const float gf = spiky(c, clamped_r(c, r2));
+        float sc = li + r.w;
+        if (scorr) {
+          const float ratio = poly6(c, r2) * c.scorr_inv_wdq;
+          sc += c.scorr_neg_k * pow_k<kPow>(ratio, c.scorr_n);
+        }
+        t.f[0] = sc * gf * dx;
+        t.f[1] = sc * gf * dy;
+        t.f[2] = sc * gf * dz;
+      } else {
+        t.f[0] = t.f[1] = t.f[2] = 0.0f;
+      }
+      return t;
+    };
+    auto add = [&](const Terms<3>& t) {
+      ax += t.f[0];
+      ay += t.f[1];
+      az += t.f[2];
+    };
+    walk_lanes<G, 3>(list, n, L, load, term, add);
+  }
+  if (L.sub != 0) return;
+  delta_out(a, c, i, p, ax, ay, az, in, last, to_v2, rest, q_out);
+}
+
+template <int G, bool kLiveOut>
+__global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_xsph_lanes(StepArgs a, int rest, const float4* xr,
+                                                                                int bound_par) {
+  if (failed(a.status)) return;
+  const LaneGroup<G> L;
+  const int i = L.i;
+  if (i >= a.n) return;
+  const float4* __restrict__ xs = xr;
+  const float4* __restrict__ vs = a.v2;
+  const float4 xi = xs[i];
+  const float4 vi = vs[i];
+  const int scene = __float_as_int(vi.w);
+  const SceneConst& c = a.sc[scene];
+  float vx = vi.x, vy = vi.y, vz = vi.z;
+  unsigned long long bits = ~0ull;
+  bool skip = false;
+  if (c.xsph_on && bound_par >= 0) {
+    const float4 q = a.p[bound_par][i];
+    float bound;
+    skip = beyond_reach(c, a.reach[i], moved_by(xi.x - q.x, xi.y - q.y, xi.z - q.z),
+                        moved_around(a, c, scene, i, bound_par), bound);
+    if (skip) bits = 0ull;
+  }
+  if (bound_par >= 0) count_skipped(a.status, skip && L.sub == 0);
+  if (c.xsph_on && !skip) {
+    const int n = a.cnt[i];
+    const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (i & 31);
+    const float h2 = c.h2;
+    float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+    auto load = [&](int j) { return PosVel{__ldg(xs + j), __ldg(vs + j)}; };
+    auto term = [&](const PosVel r, bool in_list) {  // k_xsph's one(), term by term
+      Terms<3> t;
+      const float r2 = dist2(xi.x - r.x.x, xi.y - r.x.y, xi.z - r.x.z);
+      t.live = in_list && r2 < h2;
+      if (t.live) {
+        const float W = poly6(c, r2);
+        const float inv_rho_j = r.x.w;
+        t.f[0] = (r.v.x - vi.x) * W * inv_rho_j;
+        t.f[1] = (r.v.y - vi.y) * W * inv_rho_j;
+        t.f[2] = (r.v.z - vi.z) * W * inv_rho_j;
+      } else {
+        t.f[0] = t.f[1] = t.f[2] = 0.0f;
+      }
+      return t;
+    };
+    auto add = [&](const Terms<3>& t) {
+      sx += t.f[0];
+      sy += t.f[1];
+      sz += t.f[2];
+    };
+    bits = walk_lanes<G, 3>(list, n, L, load, term, add);
+    vx += c.visc_c * sx;
+    vy += c.visc_c * sy;
+    vz += c.visc_c * sz;
+  }
+  if (L.sub != 0) return;
+  if (kLiveOut) store_live(a.live, a.n, i, bits);
+  if (rest && c.rest_on) restitution(c, xi.x, xi.y, xi.z, vx, vy, vz);
+  a.v[i] = make_float4(vx, vy, vz, vi.w);
+}
+
+// kLive: 1 = live bits given (unused: every entry is walked); 2 = record them.
+template <int G, int kLive>
+__global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_omega_lanes(StepArgs a) {
+  if (failed(a.status)) return;
+  const LaneGroup<G> L;
+  const int i = L.i;
+  if (i >= a.n) return;
+  const float4* __restrict__ xs = a.x;
+  const float4* __restrict__ vs = a.v;
+  const float4 xi = xs[i];
+  const float4 vi = vs[i];
+  const SceneConst& c = a.sc[__float_as_int(vi.w)];
+  float ox = 0.0f, oy = 0.0f, oz = 0.0f;
+  unsigned long long bits = ~0ull;
+  if (c.vort_on) {
+    const int n = a.cnt[i];
+    const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (i & 31);
+    const float h2 = c.h2;
+    auto load = [&](int j) { return PosVel{__ldg(xs + j), __ldg(vs + j)}; };
+    auto term = [&](const PosVel r, bool in_list) {  // k_omega's one(), term by term
+      Terms<3> t;
+      const float dx = xi.x - r.x.x, dy = xi.y - r.x.y, dz = xi.z - r.x.z;
+      const float r2 = dist2(dx, dy, dz);
+      t.live = in_list && r2 < h2;
+      if (t.live) {
+        const float gf = spiky(c, clamped_r(c, r2));
+        const float gx = gf * dx, gy = gf * dy, gz = gf * dz;
+        const float ux = r.v.x - vi.x, uy = r.v.y - vi.y, uz = r.v.z - vi.z;
+        t.f[0] = uy * gz - uz * gy;
+        t.f[1] = uz * gx - ux * gz;
+        t.f[2] = ux * gy - uy * gx;
+      } else {
+        t.f[0] = t.f[1] = t.f[2] = 0.0f;
+      }
+      return t;
+    };
+    auto add = [&](const Terms<3>& t) {
+      ox += t.f[0];
+      oy += t.f[1];
+      oz += t.f[2];
+    };
+    bits = walk_lanes<G, 3>(list, n, L, load, term, add);
+  }
+  if (L.sub != 0) return;
+  if (kLive == 2) store_live(a.live, a.n, i, bits);
+  const float mag = sqrtf(ox * ox + oy * oy + oz * oz);
+  a.omega[i] = make_float4(ox, oy, oz, mag);
+  a.pl[i] = make_float4(xi.x, xi.y, xi.z, mag);
+}
+
+template <int G>
+__global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_eta_lanes(StepArgs a, int rest) {
+  if (failed(a.status)) return;
+  const LaneGroup<G> L;
+  const int i = L.i;
+  if (i >= a.n) return;
+  const float4* __restrict__ xo = a.pl;
+  const float4 xi = a.x[i];
+  float4 v = a.v[i];
+  const SceneConst& c = a.sc[__float_as_int(v.w)];
+  if (c.vort_on) {
+    const float4 oi = a.omega[i];
+    const int n = a.cnt[i];
+    const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (i & 31);
+    const float h2 = c.h2;
+    float ex = 0.0f, ey = 0.0f, ez = 0.0f;
+    auto load = [&](int j) { return __ldg(xo + j); };
+    auto term = [&](const float4 r, bool in_list) {  // k_eta's one(), term by term
+      Terms<3> t;
+      const float dx = xi.x - r.x, dy = xi.y - r.y, dz = xi.z - r.z;
+      const float r2 = dist2(dx, dy, dz);
+      t.live = in_list && r2 < h2;
+      if (t.live) {
+        const float gf = spiky(c, clamped_r(c, r2));
+        const float coeff = r.w - oi.w;
+        t.f[0] = coeff * (gf * dx);
+        t.f[1] = coeff * (gf * dy);
+        t.f[2] = coeff * (gf * dz);
+      } else {
+        t.f[0] = t.f[1] = t.f[2] = 0.0f;
+      }
+      return t;
+    };
+    auto add = [&](const Terms<3>& t) {
+      ex += t.f[0];
+      ey += t.f[1];
+      ez += t.f[2];
+    };
+    walk_lanes<G, 3>(list, n, L, load, term, add);
+    confine(c, oi, ex, ey, ez, v);
+  }
+  if (L.sub != 0) return;
   if (rest && c.rest_on) restitution(c, xi.x, xi.y, xi.z, v.x, v.y, v.z);
   a.v[i] = v;
 }
@@ -1649,83 +2095,141 @@ __global__ void k_reset(DevStatus* st, int* bmin, int* bmax, int scenes) {
 
 inline int blocks_for(long long n, int threads) { return static_cast<int>((n + threads - 1) / threads); }
 
-// Launches KERNEL<U> for the tuned unroll U of the plan.
-#define FGB_DISPATCH_UNROLL(u, KERNEL, grid, block, stream, ...)          \
-  do {                                                                  \
-    switch (u) {                                                        \
-      case 1: KERNEL<1><<<grid, block, 0, stream>>>(__VA_ARGS__); break;  \
-      case 2: KERNEL<2><<<grid, block, 0, stream>>>(__VA_ARGS__); break;  \
-      case 8: KERNEL<8><<<grid, block, 0, stream>>>(__VA_ARGS__); break;  \
-      default: KERNEL<4><<<grid, block, 0, stream>>>(__VA_ARGS__); break; \
-    }                                                                   \
-  } while (0)
+
+// Blocks of a list pass with `lanes` threads per particle.
+inline int list_grid(const StepArgs& a, int block, int lanes) {
+  return blocks_for(static_cast<long long>(a.n) * lanes, block);
+}
+
+// Launch shape of list kernel k in the plan: block size, records fetched
+// ahead (one lane per particle) and lanes per particle.
+struct ListShape {
+  int block, unroll, lanes;
+  ListShape(const StepPlan& plan, int k) : block(plan.block[k]), unroll(plan.unroll[k]), lanes(plan.lanes[k]) {}
+};
 
 template <int kPow, bool kLiveIn>
 struct DeltaPow {
   template <int U>
-  static void launch(int grid, int block, cudaStream_t st, const StepArgs& a, int in, int last, int to_v2, int rest,
+  static void launch(int block, cudaStream_t st, const StepArgs& a, int in, int last, int to_v2, int rest,
                      float4* q_out) {
-    k_delta<U, kPow, kLiveIn><<<grid, block, 0, st>>>(a, in, last, to_v2, rest, q_out);
+    k_delta<U, kPow, kLiveIn><<<list_grid(a, block, 1), block, 0, st>>>(a, in, last, to_v2, rest, q_out);
   }
-  static void dispatch(int u, int grid, int block, cudaStream_t st, const StepArgs& a, int in, int last, int to_v2,
+  template <int G>
+  static void launch_lanes(int block, cudaStream_t st, const StepArgs& a, int in, int last, int to_v2, int rest,
+                           float4* q_out) {
+    k_delta_lanes<G, kPow, kLiveIn><<<list_grid(a, block, G), block, 0, st>>>(a, in, last, to_v2, rest, q_out);
+  }
+  static void dispatch(const ListShape& sh, cudaStream_t st, const StepArgs& a, int in, int last, int to_v2,
                        int rest, float4* q_out) {
-    switch (u) {
-      case 1: launch<1>(grid, block, st, a, in, last, to_v2, rest, q_out); break;
-      case 2: launch<2>(grid, block, st, a, in, last, to_v2, rest, q_out); break;
-      case 8: launch<8>(grid, block, st, a, in, last, to_v2, rest, q_out); break;
-      default: launch<4>(grid, block, st, a, in, last, to_v2, rest, q_out); break;
+    const int b = sh.block;
+    switch (sh.lanes) {
+      case 2: launch_lanes<2>(b, st, a, in, last, to_v2, rest, q_out); return;
+      case 4: launch_lanes<4>(b, st, a, in, last, to_v2, rest, q_out); return;
+      case 8: launch_lanes<8>(b, st, a, in, last, to_v2, rest, q_out); return;
+      default: break;
+    }
+    switch (sh.unroll) {
+      case 1: launch<1>(b, st, a, in, last, to_v2, rest, q_out); break;
+      case 2: launch<2>(b, st, a, in, last, to_v2, rest, q_out); break;
+      case 8: launch<8>(b, st, a, in, last, to_v2, rest, q_out); break;
+      default: launch<4>(b, st, a, in, last, to_v2, rest, q_out); break;
     }
   }
 };
 
 template <bool kLiveIn>
-void launch_delta_pow(const StepPlan& plan, int grid, int block, cudaStream_t st, const StepArgs& a, int in, int last,
-                      int to_v2, int rest, float4* q_out) {
-  const int u = plan.unroll[FLUID_KERNEL_DELTA];
+void launch_delta_pow(const StepPlan& plan, cudaStream_t st, const StepArgs& a, int in, int last, int to_v2, int rest,
+                      float4* q_out) {
+  const ListShape sh(plan, FLUID_KERNEL_DELTA);
   switch (plan.scorr_pow) {
-    case 2: DeltaPow<2, kLiveIn>::dispatch(u, grid, block, st, a, in, last, to_v2, rest, q_out); break;
-    case 3: DeltaPow<3, kLiveIn>::dispatch(u, grid, block, st, a, in, last, to_v2, rest, q_out); break;
-    case 4: DeltaPow<4, kLiveIn>::dispatch(u, grid, block, st, a, in, last, to_v2, rest, q_out); break;
-    default: DeltaPow<0, kLiveIn>::dispatch(u, grid, block, st, a, in, last, to_v2, rest, q_out); break;
+    case 2: DeltaPow<2, kLiveIn>::dispatch(sh, st, a, in, last, to_v2, rest, q_out); break;
+    case 3: DeltaPow<3, kLiveIn>::dispatch(sh, st, a, in, last, to_v2, rest, q_out); break;
+    case 4: DeltaPow<4, kLiveIn>::dispatch(sh, st, a, in, last, to_v2, rest, q_out); break;
+    default: DeltaPow<0, kLiveIn>::dispatch(sh, st, a, in, last, to_v2, rest, q_out); break;
   }
 }
 
 // live: the lambda pass of this iteration recorded live bits (iterations
 // after the first).
-void launch_delta(const StepPlan& plan, int grid, int block, cudaStream_t st, const StepArgs& a, int in, int last,
-                  int to_v2, int rest, float4* q_out, bool live) {
-  if (live) launch_delta_pow<true>(plan, grid, block, st, a, in, last, to_v2, rest, q_out);
-  else launch_delta_pow<false>(plan, grid, block, st, a, in, last, to_v2, rest, q_out);
+void launch_delta(const StepPlan& plan, cudaStream_t st, const StepArgs& a, int in, int last, int to_v2, int rest,
+                  float4* q_out, bool live) {
+  if (live) launch_delta_pow<true>(plan, st, a, in, last, to_v2, rest, q_out);
+  else launch_delta_pow<false>(plan, st, a, in, last, to_v2, rest, q_out);
 }
 
 template <bool kLiveOut>
-void launch_lambda(int u, int grid, int block, cudaStream_t st, const StepArgs& a, int in) {
-  switch (u) {
-    case 1: k_lambda<1, kLiveOut><<<grid, block, 0, st>>>(a, in); break;
-    case 2: k_lambda<2, kLiveOut><<<grid, block, 0, st>>>(a, in); break;
-    case 8: k_lambda<8, kLiveOut><<<grid, block, 0, st>>>(a, in); break;
-    default: k_lambda<4, kLiveOut><<<grid, block, 0, st>>>(a, in); break;
+void launch_lambda(const StepPlan& plan, cudaStream_t st, const StepArgs& a, int in) {
+  const ListShape sh(plan, FLUID_KERNEL_LAMBDA);
+  const int b = sh.block;
+  switch (sh.lanes) {
+    case 2: k_lambda_lanes<2, kLiveOut><<<list_grid(a, b, 2), b, 0, st>>>(a, in); return;
+    case 4: k_lambda_lanes<4, kLiveOut><<<list_grid(a, b, 4), b, 0, st>>>(a, in); return;
+    case 8: k_lambda_lanes<8, kLiveOut><<<list_grid(a, b, 8), b, 0, st>>>(a, in); return;
+    default: break;
+  }
+  const int g = list_grid(a, b, 1);
+  switch (sh.unroll) {
+    case 1: k_lambda<1, kLiveOut><<<g, b, 0, st>>>(a, in); break;
+    case 2: k_lambda<2, kLiveOut><<<g, b, 0, st>>>(a, in); break;
+    case 8: k_lambda<8, kLiveOut><<<g, b, 0, st>>>(a, in); break;
+    default: k_lambda<4, kLiveOut><<<g, b, 0, st>>>(a, in); break;
   }
 }
 
 template <bool kLiveOut>
-void launch_xsph(int u, int grid, int block, cudaStream_t st, const StepArgs& a, int rest, const float4* xr,
-                 int bound_par) {
-  switch (u) {
-    case 1: k_xsph<1, kLiveOut><<<grid, block, 0, st>>>(a, rest, xr, bound_par); break;
-    case 2: k_xsph<2, kLiveOut><<<grid, block, 0, st>>>(a, rest, xr, bound_par); break;
-    case 8: k_xsph<8, kLiveOut><<<grid, block, 0, st>>>(a, rest, xr, bound_par); break;
-    default: k_xsph<4, kLiveOut><<<grid, block, 0, st>>>(a, rest, xr, bound_par); break;
+void launch_xsph(const StepPlan& plan, cudaStream_t st, const StepArgs& a, int rest, const float4* xr, int bound_par) {
+  const ListShape sh(plan, FLUID_KERNEL_XSPH);
+  const int b = sh.block;
+  switch (sh.lanes) {
+    case 2: k_xsph_lanes<2, kLiveOut><<<list_grid(a, b, 2), b, 0, st>>>(a, rest, xr, bound_par); return;
+    case 4: k_xsph_lanes<4, kLiveOut><<<list_grid(a, b, 4), b, 0, st>>>(a, rest, xr, bound_par); return;
+    case 8: k_xsph_lanes<8, kLiveOut><<<list_grid(a, b, 8), b, 0, st>>>(a, rest, xr, bound_par); return;
+    default: break;
+  }
+  const int g = list_grid(a, b, 1);
+  switch (sh.unroll) {
+    case 1: k_xsph<1, kLiveOut><<<g, b, 0, st>>>(a, rest, xr, bound_par); break;
+    case 2: k_xsph<2, kLiveOut><<<g, b, 0, st>>>(a, rest, xr, bound_par); break;
+    case 8: k_xsph<8, kLiveOut><<<g, b, 0, st>>>(a, rest, xr, bound_par); break;
+    default: k_xsph<4, kLiveOut><<<g, b, 0, st>>>(a, rest, xr, bound_par); break;
   }
 }
 
 template <int kLive>
-void launch_omega(int u, int grid, int block, cudaStream_t st, const StepArgs& a) {
-  switch (u) {
-    case 1: k_omega<1, kLive><<<grid, block, 0, st>>>(a); break;
-    case 2: k_omega<2, kLive><<<grid, block, 0, st>>>(a); break;
-    case 8: k_omega<8, kLive><<<grid, block, 0, st>>>(a); break;
-    default: k_omega<4, kLive><<<grid, block, 0, st>>>(a); break;
+void launch_omega(const StepPlan& plan, cudaStream_t st, const StepArgs& a) {
+  const ListShape sh(plan, FLUID_KERNEL_OMEGA);
+  const int b = sh.block;
+  switch (sh.lanes) {
+    case 2: k_omega_lanes<2, kLive><<<list_grid(a, b, 2), b, 0, st>>>(a); return;
+    case 4: k_omega_lanes<4, kLive><<<list_grid(a, b, 4), b, 0, st>>>(a); return;
+    case 8: k_omega_lanes<8, kLive><<<list_grid(a, b, 8), b, 0, st>>>(a); return;
+    default: break;
+  }
+  const int g = list_grid(a, b, 1);
+  switch (sh.unroll) {
+    case 1: k_omega<1, kLive><<<g, b, 0, st>>>(a); break;
+    case 2: k_omega<2, kLive><<<g, b, 0, st>>>(a); break;
+    case 8: k_omega<8, kLive><<<g, b, 0, st>>>(a); break;
+    default: k_omega<4, kLive><<<g, b, 0, st>>>(a); break;
+  }
+}
+
+void launch_eta(const StepPlan& plan, cudaStream_t st, const StepArgs& a, int rest) {
+  const ListShape sh(plan, FLUID_KERNEL_ETA);
+  const int b = sh.block;
+  switch (sh.lanes) {
+    case 2: k_eta_lanes<2><<<list_grid(a, b, 2), b, 0, st>>>(a, rest); return;
+    case 4: k_eta_lanes<4><<<list_grid(a, b, 4), b, 0, st>>>(a, rest); return;
+    case 8: k_eta_lanes<8><<<list_grid(a, b, 8), b, 0, st>>>(a, rest); return;
+    default: break;
+  }
+  const int g = list_grid(a, b, 1);
+  switch (sh.unroll) {
+    case 1: k_eta<1><<<g, b, 0, st>>>(a, rest); break;
+    case 2: k_eta<2><<<g, b, 0, st>>>(a, rest); break;
+    case 8: k_eta<8><<<g, b, 0, st>>>(a, rest); break;
+    default: k_eta<4><<<g, b, 0, st>>>(a, rest); break;
   }
 }
 
@@ -1810,17 +2314,15 @@ cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t s
   for (int it = 0; it < plan.iterations; ++it) {
     const int in = it & 1;
     {
-      const int b = plan.block[FLUID_KERNEL_LAMBDA];
-      if (it == 0) launch_lambda<false>(plan.unroll[FLUID_KERNEL_LAMBDA], blocks_for(a.n, b), b, st, a, in);
-      else launch_lambda<true>(plan.unroll[FLUID_KERNEL_LAMBDA], blocks_for(a.n, b), b, st, a, in);
+      if (it == 0) launch_lambda<false>(plan, st, a, in);
+      else launch_lambda<true>(plan, st, a, in);
       m.mark(FLUID_KERNEL_LAMBDA);
       if (rec)
         cudaMemcpyAsync(rec->lambda + static_cast<size_t>(it) * a.n, a.lambda, n1, cudaMemcpyDeviceToDevice, st);
     }
     const int last = (it == plan.iterations - 1) ? 1 : 0;
-    const int b = plan.block[FLUID_KERNEL_DELTA];
     float4* q_out = rec ? rec->q + static_cast<size_t>(it) * a.n : nullptr;
-    launch_delta(plan, blocks_for(a.n, b), b, st, a, in, last, to_v2, last ? rest_commit : 0, q_out, it > 0);
+    launch_delta(plan, st, a, in, last, to_v2, last ? rest_commit : 0, q_out, it > 0);
     m.mark(FLUID_KERNEL_DELTA);
     if (rec)  // p^(it+1); the last iteration's lands in x (commit)
       cudaMemcpyAsync(rec->p + static_cast<size_t>(it + 1) * a.n, last ? a.x : a.p[in ^ 1], n4,
@@ -1835,28 +2337,22 @@ cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t s
     cudaEventRecord(dl->positions_done, dl->aux);
   }
   if (plan.xsph) {
-    const int b = plan.block[FLUID_KERNEL_XSPH];
     // The committing pass left {x, m / rho} in the p buffer it did not use.
     const float4* xr = a.p[plan.iterations == 0 ? 1 : (plan.iterations & 1)];
     const int rest = (!plan.vorticity && plan.restitution) ? 1 : 0;
     const int bound_par = plan.iterations > 0 ? ((plan.iterations - 1) & 1) : -1;
-    if (plan.vorticity)
-      launch_xsph<true>(plan.unroll[FLUID_KERNEL_XSPH], blocks_for(a.n, b), b, st, a, rest, xr, bound_par);
-    else
-      launch_xsph<false>(plan.unroll[FLUID_KERNEL_XSPH], blocks_for(a.n, b), b, st, a, rest, xr, bound_par);
+    if (plan.vorticity) launch_xsph<true>(plan, st, a, rest, xr, bound_par);
+    else launch_xsph<false>(plan, st, a, rest, xr, bound_par);
     m.mark(FLUID_KERNEL_XSPH);
   }
   if (plan.vorticity) {
-    const int bo = plan.block[FLUID_KERNEL_OMEGA];
     // Live bits of the committed positions: from XSPH when it ran, else
     // recorded here; the eta pass reads them.
-    if (plan.xsph) launch_omega<1>(plan.unroll[FLUID_KERNEL_OMEGA], blocks_for(a.n, bo), bo, st, a);
-    else launch_omega<2>(plan.unroll[FLUID_KERNEL_OMEGA], blocks_for(a.n, bo), bo, st, a);
+    if (plan.xsph) launch_omega<1>(plan, st, a);
+    else launch_omega<2>(plan, st, a);
     m.mark(FLUID_KERNEL_OMEGA);
     if (rec && rec->omega) cudaMemcpyAsync(rec->omega, a.omega, n4, cudaMemcpyDeviceToDevice, st);
-    const int be = plan.block[FLUID_KERNEL_ETA];
-    FGB_DISPATCH_UNROLL(plan.unroll[FLUID_KERNEL_ETA], k_eta, blocks_for(a.n, be), be, st, a,
-                        plan.restitution ? 1 : 0);
+    launch_eta(plan, st, a, plan.restitution ? 1 : 0);
     m.mark(FLUID_KERNEL_ETA);
   }
   if (dl) {

@@ -25,10 +25,14 @@ struct StepPlan {
   // for the neighbour kernels.
   int unroll[FLUID_KERNEL_COUNT];
   int block[FLUID_KERNEL_COUNT];
+  // Lanes per particle of the list passes (1, 2, 4, 8; see the several-lanes
+  // kernels): above 1 the unroll is not used.
+  int lanes[FLUID_KERNEL_COUNT];
   StepPlan() {
     for (int k = 0; k < FLUID_KERNEL_COUNT; ++k) {
       unroll[k] = 4;
       block[k] = kBlock;
+      lanes[k] = 1;
     }
   }
 };

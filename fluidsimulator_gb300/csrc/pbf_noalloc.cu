@@ -52,7 +52,8 @@ constexpr size_t kPl = kOmega + kF4;
 constexpr size_t kLive = kPl + kF4;
 constexpr size_t kReach = kLive + up(2 * sizeof(uint32_t) * kMaxN);
 constexpr size_t kMoved = kReach + up(sizeof(float) * kMaxN);
-constexpr size_t kSlot0 = kMoved + up(2 * sizeof(unsigned)), kSlot1 = kSlot0 + kI32, kRho0 = kSlot1 + kI32, kRho1 = kRho0 + kI32;
+constexpr unsigned kMovedSlots = 1024;  // displacement table of the list passes' bound, per parity
+constexpr size_t kSlot0 = kMoved + up(2 * sizeof(unsigned) * kMovedSlots), kSlot1 = kSlot0 + kI32, kRho0 = kSlot1 + kI32, kRho1 = kRho0 + kI32;
 constexpr size_t kLambda = kRho1 + kI32, kKeys0 = kLambda + kI32, kKeys1 = kKeys0 + kI32;
 constexpr size_t kVals0 = kKeys1 + kI32, kVals1 = kVals0 + kI32, kCnt = kVals1 + kI32;
 constexpr size_t kDepth = kCnt + kI32, kWbase = kDepth + up(sizeof(int) * (kMaxWarps + 1));
@@ -114,6 +115,7 @@ StepArgs carve(unsigned char* b, int n) {
   a.live = at<uint32_t>(b, kLive);
   a.reach = at<float>(b, kReach);
   a.moved = at<unsigned>(b, kMoved);
+  a.moved_mask = kMovedSlots - 1u;
   a.lambda = at<float>(b, kLambda);
   a.rho = at<float>(b, kRho1);
   a.keys[0] = at<uint32_t>(b, kKeys0);

@@ -289,7 +289,11 @@ class Solver {
     ok &= pl_.alloc(np) == cudaSuccess;
     ok &= live_.alloc(2 * np) == cudaSuccess;
     ok &= reach_.alloc(np) == cudaSuccess;
-    ok &= moved_.alloc(2 * static_cast<size_t>(S_)) == cudaSuccess;
+    // Displacement table of the list passes' bound: about one slot per 16
+    // particles (a bin holds ~64 at lattice density), a power of two.
+    moved_slots_ = 4096;
+    while (moved_slots_ < n_ / 16 && moved_slots_ < (1u << 22)) moved_slots_ <<= 1;
+    ok &= moved_.alloc(2 * static_cast<size_t>(moved_slots_)) == cudaSuccess;
     ok &= lambda_.alloc(np) == cudaSuccess;
     ok &= cnt_.alloc(np) == cudaSuccess;
     ok &= depth_.alloc(static_cast<size_t>(warps_) + 1) == cudaSuccess;
@@ -589,13 +593,27 @@ class Solver {
     // than a noise pick. One entry ahead is left out: with short lists (all
     // within the live-bit head of the vorticity passes) it can win by a few
     // per cent on register count, and it is ~2x slower once lists grow.
+    // Then several lanes per particle (2, 4, 8) at each block size, for the
+    // list passes only (the list build keeps its one-lane shape).
     const int unrolls[] = {4, 2, 8};
     const int blocks[] = {256, 128, 512};
-    for (int u : unrolls) {
-      for (int b : blocks) {
+    struct Shape {
+      int u, b, g;
+    };
+    std::vector<Shape> shapes;
+    for (int u : unrolls)
+      for (int b : blocks) shapes.push_back({u, b, 1});
+    for (int g : {2, 4, 8})
+      for (int b : blocks) shapes.push_back({4, b, g});
+    for (const Shape& sh : shapes) {
+      const int u = sh.u, b = sh.b, g = sh.g;
+      {
         for (int k = 0; k < FLUID_KERNEL_COUNT; ++k) {
-          if (tunable_unroll(k)) plan_.unroll[k] = u;
-          if (tunable_block(k)) plan_.block[k] = b;
+          if (tunable_unroll(k)) {
+            plan_.unroll[k] = u;
+            plan_.lanes[k] = g;
+          }
+          if (tunable_block(k)) plan_.block[k] = g == 1 || tunable_unroll(k) ? b : best.block[k];
         }
         invalidate_graphs();
         kernel_times(nullptr, nullptr, 0, 1);
@@ -612,10 +630,14 @@ class Solver {
         for (int k = 0; k < FLUID_KERNEL_COUNT; ++k) {
           if (!tunable_block(k) || stage_launches_[k] == 0) continue;
           if (k == FLUID_KERNEL_NBR_BUILD && b > 256) continue;  // launched at 256 regardless
+          if (g > 1 && !tunable_unroll(k)) continue;              // not a list pass
           const double avg = stage_ms_[k] / static_cast<double>(stage_launches_[k]);
           if (avg < 0.98 * best_ms[k]) {
             best_ms[k] = avg;
-            if (tunable_unroll(k)) best.unroll[k] = u;
+            if (tunable_unroll(k)) {
+              best.unroll[k] = u;
+              best.lanes[k] = g;
+            }
             best.block[k] = b;
           }
         }
@@ -624,6 +646,7 @@ class Solver {
     for (int k = 0; k < FLUID_KERNEL_COUNT; ++k) {
       plan_.unroll[k] = best.unroll[k];
       plan_.block[k] = best.block[k];
+      plan_.lanes[k] = best.lanes[k];
     }
     // Sort digit width: the three radix stages' time per step under each.
     double best_sort = 1e300;
@@ -865,6 +888,27 @@ class Solver {
     return FLUID_OK;
   }
 
+  int get_lanes(int32_t* lanes, int kernels) {
+    if (!lanes) return fail(FLUID_ERR_INVALID_ARGUMENT, "null lanes");
+    for (int k = 0; k < kernels && k < FLUID_KERNEL_COUNT; ++k) lanes[k] = plan_.lanes[k];
+    return FLUID_OK;
+  }
+
+  int set_lanes(const int32_t* lanes, int kernels) {
+    if (!lanes) return fail(FLUID_ERR_INVALID_ARGUMENT, "null lanes");
+    for (int k = 0; k < kernels && k < FLUID_KERNEL_COUNT; ++k) {
+      if (!(lanes[k] == 1 || lanes[k] == 2 || lanes[k] == 4 || lanes[k] == 8))
+        return fail(FLUID_ERR_INVALID_ARGUMENT, "lanes per particle must be 1, 2, 4 or 8");
+      if (lanes[k] != 1 && !tunable_unroll(k))
+        return fail(FLUID_ERR_INVALID_ARGUMENT, "only the neighbour-list passes take several lanes per particle");
+    }
+    int rc = synchronize();
+    if (rc) return rc;
+    for (int k = 0; k < kernels && k < FLUID_KERNEL_COUNT; ++k) plan_.lanes[k] = lanes[k];
+    invalidate_graphs();
+    return FLUID_OK;
+  }
+
   int kernel_times(double* ms, int64_t* launches, int kernels, int reset) {
     for (int k = 0; k < kernels && k < FLUID_KERNEL_COUNT; ++k) {
       if (ms) ms[k] = stage_ms_[k];
@@ -1054,6 +1098,7 @@ class Solver {
     a.live = live_.p;
     a.reach = reach_.p;
     a.moved = moved_.p;
+    a.moved_mask = moved_slots_ - 1u;
     a.radix_next = radix_next_.p;
     a.digit_total = digit_total_.p;
     a.table = table_.p;
@@ -1417,6 +1462,7 @@ class Solver {
   DBuf<uint32_t> live_;
   DBuf<float> reach_;
   DBuf<unsigned> moved_;
+  unsigned moved_slots_ = 0;
   DBuf<int> radix_next_;
   DBuf<long long> wbase_;
   DBuf<int2> table_;
@@ -1612,6 +1658,16 @@ int fluid_solver_get_tuning(fluid_solver* s, int32_t* unroll, int32_t* block, in
 int fluid_solver_set_tuning(fluid_solver* s, const int32_t* unroll, const int32_t* block, int32_t kernels) {
   FLUID_CHECK_SOLVER(s);
   return s->impl.set_tuning(unroll, block, kernels);
+}
+
+int fluid_solver_get_lanes(fluid_solver* s, int32_t* lanes, int32_t kernels) {
+  FLUID_CHECK_SOLVER(s);
+  return s->impl.get_lanes(lanes, kernels);
+}
+
+int fluid_solver_set_lanes(fluid_solver* s, const int32_t* lanes, int32_t kernels) {
+  FLUID_CHECK_SOLVER(s);
+  return s->impl.set_lanes(lanes, kernels);
 }
 
 int fluid_solver_get_sort_bits(fluid_solver* s, int32_t* bits) {

@@ -155,23 +155,32 @@ class Solver:
         return self.tuning()
 
     def tuning(self) -> dict:
+        """{kernel: {"unroll", "block", "lanes"}} of the tunable kernels (lanes:
+        lanes per particle of a list pass, 1 elsewhere)."""
         n = len(_capi.KERNEL_NAMES)
         u = (ctypes.c_int32 * n)()
         b = (ctypes.c_int32 * n)()
+        g = (ctypes.c_int32 * n)()
         self._check(self.lib.fluid_solver_get_tuning(self.h, u, b, n))
-        return {name: {"unroll": u[k], "block": b[k]} for k, name in enumerate(_capi.KERNEL_NAMES)
+        self._check(self.lib.fluid_solver_get_lanes(self.h, g, n))
+        return {name: {"unroll": u[k], "block": b[k], "lanes": g[k]} for k, name in enumerate(_capi.KERNEL_NAMES)
                 if name in _capi.TUNABLE}
 
     def set_tuning(self, shapes: dict) -> None:
+        """Sets launch shapes ({kernel: {"unroll", "block"[, "lanes"]}}); kernels
+        not named keep theirs."""
         n = len(_capi.KERNEL_NAMES)
         cur = self.tuning()
         u = (ctypes.c_int32 * n)(*([4] * n))
         b = (ctypes.c_int32 * n)(*([256] * n))
+        g = (ctypes.c_int32 * n)(*([1] * n))
         for k, name in enumerate(_capi.KERNEL_NAMES):
             shape = shapes.get(name, cur.get(name))
             if shape:
                 u[k], b[k] = shape["unroll"], shape["block"]
+                g[k] = shape.get("lanes", 1)
         self._check(self.lib.fluid_solver_set_tuning(self.h, u, b, n))
+        self._check(self.lib.fluid_solver_set_lanes(self.h, g, n))
 
     def sort_bits(self) -> int:
         """Digit width of the cell-key radix sort (8, 9 or 11)."""

@@ -242,7 +242,8 @@ int fluid_solver_kernel_times(fluid_solver* solver, double* ms_out,
  * Autotuner (no reference counterpart). Times each tunable kernel (the
  * neighbour-list passes and the list build) under every launch shape --
  * neighbour entries fetched ahead in {2, 4, 8}, threads per block in
- * {128, 256, 512} -- over `trials` discarded steps of the current state. It
+ * {128, 256, 512}, and for the list passes 2, 4 or 8 lanes per particle at
+ * each block size -- over `trials` discarded steps of the current state. It
  * keeps the default shape (4, 256) unless another is at least 2 % faster,
  * and else the fastest, per kernel. It then times the cell-key sort with 8-,
  * 9- and 11-bit digits and keeps the fastest width. One entry ahead (the
@@ -259,6 +260,16 @@ int fluid_solver_get_tuning(fluid_solver* solver, int32_t* unroll, int32_t* bloc
                             int32_t kernels);
 int fluid_solver_set_tuning(fluid_solver* solver, const int32_t* unroll,
                             const int32_t* block, int32_t kernels);
+
+/* Lanes per particle of each neighbour-list pass (FLUID_KERNEL_LAMBDA, _DELTA,
+ * _XSPH, _OMEGA, _ETA): 1 (one lane walks a particle's list; the unroll of
+ * fluid_solver_set_tuning applies), or 2, 4 or 8 lanes that split the list
+ * into rounds and add the round's terms in list order, for launches short of
+ * warps. Every other kernel takes 1. The autotuner chooses it with the other
+ * shapes; results are identical under every choice. (No counterpart in the
+ * reference, whose CUDA step maps one thread to a particle.) */
+int fluid_solver_get_lanes(fluid_solver* solver, int32_t* lanes, int32_t kernels);
+int fluid_solver_set_lanes(fluid_solver* solver, const int32_t* lanes, int32_t kernels);
 
 /* Digit width of the cell-key radix sort: 8 (default), 9 or 11 bits. Keys of
  * b bits take ceil(b / width) passes; the permutation does not depend on it. */

@@ -363,8 +363,8 @@ def test_capacity_regrow_keeps_results(cuda_lib, oracle_lib):
     np.testing.assert_array_equal(b["vel"], a["vel"])
 
 
-@pytest.mark.parametrize("block", [128, 256, 512])
-def test_batched_regrow_matches_oracle(cuda_lib, oracle_lib, block):
+@pytest.mark.parametrize("block, lanes", [(128, 1), (256, 1), (512, 1), (256, 4)])
+def test_batched_regrow_matches_oracle(cuda_lib, oracle_lib, block, lanes):
     """Several collapsing scenes in one solver: the lists outgrow their
     capacity mid-run (blocks of the list build fail while others proceed) and
     the failed steps are re-run, at every list-pass block size; each scene
@@ -373,7 +373,8 @@ def test_batched_regrow_matches_oracle(cuda_lib, oracle_lib, block):
     refs = [oracle_lib.Oracle().run(sc.params, sc.pos, sc.vel, 0.0, 50) for sc in scs]
     s = Solver(0)
     s.configure([sc.params for sc in scs], [sc.count for sc in scs])
-    s.set_tuning({k: {"unroll": 4, "block": block} for k in _capi.TUNABLE})
+    s.set_tuning({k: {"unroll": 4, "block": block, "lanes": lanes if k in _capi.LIST_PASSES else 1}
+                  for k in _capi.TUNABLE})
     s.upload(np.concatenate([sc.pos for sc in scs], axis=1), np.concatenate([sc.vel for sc in scs], axis=1))
     s.step(50)
     pos, vel = s.download()
@@ -600,6 +601,61 @@ def test_every_unroll_matches_oracle(cuda_lib, oracle_lib, unroll):
     np.testing.assert_array_equal(vel, ref["vel"])
 
 
+@pytest.mark.parametrize("lanes", [2, 4, 8])
+@pytest.mark.parametrize("block", [128, 512])
+def test_every_lane_count_matches_oracle(cuda_lib, oracle_lib, lanes, block):
+    """Several lanes per particle in every list pass (rounds of `lanes`
+    entries, terms added in list order through shuffles) give the oracle's
+    bits over 15 collapsing steps with s_corr, XSPH, vorticity and planes on
+    (lists grow past the 64-entry live-bit head and regrow)."""
+    sc = scenes.dam_break(9, seed=17, flags=True)
+    ref = oracle_lib.Oracle().run(sc.params, sc.pos, sc.vel, 0.0, 15)
+    s = Solver(0)
+    s.configure([sc.params], [sc.count])
+    s.set_tuning({k: {"unroll": 4, "block": block, "lanes": lanes if k in _capi.LIST_PASSES else 1}
+                  for k in _capi.TUNABLE})
+    assert all(s.tuning()[k]["lanes"] == lanes for k in _capi.LIST_PASSES)
+    s.upload(sc.pos, sc.vel)
+    s.step(15)
+    pos, vel = s.download()
+    s.close()
+    np.testing.assert_array_equal(pos, ref["pos"])
+    np.testing.assert_array_equal(vel, ref["vel"])
+
+
+def test_mixed_lanes_on_a_one_wave_collapse(cuda_lib, oracle_lib):
+    """The 32,768-particle differentiable scene (its launches fill a fifth of
+    the SMs) over 20 steps into its collapse (~380 neighbours per particle,
+    ~1,700 at most), with a different lane count per list pass, against the
+    oracle's keys, order, counts, rho, lambda, positions and velocities."""
+    sc = scenes.differentiable_block(32, seed=0)
+    a = oracle_lib.Oracle().run(sc.params, sc.pos, sc.vel, 0.0, 20, dump=True)
+    s = Solver(0)
+    s.configure([sc.params], [sc.count])
+    lanes = {"k_lambda": 4, "k_delta": 8, "k_xsph": 2, "k_omega": 4, "k_eta": 1}
+    s.set_tuning({k: {"unroll": 2, "block": 256, "lanes": lanes.get(k, 1)} for k in _capi.TUNABLE})
+    s.upload(sc.pos, sc.vel)
+    s.step(20)
+    rec = {k: s.read_debug(w) for k, w in DEBUG.items()}
+    pos, vel = s.download()
+    s.close()
+    for k in DEBUG:
+        np.testing.assert_array_equal(rec[k], a[k], err_msg=k)
+    np.testing.assert_array_equal(pos, a["pos"])
+    np.testing.assert_array_equal(vel, a["vel"])
+
+
+def test_lanes_are_checked(cuda_lib):
+    sc = scenes.dam_break(4, seed=1)
+    s = Solver(0)
+    s.configure([sc.params], [sc.count])
+    with pytest.raises(FluidError):
+        s.set_tuning({"k_lambda": {"unroll": 4, "block": 256, "lanes": 3}})
+    with pytest.raises(FluidError):
+        s.set_tuning({"k_nbr_build": {"unroll": 4, "block": 256, "lanes": 2}})
+    s.close()
+
+
 def _corners():
     """The oracle's parameter corners plus every combination of the passes
     that follow the Jacobi loop (each takes its own commit path)."""
@@ -715,8 +771,8 @@ def test_live_bits_with_mixed_scene_flags(cuda_lib, oracle_lib):
         off += sc.count
 
 
-@pytest.mark.parametrize("unroll", [1, 2, 4, 8])
-def test_lists_longer_than_the_live_bit_head(cuda_lib, oracle_lib, unroll):
+@pytest.mark.parametrize("unroll, lanes", [(1, 1), (2, 1), (4, 1), (8, 1), (4, 2), (4, 4), (4, 8)])
+def test_lists_longer_than_the_live_bit_head(cuda_lib, oracle_lib, unroll, lanes):
     """A dense lattice (spacing 0.03 at h = 0.1, ~150 neighbours): every
     list runs past the 64 entries that carry live bits, so the XSPH and
     vorticity passes go through both halves of their walkers."""
@@ -729,7 +785,8 @@ def test_lists_longer_than_the_live_bit_head(cuda_lib, oracle_lib, unroll):
     assert ref["neighbor_counts"].mean() > 100
     s = Solver(0)
     s.configure([sc.params], [sc.count])
-    s.set_tuning({k: {"unroll": unroll, "block": 128} for k in _capi.TUNABLE})
+    s.set_tuning({k: {"unroll": unroll, "block": 128, "lanes": lanes if k in _capi.LIST_PASSES else 1}
+                  for k in _capi.TUNABLE})
     s.upload(sc.pos, sc.vel)
     s.step(1)
     got_pos, got_vel = s.download()
