@@ -10,7 +10,7 @@ from __future__ import annotations
 
 import ctypes
 import os
-from ctypes import POINTER, c_char_p, c_double, c_float, c_int, c_int32, c_int64, c_void_p
+from ctypes import POINTER, c_char_p, c_double, c_float, c_int, c_int32, c_int64, c_uint64, c_void_p
 
 MAX_PLANES = 32
 
@@ -188,6 +188,13 @@ def _declare(lib):
     lib.fluid_solver_get_tuning.restype = c_int
     lib.fluid_solver_set_tuning.argtypes = [c_void_p, POINTER(c_int32), POINTER(c_int32), c_int32]
     lib.fluid_solver_set_tuning.restype = c_int
+    lib.fluid_fill_block.argtypes = [c_int64, c_int64, c_int64, c_float, c_float, c_float, c_float, c_double,
+                                     c_uint64, c_int64, c_void_p, c_void_p, c_void_p, c_void_p]
+    lib.fluid_fill_block.restype = c_int
+    lib.fluid_fill_shape.argtypes = [c_int32, POINTER(c_float), POINTER(c_float), c_float, POINTER(c_float),
+                                     c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int64,
+                                     POINTER(c_int64), c_void_p]
+    lib.fluid_fill_shape.restype = c_int
     lib.fluid_solver_get_lanes.argtypes = [c_void_p, POINTER(c_int32), c_int32]
     lib.fluid_solver_get_lanes.restype = c_int
     lib.fluid_solver_set_lanes.argtypes = [c_void_p, POINTER(c_int32), c_int32]

@@ -29,7 +29,8 @@ LIB_DIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIB_DIR, "libfluid_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["pbf_kernels.cu", "pbf_adjoint.cu", "pbf_solver.cu", "pbf_noalloc.cu", "host/fluid_gb300.cpp", "host/vtk_output.cpp"]
+SOURCES = ["pbf_kernels.cu", "pbf_adjoint.cu", "pbf_solver.cu", "pbf_noalloc.cu", "pbf_fill.cu", "host/fluid_gb300.cpp",
+           "host/vtk_output.cpp"]
 
 
 def nvcc() -> str:

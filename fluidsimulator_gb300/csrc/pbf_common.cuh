@@ -124,6 +124,7 @@ struct StepArgs {
   uint32_t* digit_total;     // kRadixMaxPasses x kRadixMaxBins: counts, then starts
   int2* table;
   int* cnt;
+  const int* cnt_old;     // list lengths of the previous step, by its slot (zero after an upload)
   int* depth;             // per warp
   long long* wbase;       // per warp
   int* ovf;               // per warp: list longer than the shared-memory staging

@@ -913,17 +913,23 @@ __device__ __forceinline__ void for_each_pair_candidate(const StepArgs& a, const
 }
 
 // Neighbour lists in one scan (core.cpp:205-247). Each lane stages its first
-// kStage list entries in
-// shared memory while it scans; the block then claims its warps' 32-wide
-// slices with one atomic on the list cursor (placement varies run to run,
-// every list's content and order do not) and writes the staged entries out
-// as coalesced 128-byte rows. Warps with a longer list set ovf[w] and
-// k_nbr_overflow writes their remaining entries.
-__global__ void __launch_bounds__(kMaxBuildBlock) k_nbr_build(StepArgs a) {
+// kStage list entries in shared memory while it scans; the block then claims
+// its warps' 32-wide slices with one atomic on the list cursor (placement
+// varies run to run, every list's content and order do not) and writes the
+// staged entries out as coalesced 128-byte rows.
+//
+// Longer lists (the collapsed phase) would need a second scan for the entries
+// past kStage. A warp whose particles' previous-step lists were longer than
+// kStage (cnt_old, through each particle's previous slot) therefore reserves
+// its slice before the scan, sized 5/4 of the longest plus 8 rows, and writes
+// entries past kStage straight into it as it finds them; only a warp whose
+// lists outgrow that reservation (or had no previous step) falls back to a
+// fresh slice after the scan plus the re-scan of k_nbr_overflow (ovf[w]).
+__global__ void __launch_bounds__(kMaxBuildBlock, 5) k_nbr_build(StepArgs a) {
   extern __shared__ int stage[];
   // Other blocks of this launch may set the status (capacity) while this
   // one starts: read it once for the whole block, so either every warp
-  // returns here or every warp reaches the barriers and the slice claim
+  // returns here or every warp reaches the barriers and the slice claims
   // below (a warp left behind by an early return of thread 0's warp would
   // read an unset block_base).
   __shared__ int block_failed;
@@ -933,6 +939,34 @@ __global__ void __launch_bounds__(kMaxBuildBlock) k_nbr_build(StepArgs a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int* mine = stage + warp * (kStage * 32) + lane;  // entry k at mine[32 k]
+  const bool warp_live = (i - lane) < a.n;
+  // Rows reserved before the scan: 0, or 5/4 of the warp's longest previous
+  // list plus 8 when that exceeded kStage.
+  int prev = 0;
+  if (i < a.n && a.cnt_old) prev = a.cnt_old[a.slot_old[__float_as_int(a.x[i].w)]];
+  const int prev_max = __reduce_max_sync(kFull, prev);
+  const int reserve = (warp_live && prev_max > kStage) ? prev_max + prev_max / 4 + 8 : 0;
+  __shared__ int wres[kMaxBuildBlock / 32];
+  __shared__ unsigned long long woff[kMaxBuildBlock / 32];  // each warp's reserved slice
+  __shared__ int res_ok;
+  if (lane == 0) wres[warp] = reserve;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long total = 0;
+    for (int w = 0; w < static_cast<int>(blockDim.x / 32); ++w) total += 32ull * wres[w];
+    res_ok = 1;
+    if (total) {
+      unsigned long long base = atomicAdd(&a.status->cursor, total);
+      res_ok = base + total <= static_cast<unsigned long long>(a.nbr_capacity);
+      if (!res_ok) set_error(a.status, FLUID_ERR_CAPACITY);
+      for (int w = 0; w < static_cast<int>(blockDim.x / 32); ++w) {
+        woff[w] = base;
+        base += 32ull * wres[w];
+      }
+    }
+  }
+  __syncthreads();
+  if (!res_ok) return;  // the step fails (capacity) and is re-run after the lists grow
   int count = 0;
   if (i < a.n) {
     const uint32_t* ks = sorted_keys(a, a.status->npass);
@@ -944,6 +978,7 @@ __global__ void __launch_bounds__(kMaxBuildBlock) k_nbr_build(StepArgs a) {
     auto test = [&](int j, const float4 q) {
       if (dist2(p.x - q.x, p.y - q.y, p.z - q.z) < h2) {
         if (count < kStage) mine[32 * count] = j;
+        else if (count < reserve) a.nbr[woff[warp] + lane + 32ull * count] = j;  // reserved slice
         ++count;
       }
     };
@@ -953,12 +988,12 @@ __global__ void __launch_bounds__(kMaxBuildBlock) k_nbr_build(StepArgs a) {
   }
   const int mx = __reduce_max_sync(kFull, count);
   const unsigned sum = __reduce_add_sync(kFull, static_cast<unsigned>(count));
+  const bool fits = reserve && mx <= reserve;  // the reserved slice holds every list
   __shared__ int wdepth[kMaxBuildBlock / 32];
   __shared__ unsigned long long block_base;
   __shared__ int block_ok;
-  const bool warp_live = (i - lane) < a.n;
   if (lane == 0) {
-    wdepth[warp] = warp_live ? mx : 0;
+    wdepth[warp] = (warp_live && !fits) ? mx : 0;  // rows still to claim
     if (warp_live) {
       if (sum) atomicAdd(&a.status->pairs, static_cast<unsigned long long>(sum));
       if (mx) atomicMax(&a.status->nbr_max, mx);
@@ -968,15 +1003,24 @@ __global__ void __launch_bounds__(kMaxBuildBlock) k_nbr_build(StepArgs a) {
   if (threadIdx.x == 0) {
     unsigned long long total = 0;
     for (int w = 0; w < static_cast<int>(blockDim.x / 32); ++w) total += 32ull * wdepth[w];
-    const unsigned long long base = atomicAdd(&a.status->cursor, total);
-    block_ok = base + total <= static_cast<unsigned long long>(a.nbr_capacity);
-    if (!block_ok) set_error(a.status, FLUID_ERR_CAPACITY);
-    block_base = base;
+    block_ok = 1;
+    block_base = 0;
+    if (total) {
+      const unsigned long long base = atomicAdd(&a.status->cursor, total);
+      block_ok = base + total <= static_cast<unsigned long long>(a.nbr_capacity);
+      if (!block_ok) set_error(a.status, FLUID_ERR_CAPACITY);
+      block_base = base;
+    }
   }
   __syncthreads();
   if (!warp_live || !block_ok) return;
-  unsigned long long off = block_base;
-  for (int w = 0; w < warp; ++w) off += 32ull * wdepth[w];
+  unsigned long long off;
+  if (fits) {
+    off = woff[warp];
+  } else {
+    off = block_base;
+    for (int w = 0; w < warp; ++w) off += 32ull * wdepth[w];
+  }
   int* out = a.nbr + off + lane;
   const int staged = mx < kStage ? mx : kStage;
   for (int k = 0; k < staged; ++k)
@@ -984,7 +1028,7 @@ __global__ void __launch_bounds__(kMaxBuildBlock) k_nbr_build(StepArgs a) {
   if (lane == 0) {
     a.wbase[i >> 5] = static_cast<long long>(off);
     a.depth[i >> 5] = mx;
-    a.ovf[i >> 5] = mx > kStage ? 1 : 0;
+    a.ovf[i >> 5] = (mx > kStage && !fits) ? 1 : 0;
   }
 }
 
@@ -1674,21 +1718,24 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_eta(StepArgs
 // bound's skips.
 
 // Thread -> (particle slot, lane within its group, group's first warp lane).
+// Every lane of the warp takes part in the walk (a lane past the last
+// particle, or of a particle whose walk is skipped, walks an empty list), so
+// the shuffles and ballots run on the whole warp at once: shuffles whose masks
+// named only a group would let the warp's groups run their rounds apart and
+// serialise them.
 template <int G>
 struct LaneGroup {
   int i, sub, lead;
-  unsigned mask;
   __device__ __forceinline__ LaneGroup() {
     const long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
     i = static_cast<int>(t / G);
     const int lane = threadIdx.x & 31;
     sub = lane & (G - 1);
     lead = lane & ~(G - 1);
-    mask = ((1u << G) - 1u) << lead;
   }
   __device__ __forceinline__ float min_over(float v) const {
 #pragma unroll
-    for (int o = G / 2; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(mask, v, o));
+    for (int o = G / 2; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(kFull, v, o));
     return v;
   }
 };
@@ -1698,25 +1745,26 @@ template <int K>
 struct Terms {
   float f[K];
   bool live;
-  __device__ __forceinline__ Terms shfl(unsigned mask, int src) const {
+  __device__ __forceinline__ Terms shfl(int src) const {
     Terms o;
 #pragma unroll
-    for (int q = 0; q < K; ++q) o.f[q] = __shfl_sync(mask, f[q], src);
+    for (int q = 0; q < K; ++q) o.f[q] = __shfl_sync(kFull, f[q], src);
     o.live = false;
     return o;
   }
 };
 
-// Walks entries rG + sub (rounds r = 0, 1, ...) of a list of n entries:
-// term(record, in_list) gives an entry's Terms, add(Terms) accumulates, and
-// each lane of the group adds the round's G terms in list order. Returns the
-// live bits of entries 0..63 (the same on every lane of the group).
+// Walks entries rG + sub (rounds r = 0, 1, ... up to the warp's longest
+// list) of a list of n entries: term(record, in_list) gives an entry's Terms,
+// add(Terms) accumulates, and each lane of the group adds the round's G terms
+// in list order. Called by every lane of the warp. Returns the live bits of
+// entries 0..63 (the same on every lane of the group).
 template <int G, int K, typename Load, typename Term, typename Add>
 __device__ __forceinline__ unsigned long long walk_lanes(const int* __restrict__ list, int n, const LaneGroup<G>& L,
                                                          Load&& load, Term&& term, Add&& add) {
   using Rec = decltype(load(0));
   unsigned long long bits = 0ull;
-  const int rounds = (n + G - 1) / G;
+  const int rounds = __reduce_max_sync(kFull, (n + G - 1) / G);
   int k = L.sub;
   int j1 = (k + G < n) ? __ldcs(list + 32ll * (k + G)) : 0;
   Rec cur = (k < n) ? load(__ldcs(list + 32ll * k)) : Rec{};
@@ -1724,10 +1772,10 @@ __device__ __forceinline__ unsigned long long walk_lanes(const int* __restrict__
     const int j2 = (k + 2 * G < n) ? __ldcs(list + 32ll * (k + 2 * G)) : 0;
     const Rec nxt = (k + G < n) ? load(j1) : Rec{};
     const Terms<K> t = term(cur, k < n);
-    const unsigned lb = (__ballot_sync(L.mask, t.live) >> L.lead) & ((1u << G) - 1u);
+    const unsigned lb = (__ballot_sync(kFull, t.live) >> L.lead) & ((1u << G) - 1u);
 #pragma unroll
     for (int u = 0; u < G; ++u) {
-      const Terms<K> tu = t.shfl(L.mask, L.lead + u);
+      const Terms<K> tu = t.shfl(L.lead + u);
       if ((lb >> u) & 1u) add(tu);
     }
     if (r * G < kLiveEntries) bits |= static_cast<unsigned long long>(lb) << (r * G);
@@ -1743,57 +1791,56 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_lambda_lanes
   clear_moved(a.moved + static_cast<size_t>(in) * (a.moved_mask + 1u), a.moved_mask);
   const LaneGroup<G> L;
   const int i = L.i;
-  if (i >= a.n) return;
+  const bool valid = i < a.n;
   const float4* __restrict__ pos = a.p[in];
-  const float4 p = pos[i];
-  const int scene = __float_as_int(p.w);
+  const float4 p = valid ? pos[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  const int scene = valid ? __float_as_int(p.w) : 0;
   const SceneConst& c = a.sc[scene];
-  const int n = a.cnt[i];
-  const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (i & 31);
   const float h2 = c.h2;
   LambdaAcc acc;
   bool skip = false;
   float bound = 0.0f;
   if constexpr (kLiveOut) {
-    const float4 q = a.p[in ^ 1][i];
-    skip = beyond_reach(c, a.reach[i], moved_by(p.x - q.x, p.y - q.y, p.z - q.z),
-                        moved_around(a, c, scene, i, in ^ 1), bound);
+    if (valid) {
+      const float4 q = a.p[in ^ 1][i];
+      skip = beyond_reach(c, a.reach[i], moved_by(p.x - q.x, p.y - q.y, p.z - q.z),
+                          moved_around(a, c, scene, i, in ^ 1), bound);
+    }
     count_skipped(a.status, skip && L.sub == 0);
   }
-  unsigned long long bits = 0ull;
-  if (!skip) {
-    auto load = [&](int j) { return __ldg(pos + j); };
-    auto term = [&](const float4 q, bool in_list) {  // LambdaAcc::add, term by term
-      Terms<5> t;
-      const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
-      const float r2 = dist2(dx, dy, dz);
-      if (in_list) acc.r2min = fminf(acc.r2min, r2);
-      t.live = in_list && r2 < h2;
-      if (t.live) {
-        t.f[0] = poly6(c, r2);
-        const float gf = spiky(c, clamped_r(c, r2));
-        t.f[1] = gf * dx;
-        t.f[2] = gf * dy;
-        t.f[3] = gf * dz;
-        const float ng = -c.grad_scale;
-        const float jx = ng * t.f[1], jy = ng * t.f[2], jz = ng * t.f[3];
-        t.f[4] = jx * jx + jy * jy + jz * jz;
-      } else {
-        t.f[0] = t.f[1] = t.f[2] = t.f[3] = t.f[4] = 0.0f;
-      }
-      return t;
-    };
-    auto add = [&](const Terms<5>& t) {
-      acc.rho += t.f[0];
-      acc.gsx += t.f[1];
-      acc.gsy += t.f[2];
-      acc.gsz += t.f[3];
-      acc.sum_g2 += t.f[4];
-    };
-    bits = walk_lanes<G, 5>(list, n, L, load, term, add);
-    acc.r2min = L.min_over(acc.r2min);
-  }
-  if (L.sub != 0) return;
+  const int n = (valid && !skip) ? a.cnt[i] : 0;
+  const int* __restrict__ list = a.nbr + (valid ? a.wbase[i >> 5] + (i & 31) : 0);
+  auto load = [&](int j) { return __ldg(pos + j); };
+  auto term = [&](const float4 q, bool in_list) {  // LambdaAcc::add, term by term
+    Terms<5> t;
+    const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+    const float r2 = dist2(dx, dy, dz);
+    if (in_list) acc.r2min = fminf(acc.r2min, r2);
+    t.live = in_list && r2 < h2;
+    if (t.live) {
+      t.f[0] = poly6(c, r2);
+      const float gf = spiky(c, clamped_r(c, r2));
+      t.f[1] = gf * dx;
+      t.f[2] = gf * dy;
+      t.f[3] = gf * dz;
+      const float ng = -c.grad_scale;
+      const float jx = ng * t.f[1], jy = ng * t.f[2], jz = ng * t.f[3];
+      t.f[4] = jx * jx + jy * jy + jz * jz;
+    } else {
+      t.f[0] = t.f[1] = t.f[2] = t.f[3] = t.f[4] = 0.0f;
+    }
+    return t;
+  };
+  auto add = [&](const Terms<5>& t) {
+    acc.rho += t.f[0];
+    acc.gsx += t.f[1];
+    acc.gsy += t.f[2];
+    acc.gsz += t.f[3];
+    acc.sum_g2 += t.f[4];
+  };
+  const unsigned long long bits = walk_lanes<G, 5>(list, n, L, load, term, add);
+  acc.r2min = L.min_over(acc.r2min);
+  if (!valid || L.sub != 0) return;
   if constexpr (kLiveOut) store_live(a.live, a.n, i, bits);
   float rho;
   const float lam = finish_lambda(c, acc.rho, acc.gsx, acc.gsy, acc.gsz, acc.sum_g2, rho);
@@ -1809,47 +1856,46 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS)
   if (failed(a.status)) return;
   const LaneGroup<G> L;
   const int i = L.i;
-  if (i >= a.n) return;
-  const float4 p = a.p[in][i];
-  const SceneConst& c = a.sc[__float_as_int(p.w)];
-  const int n = a.cnt[i];
-  const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (i & 31);
+  const bool valid = i < a.n;
+  const float4 p = valid ? a.p[in][i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  const SceneConst& c = a.sc[valid ? __float_as_int(p.w) : 0];
   const float4* __restrict__ pl = a.pl;
-  const float li = a.lambda[i];
+  const float li = valid ? a.lambda[i] : 0.0f;
   const float h2 = c.h2;
   float ax = 0.0f, ay = 0.0f, az = 0.0f;
   const bool scorr = c.scorr_on != 0;
-  const bool none = kLiveIn && a.reach[i] >= __fmul_ru(c.h, kReachGrow);
-  if (!none) {
-    auto load = [&](int j) { return __ldg(pl + j); };
-    auto term = [&](const float4 r, bool in_list) {  // k_delta's one(), term by term
-      Terms<3> t;
-      const float dx = p.x - r.x, dy = p.y - r.y, dz = p.z - r.z;
-      const float r2 = dist2(dx, dy, dz);
-      t.live = in_list && r2 < h2;
-      if (t.live) {
-        const float gf = spiky(c, clamped_r(c, r2));
-        float sc = li + r.w;
-        if (scorr) {
-          const float ratio = poly6(c, r2) * c.scorr_inv_wdq;
-          sc += c.scorr_neg_k * pow_k<kPow>(ratio, c.scorr_n);
-        }
-        t.f[0] = sc * gf * dx;
-        t.f[1] = sc * gf * dy;
-        t.f[2] = sc * gf * dz;
-      } else {
-        t.f[0] = t.f[1] = t.f[2] = 0.0f;
+  // The lambda pass of this iteration left reach[i] at these positions.
+  const bool none = !valid || (kLiveIn && a.reach[i] >= __fmul_ru(c.h, kReachGrow));
+  const int n = none ? 0 : a.cnt[i];
+  const int* __restrict__ list = a.nbr + (valid ? a.wbase[i >> 5] + (i & 31) : 0);
+  auto load = [&](int j) { return __ldg(pl + j); };
+  auto term = [&](const float4 r, bool in_list) {  // k_delta's one(), term by term
+    Terms<3> t;
+    const float dx = p.x - r.x, dy = p.y - r.y, dz = p.z - r.z;
+    const float r2 = dist2(dx, dy, dz);
+    t.live = in_list && r2 < h2;
+    if (t.live) {
+      const float gf = spiky(c, clamped_r(c, r2));
+      float sc = li + r.w;
+      if (scorr) {
+        const float ratio = poly6(c, r2) * c.scorr_inv_wdq;
+        sc += c.scorr_neg_k * pow_k<kPow>(ratio, c.scorr_n);
       }
-      return t;
-    };
-    auto add = [&](const Terms<3>& t) {
-      ax += t.f[0];
-      ay += t.f[1];
-      az += t.f[2];
-    };
-    walk_lanes<G, 3>(list, n, L, load, term, add);
-  }
-  if (L.sub != 0) return;
+      t.f[0] = sc * gf * dx;
+      t.f[1] = sc * gf * dy;
+      t.f[2] = sc * gf * dz;
+    } else {
+      t.f[0] = t.f[1] = t.f[2] = 0.0f;
+    }
+    return t;
+  };
+  auto add = [&](const Terms<3>& t) {
+    ax += t.f[0];
+    ay += t.f[1];
+    az += t.f[2];
+  };
+  walk_lanes<G, 3>(list, n, L, load, term, add);
+  if (!valid || L.sub != 0) return;
   delta_out(a, c, i, p, ax, ay, az, in, last, to_v2, rest, q_out);
 }
 
@@ -1859,56 +1905,57 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_xsph_lanes(S
   if (failed(a.status)) return;
   const LaneGroup<G> L;
   const int i = L.i;
-  if (i >= a.n) return;
+  const bool valid = i < a.n;
   const float4* __restrict__ xs = xr;
   const float4* __restrict__ vs = a.v2;
-  const float4 xi = xs[i];
-  const float4 vi = vs[i];
-  const int scene = __float_as_int(vi.w);
+  const float4 xi = valid ? xs[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  const float4 vi = valid ? vs[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  const int scene = valid ? __float_as_int(vi.w) : 0;
   const SceneConst& c = a.sc[scene];
   float vx = vi.x, vy = vi.y, vz = vi.z;
-  unsigned long long bits = ~0ull;
   bool skip = false;
-  if (c.xsph_on && bound_par >= 0) {
+  if (valid && c.xsph_on && bound_par >= 0) {
     const float4 q = a.p[bound_par][i];
     float bound;
     skip = beyond_reach(c, a.reach[i], moved_by(xi.x - q.x, xi.y - q.y, xi.z - q.z),
                         moved_around(a, c, scene, i, bound_par), bound);
-    if (skip) bits = 0ull;
   }
   if (bound_par >= 0) count_skipped(a.status, skip && L.sub == 0);
-  if (c.xsph_on && !skip) {
-    const int n = a.cnt[i];
-    const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (i & 31);
-    const float h2 = c.h2;
-    float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-    auto load = [&](int j) { return PosVel{__ldg(xs + j), __ldg(vs + j)}; };
-    auto term = [&](const PosVel r, bool in_list) {  // k_xsph's one(), term by term
-      Terms<3> t;
-      const float r2 = dist2(xi.x - r.x.x, xi.y - r.x.y, xi.z - r.x.z);
-      t.live = in_list && r2 < h2;
-      if (t.live) {
-        const float W = poly6(c, r2);
-        const float inv_rho_j = r.x.w;
-        t.f[0] = (r.v.x - vi.x) * W * inv_rho_j;
-        t.f[1] = (r.v.y - vi.y) * W * inv_rho_j;
-        t.f[2] = (r.v.z - vi.z) * W * inv_rho_j;
-      } else {
-        t.f[0] = t.f[1] = t.f[2] = 0.0f;
-      }
-      return t;
-    };
-    auto add = [&](const Terms<3>& t) {
-      sx += t.f[0];
-      sy += t.f[1];
-      sz += t.f[2];
-    };
-    bits = walk_lanes<G, 3>(list, n, L, load, term, add);
+  const bool walk = valid && c.xsph_on && !skip;
+  const int n = walk ? a.cnt[i] : 0;
+  const int* __restrict__ list = a.nbr + (valid ? a.wbase[i >> 5] + (i & 31) : 0);
+  const float h2 = c.h2;
+  float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+  auto load = [&](int j) { return PosVel{__ldg(xs + j), __ldg(vs + j)}; };
+  auto term = [&](const PosVel r, bool in_list) {  // k_xsph's one(), term by term
+    Terms<3> t;
+    const float r2 = dist2(xi.x - r.x.x, xi.y - r.x.y, xi.z - r.x.z);
+    t.live = in_list && r2 < h2;
+    if (t.live) {
+      const float W = poly6(c, r2);
+      const float inv_rho_j = r.x.w;
+      t.f[0] = (r.v.x - vi.x) * W * inv_rho_j;
+      t.f[1] = (r.v.y - vi.y) * W * inv_rho_j;
+      t.f[2] = (r.v.z - vi.z) * W * inv_rho_j;
+    } else {
+      t.f[0] = t.f[1] = t.f[2] = 0.0f;
+    }
+    return t;
+  };
+  auto add = [&](const Terms<3>& t) {
+    sx += t.f[0];
+    sy += t.f[1];
+    sz += t.f[2];
+  };
+  unsigned long long bits = walk_lanes<G, 3>(list, n, L, load, term, add);
+  if (!valid || L.sub != 0) return;
+  if (c.xsph_on) {
     vx += c.visc_c * sx;
     vy += c.visc_c * sy;
     vz += c.visc_c * sz;
+  } else {
+    bits = ~0ull;  // no XSPH in this scene: the vorticity passes walk every entry
   }
-  if (L.sub != 0) return;
   if (kLiveOut) store_live(a.live, a.n, i, bits);
   if (rest && c.rest_on) restitution(c, xi.x, xi.y, xi.z, vx, vy, vz);
   a.v[i] = make_float4(vx, vy, vz, vi.w);
@@ -1920,44 +1967,42 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_omega_lanes(
   if (failed(a.status)) return;
   const LaneGroup<G> L;
   const int i = L.i;
-  if (i >= a.n) return;
+  const bool valid = i < a.n;
   const float4* __restrict__ xs = a.x;
   const float4* __restrict__ vs = a.v;
-  const float4 xi = xs[i];
-  const float4 vi = vs[i];
-  const SceneConst& c = a.sc[__float_as_int(vi.w)];
+  const float4 xi = valid ? xs[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  const float4 vi = valid ? vs[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  const SceneConst& c = a.sc[valid ? __float_as_int(vi.w) : 0];
   float ox = 0.0f, oy = 0.0f, oz = 0.0f;
-  unsigned long long bits = ~0ull;
-  if (c.vort_on) {
-    const int n = a.cnt[i];
-    const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (i & 31);
-    const float h2 = c.h2;
-    auto load = [&](int j) { return PosVel{__ldg(xs + j), __ldg(vs + j)}; };
-    auto term = [&](const PosVel r, bool in_list) {  // k_omega's one(), term by term
-      Terms<3> t;
-      const float dx = xi.x - r.x.x, dy = xi.y - r.x.y, dz = xi.z - r.x.z;
-      const float r2 = dist2(dx, dy, dz);
-      t.live = in_list && r2 < h2;
-      if (t.live) {
-        const float gf = spiky(c, clamped_r(c, r2));
-        const float gx = gf * dx, gy = gf * dy, gz = gf * dz;
-        const float ux = r.v.x - vi.x, uy = r.v.y - vi.y, uz = r.v.z - vi.z;
-        t.f[0] = uy * gz - uz * gy;
-        t.f[1] = uz * gx - ux * gz;
-        t.f[2] = ux * gy - uy * gx;
-      } else {
-        t.f[0] = t.f[1] = t.f[2] = 0.0f;
-      }
-      return t;
-    };
-    auto add = [&](const Terms<3>& t) {
-      ox += t.f[0];
-      oy += t.f[1];
-      oz += t.f[2];
-    };
-    bits = walk_lanes<G, 3>(list, n, L, load, term, add);
-  }
-  if (L.sub != 0) return;
+  const int n = (valid && c.vort_on) ? a.cnt[i] : 0;
+  const int* __restrict__ list = a.nbr + (valid ? a.wbase[i >> 5] + (i & 31) : 0);
+  const float h2 = c.h2;
+  auto load = [&](int j) { return PosVel{__ldg(xs + j), __ldg(vs + j)}; };
+  auto term = [&](const PosVel r, bool in_list) {  // k_omega's one(), term by term
+    Terms<3> t;
+    const float dx = xi.x - r.x.x, dy = xi.y - r.x.y, dz = xi.z - r.x.z;
+    const float r2 = dist2(dx, dy, dz);
+    t.live = in_list && r2 < h2;
+    if (t.live) {
+      const float gf = spiky(c, clamped_r(c, r2));
+      const float gx = gf * dx, gy = gf * dy, gz = gf * dz;
+      const float ux = r.v.x - vi.x, uy = r.v.y - vi.y, uz = r.v.z - vi.z;
+      t.f[0] = uy * gz - uz * gy;
+      t.f[1] = uz * gx - ux * gz;
+      t.f[2] = ux * gy - uy * gx;
+    } else {
+      t.f[0] = t.f[1] = t.f[2] = 0.0f;
+    }
+    return t;
+  };
+  auto add = [&](const Terms<3>& t) {
+    ox += t.f[0];
+    oy += t.f[1];
+    oz += t.f[2];
+  };
+  unsigned long long bits = walk_lanes<G, 3>(list, n, L, load, term, add);
+  if (!valid || L.sub != 0) return;
+  if (!c.vort_on) bits = ~0ull;
   if (kLive == 2) store_live(a.live, a.n, i, bits);
   const float mag = sqrtf(ox * ox + oy * oy + oz * oz);
   a.omega[i] = make_float4(ox, oy, oz, mag);
@@ -1969,43 +2014,41 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_eta_lanes(St
   if (failed(a.status)) return;
   const LaneGroup<G> L;
   const int i = L.i;
-  if (i >= a.n) return;
+  const bool valid = i < a.n;
   const float4* __restrict__ xo = a.pl;
-  const float4 xi = a.x[i];
-  float4 v = a.v[i];
-  const SceneConst& c = a.sc[__float_as_int(v.w)];
-  if (c.vort_on) {
-    const float4 oi = a.omega[i];
-    const int n = a.cnt[i];
-    const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (i & 31);
-    const float h2 = c.h2;
-    float ex = 0.0f, ey = 0.0f, ez = 0.0f;
-    auto load = [&](int j) { return __ldg(xo + j); };
-    auto term = [&](const float4 r, bool in_list) {  // k_eta's one(), term by term
-      Terms<3> t;
-      const float dx = xi.x - r.x, dy = xi.y - r.y, dz = xi.z - r.z;
-      const float r2 = dist2(dx, dy, dz);
-      t.live = in_list && r2 < h2;
-      if (t.live) {
-        const float gf = spiky(c, clamped_r(c, r2));
-        const float coeff = r.w - oi.w;
-        t.f[0] = coeff * (gf * dx);
-        t.f[1] = coeff * (gf * dy);
-        t.f[2] = coeff * (gf * dz);
-      } else {
-        t.f[0] = t.f[1] = t.f[2] = 0.0f;
-      }
-      return t;
-    };
-    auto add = [&](const Terms<3>& t) {
-      ex += t.f[0];
-      ey += t.f[1];
-      ez += t.f[2];
-    };
-    walk_lanes<G, 3>(list, n, L, load, term, add);
-    confine(c, oi, ex, ey, ez, v);
-  }
-  if (L.sub != 0) return;
+  const float4 xi = valid ? a.x[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  float4 v = valid ? a.v[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  const SceneConst& c = a.sc[valid ? __float_as_int(v.w) : 0];
+  const float4 oi = (valid && c.vort_on) ? a.omega[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  const int n = (valid && c.vort_on) ? a.cnt[i] : 0;
+  const int* __restrict__ list = a.nbr + (valid ? a.wbase[i >> 5] + (i & 31) : 0);
+  const float h2 = c.h2;
+  float ex = 0.0f, ey = 0.0f, ez = 0.0f;
+  auto load = [&](int j) { return __ldg(xo + j); };
+  auto term = [&](const float4 r, bool in_list) {  // k_eta's one(), term by term
+    Terms<3> t;
+    const float dx = xi.x - r.x, dy = xi.y - r.y, dz = xi.z - r.z;
+    const float r2 = dist2(dx, dy, dz);
+    t.live = in_list && r2 < h2;
+    if (t.live) {
+      const float gf = spiky(c, clamped_r(c, r2));
+      const float coeff = r.w - oi.w;
+      t.f[0] = coeff * (gf * dx);
+      t.f[1] = coeff * (gf * dy);
+      t.f[2] = coeff * (gf * dz);
+    } else {
+      t.f[0] = t.f[1] = t.f[2] = 0.0f;
+    }
+    return t;
+  };
+  auto add = [&](const Terms<3>& t) {
+    ex += t.f[0];
+    ey += t.f[1];
+    ez += t.f[2];
+  };
+  walk_lanes<G, 3>(list, n, L, load, term, add);
+  if (!valid || L.sub != 0) return;
+  if (c.vort_on) confine(c, oi, ex, ey, ez, v);
   if (rest && c.rest_on) restitution(c, xi.x, xi.y, xi.z, v.x, v.y, v.z);
   a.v[i] = v;
 }
@@ -2019,7 +2062,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_eta_lanes(St
 // the work of k_bounds, which that step's graph then leaves out.
 __global__ void __launch_bounds__(kBlock) k_upload(const float* px, const float* py, const float* pz,
                                                    const float* vx, const float* vy, const float* vz,
-                                                   float4* x, float4* v, int* slot, float* rho,
+                                                   float4* x, float4* v, int* slot, float* rho, int* cnt,
                                                    const SceneConst* sc, int scenes, int n, int* bmin, int* bmax) {
   const int o = blockIdx.x * kBlock + threadIdx.x;
   int scene = -1;
@@ -2037,6 +2080,7 @@ __global__ void __launch_bounds__(kBlock) k_upload(const float* px, const float*
     v[o] = vo;
     slot[o] = o;
     rho[o] = 0.0f;
+    if (cnt) cnt[o] = 0;  // no previous lists: the list build reserves nothing ahead
     if (bmin) {
       float4 vp = vo;
       scene = lo;
@@ -2363,11 +2407,11 @@ cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t s
 }
 
 cudaError_t enqueue_upload(const float* px, const float* py, const float* pz, const float* vx, const float* vy,
-                           const float* vz, float4* x, float4* v, int* slot, float* rho, const SceneConst* sc,
-                           int scenes, int n, cudaStream_t st, int* bmin, int* bmax) {
+                           const float* vz, float4* x, float4* v, int* slot, float* rho, int* cnt,
+                           const SceneConst* sc, int scenes, int n, cudaStream_t st, int* bmin, int* bmax) {
   if (n > 0)
-    k_upload<<<blocks_for(n, kBlock), kBlock, 0, st>>>(px, py, pz, vx, vy, vz, x, v, slot, rho, sc, scenes, n, bmin,
-                                                       bmax);
+    k_upload<<<blocks_for(n, kBlock), kBlock, 0, st>>>(px, py, pz, vx, vy, vz, x, v, slot, rho, cnt, sc, scenes, n,
+                                                       bmin, bmax);
   return cudaGetLastError();
 }
 

@@ -113,12 +113,13 @@ cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan,
                          cudaStream_t stream, LaunchMarks& marks,
                          const StepRecord* rec = nullptr, const StepDownload* dl = nullptr);
 
-// Packs caller-order SoA arrays (device) into slot-order x/v of one parity;
+// Packs caller-order SoA arrays (device) into slot-order x/v of one parity
+// (and zeroes that parity's list lengths, cnt, when given);
 // with bmin/bmax it also accumulates the predicted cells' bounding box (what
 // k_bounds does), for a step launched with StepDownload::bounds_done.
 cudaError_t enqueue_upload(const float* px, const float* py, const float* pz,
                            const float* vx, const float* vy, const float* vz,
-                           float4* x, float4* v, int* slot, float* rho,
+                           float4* x, float4* v, int* slot, float* rho, int* cnt,
                            const SceneConst* sc, int scenes, int n,
                            cudaStream_t stream, int* bmin = nullptr, int* bmax = nullptr);
 

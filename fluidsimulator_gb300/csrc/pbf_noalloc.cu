@@ -127,6 +127,7 @@ StepArgs carve(unsigned char* b, int n) {
   a.digit_total = at<uint32_t>(b, kDigits);
   a.table = at<int2>(b, kTable);
   a.cnt = at<int>(b, kCnt);
+  a.cnt_old = nullptr;  // one step per call: no previous lists to size the build's reservations
   a.depth = at<int>(b, kDepth);
   a.wbase = at<long long>(b, kWbase);
   a.ovf = at<int>(b, kOvf);
@@ -185,7 +186,7 @@ extern "C" int fluid_gb300_step_noalloc(const fluid_params* params, int64_t coun
   if (enqueue_reset(a.status, a.bmin, a.bmax, 1, st) != cudaSuccess) return FLUID_ERR_CUDA;
   if (enqueue_upload(pos_x, pos_y, pos_z, vel_x, vel_y, vel_z, const_cast<float4*>(a.x_old),
                      const_cast<float4*>(a.v_old), const_cast<int*>(a.slot_old), const_cast<float*>(a.rho_old),
-                     a.sc, 1, n, st) != cudaSuccess)
+                     nullptr, a.sc, 1, n, st) != cudaSuccess)
     return FLUID_ERR_CUDA;
   if (enqueue_step(a, plan, st, marks) != cudaSuccess) return FLUID_ERR_CUDA;
   // The status word is read on the caller's stream, behind the step, so the

@@ -295,7 +295,8 @@ class Solver {
     while (moved_slots_ < n_ / 16 && moved_slots_ < (1u << 22)) moved_slots_ <<= 1;
     ok &= moved_.alloc(2 * static_cast<size_t>(moved_slots_)) == cudaSuccess;
     ok &= lambda_.alloc(np) == cudaSuccess;
-    ok &= cnt_.alloc(np) == cudaSuccess;
+    ok &= cnt_[0].alloc(np) == cudaSuccess;
+    ok &= cnt_[1].alloc(np) == cudaSuccess;
     ok &= depth_.alloc(static_cast<size_t>(warps_) + 1) == cudaSuccess;
     ok &= ovf_.alloc(static_cast<size_t>(warps_) + 1) == cudaSuccess;
     ok &= wbase_.alloc(static_cast<size_t>(warps_) + 1) == cudaSuccess;
@@ -384,7 +385,7 @@ class Solver {
         for (int k = 0; k < 6; ++k) dev[k] = src[k];
       }
       if (enqueue_upload(dev[0], dev[1], dev[2], dev[3], dev[4], dev[5], x_[parity_].p, v_[parity_].p,
-                         slot_[parity_].p, rho_[parity_].p, sc_.p, S_, n_, stream_,
+                         slot_[parity_].p, rho_[parity_].p, cnt_[parity_].p, sc_.p, S_, n_, stream_,
                          bounds_ready_ ? bmin_.p : nullptr, bounds_ready_ ? bmax_.p : nullptr) != cudaSuccess)
         return cuda_fail("upload kernel");
       if (wait && cudaStreamSynchronize(stream_) != cudaSuccess) return cuda_fail("upload");
@@ -999,7 +1000,7 @@ class Solver {
     }
     std::vector<int32_t> buf(n);
     const void* src = nullptr;
-    if (what == FLUID_DEBUG_NEIGHBOR_COUNTS) src = cnt_.p;
+    if (what == FLUID_DEBUG_NEIGHBOR_COUNTS) src = cnt_[parity_].p;
     else if (what == FLUID_DEBUG_RHO) src = rho_[parity_].p;
     else if (what == FLUID_DEBUG_LAMBDA) src = lambda_.p;
     else return fail(FLUID_ERR_INVALID_ARGUMENT, "unknown debug record");
@@ -1102,7 +1103,8 @@ class Solver {
     a.radix_next = radix_next_.p;
     a.digit_total = digit_total_.p;
     a.table = table_.p;
-    a.cnt = cnt_.p;
+    a.cnt = cnt_[par ^ 1].p;
+    a.cnt_old = cnt_[par].p;
     a.depth = depth_.p;
     a.ovf = ovf_.p;
     a.wbase = wbase_.p;
@@ -1344,7 +1346,7 @@ class Solver {
       const size_t len = static_cast<size_t>(st.cursor);
       if (tp.nbr.n < len && tp.nbr.alloc(len + len / 4 + 32)) return fail(FLUID_ERR_OUT_OF_MEMORY, "adjoint tape");
       cudaMemcpyAsync(tp.nbr.p, nbr_.p, len * sizeof(int), cudaMemcpyDeviceToDevice, stream_);
-      cudaMemcpyAsync(tp.cnt.p, cnt_.p, n * sizeof(int), cudaMemcpyDeviceToDevice, stream_);
+      cudaMemcpyAsync(tp.cnt.p, cnt_[parity_ ^ 1].p, n * sizeof(int), cudaMemcpyDeviceToDevice, stream_);
       cudaMemcpyAsync(tp.wbase.p, wbase_.p, (static_cast<size_t>(warps_) + 1) * sizeof(long long),
                       cudaMemcpyDeviceToDevice, stream_);
       last_pairs_ = static_cast<long long>(st.pairs);
@@ -1455,7 +1457,7 @@ class Solver {
   long long last_skipped_ = 0;
   int last_max_ = 0, last_cells_ = 0, last_npass_ = 0;
   DBuf<float4> x_[2], v_[2], p_[2], v2_, omega_, pl_;
-  DBuf<int> slot_[2], vals_[2], cnt_, depth_, ovf_, nbr_, bmin_, bmax_;
+  DBuf<int> slot_[2], vals_[2], cnt_[2], depth_, ovf_, nbr_, bmin_, bmax_;
   DBuf<float> rho_[2], lambda_;
   DBuf<uint32_t> keys_[2], digit_total_;
   DBuf<unsigned long long> look_;

@@ -407,3 +407,65 @@ def load_scene_json(path: str) -> Scene:
     import os
 
     return Scene(os.path.splitext(os.path.basename(path))[0], p, pos, vel, steps=1, info={"path": path})
+
+
+# ---------------------------------------------------------------------------
+# Fills generated on the device (fluid_fill_block / fluid_fill_shape): the
+# same particles as init_block + jitter and the scene file's shapes above, bit
+# for bit, written straight into device memory.
+
+def _device_rows(count: int, device: int):
+    import torch
+
+    return torch.empty((3, count), dtype=torch.float32, device=torch.device("cuda", device))
+
+
+def _row_ptrs(t):
+    import ctypes
+
+    base = t.data_ptr()
+    return [ctypes.c_void_p(base + k * t.stride(0) * 4) for k in range(3)]
+
+
+def fill_block_device(nx: int, ny: int, nz: int, origin, spacing: float, jitter_amplitude: float = 0.0,
+                      seed: int = 0, first: int = 0, device: int = 0):
+    """init_block (+ jitter with the same draws as `jitter`, the first particle
+    taking draw 3 * first + 1) generated on the GPU; returns a (3, N) float32
+    tensor on that device."""
+    from fluidsimulator_gb300 import _capi
+
+    lib = _capi.load()
+    out = _device_rows(nx * ny * nz, device)
+    rc = lib.fluid_fill_block(nx, ny, nz, float(np.float32(origin[0])), float(np.float32(origin[1])),
+                              float(np.float32(origin[2])), float(np.float32(spacing)), float(jitter_amplitude),
+                              int(seed) & 0xFFFFFFFFFFFFFFFF, int(first), *_row_ptrs(out), None)
+    if rc != 0:
+        raise RuntimeError(f"fluid_fill_block failed with status {rc}")
+    return out
+
+
+def fill_shape_device(kind: str, origin, extent, spacing: float, velocity=(0.0, 0.0, 0.0), device: int = 0):
+    """A scene file's cube (extent = size) or sphere (extent = (radius,)) fill
+    generated on the GPU; returns (pos, vel) (3, N) float32 tensors."""
+    import ctypes
+
+    from fluidsimulator_gb300 import _capi
+
+    lib = _capi.load()
+    k = {"cube": 0, "sphere": 1}[kind]
+    o = (ctypes.c_float * 3)(*[float(np.float32(v)) for v in origin])
+    ext = list(extent) + [0.0] * (3 - len(extent))
+    e = (ctypes.c_float * 3)(*[float(np.float32(v)) for v in ext])
+    v = (ctypes.c_float * 3)(*[float(np.float32(c)) for c in velocity])
+    count = ctypes.c_int64(0)
+    sp = float(np.float32(spacing))
+    rc = lib.fluid_fill_shape(k, o, e, sp, v, None, None, None, None, None, None, 0, ctypes.byref(count), None)
+    if rc not in (0, 3):
+        raise RuntimeError(f"fluid_fill_shape failed with status {rc}")
+    pos, vel = _device_rows(count.value, device), _device_rows(count.value, device)
+    if count.value:
+        rc = lib.fluid_fill_shape(k, o, e, sp, v, *_row_ptrs(pos), *_row_ptrs(vel), count.value, ctypes.byref(count),
+                                  None)
+        if rc != 0:
+            raise RuntimeError(f"fluid_fill_shape failed with status {rc}")
+    return pos, vel

@@ -143,6 +143,42 @@ int fluid_gb300_step_noalloc(const fluid_params* params, int64_t count,
                              float* vel_x, float* vel_y, float* vel_z,
                              float* time, void* stream);
 
+/* ---- Scene fills generated on the device ------------------------------- */
+
+enum { FLUID_SHAPE_CUBE = 0, FLUID_SHAPE_SPHERE = 1 };
+
+/*
+ * init_block (core/src/init.cpp:72-106) written straight into the caller's
+ * DEVICE arrays: particle (z * ny + y) * nx + x at origin + float(i) *
+ * spacing per axis, the reference's order and float arithmetic. With jitter
+ * > 0 each coordinate then gets + U(-jitter, jitter) from SplitMix64(seed)
+ * draw 3m + axis + 1 (m = first + particle index), rounded to float and added
+ * in float -- the seeded jitter of this project's benchmark scenes, so a
+ * device-filled scene equals the host-filled one bit for bit. The arrays hold
+ * nx * ny * nz floats. Synchronises `stream` before returning.
+ */
+int fluid_fill_block(int64_t nx, int64_t ny, int64_t nz, float origin_x,
+                     float origin_y, float origin_z, float spacing,
+                     double jitter, uint64_t seed, int64_t first,
+                     float* pos_x, float* pos_y, float* pos_z, void* stream);
+
+/*
+ * One "shape" of a scene file (core/src/init.cpp:285-345): kind
+ * FLUID_SHAPE_CUBE fills origin + spacing/2 + k * spacing below origin +
+ * extent[d] on each axis; FLUID_SHAPE_SPHERE fills the cube around origin of
+ * half-width extent[0] (the radius) and keeps the points with (dx*dx + dy*dy)
+ * + dz*dz < r*r. Axes are accumulated in float as the reference's loops do,
+ * points are in its loop order (x outermost, z innermost), velocities are
+ * `velocity` (NULL = zero). Writes *count; when it exceeds `capacity`,
+ * returns FLUID_ERR_CAPACITY without writing (call again with capacity >=
+ * *count). Allocates a little device memory for the axes for the call.
+ */
+int fluid_fill_shape(int32_t kind, const float origin[3], const float extent[3],
+                     float spacing, const float velocity[3], float* pos_x,
+                     float* pos_y, float* pos_z, float* vel_x, float* vel_y,
+                     float* vel_z, int64_t capacity, int64_t* count,
+                     void* stream);
+
 /* ---- Device-resident solver (no reference counterpart: the reference keeps
  * no device state between steps; this is the handle the drop-in above uses). */
 
