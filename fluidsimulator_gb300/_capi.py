@@ -103,7 +103,6 @@ class FluidStats(ctypes.Structure):
         ("grid_capacity", c_int64),
         ("regrows", c_int64),
         ("kernel_launches", c_int64),
-        ("skipped_walks", c_int64),
     ]
 
 

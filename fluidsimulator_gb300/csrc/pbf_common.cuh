@@ -12,8 +12,6 @@
 //   pl            float4 {p.xyz, lambda} of the current Jacobi iteration, so
 //                 the delta pass gathers one record per neighbour.
 //   lambda, rho[2] float per slot.
-//   reach         float per slot: lower bound on the distance to the nearest
-//                 list entry (see StepArgs::reach).
 //   keys/vals     radix-sort ping-pong (u32 cell key, int caller index).
 //   table         int2 (first, end) per cell of the per-scene bounding grids.
 //   cnt, nbr      neighbour lists in 32-wide slices: warp w (slots 32w..32w+31)
@@ -89,7 +87,6 @@ struct DevStatus {
   unsigned long long cursor; // list entries claimed by the slices, this step
   int nbr_max;
   int pad;
-  unsigned long long skipped;  // list walks the displacement bound skipped, this step
 };
 
 // Every pointer one step needs, parity already resolved.
@@ -106,15 +103,6 @@ struct StepArgs {
   float4* omega;
   float4* pl;              // {p.xyz, lambda}, written by the lambda pass
   uint32_t* live;          // 2 x n: live bits of each list's first 64 entries at one set of positions
-  // Displacement bound of the Jacobi passes (a pass may skip a list it can
-  // prove holds no entry within h): reach[i] is a lower bound on the
-  // distance from particle i to its nearest list entry at the positions of
-  // the last lambda pass; moved holds two parities (iteration k uses k & 1)
-  // of moved_mask + 1 slots: the largest distance (rounded up, float bits)
-  // any particle of a bin of build cells moved in that iteration's delta pass.
-  float* reach;
-  unsigned* moved;
-  unsigned moved_mask;
   float* lambda;
   float* rho;
   uint32_t* keys[2];
@@ -124,7 +112,6 @@ struct StepArgs {
   uint32_t* digit_total;     // kRadixMaxPasses x kRadixMaxBins: counts, then starts
   int2* table;
   int* cnt;
-  const int* cnt_old;     // list lengths of the previous step, by its slot (zero after an upload)
   int* depth;             // per warp
   long long* wbase;       // per warp
   int* ovf;               // per warp: list longer than the shared-memory staging

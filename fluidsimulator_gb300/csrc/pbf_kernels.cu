@@ -206,136 +206,6 @@ __device__ __forceinline__ const uint32_t* sorted_keys(const StepArgs& a, int np
   return a.keys[npass & 1];
 }
 
-// Displacement bound of the list passes (the "skin" argument of molecular
-// dynamics neighbour lists). If every list entry of particle i was at least
-// `reach` away at the positions of the last lambda pass, i has moved at most
-// d_self since and every listed neighbour at most d_nb, then no entry is
-// closer than reach - d_self - d_nb now; when that exceeds h, no entry can
-// pass the pass's r2 < h2 test and its walk adds nothing (the reference's own
-// loop adds only within-h terms, or poly6 = 0 beyond h), so the walk is
-// skipped and the result is the same bits. Every quantity is rounded the
-// conservative way: reach is the square root of the smallest r2 seen rounded
-// down and shrunk by 2^-20 (an r2 computed with round-to-nearest operations is
-// within ~3e-7 of the exact squared distance of the float positions),
-// displacements are rounded up and grown by 2^-20, the subtractions round
-// down, and the bound must reach h grown by 2^-20, above which every
-// round-to-nearest r2 exceeds h2 = RN(h * h).
-//
-// d_nb comes from a table the delta pass fills: each particle adds its
-// displacement (atomic max) to the slot of its bin, the 2x2x2 block of grid
-// cells around the cell it was listed in (the step's build cell, decoded from
-// its sorted key), slots addressed by a hash of (scene, bin). A listed
-// neighbour's build cell is within one cell of the particle's on every axis,
-// so its bin is one of the 8 bins those 3x3x3 cells touch, and the largest of
-// their slots bounds every neighbour's displacement; two bins sharing a slot
-// only raise it. Lists from all pairs (use_uniform_grid = 0) span the scene
-// and take no bound.
-constexpr float kReachShrink = 1.0f - 9.5367431640625e-07f;  // 1 - 2^-20
-constexpr float kReachGrow = 1.0f + 9.5367431640625e-07f;    // 1 + 2^-20
-
-__device__ __forceinline__ float reach_from_r2(float r2min) {  // +inf for an empty list
-  return __fmul_rd(__fsqrt_rd(r2min), kReachShrink);
-}
-
-__device__ __forceinline__ float moved_by(float dx, float dy, float dz) {
-  return __fmul_ru(__fsqrt_ru(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz))),
-                   kReachGrow);
-}
-
-// True when no list entry of a particle with this reach, own displacement and
-// neighbours' displacement can be within h; `bound` is then a lower bound on
-// its distance to every entry now (NaN anywhere gives false).
-__device__ __forceinline__ bool beyond_reach(const SceneConst& c, float reach, float d_self, float d_nb,
-                                             float& bound) {
-  bound = __fsub_rd(__fsub_rd(reach, d_self), d_nb);
-  return bound >= __fmul_ru(c.h, kReachGrow);
-}
-
-// Build cell (the cell whose 27-cell neighbourhood the step's lists were built
-// from) of the particle at sorted slot i, decoded from its sorted key.
-__device__ __forceinline__ void build_cell(const uint32_t* ks, const GridInfo& g, int i, int& cx, int& cy, int& cz) {
-  const uint32_t l = ks[i] - g.base;
-  const uint32_t yz = static_cast<uint32_t>(g.dimy) * static_cast<uint32_t>(g.dimz);
-  cx = g.minx + static_cast<int>(l / yz);
-  const uint32_t r = l % yz;
-  cy = g.miny + static_cast<int>(r / static_cast<uint32_t>(g.dimz));
-  cz = g.minz + static_cast<int>(r % static_cast<uint32_t>(g.dimz));
-}
-
-// Slot of bin (bx, by, bz) of a scene in the displacement table (mask + 1
-// slots, a power of two).
-__device__ __forceinline__ uint32_t moved_slot(int scene, int bx, int by, int bz, uint32_t mask) {
-  uint32_t h = static_cast<uint32_t>(scene) * 0x9E3779B1u ^ static_cast<uint32_t>(bx) * 0x85EBCA77u ^
-               static_cast<uint32_t>(by) * 0xC2B2AE3Du ^ static_cast<uint32_t>(bz) * 0x27D4EB2Fu;
-  h ^= h >> 15;
-  h *= 0x2C1B3C6Du;
-  h ^= h >> 12;
-  return h & mask;
-}
-
-// Largest displacement recorded in the 8 bins around build cell (cx, cy, cz).
-__device__ __forceinline__ float moved_near(const unsigned* table, uint32_t mask, int scene, int cx, int cy,
-                                            int cz) {
-  unsigned m = 0u;
-  const int bx = (cx - 1) >> 1, by = (cy - 1) >> 1, bz = (cz - 1) >> 1;
-#pragma unroll
-  for (int t = 0; t < 8; ++t)
-    m = max(m, table[moved_slot(scene, bx + (t & 1), by + ((t >> 1) & 1), bz + (t >> 2), mask)]);
-  return __uint_as_float(m);
-}
-
-// Adds displacement d of a particle in build cell (cx, cy, cz) to its bin's
-// slot: one atomic max per distinct slot of the warp's running lanes (after
-// their list walks have reconverged). Non-negative float bits order as
-// unsigned ints.
-__device__ __forceinline__ void record_moved(unsigned* table, uint32_t mask, int scene, int cx, int cy, int cz,
-                                             float d) {
-  const unsigned active = __activemask();
-  const uint32_t slot = moved_slot(scene, cx >> 1, cy >> 1, cz >> 1, mask);
-  const unsigned bits = __float_as_uint(d);
-  unsigned todo = active;
-  while (todo) {
-    const int leader = __ffs(todo) - 1;
-    const uint32_t s0 = __shfl_sync(active, slot, leader);
-    const bool mine = slot == s0;
-    const unsigned peers = __ballot_sync(active, mine);
-    const unsigned m = __reduce_max_sync(active, mine ? bits : 0u);
-    if ((threadIdx.x & 31) == leader) atomicMax(table + s0, m);
-    todo &= ~peers;
-  }
-}
-
-// Counts the warp's skipped walks into the status word (statistics only).
-__device__ __forceinline__ void count_skipped(DevStatus* st, bool skip) {
-  const unsigned mask = __activemask();
-  const unsigned b = __ballot_sync(mask, skip);
-  if (b && (threadIdx.x & 31) == __ffs(mask) - 1) atomicAdd(&st->skipped, static_cast<unsigned long long>(__popc(b)));
-}
-
-// Clears one parity of the displacement table: every thread of a list-pass
-// launch takes a grid-stride share.
-__device__ __forceinline__ void clear_moved(unsigned* table, uint32_t mask) {
-  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
-  for (long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; t <= mask; t += stride)
-    table[t] = 0u;
-}
-
-// d_nb of particle i (sorted slot) from the table of one parity; +inf (no
-// bound) for lists from all pairs.
-__device__ __forceinline__ float moved_around(const StepArgs& a, const SceneConst& c, int scene, int i, int par) {
-  if (c.all_pairs) return INFINITY;
-  int cx, cy, cz;
-  build_cell(sorted_keys(a, a.status->npass), a.grid[scene], i, cx, cy, cz);
-  return moved_near(a.moved + static_cast<size_t>(par) * (a.moved_mask + 1u), a.moved_mask, scene, cx, cy, cz);
-}
-
-// Records particle i's displacement d in the table of one parity.
-__device__ __forceinline__ void record_moved_at(const StepArgs& a, int scene, int i, int par, float d) {
-  int cx, cy, cz;
-  build_cell(sorted_keys(a, a.status->npass), a.grid[scene], i, cx, cy, cz);
-  record_moved(a.moved + static_cast<size_t>(par) * (a.moved_mask + 1u), a.moved_mask, scene, cx, cy, cz, d);
-}
-
 __device__ __forceinline__ uint32_t cell_key(const GridInfo& g, int cx, int cy, int cz) {
   const long long l = (static_cast<long long>(cx - g.minx) * g.dimy + (cy - g.miny)) * g.dimz + (cz - g.minz);
   return g.base + static_cast<uint32_t>(l);
@@ -436,7 +306,6 @@ __global__ void __launch_bounds__(kBlock) k_grid_setup(StepArgs a, int radix_bit
   st->started = st->started + 1;
   st->pairs = 0ull;
   st->cursor = 0ull;
-  st->skipped = 0ull;
   st->nbr_max = 0;
   unsigned long long total = 0;
   bool domain = false;
@@ -852,7 +721,6 @@ __device__ __forceinline__ float finish_lambda(const SceneConst& c, float rho, f
 // Per-neighbour density / gradient terms (core.cpp:300-316).
 struct LambdaAcc {
   float rho = 0.0f, gsx = 0.0f, gsy = 0.0f, gsz = 0.0f, sum_g2 = 0.0f;
-  float r2min = INFINITY;  // smallest r2 of the walk (the displacement bound's reach)
   __device__ __forceinline__ void add(const SceneConst& c, float dx, float dy, float dz, float r2) {
     rho += poly6(c, r2);
     const float gf = spiky(c, clamped_r(c, r2));
@@ -872,7 +740,6 @@ struct LambdaAcc {
                                                const float2 pz, const float4 qa, const float4 qb) {
     const float2 nz = f2(c.neg_zero);
     const PairGeom g = pair_geom(px, py, pz, qa, qb, nz);
-    r2min = fminf(r2min, fminf(g.r2.x, g.r2.y));
     const bool oka = g.r2.x < c.h2, okb = g.r2.y < c.h2;
     if (!oka && !okb) return 0u;
     const float2 w = poly6_pair(c, g.r2, nz);
@@ -913,23 +780,17 @@ __device__ __forceinline__ void for_each_pair_candidate(const StepArgs& a, const
 }
 
 // Neighbour lists in one scan (core.cpp:205-247). Each lane stages its first
-// kStage list entries in shared memory while it scans; the block then claims
-// its warps' 32-wide slices with one atomic on the list cursor (placement
-// varies run to run, every list's content and order do not) and writes the
-// staged entries out as coalesced 128-byte rows.
-//
-// Longer lists (the collapsed phase) would need a second scan for the entries
-// past kStage. A warp whose particles' previous-step lists were longer than
-// kStage (cnt_old, through each particle's previous slot) therefore reserves
-// its slice before the scan, sized 5/4 of the longest plus 8 rows, and writes
-// entries past kStage straight into it as it finds them; only a warp whose
-// lists outgrow that reservation (or had no previous step) falls back to a
-// fresh slice after the scan plus the re-scan of k_nbr_overflow (ovf[w]).
-__global__ void __launch_bounds__(kMaxBuildBlock, 5) k_nbr_build(StepArgs a) {
+// kStage list entries in
+// shared memory while it scans; the block then claims its warps' 32-wide
+// slices with one atomic on the list cursor (placement varies run to run,
+// every list's content and order do not) and writes the staged entries out
+// as coalesced 128-byte rows. Warps with a longer list set ovf[w] and
+// k_nbr_overflow writes their remaining entries.
+__global__ void __launch_bounds__(kMaxBuildBlock) k_nbr_build(StepArgs a) {
   extern __shared__ int stage[];
   // Other blocks of this launch may set the status (capacity) while this
   // one starts: read it once for the whole block, so either every warp
-  // returns here or every warp reaches the barriers and the slice claims
+  // returns here or every warp reaches the barriers and the slice claim
   // below (a warp left behind by an early return of thread 0's warp would
   // read an unset block_base).
   __shared__ int block_failed;
@@ -939,34 +800,6 @@ __global__ void __launch_bounds__(kMaxBuildBlock, 5) k_nbr_build(StepArgs a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int* mine = stage + warp * (kStage * 32) + lane;  // entry k at mine[32 k]
-  const bool warp_live = (i - lane) < a.n;
-  // Rows reserved before the scan: 0, or 5/4 of the warp's longest previous
-  // list plus 8 when that exceeded kStage.
-  int prev = 0;
-  if (i < a.n && a.cnt_old) prev = a.cnt_old[a.slot_old[__float_as_int(a.x[i].w)]];
-  const int prev_max = __reduce_max_sync(kFull, prev);
-  const int reserve = (warp_live && prev_max > kStage) ? prev_max + prev_max / 4 + 8 : 0;
-  __shared__ int wres[kMaxBuildBlock / 32];
-  __shared__ unsigned long long woff[kMaxBuildBlock / 32];  // each warp's reserved slice
-  __shared__ int res_ok;
-  if (lane == 0) wres[warp] = reserve;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned long long total = 0;
-    for (int w = 0; w < static_cast<int>(blockDim.x / 32); ++w) total += 32ull * wres[w];
-    res_ok = 1;
-    if (total) {
-      unsigned long long base = atomicAdd(&a.status->cursor, total);
-      res_ok = base + total <= static_cast<unsigned long long>(a.nbr_capacity);
-      if (!res_ok) set_error(a.status, FLUID_ERR_CAPACITY);
-      for (int w = 0; w < static_cast<int>(blockDim.x / 32); ++w) {
-        woff[w] = base;
-        base += 32ull * wres[w];
-      }
-    }
-  }
-  __syncthreads();
-  if (!res_ok) return;  // the step fails (capacity) and is re-run after the lists grow
   int count = 0;
   if (i < a.n) {
     const uint32_t* ks = sorted_keys(a, a.status->npass);
@@ -978,7 +811,6 @@ __global__ void __launch_bounds__(kMaxBuildBlock, 5) k_nbr_build(StepArgs a) {
     auto test = [&](int j, const float4 q) {
       if (dist2(p.x - q.x, p.y - q.y, p.z - q.z) < h2) {
         if (count < kStage) mine[32 * count] = j;
-        else if (count < reserve) a.nbr[woff[warp] + lane + 32ull * count] = j;  // reserved slice
         ++count;
       }
     };
@@ -988,12 +820,12 @@ __global__ void __launch_bounds__(kMaxBuildBlock, 5) k_nbr_build(StepArgs a) {
   }
   const int mx = __reduce_max_sync(kFull, count);
   const unsigned sum = __reduce_add_sync(kFull, static_cast<unsigned>(count));
-  const bool fits = reserve && mx <= reserve;  // the reserved slice holds every list
   __shared__ int wdepth[kMaxBuildBlock / 32];
   __shared__ unsigned long long block_base;
   __shared__ int block_ok;
+  const bool warp_live = (i - lane) < a.n;
   if (lane == 0) {
-    wdepth[warp] = (warp_live && !fits) ? mx : 0;  // rows still to claim
+    wdepth[warp] = warp_live ? mx : 0;
     if (warp_live) {
       if (sum) atomicAdd(&a.status->pairs, static_cast<unsigned long long>(sum));
       if (mx) atomicMax(&a.status->nbr_max, mx);
@@ -1003,24 +835,15 @@ __global__ void __launch_bounds__(kMaxBuildBlock, 5) k_nbr_build(StepArgs a) {
   if (threadIdx.x == 0) {
     unsigned long long total = 0;
     for (int w = 0; w < static_cast<int>(blockDim.x / 32); ++w) total += 32ull * wdepth[w];
-    block_ok = 1;
-    block_base = 0;
-    if (total) {
-      const unsigned long long base = atomicAdd(&a.status->cursor, total);
-      block_ok = base + total <= static_cast<unsigned long long>(a.nbr_capacity);
-      if (!block_ok) set_error(a.status, FLUID_ERR_CAPACITY);
-      block_base = base;
-    }
+    const unsigned long long base = atomicAdd(&a.status->cursor, total);
+    block_ok = base + total <= static_cast<unsigned long long>(a.nbr_capacity);
+    if (!block_ok) set_error(a.status, FLUID_ERR_CAPACITY);
+    block_base = base;
   }
   __syncthreads();
   if (!warp_live || !block_ok) return;
-  unsigned long long off;
-  if (fits) {
-    off = woff[warp];
-  } else {
-    off = block_base;
-    for (int w = 0; w < warp; ++w) off += 32ull * wdepth[w];
-  }
+  unsigned long long off = block_base;
+  for (int w = 0; w < warp; ++w) off += 32ull * wdepth[w];
   int* out = a.nbr + off + lane;
   const int staged = mx < kStage ? mx : kStage;
   for (int k = 0; k < staged; ++k)
@@ -1028,7 +851,7 @@ __global__ void __launch_bounds__(kMaxBuildBlock, 5) k_nbr_build(StepArgs a) {
   if (lane == 0) {
     a.wbase[i >> 5] = static_cast<long long>(off);
     a.depth[i >> 5] = mx;
-    a.ovf[i >> 5] = (mx > kStage && !fits) ? 1 : 0;
+    a.ovf[i >> 5] = mx > kStage ? 1 : 0;
   }
 }
 
@@ -1214,46 +1037,26 @@ __device__ __forceinline__ void for_each_live_then(const int* __restrict__ list,
 // kLiveOut: record the live bits of these positions for the delta pass
 // (iterations after the first; the first runs at the positions the lists
 // were built from, where every entry is live).
-//
-// Every iteration's pass also leaves reach[i] (the displacement bound's lower
-// bound on the distance to the nearest list entry at these positions) and
-// clears the scene displacement words its delta pass will fill. Iterations
-// after the first (kLiveOut) first try the bound against the previous
-// iteration's positions (p[in ^ 1], which the previous delta pass read) and
-// skip the walk when it proves every entry beyond h.
 template <int U, bool kLiveOut>
 __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_lambda(StepArgs a, int in) {
   if (failed(a.status)) return;
-  clear_moved(a.moved + static_cast<size_t>(in) * (a.moved_mask + 1u), a.moved_mask);
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   const float4* __restrict__ pos = a.p[in];
   const float4 p = pos[i];
-  const int scene = __float_as_int(p.w);
-  const SceneConst& c = a.sc[scene];
+  const SceneConst& c = a.sc[__float_as_int(p.w)];
   const int n = a.cnt[i];
   const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
   const float h2 = c.h2;
   LambdaAcc acc;
-  bool skip = false;
-  float bound = 0.0f;
-  if constexpr (kLiveOut) {
-    const float4 q = a.p[in ^ 1][i];
-    skip = beyond_reach(c, a.reach[i], moved_by(p.x - q.x, p.y - q.y, p.z - q.z),
-                        moved_around(a, c, scene, i, in ^ 1), bound);
-    count_skipped(a.status, skip);
-  }
   auto one = [&](const float4 q) {
     const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
     const float r2 = dist2(dx, dy, dz);
-    acc.r2min = fminf(acc.r2min, r2);
     if (r2 < h2) acc.add(c, dx, dy, dz, r2);
     return r2 < h2;
   };
   auto load = [&](int j) { return __ldg(pos + j); };
-  if (skip) {
-    if constexpr (kLiveOut) store_live(a.live, a.n, i, 0ull);
-  } else if constexpr (U == 1) {
+  if constexpr (U == 1) {
     if constexpr (kLiveOut) {
       unsigned long long bits = 0ull;
       int k = 0;
@@ -1276,7 +1079,6 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_lambda(StepA
   a.lambda[i] = lam;
   a.rho[i] = rho;
   a.pl[i] = make_float4(p.x, p.y, p.z, lam);
-  a.reach[i] = skip ? bound : reach_from_r2(acc.r2min);
 }
 
 // Commit v = (p - x)/dt, x = p (core.cpp:414-421); restitution when this is
@@ -1302,8 +1104,8 @@ __device__ __forceinline__ void commit(const StepArgs& a, const SceneConst& c, i
 }
 
 // The rest of a delta pass once the sums (ax, ay, az) of particle i are
-// complete: scale by 1/rho0, plane projection (core.cpp:368-393), the scene's
-// displacement word, then the next iteration's p* or the commit.
+// complete: scale by 1/rho0, plane projection (core.cpp:368-393), then the
+// next iteration's p* or the commit.
 __device__ __forceinline__ void delta_out(const StepArgs& a, const SceneConst& c, int i, const float4 p, float ax,
                                           float ay, float az, int in, int last, int to_v2, int rest,
                                           float4* q_out) {
@@ -1328,7 +1130,6 @@ __device__ __forceinline__ void delta_out(const StepArgs& a, const SceneConst& c
     az = qz - p.z;
   }
   const float nx = p.x + ax, ny = p.y + ay, nz = p.z + az;  // core.cpp:404-406
-  record_moved_at(a, __float_as_int(p.w), i, in, moved_by(nx - p.x, ny - p.y, nz - p.z));
   if (!last) {
     a.p[in ^ 1][i] = make_float4(nx, ny, nz, p.w);
   } else {
@@ -1374,12 +1175,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_delta(StepAr
       kLiveIn ? (static_cast<unsigned long long>(a.live[i]) | (static_cast<unsigned long long>(a.live[a.n + i]) << 32))
               : 0ull;
   const float4 dead = make_float4(INFINITY, p.y, p.z, 0.0f);
-  // The lambda pass of this iteration (same positions) left reach[i]: at or
-  // beyond h (grown as in beyond_reach) no entry is within h, so nothing past
-  // the live-bit head can add either.
-  const bool none = kLiveIn && a.reach[i] >= __fmul_ru(c.h, kReachGrow);
-  if (none) {
-  } else if constexpr (U == 1) {
+  if constexpr (U == 1) {
     if constexpr (kLiveIn) for_each_live_then<1>(list, n, live, load, dead, one, one);
     else for_each_neighbor<1>(list, n, load, one);
   } else {
@@ -1440,13 +1236,8 @@ __global__ void __launch_bounds__(kMaxBlock) k_commit(StepArgs a, int to_v2, int
 // {x, m / rho} records xr, writes v.
 // kLiveOut: record the live bits of the committed positions for the
 // vorticity passes (all ones where this scene skips XSPH).
-// bound_par: parity of the step's last Jacobi iteration (-1 without
-// iterations): its lambda pass left reach[] at the positions p[bound_par],
-// and its delta pass the scene displacements, so the displacement bound can
-// skip walks whose entries are all beyond h at the committed positions.
 template <int U, bool kLiveOut>
-__global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_xsph(StepArgs a, int rest, const float4* xr,
-                                                                          int bound_par) {
+__global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_xsph(StepArgs a, int rest, const float4* xr) {
   if (failed(a.status)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
@@ -1454,20 +1245,10 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_xsph(StepArg
   const float4* __restrict__ vs = a.v2;
   const float4 xi = xs[i];
   const float4 vi = vs[i];
-  const int scene = __float_as_int(vi.w);
-  const SceneConst& c = a.sc[scene];
+  const SceneConst& c = a.sc[__float_as_int(vi.w)];
   float vx = vi.x, vy = vi.y, vz = vi.z;
   unsigned long long bits = ~0ull;
-  bool skip = false;
-  if (c.xsph_on && bound_par >= 0) {
-    const float4 q = a.p[bound_par][i];
-    float bound;
-    skip = beyond_reach(c, a.reach[i], moved_by(xi.x - q.x, xi.y - q.y, xi.z - q.z),
-                        moved_around(a, c, scene, i, bound_par), bound);
-    if (skip) bits = 0ull;
-  }
-  if (bound_par >= 0) count_skipped(a.status, skip);
-  if (c.xsph_on && !skip) {
+  if (c.xsph_on) {
     const int n = a.cnt[i];
     const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
     const float h2 = c.h2;
@@ -1714,12 +1495,11 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_eta(StepArgs
 // lasts as long as its deepest lists) and loses in a launch that fills every
 // SM, so the autotuner chooses G per kernel on the live state. Live bits are
 // assembled from each round's ballot; passes that would read live bits walk
-// every entry instead (a dead entry adds nothing), and keep the displacement
-// bound's skips.
+// every entry instead (a dead entry adds nothing).
 
 // Thread -> (particle slot, lane within its group, group's first warp lane).
 // Every lane of the warp takes part in the walk (a lane past the last
-// particle, or of a particle whose walk is skipped, walks an empty list), so
+// particle, or of a scene that skips the pass, walks an empty list), so
 // the shuffles and ballots run on the whole warp at once: shuffles whose masks
 // named only a group would let the warp's groups run their rounds apart and
 // serialise them.
@@ -1788,7 +1568,6 @@ __device__ __forceinline__ unsigned long long walk_lanes(const int* __restrict__
 template <int G, bool kLiveOut>
 __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_lambda_lanes(StepArgs a, int in) {
   if (failed(a.status)) return;
-  clear_moved(a.moved + static_cast<size_t>(in) * (a.moved_mask + 1u), a.moved_mask);
   const LaneGroup<G> L;
   const int i = L.i;
   const bool valid = i < a.n;
@@ -1798,24 +1577,13 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_lambda_lanes
   const SceneConst& c = a.sc[scene];
   const float h2 = c.h2;
   LambdaAcc acc;
-  bool skip = false;
-  float bound = 0.0f;
-  if constexpr (kLiveOut) {
-    if (valid) {
-      const float4 q = a.p[in ^ 1][i];
-      skip = beyond_reach(c, a.reach[i], moved_by(p.x - q.x, p.y - q.y, p.z - q.z),
-                          moved_around(a, c, scene, i, in ^ 1), bound);
-    }
-    count_skipped(a.status, skip && L.sub == 0);
-  }
-  const int n = (valid && !skip) ? a.cnt[i] : 0;
+  const int n = valid ? a.cnt[i] : 0;
   const int* __restrict__ list = a.nbr + (valid ? a.wbase[i >> 5] + (i & 31) : 0);
   auto load = [&](int j) { return __ldg(pos + j); };
   auto term = [&](const float4 q, bool in_list) {  // LambdaAcc::add, term by term
     Terms<5> t;
     const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
     const float r2 = dist2(dx, dy, dz);
-    if (in_list) acc.r2min = fminf(acc.r2min, r2);
     t.live = in_list && r2 < h2;
     if (t.live) {
       t.f[0] = poly6(c, r2);
@@ -1839,7 +1607,6 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_lambda_lanes
     acc.sum_g2 += t.f[4];
   };
   const unsigned long long bits = walk_lanes<G, 5>(list, n, L, load, term, add);
-  acc.r2min = L.min_over(acc.r2min);
   if (!valid || L.sub != 0) return;
   if constexpr (kLiveOut) store_live(a.live, a.n, i, bits);
   float rho;
@@ -1847,7 +1614,6 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_lambda_lanes
   a.lambda[i] = lam;
   a.rho[i] = rho;
   a.pl[i] = make_float4(p.x, p.y, p.z, lam);
-  a.reach[i] = skip ? bound : reach_from_r2(acc.r2min);
 }
 
 template <int G, int kPow, bool kLiveIn>
@@ -1864,9 +1630,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS)
   const float h2 = c.h2;
   float ax = 0.0f, ay = 0.0f, az = 0.0f;
   const bool scorr = c.scorr_on != 0;
-  // The lambda pass of this iteration left reach[i] at these positions.
-  const bool none = !valid || (kLiveIn && a.reach[i] >= __fmul_ru(c.h, kReachGrow));
-  const int n = none ? 0 : a.cnt[i];
+  const int n = valid ? a.cnt[i] : 0;
   const int* __restrict__ list = a.nbr + (valid ? a.wbase[i >> 5] + (i & 31) : 0);
   auto load = [&](int j) { return __ldg(pl + j); };
   auto term = [&](const float4 r, bool in_list) {  // k_delta's one(), term by term
@@ -1900,8 +1664,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS)
 }
 
 template <int G, bool kLiveOut>
-__global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_xsph_lanes(StepArgs a, int rest, const float4* xr,
-                                                                                int bound_par) {
+__global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_xsph_lanes(StepArgs a, int rest, const float4* xr) {
   if (failed(a.status)) return;
   const LaneGroup<G> L;
   const int i = L.i;
@@ -1913,15 +1676,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_xsph_lanes(S
   const int scene = valid ? __float_as_int(vi.w) : 0;
   const SceneConst& c = a.sc[scene];
   float vx = vi.x, vy = vi.y, vz = vi.z;
-  bool skip = false;
-  if (valid && c.xsph_on && bound_par >= 0) {
-    const float4 q = a.p[bound_par][i];
-    float bound;
-    skip = beyond_reach(c, a.reach[i], moved_by(xi.x - q.x, xi.y - q.y, xi.z - q.z),
-                        moved_around(a, c, scene, i, bound_par), bound);
-  }
-  if (bound_par >= 0) count_skipped(a.status, skip && L.sub == 0);
-  const bool walk = valid && c.xsph_on && !skip;
+  const bool walk = valid && c.xsph_on;
   const int n = walk ? a.cnt[i] : 0;
   const int* __restrict__ list = a.nbr + (valid ? a.wbase[i >> 5] + (i & 31) : 0);
   const float h2 = c.h2;
@@ -2062,7 +1817,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_eta_lanes(St
 // the work of k_bounds, which that step's graph then leaves out.
 __global__ void __launch_bounds__(kBlock) k_upload(const float* px, const float* py, const float* pz,
                                                    const float* vx, const float* vy, const float* vz,
-                                                   float4* x, float4* v, int* slot, float* rho, int* cnt,
+                                                   float4* x, float4* v, int* slot, float* rho,
                                                    const SceneConst* sc, int scenes, int n, int* bmin, int* bmax) {
   const int o = blockIdx.x * kBlock + threadIdx.x;
   int scene = -1;
@@ -2080,7 +1835,6 @@ __global__ void __launch_bounds__(kBlock) k_upload(const float* px, const float*
     v[o] = vo;
     slot[o] = o;
     rho[o] = 0.0f;
-    if (cnt) cnt[o] = 0;  // no previous lists: the list build reserves nothing ahead
     if (bmin) {
       float4 vp = vo;
       scene = lo;
@@ -2222,21 +1976,21 @@ void launch_lambda(const StepPlan& plan, cudaStream_t st, const StepArgs& a, int
 }
 
 template <bool kLiveOut>
-void launch_xsph(const StepPlan& plan, cudaStream_t st, const StepArgs& a, int rest, const float4* xr, int bound_par) {
+void launch_xsph(const StepPlan& plan, cudaStream_t st, const StepArgs& a, int rest, const float4* xr) {
   const ListShape sh(plan, FLUID_KERNEL_XSPH);
   const int b = sh.block;
   switch (sh.lanes) {
-    case 2: k_xsph_lanes<2, kLiveOut><<<list_grid(a, b, 2), b, 0, st>>>(a, rest, xr, bound_par); return;
-    case 4: k_xsph_lanes<4, kLiveOut><<<list_grid(a, b, 4), b, 0, st>>>(a, rest, xr, bound_par); return;
-    case 8: k_xsph_lanes<8, kLiveOut><<<list_grid(a, b, 8), b, 0, st>>>(a, rest, xr, bound_par); return;
+    case 2: k_xsph_lanes<2, kLiveOut><<<list_grid(a, b, 2), b, 0, st>>>(a, rest, xr); return;
+    case 4: k_xsph_lanes<4, kLiveOut><<<list_grid(a, b, 4), b, 0, st>>>(a, rest, xr); return;
+    case 8: k_xsph_lanes<8, kLiveOut><<<list_grid(a, b, 8), b, 0, st>>>(a, rest, xr); return;
     default: break;
   }
   const int g = list_grid(a, b, 1);
   switch (sh.unroll) {
-    case 1: k_xsph<1, kLiveOut><<<g, b, 0, st>>>(a, rest, xr, bound_par); break;
-    case 2: k_xsph<2, kLiveOut><<<g, b, 0, st>>>(a, rest, xr, bound_par); break;
-    case 8: k_xsph<8, kLiveOut><<<g, b, 0, st>>>(a, rest, xr, bound_par); break;
-    default: k_xsph<4, kLiveOut><<<g, b, 0, st>>>(a, rest, xr, bound_par); break;
+    case 1: k_xsph<1, kLiveOut><<<g, b, 0, st>>>(a, rest, xr); break;
+    case 2: k_xsph<2, kLiveOut><<<g, b, 0, st>>>(a, rest, xr); break;
+    case 8: k_xsph<8, kLiveOut><<<g, b, 0, st>>>(a, rest, xr); break;
+    default: k_xsph<4, kLiveOut><<<g, b, 0, st>>>(a, rest, xr); break;
   }
 }
 
@@ -2384,9 +2138,8 @@ cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t s
     // The committing pass left {x, m / rho} in the p buffer it did not use.
     const float4* xr = a.p[plan.iterations == 0 ? 1 : (plan.iterations & 1)];
     const int rest = (!plan.vorticity && plan.restitution) ? 1 : 0;
-    const int bound_par = plan.iterations > 0 ? ((plan.iterations - 1) & 1) : -1;
-    if (plan.vorticity) launch_xsph<true>(plan, st, a, rest, xr, bound_par);
-    else launch_xsph<false>(plan, st, a, rest, xr, bound_par);
+    if (plan.vorticity) launch_xsph<true>(plan, st, a, rest, xr);
+    else launch_xsph<false>(plan, st, a, rest, xr);
     m.mark(FLUID_KERNEL_XSPH);
   }
   if (plan.vorticity) {
@@ -2407,11 +2160,11 @@ cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t s
 }
 
 cudaError_t enqueue_upload(const float* px, const float* py, const float* pz, const float* vx, const float* vy,
-                           const float* vz, float4* x, float4* v, int* slot, float* rho, int* cnt,
-                           const SceneConst* sc, int scenes, int n, cudaStream_t st, int* bmin, int* bmax) {
+                           const float* vz, float4* x, float4* v, int* slot, float* rho, const SceneConst* sc,
+                           int scenes, int n, cudaStream_t st, int* bmin, int* bmax) {
   if (n > 0)
-    k_upload<<<blocks_for(n, kBlock), kBlock, 0, st>>>(px, py, pz, vx, vy, vz, x, v, slot, rho, cnt, sc, scenes, n,
-                                                       bmin, bmax);
+    k_upload<<<blocks_for(n, kBlock), kBlock, 0, st>>>(px, py, pz, vx, vy, vz, x, v, slot, rho, sc, scenes, n, bmin,
+                                                       bmax);
   return cudaGetLastError();
 }
 

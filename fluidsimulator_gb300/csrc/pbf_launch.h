@@ -113,13 +113,12 @@ cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan,
                          cudaStream_t stream, LaunchMarks& marks,
                          const StepRecord* rec = nullptr, const StepDownload* dl = nullptr);
 
-// Packs caller-order SoA arrays (device) into slot-order x/v of one parity
-// (and zeroes that parity's list lengths, cnt, when given);
+// Packs caller-order SoA arrays (device) into slot-order x/v of one parity;
 // with bmin/bmax it also accumulates the predicted cells' bounding box (what
 // k_bounds does), for a step launched with StepDownload::bounds_done.
 cudaError_t enqueue_upload(const float* px, const float* py, const float* pz,
                            const float* vx, const float* vy, const float* vz,
-                           float4* x, float4* v, int* slot, float* rho, int* cnt,
+                           float4* x, float4* v, int* slot, float* rho,
                            const SceneConst* sc, int scenes, int n,
                            cudaStream_t stream, int* bmin = nullptr, int* bmax = nullptr);
 

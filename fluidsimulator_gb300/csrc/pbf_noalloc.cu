@@ -50,10 +50,7 @@ constexpr size_t kX0 = 0, kX1 = kX0 + kF4, kV0 = kX1 + kF4, kV1 = kV0 + kF4;
 constexpr size_t kP0 = kV1 + kF4, kP1 = kP0 + kF4, kV2 = kP1 + kF4, kOmega = kV2 + kF4;
 constexpr size_t kPl = kOmega + kF4;
 constexpr size_t kLive = kPl + kF4;
-constexpr size_t kReach = kLive + up(2 * sizeof(uint32_t) * kMaxN);
-constexpr size_t kMoved = kReach + up(sizeof(float) * kMaxN);
-constexpr unsigned kMovedSlots = 1024;  // displacement table of the list passes' bound, per parity
-constexpr size_t kSlot0 = kMoved + up(2 * sizeof(unsigned) * kMovedSlots), kSlot1 = kSlot0 + kI32, kRho0 = kSlot1 + kI32, kRho1 = kRho0 + kI32;
+constexpr size_t kSlot0 = kLive + up(2 * sizeof(uint32_t) * kMaxN), kSlot1 = kSlot0 + kI32, kRho0 = kSlot1 + kI32, kRho1 = kRho0 + kI32;
 constexpr size_t kLambda = kRho1 + kI32, kKeys0 = kLambda + kI32, kKeys1 = kKeys0 + kI32;
 constexpr size_t kVals0 = kKeys1 + kI32, kVals1 = kVals0 + kI32, kCnt = kVals1 + kI32;
 constexpr size_t kDepth = kCnt + kI32, kWbase = kDepth + up(sizeof(int) * (kMaxWarps + 1));
@@ -113,9 +110,6 @@ StepArgs carve(unsigned char* b, int n) {
   a.omega = at<float4>(b, kOmega);
   a.pl = at<float4>(b, kPl);
   a.live = at<uint32_t>(b, kLive);
-  a.reach = at<float>(b, kReach);
-  a.moved = at<unsigned>(b, kMoved);
-  a.moved_mask = kMovedSlots - 1u;
   a.lambda = at<float>(b, kLambda);
   a.rho = at<float>(b, kRho1);
   a.keys[0] = at<uint32_t>(b, kKeys0);
@@ -127,7 +121,6 @@ StepArgs carve(unsigned char* b, int n) {
   a.digit_total = at<uint32_t>(b, kDigits);
   a.table = at<int2>(b, kTable);
   a.cnt = at<int>(b, kCnt);
-  a.cnt_old = nullptr;  // one step per call: no previous lists to size the build's reservations
   a.depth = at<int>(b, kDepth);
   a.wbase = at<long long>(b, kWbase);
   a.ovf = at<int>(b, kOvf);
@@ -186,7 +179,7 @@ extern "C" int fluid_gb300_step_noalloc(const fluid_params* params, int64_t coun
   if (enqueue_reset(a.status, a.bmin, a.bmax, 1, st) != cudaSuccess) return FLUID_ERR_CUDA;
   if (enqueue_upload(pos_x, pos_y, pos_z, vel_x, vel_y, vel_z, const_cast<float4*>(a.x_old),
                      const_cast<float4*>(a.v_old), const_cast<int*>(a.slot_old), const_cast<float*>(a.rho_old),
-                     nullptr, a.sc, 1, n, st) != cudaSuccess)
+                     a.sc, 1, n, st) != cudaSuccess)
     return FLUID_ERR_CUDA;
   if (enqueue_step(a, plan, st, marks) != cudaSuccess) return FLUID_ERR_CUDA;
   // The status word is read on the caller's stream, behind the step, so the

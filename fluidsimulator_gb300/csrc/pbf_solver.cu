@@ -288,15 +288,8 @@ class Solver {
     ok &= omega_.alloc(np) == cudaSuccess;
     ok &= pl_.alloc(np) == cudaSuccess;
     ok &= live_.alloc(2 * np) == cudaSuccess;
-    ok &= reach_.alloc(np) == cudaSuccess;
-    // Displacement table of the list passes' bound: about one slot per 16
-    // particles (a bin holds ~64 at lattice density), a power of two.
-    moved_slots_ = 4096;
-    while (moved_slots_ < n_ / 16 && moved_slots_ < (1u << 22)) moved_slots_ <<= 1;
-    ok &= moved_.alloc(2 * static_cast<size_t>(moved_slots_)) == cudaSuccess;
     ok &= lambda_.alloc(np) == cudaSuccess;
-    ok &= cnt_[0].alloc(np) == cudaSuccess;
-    ok &= cnt_[1].alloc(np) == cudaSuccess;
+    ok &= cnt_.alloc(np) == cudaSuccess;
     ok &= depth_.alloc(static_cast<size_t>(warps_) + 1) == cudaSuccess;
     ok &= ovf_.alloc(static_cast<size_t>(warps_) + 1) == cudaSuccess;
     ok &= wbase_.alloc(static_cast<size_t>(warps_) + 1) == cudaSuccess;
@@ -315,7 +308,6 @@ class Solver {
       return fail(FLUID_ERR_OUT_OF_MEMORY, "device allocation failed");
     cudaMemsetAsync(table_.p, 0, table_.n * sizeof(int2), stream_);
     cudaMemsetAsync(look_.p, 0, look_.n * sizeof(unsigned long long), stream_);  // tag 0: never current
-    cudaMemsetAsync(moved_.p, 0, moved_.n * sizeof(unsigned), stream_);
     if (cudaMemcpyAsync(sc_.p, sc_host_.data(), S_ * sizeof(SceneConst), cudaMemcpyHostToDevice, stream_) !=
         cudaSuccess)
       return cuda_fail("upload scene constants");
@@ -385,7 +377,7 @@ class Solver {
         for (int k = 0; k < 6; ++k) dev[k] = src[k];
       }
       if (enqueue_upload(dev[0], dev[1], dev[2], dev[3], dev[4], dev[5], x_[parity_].p, v_[parity_].p,
-                         slot_[parity_].p, rho_[parity_].p, cnt_[parity_].p, sc_.p, S_, n_, stream_,
+                         slot_[parity_].p, rho_[parity_].p, sc_.p, S_, n_, stream_,
                          bounds_ready_ ? bmin_.p : nullptr, bounds_ready_ ? bmax_.p : nullptr) != cudaSuccess)
         return cuda_fail("upload kernel");
       if (wait && cudaStreamSynchronize(stream_) != cudaSuccess) return cuda_fail("upload");
@@ -515,7 +507,6 @@ class Solver {
       pending_ = 0;
       last_pairs_ = static_cast<long long>(st.pairs);
       last_max_ = st.nbr_max;
-      last_skipped_ = static_cast<long long>(st.skipped);
       last_cells_ = static_cast<int>(st.total_cells);
       last_npass_ = st.npass;
       if (enqueue_reset(status_.p, bmin_.p, bmax_.p, S_, stream_) != cudaSuccess) return cuda_fail("reset");
@@ -951,7 +942,6 @@ class Solver {
     out->grid_capacity = grid_cap_;
     out->regrows = regrows_;
     out->kernel_launches = launches_;
-    out->skipped_walks = last_skipped_;
     return FLUID_OK;
   }
 
@@ -1000,7 +990,7 @@ class Solver {
     }
     std::vector<int32_t> buf(n);
     const void* src = nullptr;
-    if (what == FLUID_DEBUG_NEIGHBOR_COUNTS) src = cnt_[parity_].p;
+    if (what == FLUID_DEBUG_NEIGHBOR_COUNTS) src = cnt_.p;
     else if (what == FLUID_DEBUG_RHO) src = rho_[parity_].p;
     else if (what == FLUID_DEBUG_LAMBDA) src = lambda_.p;
     else return fail(FLUID_ERR_INVALID_ARGUMENT, "unknown debug record");
@@ -1097,14 +1087,10 @@ class Solver {
     a.vals[1] = vals_[1].p;
     a.look = look_.p;
     a.live = live_.p;
-    a.reach = reach_.p;
-    a.moved = moved_.p;
-    a.moved_mask = moved_slots_ - 1u;
     a.radix_next = radix_next_.p;
     a.digit_total = digit_total_.p;
     a.table = table_.p;
-    a.cnt = cnt_[par ^ 1].p;
-    a.cnt_old = cnt_[par].p;
+    a.cnt = cnt_.p;
     a.depth = depth_.p;
     a.ovf = ovf_.p;
     a.wbase = wbase_.p;
@@ -1346,12 +1332,11 @@ class Solver {
       const size_t len = static_cast<size_t>(st.cursor);
       if (tp.nbr.n < len && tp.nbr.alloc(len + len / 4 + 32)) return fail(FLUID_ERR_OUT_OF_MEMORY, "adjoint tape");
       cudaMemcpyAsync(tp.nbr.p, nbr_.p, len * sizeof(int), cudaMemcpyDeviceToDevice, stream_);
-      cudaMemcpyAsync(tp.cnt.p, cnt_[parity_ ^ 1].p, n * sizeof(int), cudaMemcpyDeviceToDevice, stream_);
+      cudaMemcpyAsync(tp.cnt.p, cnt_.p, n * sizeof(int), cudaMemcpyDeviceToDevice, stream_);
       cudaMemcpyAsync(tp.wbase.p, wbase_.p, (static_cast<size_t>(warps_) + 1) * sizeof(long long),
                       cudaMemcpyDeviceToDevice, stream_);
       last_pairs_ = static_cast<long long>(st.pairs);
       last_max_ = st.nbr_max;
-      last_skipped_ = static_cast<long long>(st.skipped);
       last_cells_ = static_cast<int>(st.total_cells);
       last_npass_ = st.npass;
       commit_steps(1);
@@ -1454,17 +1439,13 @@ class Solver {
   int parity_ = 0, pending_ = 0;
   long long steps_ = 0, regrows_ = 0, launches_ = 0, launches_per_step_ = 0;
   long long last_pairs_ = 0;
-  long long last_skipped_ = 0;
   int last_max_ = 0, last_cells_ = 0, last_npass_ = 0;
   DBuf<float4> x_[2], v_[2], p_[2], v2_, omega_, pl_;
-  DBuf<int> slot_[2], vals_[2], cnt_[2], depth_, ovf_, nbr_, bmin_, bmax_;
+  DBuf<int> slot_[2], vals_[2], cnt_, depth_, ovf_, nbr_, bmin_, bmax_;
   DBuf<float> rho_[2], lambda_;
   DBuf<uint32_t> keys_[2], digit_total_;
   DBuf<unsigned long long> look_;
   DBuf<uint32_t> live_;
-  DBuf<float> reach_;
-  DBuf<unsigned> moved_;
-  unsigned moved_slots_ = 0;
   DBuf<int> radix_next_;
   DBuf<long long> wbase_;
   DBuf<int2> table_;

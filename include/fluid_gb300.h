@@ -23,6 +23,9 @@
 extern "C" {
 #endif
 
+/* 2: per-plane friction at the end of fluid_params. 3: entry points added
+ * (fluid_solver_get/set_lanes, fluid_fill_block, fluid_fill_shape); every
+ * struct is as in version 2. */
 #define FLUID_GB300_ABI_VERSION 3
 /* Planes per scene. The reference keeps an unbounded std::vector SoA
  * (core/include/fluid/core.h:44-78); every reference scene uses 6. */
@@ -355,9 +358,6 @@ typedef struct fluid_stats {
   int64_t grid_capacity;     /* allocated cell-table entries */
   int64_t regrows;           /* steps re-run after a capacity grew */
   int64_t kernel_launches;   /* kernels launched since configure */
-  int64_t skipped_walks;     /* list walks of the last step's lambda (iterations
-                                after the first) and XSPH passes that the
-                                displacement bound proved empty (ABI 3) */
 } fluid_stats;
 
 int fluid_solver_get_stats(fluid_solver* solver, fluid_stats* out);

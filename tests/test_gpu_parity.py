@@ -175,33 +175,6 @@ def test_full_size_double_dam_break_two_steps(cuda_lib, oracle_lib):
     assert np.float32(b["time"]) == np.float32(a["time"])
 
 
-@pytest.mark.parametrize("steps", [1, 3])
-def test_displacement_bound_skips_walks_and_stays_exact(cuda_lib, oracle_lib, steps):
-    """The first steps of a 64,000-particle falling block (the throughput
-    scene's spacing, h and flags): the first Jacobi corrections (scaled by
-    1/m = 125) push every listed pair past h, so the lambda passes of later
-    iterations and XSPH skip most walks by the displacement bound. Their
-    results equal the oracle's bit for bit (rho, lambda, positions,
-    velocities, and every later step that starts from them)."""
-    sc = scenes.falling_block(40, seed=0)
-    a = oracle_lib.Oracle().run(sc.params, sc.pos, sc.vel, 0.0, steps, dump=True)
-    s = Solver(0)
-    s.configure([sc.params], [sc.count])
-    s.upload(sc.pos, sc.vel)
-    skipped = []
-    for _ in range(steps):
-        s.step(1)
-        skipped.append(s.stats()["skipped_walks"])
-    rec = {k: s.read_debug(w) for k, w in DEBUG.items()}
-    pos, vel = s.download()
-    s.close()
-    assert skipped[0] > sc.count // 2, skipped  # the bound proves most walks empty
-    for k in DEBUG:
-        np.testing.assert_array_equal(rec[k], a[k], err_msg=k)
-    np.testing.assert_array_equal(pos, a["pos"])
-    np.testing.assert_array_equal(vel, a["vel"])
-
-
 def test_full_size_double_dam_break_into_the_collapse(cuda_lib, oracle_lib):
     """The 250,000-particle double dam break over its first 10 steps, by which
     it has collapsed to ~1,700 neighbours per particle (max ~6,300; the lists
