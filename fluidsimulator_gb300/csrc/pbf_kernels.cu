@@ -49,7 +49,12 @@ constexpr int kMaxBlock = 512;  // largest block the tuner may pick
 #define FGB_LIST_MIN_BLOCKS 2
 #endif
 constexpr int kMaxBuildBlock = 256;  // k_nbr_build: kStage ints per thread of shared memory
-constexpr int kStage = 40;           // list entries per lane staged in shared memory
+// List entries per lane staged in shared memory by the list build (36 KB per
+// 256-thread block). Lattice-phase lists hold at most ~32 entries; every
+// staged row is shared memory the L1 cannot use for the candidates the scan
+// reads (5 blocks per SM), so the build ran 0.295 ms at 40 and 0.284 ms at
+// 36 or 32 per 1M step. Longer lists go through k_nbr_overflow.
+constexpr int kStage = 36;
 
 __device__ __forceinline__ bool failed(const DevStatus* st) {
   return *reinterpret_cast<const volatile int*>(&st->err) != 0;

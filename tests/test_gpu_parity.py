@@ -21,9 +21,12 @@ DEBUG = {"cell_keys": _capi.DEBUG_CELL_KEYS, "sorted_order": _capi.DEBUG_SORTED_
          "neighbor_counts": _capi.DEBUG_NEIGHBOR_COUNTS, "rho": _capi.DEBUG_RHO, "lambda": _capi.DEBUG_LAMBDA}
 
 
-def run_gpu(sc, steps, graphs=True, profiling=False, records=False):
+def run_gpu(sc, steps, graphs=True, profiling=False, records=False, lanes=1):
     s = Solver(0)
     s.configure([sc.params], [sc.count])
+    if lanes != 1:
+        s.set_tuning({k: {"unroll": 4, "block": 256, "lanes": lanes if k in _capi.LIST_PASSES else 1}
+                      for k in _capi.TUNABLE})
     s.set_graphs(graphs)
     s.set_profiling(profiling)
     s.upload(sc.pos, sc.vel)
@@ -216,16 +219,23 @@ def test_full_size_double_dam_break_into_the_collapse(cuda_lib, oracle_lib):
     assert max(dmax) <= 1.005 * max(a["density_max"])
 
 
-def test_full_size_differentiable_scene_20_steps(cuda_lib, oracle_lib):
+@pytest.fixture(scope="module")
+def differentiable_20_oracle(oracle_lib):
+    sc = scenes.differentiable_block(32, seed=0)
+    return sc, oracle_lib.Oracle().run(sc.params, sc.pos, sc.vel, 0.0, 20, dump=True)
+
+
+@pytest.mark.parametrize("lanes", [1, 2, 4, 8])
+def test_full_size_differentiable_scene_20_steps(cuda_lib, differentiable_20_oracle, lanes):
     """The 32,768-particle differentiable scene (XSPH and s_corr, initial
     velocities N(0, 0.1^2)) at full size over 20 steps, by which it has
     collapsed to ~380 neighbours per particle (max ~1,700: lists regrow and
-    run past the staged and live-bit heads): the last step's records and the
-    state equal the oracle's."""
-    sc = scenes.differentiable_block(32, seed=0)
+    run past the staged and live-bit heads), with 1, 2, 4 and 8 lanes per
+    particle in every list pass: the last step's records and the state equal
+    the oracle's."""
+    sc, a = differentiable_20_oracle
     assert sc.count == 32_768
-    a = oracle_lib.Oracle().run(sc.params, sc.pos, sc.vel, 0.0, 20, dump=True)
-    b = run_gpu(sc, 20, records=True)
+    b = run_gpu(sc, 20, records=True, lanes=lanes)
     assert b["stats"]["regrows"] >= 1 and b["stats"]["neighbor_max"] > 64
     for k in ("cell_keys", "sorted_order", "neighbor_counts", "rho", "lambda", "pos", "vel"):
         np.testing.assert_array_equal(b[k], a[k], err_msg=k)
