@@ -391,6 +391,11 @@ def run_ours(args, world, rank, local):
         if differentiable:
             differentiable["fp64_checks"] = gradient_checks(args)
 
+    for part in (configs or {}).values():  # the CPU legs' inputs, left when they did not run
+        for k in [k for k in part if k.startswith("_")]:
+            part.pop(k)
+    if collapsed:
+        collapsed.pop("_state", None)
     out = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
@@ -400,7 +405,8 @@ def run_ours(args, world, rank, local):
                    "particles": n, "neighbors_per_particle": round(stats["neighbor_pairs"] / n, 2),
                    "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{world}",
                    "graphs": True, "exact_fp32": True,
-                   "tuning": ({k: [v["unroll"], v["block"]] for k, v in tuning.items()} if tuning else "default"),
+                   "tuning": ({k: [v["unroll"], v["block"], v.get("lanes", 1)] for k, v in tuning.items()}
+                              if tuning else "default"),
                    "sort_bits": sort_bits,
                    "kernel_timing": "per-kernel CUDA events in a second pass over the same steps (the timed pass "
                                     "has none); that pass's step time is ms_per_step_instrumented"},

@@ -49,11 +49,12 @@ constexpr int kMaxBlock = 512;  // largest block the tuner may pick
 #define FGB_LIST_MIN_BLOCKS 2
 #endif
 constexpr int kMaxBuildBlock = 256;  // k_nbr_build: kStage ints per thread of shared memory
-// List entries per lane staged in shared memory by the list build (36 KB per
-// 256-thread block). Lattice-phase lists hold at most ~32 entries; every
-// staged row is shared memory the L1 cannot use for the candidates the scan
-// reads (5 blocks per SM), so the build ran 0.295 ms at 40 and 0.284 ms at
-// 36 or 32 per 1M step. Longer lists go through k_nbr_overflow.
+// List entries per lane staged in shared memory by the list build (kStage + 1
+// rows, 37 KB per 256-thread block). Lattice-phase lists hold at most ~32
+// entries; every staged row is shared memory the L1 cannot use for the
+// candidates the scan reads (5 blocks per SM), so the build ran 0.295 ms at
+// 40 and 0.284 ms at 36 or 32 per 1M step. Longer lists go through
+// k_nbr_overflow.
 constexpr int kStage = 36;
 
 __device__ __forceinline__ bool failed(const DevStatus* st) {
@@ -645,7 +646,7 @@ __global__ void __launch_bounds__(kBlock) k_reorder(StepArgs a) {
 // ---------------------------------------------------------------------------
 // Neighbour lists.
 
-// Calls f(j, pos[j]) for j in [lo, hi) except j == self (kSkip), kFetch
+// Calls f(j, pos[j], ok) for j in [lo, hi), ok false for j == self (kSkip); kFetch
 // records loaded before any is used. Lanes of a warp whose particles share a
 // cell walk the same j together, so each load is a broadcast.
 template <int kFetch, bool kSkip, typename F>
@@ -656,17 +657,16 @@ __device__ __forceinline__ void scan_range(const float4* __restrict__ pos, int l
 #pragma unroll
     for (int u = 0; u < kFetch; ++u) q[u] = __ldg(pos + j + u);
 #pragma unroll
-    for (int u = 0; u < kFetch; ++u)
-      if (!kSkip || j + u != self) f(j + u, q[u]);
+    for (int u = 0; u < kFetch; ++u) f(j + u, q[u], !kSkip || j + u != self);
   }
-  for (; j < hi; ++j)
-    if (!kSkip || j != self) f(j, __ldg(pos + j));
+  for (; j < hi; ++j) f(j, __ldg(pos + j), !kSkip || j != self);
 }
 
-// Visits every j != i of the 27 cells around p in the reference's order
-// (core.cpp:211-243), calling f(j, q_j) for each candidate. Cell keys advance
-// incrementally along x; candidates are fetched kFetch at a time (issued
-// before any is tested, tested in order); only the centre cell tests j != i.
+// Visits the 27 cells around p in the reference's order (core.cpp:211-243),
+// calling f(j, q_j, ok) for each particle of them; ok is false for j == i
+// (tested in the centre cell only). Cell keys advance incrementally along x;
+// candidates are fetched kFetch at a time (issued before any is tested,
+// tested in order).
 template <int kFetch, typename F>
 __device__ __forceinline__ void for_each_candidate(const StepArgs& a, const uint32_t* ks, const GridInfo& g,
                                                    const SceneConst& c, int i, const float4 p,
@@ -785,8 +785,14 @@ __device__ __forceinline__ void for_each_pair_candidate(const StepArgs& a, const
 }
 
 // Neighbour lists in one scan (core.cpp:205-247). Each lane stages its first
-// kStage list entries in
-// shared memory while it scans; the block then claims its warps' 32-wide
+// kStage list entries in shared memory while it scans. The staging takes no
+// branch on the r2 test: every candidate is stored in the lane's next free
+// row, and the count advances only when the candidate is within h, so a
+// rejected candidate is overwritten by the next one (row kStage is a spare
+// that absorbs the stores past the staged rows). At ~13 % acceptance this
+// took the lattice build from 0.285 to 0.260 ms per 1M step and the
+// collapsed 125k build from 0.96 to 0.80 ms against a branch around the
+// store. The block then claims its warps' 32-wide
 // slices with one atomic on the list cursor (placement varies run to run,
 // every list's content and order do not) and writes the staged entries out
 // as coalesced 128-byte rows. Warps with a longer list set ovf[w] and
@@ -804,7 +810,7 @@ __global__ void __launch_bounds__(kMaxBuildBlock) k_nbr_build(StepArgs a) {
   if (block_failed) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int* mine = stage + warp * (kStage * 32) + lane;  // entry k at mine[32 k]
+  int* mine = stage + warp * ((kStage + 1) * 32) + lane;  // entry k at mine[32 k]
   int count = 0;
   if (i < a.n) {
     const uint32_t* ks = sorted_keys(a, a.status->npass);
@@ -813,13 +819,12 @@ __global__ void __launch_bounds__(kMaxBuildBlock) k_nbr_build(StepArgs a) {
     const SceneConst& c = a.sc[scene];
     const GridInfo g = a.grid[scene];
     const float h2 = c.h2;
-    auto test = [&](int j, const float4 q) {
-      if (dist2(p.x - q.x, p.y - q.y, p.z - q.z) < h2) {
-        if (count < kStage) mine[32 * count] = j;
-        ++count;
-      }
+    auto test = [&](int j, const float4 q, bool ok) {
+      const bool in = dist2(p.x - q.x, p.y - q.y, p.z - q.z) < h2 && ok;
+      mine[32 * min(count, kStage)] = j;
+      count += in ? 1 : 0;
     };
-    if (c.all_pairs) for_each_pair_candidate(a, c, i, a.p[0], test);
+    if (c.all_pairs) for_each_pair_candidate(a, c, i, a.p[0], [&](int j, const float4 q) { test(j, q, true); });
     else for_each_candidate<4>(a, ks, g, c, i, p, a.p[0], test);
     a.cnt[i] = count;
   }
@@ -874,13 +879,13 @@ __global__ void __launch_bounds__(kMaxBlock, 1) k_nbr_overflow(StepArgs a) {
   int* out = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
   const float h2 = c.h2;
   int k = 0;
-  auto test = [&](int j, const float4 q) {
-    if (dist2(p.x - q.x, p.y - q.y, p.z - q.z) < h2) {
+  auto test = [&](int j, const float4 q, bool ok) {
+    if (ok && dist2(p.x - q.x, p.y - q.y, p.z - q.z) < h2) {
       if (k >= kStage && k < depth) out[32ll * k] = j;
       ++k;
     }
   };
-  if (c.all_pairs) for_each_pair_candidate(a, c, i, a.p[0], test);
+  if (c.all_pairs) for_each_pair_candidate(a, c, i, a.p[0], [&](int j, const float4 q) { test(j, q, true); });
   else for_each_candidate<4>(a, ks, g, c, i, p, a.p[0], test);
 }
 
@@ -2101,7 +2106,7 @@ cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t s
     cudaMemcpyAsync(rec->p, a.p[0], n4, cudaMemcpyDeviceToDevice, st);
   }
   const int bc = plan.block[FLUID_KERNEL_NBR_BUILD] > kMaxBuildBlock ? kMaxBuildBlock : plan.block[FLUID_KERNEL_NBR_BUILD];
-  k_nbr_build<<<blocks_for(a.n, bc), bc, sizeof(int) * kStage * bc, st>>>(a);
+  k_nbr_build<<<blocks_for(a.n, bc), bc, sizeof(int) * (kStage + 1) * bc, st>>>(a);
   m.mark(FLUID_KERNEL_NBR_BUILD);
   const int bf = plan.block[FLUID_KERNEL_NBR_OVERFLOW];
   k_nbr_overflow<<<blocks_for(a.n, bf), bf, 0, st>>>(a);
