@@ -28,7 +28,7 @@
 namespace fgb {
 
 constexpr int kBlock = 256;
-constexpr int kRadixItems = 8;                      // keys per thread
+constexpr int kRadixItems = 16;                     // keys per thread (8: 0.074 -> 0.067 ms of sort per 1M step at 16)
 constexpr int kRadixTile = kBlock * kRadixItems;    // keys per CTA
 constexpr int kRadixMaxBins = 1 << 11;                // widest digit (11 bits)
 constexpr int kRadixMaxPasses = 4;                  // passes of a u32 key at 8-bit digits

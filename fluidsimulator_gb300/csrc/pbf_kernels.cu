@@ -483,8 +483,8 @@ __device__ __forceinline__ void digit_starts(const uint32_t* __restrict__ tot, u
 template <int kBits>
 __global__ void __launch_bounds__(kBlock) k_radix_onesweep(StepArgs a, int pass) {
   constexpr int kBins = 1 << kBits;
-  // Per-warp digit counts; at most 32 * kRadixItems * (kBlock / 32) = 2048
-  // per tile, so 16 bits hold them when 32-bit counters would not fit.
+  // Per-warp digit counts; at most kRadixTile = 4096 per tile, so 16 bits
+  // hold them where 32-bit counters would not fit in shared memory.
   using Count = typename std::conditional<(kBits <= 8), uint32_t, uint16_t>::type;
   __shared__ Count wcnt[kBlock / 32][kBins];
   __shared__ uint32_t goff[kBins];  // digit starts, then this tile's first slot per digit
