@@ -426,13 +426,17 @@ def run_ours(args, world, rank, local):
         print(json.dumps(_finite(out)), flush=True)
 
 
-def _gpu_run(sc, steps, dev, stream, pair_budget=None):
+def _gpu_run(sc, steps, dev, stream, pair_budget=None, tune=False):
     """Runs up to `steps` steps of a scene from its initial state on a fresh
-    solver (graphs on, default shapes), each step bracketed by CUDA events on
-    the solver's stream; stops early once a step's lists hold more than
-    `pair_budget` entries (the next steps of a collapse grow them further).
-    Returns per-step ms, neighbours per particle per step, the final state and
-    the stats."""
+    solver (graphs on; shapes from fluid_solver_autotune on the initial state
+    when `tune`, else the defaults), each step bracketed by CUDA events on the
+    solver's stream; stops early once a step's lists hold more than
+    `pair_budget` entries (the next steps of a collapse grow them further). A
+    step that outgrows the list or grid capacity is re-run by synchronize()
+    after a regrow, behind the closing event: such a step is timed to a third
+    event recorded after synchronize() returns (its host turnaround
+    included). Returns per-step ms, neighbours per particle per step, the
+    final state, the stats and the shapes used."""
     import torch
 
     from fluidsimulator_gb300.solver import Solver
@@ -441,22 +445,35 @@ def _gpu_run(sc, steps, dev, stream, pair_budget=None):
     s.configure([sc.params], [sc.count])
     s.set_stream(stream.cuda_stream)
     s.upload(sc.pos, sc.vel)
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    shapes = None
+    if tune:
+        tuned = s.autotune()
+        shapes = {"sort_bits": s.sort_bits(),
+                  **{k: [v["unroll"], v["block"], v["lanes"]] for k, v in tuned.items()}}
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
     ms, nbr = [], []
+    regrows = s.stats()["regrows"]
     for _ in range(steps):
         ev[0].record(stream)
         s.step_async(1)
         ev[1].record(stream)
         s.synchronize()
-        ms.append(ev[0].elapsed_time(ev[1]))
-        pairs = s.stats()["neighbor_pairs"]
+        st = s.stats()
+        if st["regrows"] != regrows:
+            regrows = st["regrows"]
+            ev[2].record(stream)
+            ev[2].synchronize()
+            ms.append(ev[0].elapsed_time(ev[2]))
+        else:
+            ms.append(ev[0].elapsed_time(ev[1]))
+        pairs = st["neighbor_pairs"]
         nbr.append(pairs / sc.count)
         if pair_budget and pairs > pair_budget:
             break
     pos, vel = s.download()
     st = s.stats()
     s.close()
-    return ms, nbr, pos, vel, st
+    return ms, nbr, pos, vel, st, shapes
 
 
 def run_configs(args, dev, stream):
@@ -464,38 +481,47 @@ def run_configs(args, dev, stream):
     each run over its full length on the GPU: c1, the plain dam break (4,096
     particles, 16^3 lattice, spacing 0.05, h 0.1, flags off, 240 steps), and
     c2, the double dam break (two 50^3 blocks, 250,000 particles, spacing
-    0.025, h 0.05, all three flags, 480 steps). c2 collapses completely
-    (with m = rho0 sp^3 the Jacobi update scales by 1/m = 64, SURVEY-style
-    collapse): each block's particles end up within h of nearly all others,
-    ~125,000 neighbours each, so its lists would grow past 87e9 entries
-    (~350 GB, the reference's CSR alike). Its GPU run stops once a step's
-    lists pass `--c2-pair-budget` entries and reports the steps it covered.
-    The CPU side (cpu_configs) times the oracle over the whole of c1 and a
-    stated prefix of c2 on the host cores and checks the GPU's state after
-    that prefix bit for bit."""
+    0.025, h 0.05, all three flags, 480 steps). Both run with the shapes the
+    autotuner picks on the initial state; c1 is also run with the default
+    shapes. c2 collapses completely (with m = rho0 sp^3 the Jacobi update
+    scales by 1/m = 64): each block's particles end up within h of nearly all
+    others, ~125,000 neighbours each, so its lists would grow past 87e9
+    entries (~350 GB, the reference's CSR alike). Its GPU run stops once a
+    step's lists pass `--c2-pair-budget` entries and reports the steps it
+    covered. The CPU side (cpu_configs) times the oracle over the whole of c1
+    and a stated prefix of c2 on the host cores and checks the GPU's state
+    after that prefix bit for bit."""
     from fluidsimulator_gb300 import scenes
 
+    def summary(ms, nbr, st):
+        ran, total = len(ms), sum(ms)
+        return {"ms_total": round(total, 3), "ms_per_step": round(total / ran, 4),
+                "particle_steps_per_s": round(sc.count * ran / (total / 1e3), 1),
+                "ms_per_step_first5": round(statistics.mean(ms[:5]), 4),
+                "ms_per_step_last5": round(statistics.mean(ms[-5:]), 4),
+                "neighbors_per_particle_step1": round(nbr[0], 2),
+                "neighbors_per_particle_last": round(nbr[-1], 2), "neighbor_max_last": st["neighbor_max"],
+                "regrows": st["regrows"]}
+
     out = {}
-    for key, sc, steps, budget in (
-            ("c1_dam_break_4096", scenes.dam_break(16, seed=0), args.c1_steps, None),
-            ("c2_double_dam_break_250k", scenes.double_dam_break(50, seed=0), args.c2_steps, args.c2_pair_budget)):
+    for key, sc, steps, budget, default_too in (
+            ("c1_dam_break_4096", scenes.dam_break(16, seed=0), args.c1_steps, None, True),
+            ("c2_double_dam_break_250k", scenes.double_dam_break(50, seed=0), args.c2_steps, args.c2_pair_budget,
+             False)):
         if steps <= 0:
             continue
         _gpu_run(sc, min(steps, 3), dev, stream)  # warm-up: kernels loaded, graphs captured once
-        ms, nbr, pos, vel, st = _gpu_run(sc, steps, dev, stream, budget)
+        ms, nbr, pos, vel, st, shapes = _gpu_run(sc, steps, dev, stream, budget, tune=True)
         ran = len(ms)
-        total = sum(ms)
         out[key] = {"particles": sc.count, "steps": ran, "steps_of_config": steps,
-                    "gpu": {"ms_total": round(total, 3), "ms_per_step": round(total / ran, 4),
-                            "particle_steps_per_s": round(sc.count * ran / (total / 1e3), 1),
-                            "ms_per_step_first5": round(statistics.mean(ms[:5]), 4),
-                            "ms_per_step_last5": round(statistics.mean(ms[-5:]), 4),
-                            "neighbors_per_particle_step1": round(nbr[0], 2),
-                            "neighbors_per_particle_last": round(nbr[-1], 2), "neighbor_max_last": st["neighbor_max"],
-                            "regrows": st["regrows"],
-                            "timing": "per-step CUDA events on the solver's stream, graphs on, default shapes, "
-                                      "whole run from the initial state"},
+                    "gpu": {**summary(ms, nbr, st), "shapes": shapes,
+                            "timing": "per-step CUDA events on the solver's stream (a step re-run after a regrow "
+                                      "timed to an event after synchronize), graphs on, autotuned shapes, whole "
+                                      "run from the initial state"},
                     "_scene": sc, "_ms": ms}
+        if default_too:
+            dms, dnbr, _, _, dst, _ = _gpu_run(sc, steps, dev, stream, budget)
+            out[key]["gpu_default_shapes"] = summary(dms, dnbr, dst)
         if ran < steps:
             out[key]["stopped"] = (f"after step {ran}: {nbr[-1]:.0f} neighbours per particle, lists past the "
                                    f"{budget:.3g}-entry budget (a complete collapse needs ~87e9)")
@@ -707,6 +733,26 @@ def run_batched(args, dev, stream, l2_flush):
         s.set_sort_bits(sort_bits)
         small.append(s)
 
+    ev2 = torch.cuda.Event(enable_timing=True)
+
+    def timed_step(solvers):
+        """One step of every solver between two events on the stream. A step
+        that outgrows a capacity is re-run by synchronize() after a regrow,
+        behind ev1: then the step is timed to an event recorded after the
+        re-run (host turnaround included)."""
+        before = sum(s.stats()["regrows"] for s in solvers)
+        ev0.record(stream)
+        for s in solvers:
+            s.step_async(1)
+        ev1.record(stream)
+        for s in solvers:
+            s.synchronize()
+        if sum(s.stats()["regrows"] for s in solvers) != before:
+            ev2.record(stream)
+            ev2.synchronize()
+            return ev0.elapsed_time(ev2)
+        return ev0.elapsed_time(ev1)
+
     def time_batched(steps, restore):
         ms = []
         if not restore:
@@ -715,11 +761,7 @@ def run_batched(args, dev, stream, l2_flush):
             if restore:
                 big.upload(pos, vel)
             l2_flush.zero_()
-            ev0.record(stream)
-            big.step_async(1)
-            ev1.record(stream)
-            big.synchronize()
-            ms.append(ev0.elapsed_time(ev1))
+            ms.append(timed_step([big]))
         return ms
 
     def time_serial(steps, restore):
@@ -732,13 +774,7 @@ def run_batched(args, dev, stream, l2_flush):
                 for s, pp, vv in zip(small, parts_p, parts_v):
                     s.upload(pp, vv)
             l2_flush.zero_()
-            ev0.record(stream)
-            for s in small:
-                s.step_async(1)
-            ev1.record(stream)
-            for s in small:
-                s.synchronize()
-            ms.append(ev0.elapsed_time(ev1))
+            ms.append(timed_step(small))
         return ms
 
     time_batched(args.warmup, True)
