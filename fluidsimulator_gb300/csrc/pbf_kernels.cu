@@ -892,6 +892,16 @@ __global__ void __launch_bounds__(kMaxBlock, 1) k_nbr_overflow(StepArgs a) {
 // ---------------------------------------------------------------------------
 // Jacobi passes over the lists.
 
+// Rows ahead of its current position at which a walk over a long list asks
+// the L2 for the list (one prefetch per row, on the lane's own entry; the
+// warp's 32 entries of a row share one 128-byte line). The walk's own index
+// loads run one group of entries ahead, which is enough for the lattice's
+// ~28-entry lists but leaves a collapsed state's thousands of rows per warp
+// streaming from DRAM one group at a time.
+constexpr int kListAhead = 32;
+
+__device__ __forceinline__ void prefetch_row(const int* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
 // Walks this lane's list entries k = 0..n-1 in order. kUnroll records are
 // fetched before any is used, and the next kUnroll list indices are fetched
 // while the current records are processed, so every warp keeps several
@@ -914,6 +924,10 @@ __device__ __forceinline__ void for_each_neighbor(const int* __restrict__ list, 
     if (k + 2 * kUnroll <= n) {
 #pragma unroll
       for (int u = 0; u < kUnroll; ++u) j[u] = __ldcs(list + 32ll * (k + kUnroll + u));
+    }
+    if (k + kListAhead + kUnroll <= n) {
+#pragma unroll
+      for (int u = 0; u < kUnroll; ++u) prefetch_row(list + 32ll * (k + kListAhead + u));
     }
 #pragma unroll
     for (int u = 0; u < kUnroll; ++u) body(r[u]);
@@ -941,6 +955,10 @@ __device__ __forceinline__ void for_each_neighbor_pair(const int* __restrict__ l
     if (k + 2 * kUnroll <= n) {
 #pragma unroll
       for (int u = 0; u < kUnroll; ++u) j[u] = __ldcs(list + 32ll * (k + kUnroll + u));
+    }
+    if (k + kListAhead + kUnroll <= n) {
+#pragma unroll
+      for (int u = 0; u < kUnroll; ++u) prefetch_row(list + 32ll * (k + kListAhead + u));
     }
 #pragma unroll
     for (int u = 0; u < kUnroll; u += 2) body2(r[u], r[u + 1]);
@@ -1560,6 +1578,7 @@ __device__ __forceinline__ unsigned long long walk_lanes(const int* __restrict__
   Rec cur = (k < n) ? load(__ldcs(list + 32ll * k)) : Rec{};
   for (int r = 0; r < rounds; ++r, k += G) {
     const int j2 = (k + 2 * G < n) ? __ldcs(list + 32ll * (k + 2 * G)) : 0;
+    if (k + kListAhead < n) prefetch_row(list + 32ll * (k + kListAhead));
     const Rec nxt = (k + G < n) ? load(j1) : Rec{};
     const Terms<K> t = term(cur, k < n);
     const unsigned lb = (__ballot_sync(kFull, t.live) >> L.lead) & ((1u << G) - 1u);
