@@ -15,10 +15,14 @@
 //   keys/vals     radix-sort ping-pong (u32 cell key, int caller index).
 //   table         int2 (first, end) per cell of the per-scene bounding grids.
 //   cnt, nbr      neighbour lists in 32-wide slices: warp w (slots 32w..32w+31)
-//                 owns 32*depth[w] ints from wbase[w] (claimed by one atomic
-//                 per block), entry k of lane l at
-//                 wbase[w] + 32k + l, so every list read is one coalesced
-//                 128-byte access per warp.
+//                 owns depth[w] rows from wbase[w] (claimed by one atomic per
+//                 block), entry k of lane l in row k, column l, so every
+//                 list read is one coalesced access per warp. A row is 32
+//                 ints, or 32 16-bit offsets from the warp's anchor (32w -
+//                 32768) when slice_fmt[w] has kSlice16: the warps whose
+//                 lists fit the shared-memory staging and whose entries all
+//                 lie within 32768 slots of that anchor (the lattice phase;
+//                 half the bytes for every pass to read).
 #pragma once
 
 #include <cstdint>
@@ -114,7 +118,7 @@ struct StepArgs {
   int* cnt;
   int* depth;             // per warp
   long long* wbase;       // per warp
-  int* ovf;               // per warp: list longer than the shared-memory staging
+  int* slice_fmt;         // per warp: slice format, kSliceOverflow | kSlice16 bits
   int* nbr;
   int* bmin;              // 3 per scene
   int* bmax;
@@ -127,6 +131,12 @@ struct StepArgs {
   int warps;              // ceil(n / 32)
   long long grid_capacity;
   long long nbr_capacity;
+  int list16;             // 1: the list build may store 16-bit slices (0 for steps recorded for the adjoint)
 };
+
+// Slice format bits (StepArgs::slice_fmt, per warp).
+constexpr int kSliceOverflow = 1;  // longer than the staging: k_nbr_overflow wrote the entries past it
+constexpr int kSlice16 = 2;        // 16-bit offsets from the warp's anchor
+constexpr int kSliceAnchorBack = 32768;  // anchor of warp w: 32 w - 32768
 
 }  // namespace fgb

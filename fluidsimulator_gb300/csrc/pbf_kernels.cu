@@ -795,7 +795,8 @@ __device__ __forceinline__ void for_each_pair_candidate(const StepArgs& a, const
 // store. The block then claims its warps' 32-wide
 // slices with one atomic on the list cursor (placement varies run to run,
 // every list's content and order do not) and writes the staged entries out
-// as coalesced 128-byte rows. Warps with a longer list set ovf[w] and
+// as coalesced 128-byte rows. Warps with a longer list set kSliceOverflow in
+// slice_fmt[w] and
 // k_nbr_overflow writes their remaining entries.
 __global__ void __launch_bounds__(kMaxBuildBlock) k_nbr_build(StepArgs a) {
   extern __shared__ int stage[];
@@ -830,12 +831,23 @@ __global__ void __launch_bounds__(kMaxBuildBlock) k_nbr_build(StepArgs a) {
   }
   const int mx = __reduce_max_sync(kFull, count);
   const unsigned sum = __reduce_add_sync(kFull, static_cast<unsigned>(count));
-  __shared__ int wdepth[kMaxBuildBlock / 32];
+  // A warp whose lists are all staged and whose entries all lie within
+  // 32768 slots of its anchor writes 16-bit offsets (half the bytes for
+  // every list pass to read; the whole 1M lattice qualifies). Its slice is
+  // rounded up to whole 128-byte lines.
+  const int anchor = (i - lane) - kSliceAnchorBack;
+  bool near = true;
+  if (a.list16 && mx <= kStage) {
+    for (int k = 0; k < count; ++k) near = near && static_cast<unsigned>(mine[32 * k] - anchor) <= 0xffffu;
+  }
+  const bool slim = __all_sync(kFull, near) && a.list16 && mx <= kStage;
+  const int ints = slim ? 32 * ((mx + 1) / 2) : 32 * mx;  // the warp's slice
+  __shared__ int wints[kMaxBuildBlock / 32];
   __shared__ unsigned long long block_base;
   __shared__ int block_ok;
   const bool warp_live = (i - lane) < a.n;
   if (lane == 0) {
-    wdepth[warp] = warp_live ? mx : 0;
+    wints[warp] = warp_live ? ints : 0;
     if (warp_live) {
       if (sum) atomicAdd(&a.status->pairs, static_cast<unsigned long long>(sum));
       if (mx) atomicMax(&a.status->nbr_max, mx);
@@ -844,7 +856,7 @@ __global__ void __launch_bounds__(kMaxBuildBlock) k_nbr_build(StepArgs a) {
   __syncthreads();
   if (threadIdx.x == 0) {
     unsigned long long total = 0;
-    for (int w = 0; w < static_cast<int>(blockDim.x / 32); ++w) total += 32ull * wdepth[w];
+    for (int w = 0; w < static_cast<int>(blockDim.x / 32); ++w) total += static_cast<unsigned long long>(wints[w]);
     const unsigned long long base = atomicAdd(&a.status->cursor, total);
     block_ok = base + total <= static_cast<unsigned long long>(a.nbr_capacity);
     if (!block_ok) set_error(a.status, FLUID_ERR_CAPACITY);
@@ -853,15 +865,21 @@ __global__ void __launch_bounds__(kMaxBuildBlock) k_nbr_build(StepArgs a) {
   __syncthreads();
   if (!warp_live || !block_ok) return;
   unsigned long long off = block_base;
-  for (int w = 0; w < warp; ++w) off += 32ull * wdepth[w];
-  int* out = a.nbr + off + lane;
-  const int staged = mx < kStage ? mx : kStage;
-  for (int k = 0; k < staged; ++k)
-    if (k < count) out[32ll * k] = mine[32 * k];
+  for (int w = 0; w < warp; ++w) off += static_cast<unsigned long long>(wints[w]);
+  if (slim) {
+    unsigned short* out = reinterpret_cast<unsigned short*>(a.nbr + off) + lane;
+    for (int k = 0; k < mx; ++k)
+      if (k < count) out[32 * k] = static_cast<unsigned short>(mine[32 * k] - anchor);
+  } else {
+    int* out = a.nbr + off + lane;
+    const int staged = mx < kStage ? mx : kStage;
+    for (int k = 0; k < staged; ++k)
+      if (k < count) out[32ll * k] = mine[32 * k];
+  }
   if (lane == 0) {
     a.wbase[i >> 5] = static_cast<long long>(off);
     a.depth[i >> 5] = mx;
-    a.ovf[i >> 5] = mx > kStage ? 1 : 0;
+    a.slice_fmt[i >> 5] = (mx > kStage ? kSliceOverflow : 0) | (slim ? kSlice16 : 0);
   }
 }
 
@@ -869,7 +887,7 @@ __global__ void __launch_bounds__(kMaxBuildBlock) k_nbr_build(StepArgs a) {
 __global__ void __launch_bounds__(kMaxBlock, 1) k_nbr_overflow(StepArgs a) {
   if (failed(a.status)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n || !a.ovf[i >> 5]) return;
+  if (i >= a.n || !(a.slice_fmt[i >> 5] & kSliceOverflow)) return;
   const uint32_t* ks = sorted_keys(a, a.status->npass);
   const float4 p = a.p[0][i];
   const int scene = __float_as_int(p.w);
@@ -900,7 +918,55 @@ __global__ void __launch_bounds__(kMaxBlock, 1) k_nbr_overflow(StepArgs a) {
 // streaming from DRAM one group at a time.
 constexpr int kListAhead = 32;
 
-__device__ __forceinline__ void prefetch_row(const int* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+__device__ __forceinline__ void prefetch_row(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
+// A lane's list in its warp's slice, in either row format: entry(k) is list
+// entry k (streamed with the evict-first hint: each pass reads a row once),
+// row(k) its address, from(k0) the list from entry k0 on.
+struct List32 {
+  const int* __restrict__ p;  // the lane's entry in row 0
+  __device__ __forceinline__ int entry(long long k) const { return __ldcs(p + 32 * k); }
+  __device__ __forceinline__ const void* row(long long k) const { return p + 32 * k; }
+  __device__ __forceinline__ List32 from(int k0) const { return {p + 32ll * k0}; }
+};
+struct List16 {
+  const unsigned short* __restrict__ p;
+  int anchor;  // 32 w - kSliceAnchorBack
+  __device__ __forceinline__ int entry(long long k) const { return anchor + static_cast<int>(__ldcs(p + 32 * k)); }
+  __device__ __forceinline__ const void* row(long long k) const { return p + 32 * k; }
+  __device__ __forceinline__ List16 from(int k0) const { return {p + 32ll * k0, anchor}; }
+};
+
+// Calls f(list) with lane i's list in the format of its warp's slice (the
+// same for every lane of a warp, so the branch does not split warps).
+template <typename F>
+__device__ __forceinline__ void with_list(const StepArgs& a, int i, F&& f) {
+  const int w = i >> 5;
+  const long long base = a.wbase[w];
+  if (a.slice_fmt[w] & kSlice16) {
+    f(List16{reinterpret_cast<const unsigned short*>(a.nbr + base) + (i & 31), (i & ~31) - kSliceAnchorBack});
+  } else {
+    f(List32{a.nbr + base + (i & 31)});
+  }
+}
+
+// with_list for the kernels with several lanes per particle, called by every
+// lane of the warp (their walk shuffles over the whole warp, so the branch
+// must not split it): the format is that of the warp's first particle, and
+// the warp's particles, consecutive and at most 32, all lie in that
+// particle's slice. A lane past the last particle gets an empty list.
+template <typename F>
+__device__ __forceinline__ void with_list_lanes(const StepArgs& a, int i, bool valid, F&& f) {
+  const int i0 = __shfl_sync(kFull, i, 0);
+  const int fmt = i0 < a.n ? a.slice_fmt[i0 >> 5] : 0;
+  const long long base = valid ? a.wbase[i >> 5] : 0;
+  if (fmt & kSlice16) {
+    f(List16{reinterpret_cast<const unsigned short*>(a.nbr + base) + (valid ? (i & 31) : 0),
+             (i & ~31) - kSliceAnchorBack});
+  } else {
+    f(List32{a.nbr + base + (valid ? (i & 31) : 0)});
+  }
+}
 
 // Walks this lane's list entries k = 0..n-1 in order. kUnroll records are
 // fetched before any is used, and the next kUnroll list indices are fetched
@@ -908,14 +974,14 @@ __device__ __forceinline__ void prefetch_row(const int* p) { asm volatile("prefe
 // independent gathers in flight and the index latency stays hidden; the body
 // still sees the entries in list order, so sums accumulate in the
 // reference's order.
-template <int kUnroll, typename Load, typename Body>
-__device__ __forceinline__ void for_each_neighbor(const int* __restrict__ list, int n, Load&& load, Body&& body) {
+template <int kUnroll, typename L, typename Load, typename Body>
+__device__ __forceinline__ void for_each_neighbor(const L& list, int n, Load&& load, Body&& body) {
   using Rec = decltype(load(0));
   int k = 0;
   int j[kUnroll];
   if (kUnroll <= n) {
 #pragma unroll
-    for (int u = 0; u < kUnroll; ++u) j[u] = __ldcs(list + 32ll * u);
+    for (int u = 0; u < kUnroll; ++u) j[u] = list.entry(u);
   }
   for (; k + kUnroll <= n; k += kUnroll) {
     Rec r[kUnroll];
@@ -923,22 +989,22 @@ __device__ __forceinline__ void for_each_neighbor(const int* __restrict__ list, 
     for (int u = 0; u < kUnroll; ++u) r[u] = load(j[u]);
     if (k + 2 * kUnroll <= n) {
 #pragma unroll
-      for (int u = 0; u < kUnroll; ++u) j[u] = __ldcs(list + 32ll * (k + kUnroll + u));
+      for (int u = 0; u < kUnroll; ++u) j[u] = list.entry(k + kUnroll + u);
     }
     if (k + kListAhead + kUnroll <= n) {
 #pragma unroll
-      for (int u = 0; u < kUnroll; ++u) prefetch_row(list + 32ll * (k + kListAhead + u));
+      for (int u = 0; u < kUnroll; ++u) prefetch_row(list.row(k + kListAhead + u));
     }
 #pragma unroll
     for (int u = 0; u < kUnroll; ++u) body(r[u]);
   }
-  for (; k < n; ++k) body(load(__ldcs(list + 32ll * k)));
+  for (; k < n; ++k) body(load(list.entry(k)));
 }
 
 // for_each_neighbor for bodies that take two consecutive entries at once
 // (a then b, in list order); an odd last entry goes to body1. kUnroll >= 2.
-template <int kUnroll, typename Load, typename Body2, typename Body1>
-__device__ __forceinline__ void for_each_neighbor_pair(const int* __restrict__ list, int n, Load&& load, Body2&& body2,
+template <int kUnroll, typename L, typename Load, typename Body2, typename Body1>
+__device__ __forceinline__ void for_each_neighbor_pair(const L& list, int n, Load&& load, Body2&& body2,
                                                        Body1&& body1) {
   static_assert(kUnroll % 2 == 0, "entries are consumed in pairs");
   using Rec = decltype(load(0));
@@ -946,7 +1012,7 @@ __device__ __forceinline__ void for_each_neighbor_pair(const int* __restrict__ l
   int j[kUnroll];
   if (kUnroll <= n) {
 #pragma unroll
-    for (int u = 0; u < kUnroll; ++u) j[u] = __ldcs(list + 32ll * u);
+    for (int u = 0; u < kUnroll; ++u) j[u] = list.entry(u);
   }
   for (; k + kUnroll <= n; k += kUnroll) {
     Rec r[kUnroll];
@@ -954,20 +1020,20 @@ __device__ __forceinline__ void for_each_neighbor_pair(const int* __restrict__ l
     for (int u = 0; u < kUnroll; ++u) r[u] = load(j[u]);
     if (k + 2 * kUnroll <= n) {
 #pragma unroll
-      for (int u = 0; u < kUnroll; ++u) j[u] = __ldcs(list + 32ll * (k + kUnroll + u));
+      for (int u = 0; u < kUnroll; ++u) j[u] = list.entry(k + kUnroll + u);
     }
     if (k + kListAhead + kUnroll <= n) {
 #pragma unroll
-      for (int u = 0; u < kUnroll; ++u) prefetch_row(list + 32ll * (k + kListAhead + u));
+      for (int u = 0; u < kUnroll; ++u) prefetch_row(list.row(k + kListAhead + u));
     }
 #pragma unroll
     for (int u = 0; u < kUnroll; u += 2) body2(r[u], r[u + 1]);
   }
   for (; k + 2 <= n; k += 2) {
-    const Rec ra = load(__ldcs(list + 32ll * k)), rb = load(__ldcs(list + 32ll * (k + 1)));
+    const Rec ra = load(list.entry(k)), rb = load(list.entry(k + 1));
     body2(ra, rb);
   }
-  if (k < n) body1(load(__ldcs(list + 32ll * k)));
+  if (k < n) body1(load(list.entry(k)));
 }
 
 struct PosVel {
@@ -991,10 +1057,9 @@ __device__ __forceinline__ void store_live(uint32_t* live, int n, int i, unsigne
 // (body2: bit 0 for a, bit 1 for b; body1: a bool); returns the live bits of
 // the first kLiveEntries entries. Entries past those go through the plain
 // walker.
-template <int kUnroll, typename Load, typename Body2, typename Body1>
-__device__ __forceinline__ unsigned long long for_each_neighbor_pair_rec(const int* __restrict__ list, int n,
-                                                                         Load&& load, Body2&& body2,
-                                                                         Body1&& body1) {
+template <int kUnroll, typename L, typename Load, typename Body2, typename Body1>
+__device__ __forceinline__ unsigned long long for_each_neighbor_pair_rec(const L& list, int n, Load&& load,
+                                                                         Body2&& body2, Body1&& body1) {
   static_assert(kUnroll % 2 == 0 && kLiveEntries % kUnroll == 0, "entries are consumed in pairs");
   using Rec = decltype(load(0));
   const int head = n < kLiveEntries ? n : kLiveEntries;
@@ -1003,7 +1068,7 @@ __device__ __forceinline__ unsigned long long for_each_neighbor_pair_rec(const i
   int j[kUnroll];
   if (kUnroll <= head) {
 #pragma unroll
-    for (int u = 0; u < kUnroll; ++u) j[u] = __ldcs(list + 32ll * u);
+    for (int u = 0; u < kUnroll; ++u) j[u] = list.entry(u);
   }
   for (; k + kUnroll <= head; k += kUnroll) {
     Rec r[kUnroll];
@@ -1011,7 +1076,7 @@ __device__ __forceinline__ unsigned long long for_each_neighbor_pair_rec(const i
     for (int u = 0; u < kUnroll; ++u) r[u] = load(j[u]);
     if (k + 2 * kUnroll <= head) {
 #pragma unroll
-      for (int u = 0; u < kUnroll; ++u) j[u] = __ldcs(list + 32ll * (k + kUnroll + u));
+      for (int u = 0; u < kUnroll; ++u) j[u] = list.entry(k + kUnroll + u);
     }
     unsigned long long got = 0ull;
 #pragma unroll
@@ -1019,11 +1084,11 @@ __device__ __forceinline__ unsigned long long for_each_neighbor_pair_rec(const i
     bits |= got << k;
   }
   for (; k + 2 <= head; k += 2) {
-    const Rec ra = load(__ldcs(list + 32ll * k)), rb = load(__ldcs(list + 32ll * (k + 1)));
+    const Rec ra = load(list.entry(k)), rb = load(list.entry(k + 1));
     bits |= static_cast<unsigned long long>(body2(ra, rb)) << k;
   }
-  if (k < head && body1(load(__ldcs(list + 32ll * k)))) bits |= 1ull << k;
-  if (n > kLiveEntries) for_each_neighbor_pair<kUnroll>(list + 32ll * kLiveEntries, n - kLiveEntries, load, body2, body1);
+  if (k < head && body1(load(list.entry(k)))) bits |= 1ull << k;
+  if (n > kLiveEntries) for_each_neighbor_pair<kUnroll>(list.from(kLiveEntries), n - kLiveEntries, load, body2, body1);
   return bits;
 }
 
@@ -1033,9 +1098,9 @@ __device__ __forceinline__ unsigned long long for_each_neighbor_pair_rec(const i
 // within h of, which the body rejects exactly as it would the real one
 // (r2 < h2 fails). The remaining entries go through for_each_neighbor_pair.
 // Sums accumulate in list order either way.
-template <int kUnroll, typename Load, typename Rec, typename Body2, typename Body1>
-__device__ __forceinline__ void for_each_live_then(const int* __restrict__ list, int n, unsigned long long bits,
-                                                   Load&& load, const Rec dead, Body2&& body2, Body1&& body1) {
+template <int kUnroll, typename L, typename Load, typename Rec, typename Body2, typename Body1>
+__device__ __forceinline__ void for_each_live_then(const L& list, int n, unsigned long long bits, Load&& load,
+                                                   const Rec dead, Body2&& body2, Body1&& body1) {
   const int head = n < kLiveEntries ? n : kLiveEntries;
   unsigned long long m = head < kLiveEntries ? bits & ((1ull << head) - 1ull) : bits;
   if (m) {
@@ -1043,11 +1108,11 @@ __device__ __forceinline__ void for_each_live_then(const int* __restrict__ list,
     // current one is used.
     int k = __ffsll(static_cast<long long>(m)) - 1;
     m &= m - 1ull;
-    auto r = load(__ldcs(list + 32ll * k));
+    auto r = load(list.entry(k));
     while (m) {
       const int kn = __ffsll(static_cast<long long>(m)) - 1;
       m &= m - 1ull;
-      const auto rn = load(__ldcs(list + 32ll * kn));
+      const auto rn = load(list.entry(kn));
       body1(r);
       r = rn;
     }
@@ -1055,9 +1120,9 @@ __device__ __forceinline__ void for_each_live_then(const int* __restrict__ list,
   }
   if (n > kLiveEntries) {
     if constexpr (kUnroll == 1) {
-      for_each_neighbor<1>(list + 32ll * kLiveEntries, n - kLiveEntries, load, body1);
+      for_each_neighbor<1>(list.from(kLiveEntries), n - kLiveEntries, load, body1);
     } else {
-      for_each_neighbor_pair<kUnroll>(list + 32ll * kLiveEntries, n - kLiveEntries, load, body2, body1);
+      for_each_neighbor_pair<kUnroll>(list.from(kLiveEntries), n - kLiveEntries, load, body2, body1);
     }
   }
 }
@@ -1074,7 +1139,6 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_lambda(StepA
   const float4 p = pos[i];
   const SceneConst& c = a.sc[__float_as_int(p.w)];
   const int n = a.cnt[i];
-  const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
   const float h2 = c.h2;
   LambdaAcc acc;
   auto one = [&](const float4 q) {
@@ -1084,24 +1148,26 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_lambda(StepA
     return r2 < h2;
   };
   auto load = [&](int j) { return __ldg(pos + j); };
-  if constexpr (U == 1) {
-    if constexpr (kLiveOut) {
-      unsigned long long bits = 0ull;
-      int k = 0;
-      for_each_neighbor<1>(list, n, load, [&](const float4 q) {
-        if (one(q) && k < kLiveEntries) bits |= 1ull << k;
-        ++k;
-      });
-      store_live(a.live, a.n, i, bits);
+  with_list(a, i, [&](const auto& list) {
+    if constexpr (U == 1) {
+      if constexpr (kLiveOut) {
+        unsigned long long bits = 0ull;
+        int k = 0;
+        for_each_neighbor<1>(list, n, load, [&](const float4 q) {
+          if (one(q) && k < kLiveEntries) bits |= 1ull << k;
+          ++k;
+        });
+        store_live(a.live, a.n, i, bits);
+      } else {
+        for_each_neighbor<1>(list, n, load, one);
+      }
     } else {
-      for_each_neighbor<1>(list, n, load, one);
+      const float2 px = f2(p.x), py = f2(p.y), pz = f2(p.z);
+      auto two = [&](const float4 qa, const float4 qb) { return acc.add_pair(c, px, py, pz, qa, qb); };
+      if constexpr (kLiveOut) store_live(a.live, a.n, i, for_each_neighbor_pair_rec<U>(list, n, load, two, one));
+      else for_each_neighbor_pair<U>(list, n, load, two, one);
     }
-  } else {
-    const float2 px = f2(p.x), py = f2(p.y), pz = f2(p.z);
-    auto two = [&](const float4 qa, const float4 qb) { return acc.add_pair(c, px, py, pz, qa, qb); };
-    if constexpr (kLiveOut) store_live(a.live, a.n, i, for_each_neighbor_pair_rec<U>(list, n, load, two, one));
-    else for_each_neighbor_pair<U>(list, n, load, two, one);
-  }
+  });
   float rho;
   const float lam = finish_lambda(c, acc.rho, acc.gsx, acc.gsy, acc.gsz, acc.sum_g2, rho);
   a.lambda[i] = lam;
@@ -1177,7 +1243,6 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_delta(StepAr
   const float4 p = a.p[in][i];
   const SceneConst& c = a.sc[__float_as_int(p.w)];
   const int n = a.cnt[i];
-  const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
   const float4* __restrict__ pl = a.pl;  // {p_j, lambda_j} in one record
   const float li = a.lambda[i];
   const float h2 = c.h2;
@@ -1203,51 +1268,53 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_delta(StepAr
       kLiveIn ? (static_cast<unsigned long long>(a.live[i]) | (static_cast<unsigned long long>(a.live[a.n + i]) << 32))
               : 0ull;
   const float4 dead = make_float4(INFINITY, p.y, p.z, 0.0f);
-  if constexpr (U == 1) {
-    if constexpr (kLiveIn) for_each_live_then<1>(list, n, live, load, dead, one, one);
-    else for_each_neighbor<1>(list, n, load, one);
-  } else {
-    // Two entries at a time: the same operations as one() on a, then on b,
-    // with the per-entry terms in paired arithmetic (pmul keeps each
-    // product rounded on its own).
-    const float2 px = f2(p.x), py = f2(p.y), pz = f2(p.z), nz = f2(c.neg_zero);
-    auto two = [&](const float4 qa, const float4 qb) {
-      const PairGeom g = pair_geom(px, py, pz, qa, qb, nz);
-      const bool oka = g.r2.x < h2, okb = g.r2.y < h2;
-      if (!oka && !okb) return;
-      const float2 gf = spiky_pair(c, g.r2, nz);
-      float2 s = padd(f2(li), make_float2(qa.w, qb.w));
-      if (scorr) {
-        const float2 ratio = pmul(poly6_pair(c, g.r2, nz), f2(c.scorr_inv_wdq), nz);
-        float2 pw;
-        if (kPow == 2) {
-          pw = pmul(ratio, ratio, nz);
-        } else if (kPow == 3) {
-          pw = pmul(pmul(ratio, ratio, nz), ratio, nz);
-        } else if (kPow == 4) {
-          const float2 sq = pmul(ratio, ratio, nz);
-          pw = pmul(sq, sq, nz);
-        } else {
-          pw = make_float2(pow_n(ratio.x, c.scorr_n), pow_n(ratio.y, c.scorr_n));
+  with_list(a, i, [&](const auto& list) {
+    if constexpr (U == 1) {
+      if constexpr (kLiveIn) for_each_live_then<1>(list, n, live, load, dead, one, one);
+      else for_each_neighbor<1>(list, n, load, one);
+    } else {
+      // Two entries at a time: the same operations as one() on a, then on b,
+      // with the per-entry terms in paired arithmetic (pmul keeps each
+      // product rounded on its own).
+      const float2 px = f2(p.x), py = f2(p.y), pz = f2(p.z), nz = f2(c.neg_zero);
+      auto two = [&](const float4 qa, const float4 qb) {
+        const PairGeom g = pair_geom(px, py, pz, qa, qb, nz);
+        const bool oka = g.r2.x < h2, okb = g.r2.y < h2;
+        if (!oka && !okb) return;
+        const float2 gf = spiky_pair(c, g.r2, nz);
+        float2 s = padd(f2(li), make_float2(qa.w, qb.w));
+        if (scorr) {
+          const float2 ratio = pmul(poly6_pair(c, g.r2, nz), f2(c.scorr_inv_wdq), nz);
+          float2 pw;
+          if (kPow == 2) {
+            pw = pmul(ratio, ratio, nz);
+          } else if (kPow == 3) {
+            pw = pmul(pmul(ratio, ratio, nz), ratio, nz);
+          } else if (kPow == 4) {
+            const float2 sq = pmul(ratio, ratio, nz);
+            pw = pmul(sq, sq, nz);
+          } else {
+            pw = make_float2(pow_n(ratio.x, c.scorr_n), pow_n(ratio.y, c.scorr_n));
+          }
+          s = padd(s, pmul(f2(c.scorr_neg_k), pw, nz));
         }
-        s = padd(s, pmul(f2(c.scorr_neg_k), pw, nz));
-      }
-      const float2 sg = pmul(s, gf, nz);
-      const float2 tx = pmul(sg, g.dx, nz), ty = pmul(sg, g.dy, nz), tz = pmul(sg, g.dz, nz);
-      if (oka) {
-        ax += tx.x;
-        ay += ty.x;
-        az += tz.x;
-      }
-      if (okb) {
-        ax += tx.y;
-        ay += ty.y;
-        az += tz.y;
-      }
-    };
-    if constexpr (kLiveIn) for_each_live_then<U>(list, n, live, load, dead, two, one);
-    else for_each_neighbor_pair<U>(list, n, load, two, one);
-  }
+        const float2 sg = pmul(s, gf, nz);
+        const float2 tx = pmul(sg, g.dx, nz), ty = pmul(sg, g.dy, nz), tz = pmul(sg, g.dz, nz);
+        if (oka) {
+          ax += tx.x;
+          ay += ty.x;
+          az += tz.x;
+        }
+        if (okb) {
+          ax += tx.y;
+          ay += ty.y;
+          az += tz.y;
+        }
+      };
+      if constexpr (kLiveIn) for_each_live_then<U>(list, n, live, load, dead, two, one);
+      else for_each_neighbor_pair<U>(list, n, load, two, one);
+    }
+  });
   delta_out(a, c, i, p, ax, ay, az, in, last, to_v2, rest, q_out);
 }
 
@@ -1278,8 +1345,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_xsph(StepArg
   unsigned long long bits = ~0ull;
   if (c.xsph_on) {
     const int n = a.cnt[i];
-    const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
-    const float h2 = c.h2;
+      const float h2 = c.h2;
     float sx = 0.0f, sy = 0.0f, sz = 0.0f;
     auto load = [&](int j) { return PosVel{__ldg(xs + j), __ldg(vs + j)}; };
     auto one = [&](const PosVel r) {
@@ -1293,44 +1359,46 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_xsph(StepArg
       }
       return r2 < h2;
     };
-    if constexpr (U == 1) {
-      if constexpr (kLiveOut) {
-        bits = 0ull;
-        int k = 0;
-        for_each_neighbor<1>(list, n, load, [&](const PosVel r) {
-          if (one(r) && k < kLiveEntries) bits |= 1ull << k;
-          ++k;
-        });
+    with_list(a, i, [&](const auto& list) {
+      if constexpr (U == 1) {
+        if constexpr (kLiveOut) {
+          bits = 0ull;
+          int k = 0;
+          for_each_neighbor<1>(list, n, load, [&](const PosVel r) {
+            if (one(r) && k < kLiveEntries) bits |= 1ull << k;
+            ++k;
+          });
+        } else {
+          for_each_neighbor<1>(list, n, load, one);
+        }
       } else {
-        for_each_neighbor<1>(list, n, load, one);
+        // Two entries at a time, as one() on a then on b (paired arithmetic).
+        const float2 px = f2(xi.x), py = f2(xi.y), pz = f2(xi.z), nz = f2(c.neg_zero);
+        auto two = [&](const PosVel ra, const PosVel rb) -> unsigned {
+          const PairGeom g = pair_geom(px, py, pz, ra.x, rb.x, nz);
+          const bool oka = g.r2.x < h2, okb = g.r2.y < h2;
+          if (!oka && !okb) return 0u;
+          const float2 w = poly6_pair(c, g.r2, nz);
+          const float2 ir = make_float2(ra.x.w, rb.x.w);
+          const float2 tx = pmul(pmul(psub(make_float2(ra.v.x, rb.v.x), f2(vi.x)), w, nz), ir, nz);
+          const float2 ty = pmul(pmul(psub(make_float2(ra.v.y, rb.v.y), f2(vi.y)), w, nz), ir, nz);
+          const float2 tz = pmul(pmul(psub(make_float2(ra.v.z, rb.v.z), f2(vi.z)), w, nz), ir, nz);
+          if (oka) {
+            sx += tx.x;
+            sy += ty.x;
+            sz += tz.x;
+          }
+          if (okb) {
+            sx += tx.y;
+            sy += ty.y;
+            sz += tz.y;
+          }
+          return (oka ? 1u : 0u) | (okb ? 2u : 0u);
+        };
+        if constexpr (kLiveOut) bits = for_each_neighbor_pair_rec<U>(list, n, load, two, one);
+        else for_each_neighbor_pair<U>(list, n, load, two, one);
       }
-    } else {
-      // Two entries at a time, as one() on a then on b (paired arithmetic).
-      const float2 px = f2(xi.x), py = f2(xi.y), pz = f2(xi.z), nz = f2(c.neg_zero);
-      auto two = [&](const PosVel ra, const PosVel rb) -> unsigned {
-        const PairGeom g = pair_geom(px, py, pz, ra.x, rb.x, nz);
-        const bool oka = g.r2.x < h2, okb = g.r2.y < h2;
-        if (!oka && !okb) return 0u;
-        const float2 w = poly6_pair(c, g.r2, nz);
-        const float2 ir = make_float2(ra.x.w, rb.x.w);
-        const float2 tx = pmul(pmul(psub(make_float2(ra.v.x, rb.v.x), f2(vi.x)), w, nz), ir, nz);
-        const float2 ty = pmul(pmul(psub(make_float2(ra.v.y, rb.v.y), f2(vi.y)), w, nz), ir, nz);
-        const float2 tz = pmul(pmul(psub(make_float2(ra.v.z, rb.v.z), f2(vi.z)), w, nz), ir, nz);
-        if (oka) {
-          sx += tx.x;
-          sy += ty.x;
-          sz += tz.x;
-        }
-        if (okb) {
-          sx += tx.y;
-          sy += ty.y;
-          sz += tz.y;
-        }
-        return (oka ? 1u : 0u) | (okb ? 2u : 0u);
-      };
-      if constexpr (kLiveOut) bits = for_each_neighbor_pair_rec<U>(list, n, load, two, one);
-      else for_each_neighbor_pair<U>(list, n, load, two, one);
-    }
+    });
     vx += c.visc_c * sx;
     vy += c.visc_c * sy;
     vz += c.visc_c * sz;
@@ -1357,8 +1425,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_omega(StepAr
   unsigned long long bits = ~0ull;
   if (c.vort_on) {
     const int n = a.cnt[i];
-    const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
-    const float h2 = c.h2;
+      const float h2 = c.h2;
     auto load = [&](int j) { return PosVel{__ldg(xs + j), __ldg(vs + j)}; };
     auto one = [&](const PosVel r) {
       const float dx = xi.x - r.x.x, dy = xi.y - r.x.y, dz = xi.z - r.x.z;
@@ -1399,21 +1466,23 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_omega(StepAr
       }
       return (oka ? 1u : 0u) | (okb ? 2u : 0u);
     };
-    if constexpr (kLive == 1) {
-      const PosVel dead{make_float4(INFINITY, xi.y, xi.z, 0.0f), make_float4(0.0f, 0.0f, 0.0f, 0.0f)};
-      for_each_live_then<U>(list, n, static_cast<unsigned long long>(a.live[i]) |
-                                         (static_cast<unsigned long long>(a.live[a.n + i]) << 32),
-                            load, dead, two, one);
-    } else if constexpr (U == 1) {
-      bits = 0ull;
-      int k = 0;
-      for_each_neighbor<1>(list, n, load, [&](const PosVel r) {
-        if (one(r) && k < kLiveEntries) bits |= 1ull << k;
-        ++k;
-      });
-    } else {
-      bits = for_each_neighbor_pair_rec<U>(list, n, load, two, one);
-    }
+    with_list(a, i, [&](const auto& list) {
+      if constexpr (kLive == 1) {
+        const PosVel dead{make_float4(INFINITY, xi.y, xi.z, 0.0f), make_float4(0.0f, 0.0f, 0.0f, 0.0f)};
+        for_each_live_then<U>(list, n, static_cast<unsigned long long>(a.live[i]) |
+                                           (static_cast<unsigned long long>(a.live[a.n + i]) << 32),
+                              load, dead, two, one);
+      } else if constexpr (U == 1) {
+        bits = 0ull;
+        int k = 0;
+        for_each_neighbor<1>(list, n, load, [&](const PosVel r) {
+          if (one(r) && k < kLiveEntries) bits |= 1ull << k;
+          ++k;
+        });
+      } else {
+        bits = for_each_neighbor_pair_rec<U>(list, n, load, two, one);
+      }
+    });
   }
   if (kLive == 2) store_live(a.live, a.n, i, bits);
   const float mag = sqrtf(ox * ox + oy * oy + oz * oz);
@@ -1455,8 +1524,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_eta(StepArgs
   if (c.vort_on) {
     const float4 oi = a.omega[i];
     const int n = a.cnt[i];
-    const int* __restrict__ list = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
-    const float h2 = c.h2;
+      const float h2 = c.h2;
     float ex = 0.0f, ey = 0.0f, ez = 0.0f;
     auto load = [&](int j) { return __ldg(xo + j); };
     auto one = [&](const float4 r) {
@@ -1493,9 +1561,11 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_eta(StepArgs
       }
     };
     const float4 dead = make_float4(INFINITY, xi.y, xi.z, 0.0f);
-    for_each_live_then<U>(list, n, static_cast<unsigned long long>(a.live[i]) |
-                                       (static_cast<unsigned long long>(a.live[a.n + i]) << 32),
-                          load, dead, two, one);
+    with_list(a, i, [&](const auto& list) {
+      for_each_live_then<U>(list, n, static_cast<unsigned long long>(a.live[i]) |
+                                         (static_cast<unsigned long long>(a.live[a.n + i]) << 32),
+                            load, dead, two, one);
+    });
     confine(c, oi, ex, ey, ez, v);
   }
   if (rest && c.rest_on) restitution(c, xi.x, xi.y, xi.z, v.x, v.y, v.z);
@@ -1567,18 +1637,18 @@ struct Terms {
 // add(Terms) accumulates, and each lane of the group adds the round's G terms
 // in list order. Called by every lane of the warp. Returns the live bits of
 // entries 0..63 (the same on every lane of the group).
-template <int G, int K, typename Load, typename Term, typename Add>
-__device__ __forceinline__ unsigned long long walk_lanes(const int* __restrict__ list, int n, const LaneGroup<G>& L,
+template <int G, int K, typename LS, typename Load, typename Term, typename Add>
+__device__ __forceinline__ unsigned long long walk_lanes(const LS& list, int n, const LaneGroup<G>& L,
                                                          Load&& load, Term&& term, Add&& add) {
   using Rec = decltype(load(0));
   unsigned long long bits = 0ull;
   const int rounds = __reduce_max_sync(kFull, (n + G - 1) / G);
   int k = L.sub;
-  int j1 = (k + G < n) ? __ldcs(list + 32ll * (k + G)) : 0;
-  Rec cur = (k < n) ? load(__ldcs(list + 32ll * k)) : Rec{};
+  int j1 = (k + G < n) ? list.entry(k + G) : 0;
+  Rec cur = (k < n) ? load(list.entry(k)) : Rec{};
   for (int r = 0; r < rounds; ++r, k += G) {
-    const int j2 = (k + 2 * G < n) ? __ldcs(list + 32ll * (k + 2 * G)) : 0;
-    if (k + kListAhead < n) prefetch_row(list + 32ll * (k + kListAhead));
+    const int j2 = (k + 2 * G < n) ? list.entry(k + 2 * G) : 0;
+    if (k + kListAhead < n) prefetch_row(list.row(k + kListAhead));
     const Rec nxt = (k + G < n) ? load(j1) : Rec{};
     const Terms<K> t = term(cur, k < n);
     const unsigned lb = (__ballot_sync(kFull, t.live) >> L.lead) & ((1u << G) - 1u);
@@ -1607,7 +1677,6 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_lambda_lanes
   const float h2 = c.h2;
   LambdaAcc acc;
   const int n = valid ? a.cnt[i] : 0;
-  const int* __restrict__ list = a.nbr + (valid ? a.wbase[i >> 5] + (i & 31) : 0);
   auto load = [&](int j) { return __ldg(pos + j); };
   auto term = [&](const float4 q, bool in_list) {  // LambdaAcc::add, term by term
     Terms<5> t;
@@ -1635,7 +1704,8 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_lambda_lanes
     acc.gsz += t.f[3];
     acc.sum_g2 += t.f[4];
   };
-  const unsigned long long bits = walk_lanes<G, 5>(list, n, L, load, term, add);
+  unsigned long long bits = 0ull;
+  with_list_lanes(a, i, valid, [&](const auto& list) { bits = walk_lanes<G, 5>(list, n, L, load, term, add); });
   if (!valid || L.sub != 0) return;
   if constexpr (kLiveOut) store_live(a.live, a.n, i, bits);
   float rho;
@@ -1660,7 +1730,6 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS)
   float ax = 0.0f, ay = 0.0f, az = 0.0f;
   const bool scorr = c.scorr_on != 0;
   const int n = valid ? a.cnt[i] : 0;
-  const int* __restrict__ list = a.nbr + (valid ? a.wbase[i >> 5] + (i & 31) : 0);
   auto load = [&](int j) { return __ldg(pl + j); };
   auto term = [&](const float4 r, bool in_list) {  // k_delta's one(), term by term
     Terms<3> t;
@@ -1687,7 +1756,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS)
     ay += t.f[1];
     az += t.f[2];
   };
-  walk_lanes<G, 3>(list, n, L, load, term, add);
+  with_list_lanes(a, i, valid, [&](const auto& list) { walk_lanes<G, 3>(list, n, L, load, term, add); });
   if (!valid || L.sub != 0) return;
   delta_out(a, c, i, p, ax, ay, az, in, last, to_v2, rest, q_out);
 }
@@ -1707,7 +1776,6 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_xsph_lanes(S
   float vx = vi.x, vy = vi.y, vz = vi.z;
   const bool walk = valid && c.xsph_on;
   const int n = walk ? a.cnt[i] : 0;
-  const int* __restrict__ list = a.nbr + (valid ? a.wbase[i >> 5] + (i & 31) : 0);
   const float h2 = c.h2;
   float sx = 0.0f, sy = 0.0f, sz = 0.0f;
   auto load = [&](int j) { return PosVel{__ldg(xs + j), __ldg(vs + j)}; };
@@ -1731,7 +1799,8 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_xsph_lanes(S
     sy += t.f[1];
     sz += t.f[2];
   };
-  unsigned long long bits = walk_lanes<G, 3>(list, n, L, load, term, add);
+  unsigned long long bits = 0ull;
+  with_list_lanes(a, i, valid, [&](const auto& list) { bits = walk_lanes<G, 3>(list, n, L, load, term, add); });
   if (!valid || L.sub != 0) return;
   if (c.xsph_on) {
     vx += c.visc_c * sx;
@@ -1759,7 +1828,6 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_omega_lanes(
   const SceneConst& c = a.sc[valid ? __float_as_int(vi.w) : 0];
   float ox = 0.0f, oy = 0.0f, oz = 0.0f;
   const int n = (valid && c.vort_on) ? a.cnt[i] : 0;
-  const int* __restrict__ list = a.nbr + (valid ? a.wbase[i >> 5] + (i & 31) : 0);
   const float h2 = c.h2;
   auto load = [&](int j) { return PosVel{__ldg(xs + j), __ldg(vs + j)}; };
   auto term = [&](const PosVel r, bool in_list) {  // k_omega's one(), term by term
@@ -1784,7 +1852,8 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_omega_lanes(
     oy += t.f[1];
     oz += t.f[2];
   };
-  unsigned long long bits = walk_lanes<G, 3>(list, n, L, load, term, add);
+  unsigned long long bits = 0ull;
+  with_list_lanes(a, i, valid, [&](const auto& list) { bits = walk_lanes<G, 3>(list, n, L, load, term, add); });
   if (!valid || L.sub != 0) return;
   if (!c.vort_on) bits = ~0ull;
   if (kLive == 2) store_live(a.live, a.n, i, bits);
@@ -1805,7 +1874,6 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_eta_lanes(St
   const SceneConst& c = a.sc[valid ? __float_as_int(v.w) : 0];
   const float4 oi = (valid && c.vort_on) ? a.omega[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   const int n = (valid && c.vort_on) ? a.cnt[i] : 0;
-  const int* __restrict__ list = a.nbr + (valid ? a.wbase[i >> 5] + (i & 31) : 0);
   const float h2 = c.h2;
   float ex = 0.0f, ey = 0.0f, ez = 0.0f;
   auto load = [&](int j) { return __ldg(xo + j); };
@@ -1830,7 +1898,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_eta_lanes(St
     ey += t.f[1];
     ez += t.f[2];
   };
-  walk_lanes<G, 3>(list, n, L, load, term, add);
+  with_list_lanes(a, i, valid, [&](const auto& list) { walk_lanes<G, 3>(list, n, L, load, term, add); });
   if (!valid || L.sub != 0) return;
   if (c.vort_on) confine(c, oi, ex, ey, ez, v);
   if (rest && c.rest_on) restitution(c, xi.x, xi.y, xi.z, v.x, v.y, v.z);
@@ -2099,8 +2167,10 @@ void LaunchMarks::mark(int stage) {
   ++next;
 }
 
-cudaError_t enqueue_step(const StepArgs& a, const StepPlan& plan, cudaStream_t st, LaunchMarks& m,
+cudaError_t enqueue_step(const StepArgs& args, const StepPlan& plan, cudaStream_t st, LaunchMarks& m,
                          const StepRecord* rec, const StepDownload* dl) {
+  StepArgs a = args;
+  if (rec) a.list16 = 0;  // the adjoint reads the recorded lists as 32-bit rows
   const int nb = blocks_for(a.n, kBlock);
   m.start();
   if (!(dl && dl->bounds_done)) {

@@ -123,7 +123,8 @@ StepArgs carve(unsigned char* b, int n) {
   a.cnt = at<int>(b, kCnt);
   a.depth = at<int>(b, kDepth);
   a.wbase = at<long long>(b, kWbase);
-  a.ovf = at<int>(b, kOvf);
+  a.slice_fmt = at<int>(b, kOvf);
+  a.list16 = 1;
   a.nbr = at<int>(b, kNbr);
   a.bmin = at<int>(b, kBmin);
   a.bmax = at<int>(b, kBmax);

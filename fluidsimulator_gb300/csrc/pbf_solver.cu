@@ -1092,7 +1092,8 @@ class Solver {
     a.table = table_.p;
     a.cnt = cnt_.p;
     a.depth = depth_.p;
-    a.ovf = ovf_.p;
+    a.slice_fmt = ovf_.p;
+    a.list16 = 1;
     a.wbase = wbase_.p;
     a.nbr = nbr_.p;
     a.bmin = bmin_.p;
