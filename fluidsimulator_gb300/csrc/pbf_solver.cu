@@ -260,6 +260,8 @@ class Solver {
     times_.assign(scenes, 0.0f);
     steps_ = 0;
     regrows_ = 0;
+    grows_ahead_ = 0;
+    last_list_ints_ = 0;
     parity_ = 0;
     pending_ = 0;
     uploaded_ = false;
@@ -383,6 +385,7 @@ class Solver {
       if (wait && cudaStreamSynchronize(stream_) != cudaSuccess) return cuda_fail("upload");
     }
     uploaded_ = true;
+    last_list_ints_ = 0;  // a new state: its lists' growth starts over
     return FLUID_OK;
   }
 
@@ -510,7 +513,7 @@ class Solver {
       last_cells_ = static_cast<int>(st.total_cells);
       last_npass_ = st.npass;
       if (enqueue_reset(status_.p, bmin_.p, bmax_.p, S_, stream_) != cudaSuccess) return cuda_fail("reset");
-      if (!st.err) return FLUID_OK;
+      if (!st.err) return grow_ahead(st.cursor);
       if (st.err != FLUID_ERR_CAPACITY) {
         cudaStreamSynchronize(stream_);
         return fail(st.err, st.err == FLUID_ERR_NONFINITE ? "non-finite predicted position"
@@ -1215,6 +1218,40 @@ class Solver {
     }
   }
 
+  // Grows the list capacity before a step needs it. After a step that
+  // succeeded, nothing is in flight: if this step's lists, times their
+  // growth over the previous step's (1-4x) and a quarter more, would not fit,
+  // the buffer is reallocated now, to at least twice its size. A neighbourhood that grows step after step
+  // (a collapse) then rarely fails a step, whose re-run after a regrow costs
+  // as much as the step itself. An allocation that fails here keeps the old
+  // capacity; the step that outgrows it regrows as before.
+  int grow_ahead(unsigned long long used) {
+    const unsigned long long prev = last_list_ints_;
+    last_list_ints_ = used;
+    if (prev == 0 || used == 0) return FLUID_OK;
+    const double ratio = std::min(4.0, std::max(1.0, double(used) / double(prev)));
+    const double want = double(used) * ratio * 1.25;
+    if (want <= double(nbr_cap_)) return FLUID_OK;
+    const long long old = nbr_cap_;
+    // At least double: a reallocation of several GB costs tens of ms, so the
+    // capacity grows geometrically rather than to each step's projection.
+    const long long cap = round_up(std::max(static_cast<long long>(std::ceil(want)), 2 * old), 32);
+    nbr_.release();
+    if (nbr_.alloc(static_cast<size_t>(cap)) != cudaSuccess) {
+      cudaGetLastError();  // the failed allocation is not an error of the solver
+      if (nbr_.alloc(static_cast<size_t>(old)) != cudaSuccess) {
+        nbr_cap_ = 0;
+        return fail(FLUID_ERR_OUT_OF_MEMORY, "neighbour lists of " + std::to_string(old) + " entries");
+      }
+      return FLUID_OK;
+    }
+    nbr_cap_ = cap;
+    ++grows_ahead_;
+    make_plan();
+    invalidate_graphs();
+    return FLUID_OK;
+  }
+
   int grow(unsigned long long need_grid, unsigned long long need_nbr) {
     cudaStreamSynchronize(stream_);
     float f = 1.5f;
@@ -1439,6 +1476,8 @@ class Solver {
   bool uploaded_ = false;
   int parity_ = 0, pending_ = 0;
   long long steps_ = 0, regrows_ = 0, launches_ = 0, launches_per_step_ = 0;
+  long long grows_ahead_ = 0;              // list reallocations before a step needed them
+  unsigned long long last_list_ints_ = 0;  // list ints the last completed step claimed
   long long last_pairs_ = 0;
   int last_max_ = 0, last_cells_ = 0, last_npass_ = 0;
   DBuf<float4> x_[2], v_[2], p_[2], v2_, omega_, pl_;
