@@ -50,12 +50,25 @@ __device__ __forceinline__ float plane_sd(const float4 pl, float x, float y, flo
   return __fsub_rn(__fadd_rn(__fadd_rn(__fmul_rn(pl.x, x), __fmul_rn(pl.y, y)), __fmul_rn(pl.z, z)), pl.w);
 }
 
+// Rows ahead at which a walk over a long recorded list asks the L2 for the
+// list (one prefetch per row, on the lane's own entry; nothing for lists
+// shorter than that), as the forward's list walkers do.
+constexpr int kListAhead = 32;
+
+__device__ __forceinline__ void prefetch_row(const int* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
+// The recorded lists are 32-bit rows (the forward keeps them so on a step it
+// records for the adjoint).
 template <typename Body>
 __device__ __forceinline__ void for_list(const StepArgs& s, int i, Body&& body) {
   const int n = s.cnt[i];
   const int* __restrict__ list = s.nbr + s.wbase[i >> 5] + (i & 31);
   int k = 0;
   for (; k + 4 <= n; k += 4) {
+    if (k + kListAhead + 4 <= n) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) prefetch_row(list + 32ll * (k + kListAhead + u));
+    }
     const int j0 = __ldcs(list + 32ll * k), j1 = __ldcs(list + 32ll * (k + 1));
     const int j2 = __ldcs(list + 32ll * (k + 2)), j3 = __ldcs(list + 32ll * (k + 3));
     body(j0);
@@ -87,6 +100,10 @@ __device__ __forceinline__ void for_list_rec(const StepArgs& s, int i, Load&& lo
     if (k + 2 * kAhead <= n) {
 #pragma unroll
       for (int u = 0; u < kAhead; ++u) j[u] = __ldcs(list + 32ll * (k + kAhead + u));
+    }
+    if (k + kListAhead + kAhead <= n) {
+#pragma unroll
+      for (int u = 0; u < kAhead; ++u) prefetch_row(list + 32ll * (k + kListAhead + u));
     }
 #pragma unroll
     for (int u = 0; u < kAhead; ++u) body(r[u]);
