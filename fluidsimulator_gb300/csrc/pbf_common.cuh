@@ -132,6 +132,7 @@ struct StepArgs {
   long long grid_capacity;
   long long nbr_capacity;
   int list16;             // 1: the list build may store 16-bit slices (0 for steps recorded for the adjoint)
+  int stage_rows;         // list entries per lane the build stages in shared memory
 };
 
 // Slice format bits (StepArgs::slice_fmt, per warp).

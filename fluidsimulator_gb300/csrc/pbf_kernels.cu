@@ -48,14 +48,14 @@ constexpr int kMaxBlock = 512;  // largest block the tuner may pick
 #ifndef FGB_LIST_MIN_BLOCKS
 #define FGB_LIST_MIN_BLOCKS 2
 #endif
-constexpr int kMaxBuildBlock = 256;  // k_nbr_build: kStage ints per thread of shared memory
-// List entries per lane staged in shared memory by the list build (kStage + 1
-// rows, 37 KB per 256-thread block). Lattice-phase lists hold at most ~32
-// entries; every staged row is shared memory the L1 cannot use for the
-// candidates the scan reads (5 blocks per SM), so the build ran 0.295 ms at
-// 40 and 0.284 ms at 36 or 32 per 1M step. Longer lists go through
-// k_nbr_overflow.
-constexpr int kStage = 36;
+constexpr int kMaxBuildBlock = kMaxStageBlock;  // k_nbr_build: stage_rows + 1 ints per thread of shared memory
+// List entries per lane staged in shared memory by the list build: the step
+// plan's stage_rows (+ a spare row), kStageRowsDefault = 36 unless a step's
+// lists were longer and fit kMaxStageRows (37 KB per 256-thread block at 36).
+// Lattice-phase lists hold at most ~32 entries; every staged row is shared
+// memory the L1 cannot use for the candidates the scan reads (5 blocks per
+// SM), so the build ran 0.295 ms at 40 and 0.284 ms at 36 or 32 per 1M step.
+// Longer lists go through k_nbr_overflow.
 
 __device__ __forceinline__ bool failed(const DevStatus* st) {
   return *reinterpret_cast<const volatile int*>(&st->err) != 0;
@@ -785,10 +785,10 @@ __device__ __forceinline__ void for_each_pair_candidate(const StepArgs& a, const
 }
 
 // Neighbour lists in one scan (core.cpp:205-247). Each lane stages its first
-// kStage list entries in shared memory while it scans. The staging takes no
+// stage_rows list entries in shared memory while it scans. The staging takes no
 // branch on the r2 test: every candidate is stored in the lane's next free
 // row, and the count advances only when the candidate is within h, so a
-// rejected candidate is overwritten by the next one (row kStage is a spare
+// rejected candidate is overwritten by the next one (row stage_rows is a spare
 // that absorbs the stores past the staged rows). At ~13 % acceptance this
 // took the lattice build from 0.285 to 0.260 ms per 1M step and the
 // collapsed 125k build from 0.96 to 0.80 ms against a branch around the
@@ -798,6 +798,9 @@ __device__ __forceinline__ void for_each_pair_candidate(const StepArgs& a, const
 // as coalesced 128-byte rows. Warps with a longer list set kSliceOverflow in
 // slice_fmt[w] and
 // k_nbr_overflow writes their remaining entries.
+// kRows: the staged rows when fixed at compile time (the default, which the
+// lattice phase uses), 0 to read them from the plan (a.stage_rows).
+template <int kRows>
 __global__ void __launch_bounds__(kMaxBuildBlock) k_nbr_build(StepArgs a) {
   extern __shared__ int stage[];
   // Other blocks of this launch may set the status (capacity) while this
@@ -811,7 +814,8 @@ __global__ void __launch_bounds__(kMaxBuildBlock) k_nbr_build(StepArgs a) {
   if (block_failed) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int* mine = stage + warp * ((kStage + 1) * 32) + lane;  // entry k at mine[32 k]
+  const int rows = kRows > 0 ? kRows : a.stage_rows;
+  int* mine = stage + warp * ((rows + 1) * 32) + lane;  // entry k at mine[32 k]
   int count = 0;
   if (i < a.n) {
     const uint32_t* ks = sorted_keys(a, a.status->npass);
@@ -822,7 +826,7 @@ __global__ void __launch_bounds__(kMaxBuildBlock) k_nbr_build(StepArgs a) {
     const float h2 = c.h2;
     auto test = [&](int j, const float4 q, bool ok) {
       const bool in = dist2(p.x - q.x, p.y - q.y, p.z - q.z) < h2 && ok;
-      mine[32 * min(count, kStage)] = j;
+      mine[32 * min(count, rows)] = j;
       count += in ? 1 : 0;
     };
     if (c.all_pairs) for_each_pair_candidate(a, c, i, a.p[0], [&](int j, const float4 q) { test(j, q, true); });
@@ -837,10 +841,10 @@ __global__ void __launch_bounds__(kMaxBuildBlock) k_nbr_build(StepArgs a) {
   // rounded up to whole 128-byte lines.
   const int anchor = (i - lane) - kSliceAnchorBack;
   bool near = true;
-  if (a.list16 && mx <= kStage) {
+  if (a.list16 && mx <= rows) {
     for (int k = 0; k < count; ++k) near = near && static_cast<unsigned>(mine[32 * k] - anchor) <= 0xffffu;
   }
-  const bool slim = __all_sync(kFull, near) && a.list16 && mx <= kStage;
+  const bool slim = __all_sync(kFull, near) && a.list16 && mx <= rows;
   const int ints = slim ? 32 * ((mx + 1) / 2) : 32 * mx;  // the warp's slice
   __shared__ int wints[kMaxBuildBlock / 32];
   __shared__ unsigned long long block_base;
@@ -872,18 +876,18 @@ __global__ void __launch_bounds__(kMaxBuildBlock) k_nbr_build(StepArgs a) {
       if (k < count) out[32 * k] = static_cast<unsigned short>(mine[32 * k] - anchor);
   } else {
     int* out = a.nbr + off + lane;
-    const int staged = mx < kStage ? mx : kStage;
+    const int staged = mx < rows ? mx : rows;
     for (int k = 0; k < staged; ++k)
       if (k < count) out[32ll * k] = mine[32 * k];
   }
   if (lane == 0) {
     a.wbase[i >> 5] = static_cast<long long>(off);
     a.depth[i >> 5] = mx;
-    a.slice_fmt[i >> 5] = (mx > kStage ? kSliceOverflow : 0) | (slim ? kSlice16 : 0);
+    a.slice_fmt[i >> 5] = (mx > rows ? kSliceOverflow : 0) | (slim ? kSlice16 : 0);
   }
 }
 
-// List entries kStage and above, for the warps k_nbr_build flagged.
+// List entries stage_rows and above, for the warps k_nbr_build flagged.
 __global__ void __launch_bounds__(kMaxBlock, 1) k_nbr_overflow(StepArgs a) {
   if (failed(a.status)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -899,7 +903,7 @@ __global__ void __launch_bounds__(kMaxBlock, 1) k_nbr_overflow(StepArgs a) {
   int k = 0;
   auto test = [&](int j, const float4 q, bool ok) {
     if (ok && dist2(p.x - q.x, p.y - q.y, p.z - q.z) < h2) {
-      if (k >= kStage && k < depth) out[32ll * k] = j;
+      if (k >= a.stage_rows && k < depth) out[32ll * k] = j;
       ++k;
     }
   };
@@ -2195,7 +2199,10 @@ cudaError_t enqueue_step(const StepArgs& args, const StepPlan& plan, cudaStream_
     cudaMemcpyAsync(rec->p, a.p[0], n4, cudaMemcpyDeviceToDevice, st);
   }
   const int bc = plan.block[FLUID_KERNEL_NBR_BUILD] > kMaxBuildBlock ? kMaxBuildBlock : plan.block[FLUID_KERNEL_NBR_BUILD];
-  k_nbr_build<<<blocks_for(a.n, bc), bc, sizeof(int) * (kStage + 1) * bc, st>>>(a);
+  a.stage_rows = plan.stage_rows;
+  const size_t stage_bytes = sizeof(int) * (plan.stage_rows + 1) * bc;
+  if (plan.stage_rows == kStageRowsDefault) k_nbr_build<kStageRowsDefault><<<blocks_for(a.n, bc), bc, stage_bytes, st>>>(a);
+  else k_nbr_build<0><<<blocks_for(a.n, bc), bc, stage_bytes, st>>>(a);
   m.mark(FLUID_KERNEL_NBR_BUILD);
   const int bf = plan.block[FLUID_KERNEL_NBR_OVERFLOW];
   k_nbr_overflow<<<blocks_for(a.n, bf), bf, 0, st>>>(a);

@@ -11,6 +11,12 @@ namespace fgb {
 
 // What one step launches; fixed for a configuration, so a captured graph of
 // it stays valid until buffers are reallocated or the flags change.
+// Staged list rows of the build: the default, and the most a block of
+// kMaxStageBlock threads can stage in 48 KB of shared memory with a spare row.
+constexpr int kStageRowsDefault = 36;
+constexpr int kMaxStageBlock = 256;
+constexpr int kMaxStageRows = 44;
+
 struct StepPlan {
   int iterations = 0;
   bool xsph = false;      // some scene runs XSPH
@@ -19,6 +25,9 @@ struct StepPlan {
   int radix_passes = 1;   // passes launched (cover the grid capacity)
   int radix_bits = 8;     // digit width of the sort: 8, 9 or 11
   int scorr_pow = 0;      // s_corr exponent shared by every s_corr scene (2-4), else 0
+  // List entries per lane the list build stages in shared memory; a warp with
+  // a longer list is finished by k_nbr_overflow (a second scan).
+  int stage_rows = kStageRowsDefault;
   // Per-kernel launch shape (indexed by FLUID_KERNEL_*), chosen by the
   // autotuner: neighbour entries fetched ahead (2, 4, 8; 1 when set
   // explicitly) in the list passes, and threads per block (128, 256, 512)

@@ -513,7 +513,10 @@ class Solver {
       last_cells_ = static_cast<int>(st.total_cells);
       last_npass_ = st.npass;
       if (enqueue_reset(status_.p, bmin_.p, bmax_.p, S_, stream_) != cudaSuccess) return cuda_fail("reset");
-      if (!st.err) return grow_ahead(st.cursor);
+      if (!st.err) {
+        adapt_stage_rows(st.nbr_max);
+        return grow_ahead(st.cursor);
+      }
       if (st.err != FLUID_ERR_CAPACITY) {
         cudaStreamSynchronize(stream_);
         return fail(st.err, st.err == FLUID_ERR_NONFINITE ? "non-finite predicted position"
@@ -1216,6 +1219,22 @@ class Solver {
         stage_launches_[st] += 1;
       }
     }
+  }
+
+  // The list build's staged rows follow the lists: raised (never lowered
+  // while the lists fit) to cover the longest list of a step when that fits
+  // kMaxStageRows, so a scene whose longest list sits just above the default
+  // (the 4,096-particle dam break: 35-40) has its lists staged whole instead
+  // of re-scanned by k_nbr_overflow; back to the default once lists outgrow
+  // it (a collapse, where the overflow pass runs anyway and a smaller stage
+  // leaves the L1 more room for the candidates).
+  void adapt_stage_rows(int longest) {
+    int rows = plan_.stage_rows;
+    if (longest > kMaxStageRows) rows = kStageRowsDefault;
+    else if (longest > rows) rows = std::min(kMaxStageRows, static_cast<int>(round_up(longest + 2, 4)));
+    if (rows == plan_.stage_rows) return;
+    plan_.stage_rows = rows;
+    invalidate_graphs();
   }
 
   // Grows the list capacity before a step needs it. After a step that
