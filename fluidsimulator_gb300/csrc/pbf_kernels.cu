@@ -608,6 +608,98 @@ __global__ void __launch_bounds__(kBlock) k_radix_onesweep(StepArgs a, int pass)
   }
 }
 
+// The whole sort in one block, for a batch of at most one tile (kRadixTile
+// keys): every 8-bit pass ranks the keys as k_radix_onesweep does (warp-
+// private digit counts in key order, then the warps' offsets per digit) and
+// places them through shared memory, the keys staying in registers between
+// passes; no digit-count kernel, no look-back, one launch instead of one per
+// pass. The result is the same stable order, written where k_reorder reads
+// the last pass's output (keys/vals[npass & 1] for the plan's pass count).
+__global__ void __launch_bounds__(kBlock) k_radix_tile(StepArgs a) {
+  constexpr int kBits = 8, kBins = 1 << kBits;
+  static_assert(kBins == kBlock, "thread t owns digit t");
+  __shared__ uint32_t wcnt[kBlock / 32][kBins];
+  __shared__ uint32_t total[kBins], start[kBins];
+  __shared__ uint32_t sk[kRadixTile];
+  __shared__ int sv[kRadixTile];
+  __shared__ int s_skip;
+  if (threadIdx.x == 0) s_skip = (failed(a.status) || a.status->npass == 0) ? 1 : 0;
+  __syncthreads();
+  if (s_skip) return;
+  const DevStatus* st = a.status;
+  const unsigned long long cells = st->total_cells;
+  const int bits = 32 - __clz(static_cast<int>(cells - 1ull));
+  const int passes = (bits + kBits - 1) / kBits;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int base = warp * (32 * kRadixItems);  // warp w holds keys [base, base + 32 kRadixItems)
+  uint32_t key[kRadixItems];
+  int val[kRadixItems];
+#pragma unroll
+  for (int r = 0; r < kRadixItems; ++r) {
+    const int idx = base + r * 32 + lane;
+    const bool ok = idx < a.n;
+    key[r] = ok ? a.keys[0][idx] : 0xffffffffu;  // padding sorts last and is not written
+    val[r] = ok ? idx : -1;
+  }
+  for (int pass = 0; pass < passes; ++pass) {
+    const int shift = kBits * pass;
+    for (int i = threadIdx.x; i < (kBlock / 32) * kBins; i += kBlock) (&wcnt[0][0])[i] = 0;
+    __syncthreads();
+    uint32_t rank[kRadixItems];
+    int dig[kRadixItems];
+#pragma unroll
+    for (int r = 0; r < kRadixItems; ++r) {
+      const int d = static_cast<int>((key[r] >> shift) & (kBins - 1u));
+      dig[r] = d;
+      const unsigned peers = __match_any_sync(kFull, d);
+      const uint32_t before = __popc(peers & lanemask_lt(lane));
+      const uint32_t run = wcnt[warp][d];
+      __syncwarp();
+      if (before == 0) wcnt[warp][d] = run + __popc(peers);
+      __syncwarp();
+      rank[r] = run + before;
+    }
+    __syncthreads();
+    // Thread t owns digit t: the warps' offsets within it, and its total.
+    {
+      const int d = threadIdx.x;  // kBlock == kBins
+      uint32_t run = 0;
+#pragma unroll
+      for (int w = 0; w < kBlock / 32; ++w) {
+        const uint32_t t = wcnt[w][d];
+        wcnt[w][d] = run;
+        run += t;
+      }
+      total[d] = run;
+    }
+    __syncthreads();
+    digit_starts<kBits>(total, start);
+#pragma unroll
+    for (int r = 0; r < kRadixItems; ++r) {
+      const uint32_t pos = start[dig[r]] + wcnt[warp][dig[r]] + rank[r];
+      sk[pos] = key[r];
+      sv[pos] = val[r];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kRadixItems; ++r) {
+      key[r] = sk[base + r * 32 + lane];
+      val[r] = sv[base + r * 32 + lane];
+    }
+    __syncthreads();
+  }
+  uint32_t* kout = a.keys[st->npass & 1];
+  int* vout = a.vals[st->npass & 1];
+#pragma unroll
+  for (int r = 0; r < kRadixItems; ++r) {
+    const int idx = base + r * 32 + lane;
+    if (idx < a.n) {
+      kout[idx] = key[r];
+      vout[idx] = val[r];
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Reorder into cell order and cell table.
 
@@ -2185,10 +2277,15 @@ cudaError_t enqueue_step(const StepArgs& args, const StepPlan& plan, cudaStream_
   m.mark(FLUID_KERNEL_GRID);
   k_keys<<<nb, kBlock, 0, st>>>(a);
   m.mark(FLUID_KERNEL_KEYS);
-  switch (plan.radix_bits) {
-    case 11: launch_sort<11>(a, plan.radix_passes, st, m); break;
-    case 9: launch_sort<9>(a, plan.radix_passes, st, m); break;
-    default: launch_sort<8>(a, plan.radix_passes, st, m); break;
+  if (a.n <= kRadixTile) {  // one tile: the whole sort in one block
+    k_radix_tile<<<1, kBlock, 0, st>>>(a);
+    m.mark(FLUID_KERNEL_RADIX_SCATTER);
+  } else {
+    switch (plan.radix_bits) {
+      case 11: launch_sort<11>(a, plan.radix_passes, st, m); break;
+      case 9: launch_sort<9>(a, plan.radix_passes, st, m); break;
+      default: launch_sort<8>(a, plan.radix_passes, st, m); break;
+    }
   }
   k_reorder<<<nb, kBlock, 0, st>>>(a);
   m.mark(FLUID_KERNEL_REORDER);
