@@ -47,6 +47,11 @@ if ROOT not in sys.path:
 
 N_SIDE = 100
 METRIC = "particle-steps/s @1M"
+# The workload both arms name in `config` (the reference arm times the same
+# step on the host cores, on as many of the scene's particles as its budget
+# allows; `particles` says how many).
+WORKLOAD = ("falling_block_1M: 100^3 lattice, sp 0.02, h 0.04, 8x4x4 box, s_corr+XSPH+vorticity, "
+            "4 iterations, one step over the initial batch per timed step")
 UNIT = "particle-steps/s"
 
 # Algorithmic bytes per particle per launch (compulsory per-particle array
@@ -400,9 +405,7 @@ def run_ours(args, world, rank, local):
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "falling_block_1M: 100^3 lattice, sp 0.02, h 0.04, 8x4x4 box, s_corr+XSPH+vorticity, "
-                               "4 iterations, one step over the initial batch per timed step",
-                   "particles": n, "neighbors_per_particle": round(stats["neighbor_pairs"] / n, 2),
+        "config": {"workload": WORKLOAD, "particles": n, "neighbors_per_particle": round(stats["neighbor_pairs"] / n, 2),
                    "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{world}",
                    "graphs": True, "exact_fp32": True,
                    "tuning": ({k: [v["unroll"], v["block"], v.get("lanes", 1)] for k, v in tuning.items()}
@@ -1058,7 +1061,7 @@ def run_reference(args, world, rank):
     out = {"metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 3), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
-           "config": {"workload": "falling_block_1M (CPU sample)", "particles": sample.count},
+           "config": {"workload": WORKLOAD, "particles": sample.count},
            "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": threads, "kind": "port", "sample": desc},
            "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
