@@ -23,7 +23,7 @@ struct StepPlan {
   bool vorticity = false; // some scene runs vorticity confinement
   bool restitution = false;
   int radix_passes = 1;   // passes launched (cover the grid capacity)
-  int radix_bits = 8;     // digit width of the sort: 8, 9 or 11
+  int radix_bits = 9;     // digit width of the sort: 8, 9 or 11 (9: two passes for keys of up to 18 bits, the 1M scene's)
   int scorr_pow = 0;      // s_corr exponent shared by every s_corr scene (2-4), else 0
   // List entries per lane the list build stages in shared memory; a warp with
   // a longer list is finished by k_nbr_overflow (a second scan).

@@ -310,7 +310,7 @@ int fluid_solver_set_tuning(fluid_solver* solver, const int32_t* unroll,
 int fluid_solver_get_lanes(fluid_solver* solver, int32_t* lanes, int32_t kernels);
 int fluid_solver_set_lanes(fluid_solver* solver, const int32_t* lanes, int32_t kernels);
 
-/* Digit width of the cell-key radix sort: 8 (default), 9 or 11 bits. Keys of
+/* Digit width of the cell-key radix sort: 8, 9 (default) or 11 bits. Keys of
  * b bits take ceil(b / width) passes; the permutation does not depend on it. */
 int fluid_solver_get_sort_bits(fluid_solver* solver, int32_t* bits);
 int fluid_solver_set_sort_bits(fluid_solver* solver, int32_t bits);
