@@ -370,6 +370,34 @@ def test_batched_regrow_matches_oracle(cuda_lib, oracle_lib, block, lanes):
         off += sc.count
 
 
+def test_lists_grown_ahead_of_need_match_oracle(cuda_lib, oracle_lib):
+    """A collapse stepped one synchronised step at a time: after each step
+    the solver reallocates the list buffer ahead of the next step's need, so
+    no step outgrows it (the same 40 steps in one call, where growth waits
+    for a failure, regrow and re-run three times). Both runs stay bit-exact
+    with the oracle."""
+    sc = scenes.dam_break(12, seed=7, flags=True)  # 1,728 particles, 25 -> 129 neighbours
+    steps = 40
+    ref = oracle_lib.Oracle().run(sc.params, sc.pos, sc.vel, 0.0, steps)
+    regrows = {}
+    for mode in ("per_step", "one_call"):
+        s = Solver(0)
+        s.configure([sc.params], [sc.count])
+        s.upload(sc.pos, sc.vel)
+        if mode == "per_step":
+            for _ in range(steps):
+                s.step(1)
+        else:
+            s.step(steps)
+        pos, vel = s.download()
+        regrows[mode] = s.stats()["regrows"]
+        s.close()
+        np.testing.assert_array_equal(pos, ref["pos"])
+        np.testing.assert_array_equal(vel, ref["vel"])
+    assert regrows["per_step"] == 0, regrows
+    assert regrows["one_call"] >= 1, regrows
+
+
 def test_nonfinite_input_reports_error_and_keeps_state(cuda_lib):
     sc = scenes.dam_break(6, seed=1)
     pos = sc.pos.copy()
