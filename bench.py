@@ -61,7 +61,6 @@ ALGO_BYTES_PER_PARTICLE = {
     "k_keys": 28,          # R x 12, v 12; W key 4
     "k_reorder": 76,       # R key 4, index 4, slot 4, x 12, v 12; W x 12, v 12, p* 12, slot 4
     "k_nbr_build": 16,     # R p* 12; W count 4 (lists excluded)
-    "k_nbr_overflow": 12,  # R p* 12 (only for warps whose lists outgrew the staging)
     "k_lambda": 20,        # R p* 12; W lambda 4, rho 4
     "k_delta": 28,         # R p* 12, lambda 4; W p* 12
     "k_xsph": 40,          # R x 12, v 12, rho 4; W v 12

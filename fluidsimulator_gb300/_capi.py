@@ -44,7 +44,7 @@ DEBUG_LAMBDA = 4
 KERNEL_NAMES = ["k_bounds", "k_grid_setup", "k_keys", "k_radix_digits", "k_radix_starts", "k_radix_onesweep",
                 "k_reorder", "k_nbr_build", "k_nbr_overflow", "k_lambda", "k_delta", "k_commit",
                 "k_xsph", "k_omega", "k_eta"]
-TUNABLE = ("k_nbr_build", "k_nbr_overflow", "k_lambda", "k_delta", "k_xsph", "k_omega", "k_eta")
+TUNABLE = ("k_nbr_build", "k_lambda", "k_delta", "k_xsph", "k_omega", "k_eta")
 LIST_PASSES = ("k_lambda", "k_delta", "k_xsph", "k_omega", "k_eta")  # may take several lanes per particle
 
 

@@ -11,8 +11,8 @@
 //                   cell (first, end) table by warp-shuffle boundary detection
 //   k_nbr_build     27-cell scan: lists in scan order staged in shared memory,
 //                   slices claimed by one atomic per block, coalesced copy-out;
-//                   capacity check
-//   k_nbr_overflow  re-scan for warps whose lists outgrew the staging
+//                   capacity check; a second scan for warps whose lists
+//                   outgrew the staging
 //   k_lambda        density / lambda (iterations 1-3 also record which of
 //                   each list's first 64 entries are within h: live bits)
 //   k_delta         position correction, s_corr, plane projection (last
@@ -55,7 +55,7 @@ constexpr int kMaxBuildBlock = kMaxStageBlock;  // k_nbr_build: stage_rows + 1 i
 // Lattice-phase lists hold at most ~32 entries; every staged row is shared
 // memory the L1 cannot use for the candidates the scan reads (5 blocks per
 // SM), so the build ran 0.295 ms at 40 and 0.284 ms at 36 or 32 per 1M step.
-// Longer lists go through k_nbr_overflow.
+// A warp with longer lists scans its candidates a second time.
 
 __device__ __forceinline__ bool failed(const DevStatus* st) {
   return *reinterpret_cast<const volatile int*>(&st->err) != 0;
@@ -887,9 +887,12 @@ __device__ __forceinline__ void for_each_pair_candidate(const StepArgs& a, const
 // store. The block then claims its warps' 32-wide
 // slices with one atomic on the list cursor (placement varies run to run,
 // every list's content and order do not) and writes the staged entries out
-// as coalesced 128-byte rows. Warps with a longer list set kSliceOverflow in
-// slice_fmt[w] and
-// k_nbr_overflow writes their remaining entries.
+// as coalesced 128-byte rows. A warp with a longer list (kSliceOverflow in
+// slice_fmt[w]) then scans its candidates a second time and writes the
+// entries past the staged rows straight into its slice: the same work a
+// separate pass over all particles did after the build, without that pass's
+// launch (14 us per 1M lattice step with nothing to do; 2 ms less per 1M
+// collapsed step).
 // kRows: the staged rows when fixed at compile time (the default, which the
 // lattice phase uses), 0 to read them from the plan (a.stage_rows).
 template <int kRows>
@@ -909,13 +912,14 @@ __global__ void __launch_bounds__(kMaxBuildBlock) k_nbr_build(StepArgs a) {
   const int rows = kRows > 0 ? kRows : a.stage_rows;
   int* mine = stage + warp * ((rows + 1) * 32) + lane;  // entry k at mine[32 k]
   int count = 0;
-  if (i < a.n) {
-    const uint32_t* ks = sorted_keys(a, a.status->npass);
-    const float4 p = a.p[0][i];
-    const int scene = __float_as_int(p.w);
-    const SceneConst& c = a.sc[scene];
-    const GridInfo g = a.grid[scene];
-    const float h2 = c.h2;
+  const bool live = i < a.n;
+  const uint32_t* ks = sorted_keys(a, a.status->npass);
+  const float4 p = live ? a.p[0][i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  const int scene = __float_as_int(p.w);
+  const SceneConst& c = a.sc[scene];
+  const GridInfo g = a.grid[scene];
+  const float h2 = c.h2;
+  if (live) {
     auto test = [&](int j, const float4 q, bool ok) {
       const bool in = dist2(p.x - q.x, p.y - q.y, p.z - q.z) < h2 && ok;
       mine[32 * min(count, rows)] = j;
@@ -977,30 +981,19 @@ __global__ void __launch_bounds__(kMaxBuildBlock) k_nbr_build(StepArgs a) {
     a.depth[i >> 5] = mx;
     a.slice_fmt[i >> 5] = (mx > rows ? kSliceOverflow : 0) | (slim ? kSlice16 : 0);
   }
-}
-
-// List entries stage_rows and above, for the warps k_nbr_build flagged.
-__global__ void __launch_bounds__(kMaxBlock, 1) k_nbr_overflow(StepArgs a) {
-  if (failed(a.status)) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n || !(a.slice_fmt[i >> 5] & kSliceOverflow)) return;
-  const uint32_t* ks = sorted_keys(a, a.status->npass);
-  const float4 p = a.p[0][i];
-  const int scene = __float_as_int(p.w);
-  const SceneConst& c = a.sc[scene];
-  const GridInfo g = a.grid[scene];
-  const int depth = a.depth[i >> 5];
-  int* out = a.nbr + a.wbase[i >> 5] + (threadIdx.x & 31);
-  const float h2 = c.h2;
-  int k = 0;
-  auto test = [&](int j, const float4 q, bool ok) {
-    if (ok && dist2(p.x - q.x, p.y - q.y, p.z - q.z) < h2) {
-      if (k >= a.stage_rows && k < depth) out[32ll * k] = j;
-      ++k;
-    }
-  };
-  if (c.all_pairs) for_each_pair_candidate(a, c, i, a.p[0], [&](int j, const float4 q) { test(j, q, true); });
-  else for_each_candidate<4>(a, ks, g, c, i, p, a.p[0], test);
+  if (mx > rows && live) {
+    // Entries rows and above: a second scan, written straight into the slice.
+    int* out = a.nbr + off + lane;
+    int k = 0;
+    auto rest = [&](int j, const float4 q, bool ok) {
+      if (ok && dist2(p.x - q.x, p.y - q.y, p.z - q.z) < h2) {
+        if (k >= rows && k < mx) out[32ll * k] = j;
+        ++k;
+      }
+    };
+    if (c.all_pairs) for_each_pair_candidate(a, c, i, a.p[0], [&](int j, const float4 q) { rest(j, q, true); });
+    else for_each_candidate<4>(a, ks, g, c, i, p, a.p[0], rest);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -2301,9 +2294,7 @@ cudaError_t enqueue_step(const StepArgs& args, const StepPlan& plan, cudaStream_
   if (plan.stage_rows == kStageRowsDefault) k_nbr_build<kStageRowsDefault><<<blocks_for(a.n, bc), bc, stage_bytes, st>>>(a);
   else k_nbr_build<0><<<blocks_for(a.n, bc), bc, stage_bytes, st>>>(a);
   m.mark(FLUID_KERNEL_NBR_BUILD);
-  const int bf = plan.block[FLUID_KERNEL_NBR_OVERFLOW];
-  k_nbr_overflow<<<blocks_for(a.n, bf), bf, 0, st>>>(a);
-  m.mark(FLUID_KERNEL_NBR_OVERFLOW);
+
 
   const bool post = plan.xsph || plan.vorticity;
   const int to_v2 = plan.xsph ? 1 : 0;

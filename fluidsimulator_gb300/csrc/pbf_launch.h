@@ -26,7 +26,7 @@ struct StepPlan {
   int radix_bits = 9;     // digit width of the sort: 8, 9 or 11 (9: two passes for keys of up to 18 bits, the 1M scene's)
   int scorr_pow = 0;      // s_corr exponent shared by every s_corr scene (2-4), else 0
   // List entries per lane the list build stages in shared memory; a warp with
-  // a longer list is finished by k_nbr_overflow (a second scan).
+  // a longer list is finished by a second scan of its candidates.
   int stage_rows = kStageRowsDefault;
   // Per-kernel launch shape (indexed by FLUID_KERNEL_*), chosen by the
   // autotuner: neighbour entries fetched ahead (2, 4, 8; 1 when set
@@ -64,7 +64,7 @@ inline bool tunable_unroll(int k) {
          k == FLUID_KERNEL_ETA;
 }
 inline bool tunable_block(int k) {
-  return tunable_unroll(k) || k == FLUID_KERNEL_NBR_BUILD || k == FLUID_KERNEL_NBR_OVERFLOW;
+  return tunable_unroll(k) || k == FLUID_KERNEL_NBR_BUILD;
 }
 
 // Records an event after selected launches when profiling is on.

@@ -1225,7 +1225,7 @@ class Solver {
   // while the lists fit) to cover the longest list of a step when that fits
   // kMaxStageRows, so a scene whose longest list sits just above the default
   // (the 4,096-particle dam break: 35-40) has its lists staged whole instead
-  // of re-scanned by k_nbr_overflow; back to the default once lists outgrow
+  // of scanned a second time; back to the default once lists outgrow
   // it (a collapse, where the overflow pass runs anyway and a smaller stage
   // leaves the L1 more room for the candidates).
   void adapt_stage_rows(int longest) {

@@ -258,7 +258,8 @@ enum {
   FLUID_KERNEL_RADIX_SCATTER = 5, /* sort: one pass per digit (rank, look-back, scatter) */
   FLUID_KERNEL_REORDER = 6,  /* gather into cell order + cell table */
   FLUID_KERNEL_NBR_BUILD = 7, /* lists (one scan) + slices */
-  FLUID_KERNEL_NBR_OVERFLOW = 8, /* long lists' remaining entries */
+  FLUID_KERNEL_NBR_OVERFLOW = 8, /* no launches: the list build writes long lists'
+                                    remaining entries itself (second scan) */
   FLUID_KERNEL_LAMBDA = 9,
   FLUID_KERNEL_DELTA = 10,   /* position correction (+ commit on the last) */
   FLUID_KERNEL_COMMIT = 11,  /* commit when solver_iterations == 0 */
