@@ -1434,7 +1434,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_xsph(StepArg
   unsigned long long bits = ~0ull;
   if (c.xsph_on) {
     const int n = a.cnt[i];
-      const float h2 = c.h2;
+    const float h2 = c.h2;
     float sx = 0.0f, sy = 0.0f, sz = 0.0f;
     auto load = [&](int j) { return PosVel{__ldg(xs + j), __ldg(vs + j)}; };
     auto one = [&](const PosVel r) {
@@ -1514,7 +1514,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_omega(StepAr
   unsigned long long bits = ~0ull;
   if (c.vort_on) {
     const int n = a.cnt[i];
-      const float h2 = c.h2;
+    const float h2 = c.h2;
     auto load = [&](int j) { return PosVel{__ldg(xs + j), __ldg(vs + j)}; };
     auto one = [&](const PosVel r) {
       const float dx = xi.x - r.x.x, dy = xi.y - r.x.y, dz = xi.z - r.x.z;
@@ -1613,7 +1613,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_eta(StepArgs
   if (c.vort_on) {
     const float4 oi = a.omega[i];
     const int n = a.cnt[i];
-      const float h2 = c.h2;
+    const float h2 = c.h2;
     float ex = 0.0f, ey = 0.0f, ez = 0.0f;
     auto load = [&](int j) { return __ldg(xo + j); };
     auto one = [&](const float4 r) {
