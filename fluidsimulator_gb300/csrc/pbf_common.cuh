@@ -136,7 +136,7 @@ struct StepArgs {
 };
 
 // Slice format bits (StepArgs::slice_fmt, per warp).
-constexpr int kSliceOverflow = 1;  // longer than the staging: k_nbr_overflow wrote the entries past it
+constexpr int kSliceOverflow = 1;  // longer than the staging: the build's second scan wrote the entries past it
 constexpr int kSlice16 = 2;        // 16-bit offsets from the warp's anchor
 constexpr int kSliceAnchorBack = 32768;  // anchor of warp w: 32 w - 32768
 

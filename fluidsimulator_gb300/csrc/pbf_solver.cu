@@ -1226,7 +1226,7 @@ class Solver {
   // kMaxStageRows, so a scene whose longest list sits just above the default
   // (the 4,096-particle dam break: 35-40) has its lists staged whole instead
   // of scanned a second time; back to the default once lists outgrow
-  // it (a collapse, where the overflow pass runs anyway and a smaller stage
+  // it (a collapse, where the second scan runs anyway and a smaller stage
   // leaves the L1 more room for the candidates).
   void adapt_stage_rows(int longest) {
     int rows = plan_.stage_rows;
