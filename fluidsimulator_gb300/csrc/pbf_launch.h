@@ -17,6 +17,8 @@ constexpr int kStageRowsDefault = 36;
 constexpr int kMaxStageBlock = 256;
 constexpr int kMaxStageRows = 44;
 
+constexpr int kDefaultListBlock = 128;  // threads per block of the list passes unless tuned
+
 struct StepPlan {
   int iterations = 0;
   bool xsph = false;      // some scene runs XSPH
@@ -43,6 +45,11 @@ struct StepPlan {
       block[k] = kBlock;
       lanes[k] = 1;
     }
+    // 128-thread blocks for the list passes: faster than 256 in the 1M lattice
+    // step (0.974 -> 0.959 ms) and in collapsed states (125k: 8.17 -> 7.94 ms;
+    // 1M step 22: 192.9 -> 187.8 ms) with four records ahead.
+    for (int k : {FLUID_KERNEL_LAMBDA, FLUID_KERNEL_DELTA, FLUID_KERNEL_XSPH, FLUID_KERNEL_OMEGA, FLUID_KERNEL_ETA})
+      block[k] = kDefaultListBlock;
   }
 };
 

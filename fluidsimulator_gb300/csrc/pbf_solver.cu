@@ -585,20 +585,21 @@ class Solver {
     StepPlan best = plan_;
     double best_ms[FLUID_KERNEL_COUNT];
     std::fill(std::begin(best_ms), std::end(best_ms), 1e300);
-    // The default shape (4 ahead, 256 threads) is timed first and another
-    // replaces the best only when at least 2 % faster, so a kernel that runs
-    // alike under several shapes in the tuned state keeps the default rather
-    // than a noise pick. One entry ahead is left out: with short lists (all
+    // Each kernel's default shape (4 ahead; 128 threads for the list passes,
+    // 256 for the build) is timed first and another replaces the best only
+    // when at least 2 % faster, so a kernel that runs alike under several
+    // shapes in the tuned state keeps its default rather than a noise pick. One entry ahead is left out: with short lists (all
     // within the live-bit head of the vorticity passes) it can win by a few
     // per cent on register count, and it is ~2x slower once lists grow.
     // Then several lanes per particle (2, 4, 8) at each block size, for the
     // list passes only (the list build keeps its one-lane shape).
     const int unrolls[] = {4, 2, 8};
-    const int blocks[] = {256, 128, 512};
+    const int blocks[] = {128, 256, 512};
     struct Shape {
-      int u, b, g;
+      int u, b, g;  // b = 0: each kernel's default block
     };
-    std::vector<Shape> shapes;
+    const StepPlan defaults;
+    std::vector<Shape> shapes{{4, 0, 1}};
     for (int u : unrolls)
       for (int b : blocks) shapes.push_back({u, b, 1});
     for (int g : {2, 4, 8})
@@ -611,7 +612,8 @@ class Solver {
             plan_.unroll[k] = u;
             plan_.lanes[k] = g;
           }
-          if (tunable_block(k)) plan_.block[k] = g == 1 || tunable_unroll(k) ? b : best.block[k];
+          if (tunable_block(k))
+            plan_.block[k] = b == 0 ? defaults.block[k] : (g == 1 || tunable_unroll(k) ? b : best.block[k]);
         }
         invalidate_graphs();
         kernel_times(nullptr, nullptr, 0, 1);
@@ -636,7 +638,7 @@ class Solver {
               best.unroll[k] = u;
               best.lanes[k] = g;
             }
-            best.block[k] = b;
+            best.block[k] = plan_.block[k];  // the block this shape launched (b = 0: the default)
           }
         }
       }
