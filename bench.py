@@ -24,6 +24,18 @@ the last 5, and neighbour-count histograms at steps 1, 5 and the last.
   parity_step1  that sample's first step on the GPU against the oracle
           (untimed): per-particle neighbour counts and their histogram,
           positions and velocities, bit for bit.
+  configs c1 (4,096-particle dam break, all 240 steps) and c2 (250k double
+          dam break, until its lists pass --c2-pair-budget entries) from
+          their initial states with autotuned shapes (c1 also with the
+          defaults); the oracle on the host over all of c1 and a prefix of
+          c2, the states compared bit for bit.
+  collapsed  one collapsed-phase step (the 125k falling block at step 21),
+          the GPU and the oracle from the same state.
+  batched 64 scenes in one solver against 64 solvers stepped in turn.
+  differentiable  the 60-step adjoint scene: forward and forward + adjoint
+          times and gradient norms (FP64 checks in the CPU leg).
+  output  one step plus one frame written per iteration at 1M, the
+          reference's ASCII writer against the asynchronous binary one.
 
 `--impl reference` times the reference's CPU step (the oracle restatement;
 the reference binary is not buildable on the GPU host) on the host cores.
