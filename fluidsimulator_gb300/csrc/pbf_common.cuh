@@ -34,6 +34,10 @@ namespace fgb {
 constexpr int kBlock = 256;
 constexpr int kRadixItems = 16;                     // keys per thread (8: 0.074 -> 0.067 ms of sort per 1M step at 16)
 constexpr int kRadixTile = kBlock * kRadixItems;    // keys per CTA
+// k_radix_onesweep's block at a digit width: 512 threads (8 keys each) up to
+// 9-bit digits; 256 at 11 bits, where 16 warps' digit counts would not fit
+// in static shared memory.
+constexpr int sort_threads(int bits) { return bits <= 9 ? 512 : 256; }
 constexpr int kRadixMaxBins = 1 << 11;                // widest digit (11 bits)
 constexpr int kRadixMaxPasses = 4;                  // passes of a u32 key at 8-bit digits
 constexpr int kRadixDigitBlocks = 304;              // k_radix_digits grid (stride over tiles)

@@ -444,11 +444,11 @@ __global__ void __launch_bounds__(kBlock) k_radix_digits(StepArgs a) {
 
 // Exclusive prefix over the kBins digit counts `tot` into starts[] (shared),
 // by the whole block; ends with a barrier.
-template <int kBits>
+template <int kBits, int kThreads = kBlock>
 __device__ __forceinline__ void digit_starts(const uint32_t* __restrict__ tot, uint32_t* starts) {
   constexpr int kBins = 1 << kBits;
-  constexpr int kPer = (kBins + kBlock - 1) / kBlock;  // contiguous digits per thread
-  __shared__ uint32_t warp_sums[kBlock / 32];
+  constexpr int kPer = (kBins + kThreads - 1) / kThreads;  // contiguous digits per thread
+  __shared__ uint32_t warp_sums[kThreads / 32];
   uint32_t v[kPer];
   uint32_t sum = 0;
 #pragma unroll
@@ -480,13 +480,14 @@ __device__ __forceinline__ void digit_starts(const uint32_t* __restrict__ tot, u
 // One pass: tiles are taken in launch order from a counter (so every tile a
 // tile waits for has started, and the waits always end), ranked in shared
 // memory, placed by the look-back, and scattered.
-template <int kBits>
-__global__ void __launch_bounds__(kBlock) k_radix_onesweep(StepArgs a, int pass) {
+template <int kBits, int kSortThreads = sort_threads(kBits)>
+__global__ void __launch_bounds__(kSortThreads) k_radix_onesweep(StepArgs a, int pass) {
   constexpr int kBins = 1 << kBits;
+  constexpr int kItems = kRadixTile / kSortThreads;  // keys per thread
   // Per-warp digit counts; at most kRadixTile = 4096 per tile, so 16 bits
   // hold them where 32-bit counters would not fit in shared memory.
   using Count = typename std::conditional<(kBits <= 8), uint32_t, uint16_t>::type;
-  __shared__ Count wcnt[kBlock / 32][kBins];
+  __shared__ Count wcnt[kSortThreads / 32][kBins];
   __shared__ uint32_t goff[kBins];  // digit starts, then this tile's first slot per digit
   __shared__ int s_tile, s_skip;
   if (threadIdx.x == 0) {
@@ -497,21 +498,21 @@ __global__ void __launch_bounds__(kBlock) k_radix_onesweep(StepArgs a, int pass)
   if (s_skip) return;
   const int tile = s_tile;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int i = threadIdx.x; i < (kBlock / 32) * kBins; i += kBlock) (&wcnt[0][0])[i] = 0;
-  digit_starts<kBits>(a.digit_total + pass * kBins, goff);
+  for (int i = threadIdx.x; i < (kSortThreads / 32) * kBins; i += kSortThreads) (&wcnt[0][0])[i] = 0;
+  digit_starts<kBits, kSortThreads>(a.digit_total + pass * kBins, goff);
   const uint32_t* kin = a.keys[pass & 1];
   const int* vin = a.vals[pass & 1];
   uint32_t* kout = a.keys[(pass + 1) & 1];
   int* vout = a.vals[(pass + 1) & 1];
   const int shift = kBits * pass;
-  // Warp w ranks its contiguous 32*kRadixItems keys in order, 32 at a time.
-  const long long base = static_cast<long long>(tile) * kRadixTile + warp * (32 * kRadixItems);
-  uint32_t key[kRadixItems];
-  int val[kRadixItems];
-  int dig[kRadixItems];
-  uint32_t rank[kRadixItems];
+  // Warp w ranks its contiguous 32*kItems keys in order, 32 at a time.
+  const long long base = static_cast<long long>(tile) * kRadixTile + warp * (32 * kItems);
+  uint32_t key[kItems];
+  int val[kItems];
+  int dig[kItems];
+  uint32_t rank[kItems];
 #pragma unroll
-  for (int r = 0; r < kRadixItems; ++r) {
+  for (int r = 0; r < kItems; ++r) {
     const long long idx = base + r * 32 + lane;
     const bool ok = idx < a.n;
     key[r] = ok ? kin[idx] : 0u;
@@ -529,19 +530,19 @@ __global__ void __launch_bounds__(kBlock) k_radix_onesweep(StepArgs a, int pass)
   __syncthreads();
   // Every digit's count goes out first (tile 0's as a prefix), so a tile
   // behind this one never waits on this tile's own look-back. Thread t owns
-  // digits t, t + kBlock, ... in both loops.
-  constexpr int kOwn = (kBins + kBlock - 1) / kBlock;
+  // digits t, t + kSortThreads, ... in both loops.
+  constexpr int kOwn = (kBins + kSortThreads - 1) / kSortThreads;
   const uint32_t tag = look_tag(a.status, pass);
   unsigned long long* look = a.look + static_cast<long long>(tile) * kBins;
   uint32_t runs[kOwn];
 #pragma unroll
   for (int k = 0; k < kOwn; ++k) {
-    const int d = threadIdx.x + k * kBlock;
+    const int d = threadIdx.x + k * kSortThreads;
     runs[k] = 0;
     if (d >= kBins) continue;
     uint32_t run = 0;
 #pragma unroll
-    for (int w = 0; w < kBlock / 32; ++w) {
+    for (int w = 0; w < kSortThreads / 32; ++w) {
       const uint32_t t = wcnt[w][d];
       wcnt[w][d] = static_cast<Count>(run);
       run += t;
@@ -552,7 +553,7 @@ __global__ void __launch_bounds__(kBlock) k_radix_onesweep(StepArgs a, int pass)
   bool timed_out = false;
 #pragma unroll
   for (int k = 0; k < kOwn; ++k) {
-    const int d = threadIdx.x + k * kBlock;
+    const int d = threadIdx.x + k * kSortThreads;
     if (d >= kBins) continue;
     uint32_t excl = 0;
     if (tile > 0) {
@@ -594,7 +595,7 @@ __global__ void __launch_bounds__(kBlock) k_radix_onesweep(StepArgs a, int pass)
   if (timed_out) set_error(a.status, FLUID_ERR_CUDA);
   __syncthreads();
 #pragma unroll
-  for (int r = 0; r < kRadixItems; ++r) {
+  for (int r = 0; r < kItems; ++r) {
     const int d = dig[r];
     if (d < kBins) {
       const uint32_t pos = goff[d] + wcnt[warp][d] + rank[r];
@@ -2225,7 +2226,7 @@ void launch_sort(const StepArgs& a, int passes, cudaStream_t st, LaunchMarks& m)
   k_radix_digits<kBits><<<digit_blocks, kBlock, 0, st>>>(a);
   m.mark(FLUID_KERNEL_RADIX_HIST);
   for (int pass = 0; pass < passes; ++pass) {
-    k_radix_onesweep<kBits><<<a.tiles, kBlock, 0, st>>>(a, pass);
+    k_radix_onesweep<kBits><<<a.tiles, sort_threads(kBits), 0, st>>>(a, pass);
     m.mark(FLUID_KERNEL_RADIX_SCATTER);
   }
 }
@@ -2294,7 +2295,6 @@ cudaError_t enqueue_step(const StepArgs& args, const StepPlan& plan, cudaStream_
   if (plan.stage_rows == kStageRowsDefault) k_nbr_build<kStageRowsDefault><<<blocks_for(a.n, bc), bc, stage_bytes, st>>>(a);
   else k_nbr_build<0><<<blocks_for(a.n, bc), bc, stage_bytes, st>>>(a);
   m.mark(FLUID_KERNEL_NBR_BUILD);
-
 
   const bool post = plan.xsph || plan.vorticity;
   const int to_v2 = plan.xsph ? 1 : 0;
