@@ -18,6 +18,8 @@ constexpr int kMaxStageBlock = 256;
 constexpr int kMaxStageRows = 44;
 
 constexpr int kDefaultListBlock = 128;  // threads per block of the list passes unless tuned
+constexpr long long kFewParticles = 16384;   // at most this many in all: eight lanes in lambda and delta
+constexpr long long kSomeParticles = 32768;  // at most this many: four
 
 struct StepPlan {
   int iterations = 0;
@@ -50,6 +52,21 @@ struct StepPlan {
     // 1M step 22: 192.9 -> 187.8 ms) with four records ahead.
     for (int k : {FLUID_KERNEL_LAMBDA, FLUID_KERNEL_DELTA, FLUID_KERNEL_XSPH, FLUID_KERNEL_OMEGA, FLUID_KERNEL_ETA})
       block[k] = kDefaultListBlock;
+  }
+  // The default lanes per particle for a solver of `particles` in all. At
+  // one lane a launch over a few thousand particles holds under a warp per
+  // SM, so lambda and delta split each list over eight lanes there (four up
+  // to 32,768); larger launches keep one, as the lanes' shuffles cost more
+  // than they fill once the SMs have warps. Steps 1-20 from rest, ms per
+  // step, one lane -> the default: dam breaks of 4,096 0.138 -> 0.094,
+  // 15,625 1.45 -> 1.08, 21,952 2.88 -> 2.29, 32,768 5.35 -> 4.71 particles;
+  // falling blocks of the same sizes 0.086 -> 0.080, 0.221 -> 0.173, 0.331 ->
+  // 0.263, 0.508 -> 0.402. The 64,000-particle dam break (7k neighbours)
+  // runs 13.1 ms at one lane and 16.7 at four.
+  void size_for(long long particles) {
+    const int g = particles <= kFewParticles ? 8 : particles <= kSomeParticles ? 4 : 1;
+    lanes[FLUID_KERNEL_LAMBDA] = g;
+    lanes[FLUID_KERNEL_DELTA] = g;
   }
 };
 

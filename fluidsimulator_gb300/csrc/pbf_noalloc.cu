@@ -166,6 +166,7 @@ extern "C" int fluid_gb300_step_noalloc(const fluid_params* params, int64_t coun
   StepArgs a = carve(base, n);
   const SceneConst c = scene_const_for(*params, 0, n);
   StepPlan plan;
+  plan.size_for(n);
   plan.iterations = c.iterations;
   plan.xsph = c.xsph_on != 0;
   plan.vorticity = c.vort_on != 0;

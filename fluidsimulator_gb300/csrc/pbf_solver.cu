@@ -267,6 +267,7 @@ class Solver {
     uploaded_ = false;
     build_scene_consts();
     plan_ = StepPlan();
+    plan_.size_for(n_);
     checkpoints_.clear();
     tapes_.clear();
     rec_steps_ = 0;
@@ -586,7 +587,7 @@ class Solver {
     double best_ms[FLUID_KERNEL_COUNT];
     std::fill(std::begin(best_ms), std::end(best_ms), 1e300);
     // Each kernel's default shape (4 ahead; 128 threads for the list passes,
-    // 256 for the build) is timed first and another replaces the best only
+    // 256 for the build; the default lanes for this particle count) is timed first and another replaces the best only
     // when at least 2 % faster, so a kernel that runs alike under several
     // shapes in the tuned state keeps its default rather than a noise pick. One entry ahead is left out: with short lists (all
     // within the live-bit head of the vorticity passes) it can win by a few
@@ -596,10 +597,11 @@ class Solver {
     const int unrolls[] = {4, 2, 8};
     const int blocks[] = {128, 256, 512};
     struct Shape {
-      int u, b, g;  // b = 0: each kernel's default block
+      int u, b, g;  // b = 0, g = 0: each kernel's default block, lanes
     };
-    const StepPlan defaults;
-    std::vector<Shape> shapes{{4, 0, 1}};
+    StepPlan defaults;
+    defaults.size_for(n_);
+    std::vector<Shape> shapes{{4, 0, 0}};
     for (int u : unrolls)
       for (int b : blocks) shapes.push_back({u, b, 1});
     for (int g : {2, 4, 8})
@@ -610,7 +612,7 @@ class Solver {
         for (int k = 0; k < FLUID_KERNEL_COUNT; ++k) {
           if (tunable_unroll(k)) {
             plan_.unroll[k] = u;
-            plan_.lanes[k] = g;
+            plan_.lanes[k] = g == 0 ? defaults.lanes[k] : g;
           }
           if (tunable_block(k))
             plan_.block[k] = b == 0 ? defaults.block[k] : (g == 1 || tunable_unroll(k) ? b : best.block[k]);
@@ -636,7 +638,7 @@ class Solver {
             best_ms[k] = avg;
             if (tunable_unroll(k)) {
               best.unroll[k] = u;
-              best.lanes[k] = g;
+              best.lanes[k] = plan_.lanes[k];
             }
             best.block[k] = plan_.block[k];  // the block this shape launched (b = 0: the default)
           }

@@ -284,8 +284,9 @@ int fluid_solver_kernel_times(fluid_solver* solver, double* ms_out,
  * neighbour entries fetched ahead in {2, 4, 8}, threads per block in
  * {128, 256, 512}, and for the list passes 2, 4 or 8 lanes per particle at
  * each block size -- over `trials` discarded steps of the current state. It
- * keeps the default shape (4, 256) unless another is at least 2 % faster,
- * and else the fastest, per kernel. It then times the cell-key sort with 8-,
+ * keeps each kernel's default shape (4 ahead; 128 threads for the list
+ * passes, 256 for the build; the default lanes below) unless another is at
+ * least 2 % faster, and else the fastest, per kernel. It then times the cell-key sort with 8-,
  * 9- and 11-bit digits and keeps the fastest width. One entry ahead (the
  * single-entry walker) is left out of the sweep: where all lists are short
  * it can win narrowly and then lose by far once they grow; set it with
@@ -305,7 +306,9 @@ int fluid_solver_set_tuning(fluid_solver* solver, const int32_t* unroll,
  * _XSPH, _OMEGA, _ETA): 1 (one lane walks a particle's list; the unroll of
  * fluid_solver_set_tuning applies), or 2, 4 or 8 lanes that split the list
  * into rounds and add the round's terms in list order, for launches short of
- * warps. Every other kernel takes 1. The autotuner chooses it with the other
+ * warps. Every other kernel takes 1. By default lambda and delta take 8
+ * when the solver's scenes hold at most 16,384 particles in all, 4 up to
+ * 32,768, and 1 above; the other list passes take 1. The autotuner chooses it with the other
  * shapes; results are identical under every choice. (No counterpart in the
  * reference, whose CUDA step maps one thread to a particle.) */
 int fluid_solver_get_lanes(fluid_solver* solver, int32_t* lanes, int32_t kernels);

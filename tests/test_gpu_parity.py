@@ -21,10 +21,10 @@ DEBUG = {"cell_keys": _capi.DEBUG_CELL_KEYS, "sorted_order": _capi.DEBUG_SORTED_
          "neighbor_counts": _capi.DEBUG_NEIGHBOR_COUNTS, "rho": _capi.DEBUG_RHO, "lambda": _capi.DEBUG_LAMBDA}
 
 
-def run_gpu(sc, steps, graphs=True, profiling=False, records=False, lanes=1):
+def run_gpu(sc, steps, graphs=True, profiling=False, records=False, lanes=None):
     s = Solver(0)
     s.configure([sc.params], [sc.count])
-    if lanes != 1:
+    if lanes is not None:  # else the solver's default shapes
         s.set_tuning({k: {"unroll": 4, "block": 256, "lanes": lanes if k in _capi.LIST_PASSES else 1}
                       for k in _capi.TUNABLE})
     s.set_graphs(graphs)
@@ -665,6 +665,30 @@ def test_lanes_are_checked(cuda_lib):
     with pytest.raises(FluidError):
         s.set_tuning({"k_nbr_build": {"unroll": 4, "block": 256, "lanes": 2}})
     s.close()
+
+
+@pytest.mark.parametrize("side, lanes", [(16, 8), (25, 8), (26, 4), (32, 4), (33, 1)])
+def test_default_lanes_follow_particle_count(cuda_lib, side, lanes):
+    """Lambda and delta default to eight lanes per particle up to 16,384
+    particles in all (25^3 = 15,625), four up to 32,768 (26^3 = 17,576 and
+    32^3) and one above (33^3 = 35,937); the other list passes to one."""
+    sc = scenes.dam_break(side, seed=1)
+    s = Solver(0)
+    s.configure([sc.params], [sc.count])
+    got = {k: v["lanes"] for k, v in s.tuning().items() if k in _capi.LIST_PASSES}
+    s.close()
+    assert got == {k: lanes if k in ("k_lambda", "k_delta") else 1 for k in _capi.LIST_PASSES}
+
+
+def test_one_lane_on_a_small_scene_matches_oracle(cuda_lib, oracle_lib):
+    """The 4,096-particle dam break (flags on) over 30 steps with one lane in
+    every list pass, set explicitly (the default there is eight in lambda and
+    delta), against the oracle."""
+    sc = scenes.dam_break(16, seed=3, flags=True)
+    ref = oracle_lib.Oracle().run(sc.params, sc.pos, sc.vel, 0.0, 30)
+    b = run_gpu(sc, 30, lanes=1)
+    np.testing.assert_array_equal(b["pos"], ref["pos"])
+    np.testing.assert_array_equal(b["vel"], ref["vel"])
 
 
 def _corners():
