@@ -30,7 +30,8 @@ the last 5, and neighbour-count histograms at steps 1, 5 and the last.
           defaults); the oracle on the host over all of c1 and a prefix of
           c2, the states compared bit for bit.
   collapsed  one collapsed-phase step (the 125k falling block at step 21),
-          the GPU and the oracle from the same state.
+          the GPU (autotuned on that state, and default shapes) and the
+          oracle from the same state.
   batched 64 scenes in one solver against 64 solvers stepped in turn.
   differentiable  the 60-step adjoint scene: forward and forward + adjoint
           times and gradient norms (FP64 checks in the CPU leg).
@@ -547,7 +548,9 @@ def run_collapsed(args, dev, stream):
     same state: the 125,000-particle falling block (50^3, the 1M scene's
     spacing, h and flags) stepped `collapsed_at - 1` steps on the GPU, its
     state downloaded, then step `collapsed_at` timed from that state (re-
-    uploaded before each of a few repetitions; median)."""
+    uploaded before each of a few repetitions; median), first with the default
+    shapes, then with the shapes fluid_solver_autotune picks on that state."""
+    import numpy as np
     import torch
 
     from fluidsimulator_gb300 import scenes
@@ -564,23 +567,38 @@ def run_collapsed(args, dev, stream):
     pos, vel = s.download()
     t0 = s.time()
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
-    ms = []
-    for _ in range(4):
-        s.upload(pos, vel)
-        s.set_time(t0)
-        ev[0].record(stream)
-        s.step_async(1)
-        ev[1].record(stream)
-        s.synchronize()
-        ms.append(ev[0].elapsed_time(ev[1]))
+
+    def one_step_ms():
+        ms = []
+        for _ in range(4):
+            s.upload(pos, vel)
+            s.set_time(t0)
+            ev[0].record(stream)
+            s.step_async(1)
+            ev[1].record(stream)
+            s.synchronize()
+            ms.append(ev[0].elapsed_time(ev[1]))
+        return statistics.median(ms[1:])
+
+    dms = one_step_ms()
     st = s.stats()
     after = s.download()
+    s.upload(pos, vel)
+    s.set_time(t0)
+    tuned = s.autotune()
+    shapes = {"sort_bits": s.sort_bits(), **{k: [v["unroll"], v["block"], v["lanes"]] for k, v in tuned.items()}}
+    gms = one_step_ms()
+    after_tuned = s.download()
     s.close()
-    gms = statistics.median(ms[1:])
+    timing = "CUDA events around one step from the uploaded state; median of 3 after one warm-up"
     return {"scene": f"falling_block_{sc.count}", "particles": sc.count, "step": args.collapsed_at,
             "neighbors_per_particle": round(st["neighbor_pairs"] / sc.count, 2), "neighbor_max": st["neighbor_max"],
             "gpu": {"ms_per_step": round(gms, 4), "particle_steps_per_s": round(sc.count / (gms / 1e3), 1),
-                    "timing": "CUDA events around one step from the uploaded state; median of 3 after one warm-up"},
+                    "shapes": shapes, "timing": timing + ", shapes autotuned on this state"},
+            "gpu_default_shapes": {"ms_per_step": round(dms, 4),
+                                   "particle_steps_per_s": round(sc.count / (dms / 1e3), 1), "timing": timing},
+            "tuned_equals_default": bool(np.array_equal(after[0], after_tuned[0])
+                                         and np.array_equal(after[1], after_tuned[1])),
             "_state": (sc, pos, vel, t0, after)}
 
 
