@@ -28,6 +28,7 @@
 #include <cstdint>
 
 #include "fluid_gb300.h"
+#include "pbf_sqrt.cuh"
 
 namespace fgb {
 
@@ -66,6 +67,7 @@ struct SceneConst {
   int all_pairs;                  // use_uniform_grid == 0: lists from all pairs
   int first_slot, count;          // particle range of the scene
   float neg_zero;                 // -0.0f, read at run time (see pmul in the kernels)
+  int exact_sqrt;                 // 1: clamped r^2 range outside rn_sqrt's checked range (the plan then uses sqrtf)
   float4 planes[FLUID_MAX_PLANES];  // (nx, ny, nz, d)
   float rest_scale[FLUID_MAX_PLANES];  // 1 - friction of each plane
 };

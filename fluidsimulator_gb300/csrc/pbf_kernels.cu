@@ -127,9 +127,13 @@ __device__ __forceinline__ float spiky(const SceneConst& c, float r) {
   return c.spiky_c * d * d;
 }
 
-// r from r^2 with the 0.01 h floor (core.cpp:303).
+// r from r^2 with the 0.01 h floor (core.cpp:303), correctly rounded:
+// rn_sqrt (checked over every scene's clamped r^2 range unless the step's
+// plan says otherwise), or sqrtf in the kIeee instantiations.
+template <bool kIeee = false>
 __device__ __forceinline__ float clamped_r(const SceneConst& c, float r2) {
-  return sqrtf(r2 < c.min_r2 ? c.min_r2 : r2);
+  const float x = r2 < c.min_r2 ? c.min_r2 : r2;
+  return kIeee ? sqrtf(x) : rn_sqrt(x);
 }
 
 // ratio^n (core.cpp:59-71).
@@ -177,8 +181,10 @@ __device__ __forceinline__ float2 poly6_pair(const SceneConst& c, const float2 r
   return pmul(f2(c.poly6_c), pmul(pmul(d, d, nz), d, nz), nz);
 }
 // spiky(clamped_r(r2)) of both lanes.
+template <bool kIeee = false>
 __device__ __forceinline__ float2 spiky_pair(const SceneConst& c, const float2 r2, const float2 nz) {
-  const float2 r = make_float2(clamped_r(c, r2.x), clamped_r(c, r2.y));
+  const float2 x = make_float2(r2.x < c.min_r2 ? c.min_r2 : r2.x, r2.y < c.min_r2 ? c.min_r2 : r2.y);
+  const float2 r = kIeee ? make_float2(sqrtf(x.x), sqrtf(x.y)) : rn_sqrt2(x, nz);
   const float2 e = psub(f2(c.h), r);
   float2 gf = pmul(pmul(f2(c.spiky_c), e, nz), e, nz);
   if (r.x > c.h) gf.x = 0.0f;
@@ -819,9 +825,10 @@ __device__ __forceinline__ float finish_lambda(const SceneConst& c, float rho, f
 // Per-neighbour density / gradient terms (core.cpp:300-316).
 struct LambdaAcc {
   float rho = 0.0f, gsx = 0.0f, gsy = 0.0f, gsz = 0.0f, sum_g2 = 0.0f;
+  template <bool kIeee = false>
   __device__ __forceinline__ void add(const SceneConst& c, float dx, float dy, float dz, float r2) {
     rho += poly6(c, r2);
-    const float gf = spiky(c, clamped_r(c, r2));
+    const float gf = spiky(c, clamped_r<kIeee>(c, r2));
     const float gx = gf * dx, gy = gf * dy, gz = gf * dz;
     gsx += gx;
     gsy += gy;
@@ -834,6 +841,7 @@ struct LambdaAcc {
   // r2 < h2: the same operations as the membership test plus add() on a,
   // then on b, with the per-entry terms formed in paired arithmetic.
   // Returns which of a (bit 0) and b (bit 1) were within h.
+  template <bool kIeee = false>
   __device__ __forceinline__ unsigned add_pair(const SceneConst& c, const float2 px, const float2 py,
                                                const float2 pz, const float4 qa, const float4 qb) {
     const float2 nz = f2(c.neg_zero);
@@ -841,7 +849,7 @@ struct LambdaAcc {
     const bool oka = g.r2.x < c.h2, okb = g.r2.y < c.h2;
     if (!oka && !okb) return 0u;
     const float2 w = poly6_pair(c, g.r2, nz);
-    const float2 gf = spiky_pair(c, g.r2, nz);
+    const float2 gf = spiky_pair<kIeee>(c, g.r2, nz);
     const float2 gx = pmul(gf, g.dx, nz), gy = pmul(gf, g.dy, nz), gz = pmul(gf, g.dz, nz);
     const float2 ng = f2(-c.grad_scale);
     const float2 jx = pmul(ng, gx, nz), jy = pmul(ng, gy, nz), jz = pmul(ng, gz, nz);
@@ -1220,7 +1228,7 @@ __device__ __forceinline__ void for_each_live_then(const L& list, int n, unsigne
 // kLiveOut: record the live bits of these positions for the delta pass
 // (iterations after the first; the first runs at the positions the lists
 // were built from, where every entry is live).
-template <int U, bool kLiveOut>
+template <int U, bool kLiveOut, bool kIeee = false>
 __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_lambda(StepArgs a, int in) {
   if (failed(a.status)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1234,7 +1242,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_lambda(StepA
   auto one = [&](const float4 q) {
     const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
     const float r2 = dist2(dx, dy, dz);
-    if (r2 < h2) acc.add(c, dx, dy, dz, r2);
+    if (r2 < h2) acc.add<kIeee>(c, dx, dy, dz, r2);
     return r2 < h2;
   };
   auto load = [&](int j) { return __ldg(pos + j); };
@@ -1253,7 +1261,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_lambda(StepA
       }
     } else {
       const float2 px = f2(p.x), py = f2(p.y), pz = f2(p.z);
-      auto two = [&](const float4 qa, const float4 qb) { return acc.add_pair(c, px, py, pz, qa, qb); };
+      auto two = [&](const float4 qa, const float4 qb) { return acc.add_pair<kIeee>(c, px, py, pz, qa, qb); };
       if constexpr (kLiveOut) store_live(a.live, a.n, i, for_each_neighbor_pair_rec<U>(list, n, load, two, one));
       else for_each_neighbor_pair<U>(list, n, load, two, one);
     }
@@ -1325,7 +1333,7 @@ __device__ __forceinline__ void delta_out(const StepArgs& a, const SceneConst& c
 // 4), else 0 (read per scene).
 // kLiveIn: only the live ones among the first entries (live bits from the
 // lambda pass of this iteration, same positions).
-template <int U, int kPow, bool kLiveIn>
+template <int U, int kPow, bool kLiveIn, bool kIeee = false>
 __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_delta(StepArgs a, int in, int last, int to_v2, int rest, float4* q_out) {
   if (failed(a.status)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1342,7 +1350,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_delta(StepAr
     const float dx = p.x - r.x, dy = p.y - r.y, dz = p.z - r.z;
     const float r2 = dist2(dx, dy, dz);
     if (r2 < h2) {
-      const float gf = spiky(c, clamped_r(c, r2));
+      const float gf = spiky(c, clamped_r<kIeee>(c, r2));
       float s = li + r.w;
       if (scorr) {
         const float ratio = poly6(c, r2) * c.scorr_inv_wdq;
@@ -1371,7 +1379,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_delta(StepAr
         const PairGeom g = pair_geom(px, py, pz, qa, qb, nz);
         const bool oka = g.r2.x < h2, okb = g.r2.y < h2;
         if (!oka && !okb) return;
-        const float2 gf = spiky_pair(c, g.r2, nz);
+        const float2 gf = spiky_pair<kIeee>(c, g.r2, nz);
         float2 s = padd(f2(li), make_float2(qa.w, qb.w));
         if (scorr) {
           const float2 ratio = pmul(poly6_pair(c, g.r2, nz), f2(c.scorr_inv_wdq), nz);
@@ -1501,7 +1509,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_xsph(StepArg
 // Vorticity omega and |omega| (core.cpp:472-508). kLive: 1 = only the live
 // ones among the first entries (live bits from XSPH, same positions); 2 =
 // record the live bits for the eta pass (no XSPH this step).
-template <int U, int kLive>
+template <int U, int kLive, bool kIeee = false>
 __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_omega(StepArgs a) {
   if (failed(a.status)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1521,7 +1529,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_omega(StepAr
       const float dx = xi.x - r.x.x, dy = xi.y - r.x.y, dz = xi.z - r.x.z;
       const float r2 = dist2(dx, dy, dz);
       if (r2 < h2) {
-        const float gf = spiky(c, clamped_r(c, r2));
+        const float gf = spiky(c, clamped_r<kIeee>(c, r2));
         const float gx = gf * dx, gy = gf * dy, gz = gf * dz;
         const float ux = r.v.x - vi.x, uy = r.v.y - vi.y, uz = r.v.z - vi.z;
         ox += uy * gz - uz * gy;
@@ -1536,7 +1544,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_omega(StepAr
       const PairGeom g = pair_geom(px, py, pz, ra.x, rb.x, nz);
       const bool oka = g.r2.x < h2, okb = g.r2.y < h2;
       if (!oka && !okb) return 0u;
-      const float2 gf = spiky_pair(c, g.r2, nz);
+      const float2 gf = spiky_pair<kIeee>(c, g.r2, nz);
       const float2 gx = pmul(gf, g.dx, nz), gy = pmul(gf, g.dy, nz), gz = pmul(gf, g.dz, nz);
       const float2 ux = psub(make_float2(ra.v.x, rb.v.x), f2(vi.x));
       const float2 uy = psub(make_float2(ra.v.y, rb.v.y), f2(vi.y));
@@ -1602,7 +1610,7 @@ __device__ __forceinline__ void confine(const SceneConst& c, const float4 oi, fl
 // Eta, confinement force, velocity update (core.cpp:512-570) and plane
 // restitution (core.cpp:573-612); only the live ones among the first
 // entries (live bits of these positions from XSPH or omega).
-template <int U>
+template <int U, bool kIeee = false>
 __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_eta(StepArgs a, int rest) {
   if (failed(a.status)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1621,7 +1629,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_eta(StepArgs
       const float dx = xi.x - r.x, dy = xi.y - r.y, dz = xi.z - r.z;
       const float r2 = dist2(dx, dy, dz);
       if (r2 < h2) {
-        const float gf = spiky(c, clamped_r(c, r2));
+        const float gf = spiky(c, clamped_r<kIeee>(c, r2));
         const float coeff = r.w - oi.w;
         ex += coeff * (gf * dx);
         ey += coeff * (gf * dy);
@@ -1634,7 +1642,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_eta(StepArgs
       const PairGeom g = pair_geom(px, py, pz, ra, rb, nz);
       const bool oka = g.r2.x < h2, okb = g.r2.y < h2;
       if (!oka && !okb) return;
-      const float2 gf = spiky_pair(c, g.r2, nz);
+      const float2 gf = spiky_pair<kIeee>(c, g.r2, nz);
       const float2 coeff = psub(make_float2(ra.w, rb.w), f2(oi.w));
       const float2 tx = pmul(coeff, pmul(gf, g.dx, nz), nz);
       const float2 ty = pmul(coeff, pmul(gf, g.dy, nz), nz);
@@ -2088,9 +2096,14 @@ inline int list_grid(const StepArgs& a, int block, int lanes) {
 
 // Launch shape of list kernel k in the plan: block size, records fetched
 // ahead (one lane per particle) and lanes per particle.
+// A list pass's launch shape. ieee: some scene's clamped r^2 range lies
+// outside rn_sqrt's checked range, so the passes that take square roots run
+// their one-lane, four-ahead form with sqrtf (any shape gives the same bits).
 struct ListShape {
   int block, unroll, lanes;
-  ListShape(const StepPlan& plan, int k) : block(plan.block[k]), unroll(plan.unroll[k]), lanes(plan.lanes[k]) {}
+  bool ieee;
+  ListShape(const StepPlan& plan, int k)
+      : block(plan.block[k]), unroll(plan.unroll[k]), lanes(plan.lanes[k]), ieee(plan.ieee_sqrt) {}
 };
 
 template <int kPow, bool kLiveIn>
@@ -2108,6 +2121,10 @@ struct DeltaPow {
   static void dispatch(const ListShape& sh, cudaStream_t st, const StepArgs& a, int in, int last, int to_v2,
                        int rest, float4* q_out) {
     const int b = sh.block;
+    if (sh.ieee) {
+      k_delta<4, kPow, kLiveIn, true><<<list_grid(a, b, 1), b, 0, st>>>(a, in, last, to_v2, rest, q_out);
+      return;
+    }
     switch (sh.lanes) {
       case 2: launch_lanes<2>(b, st, a, in, last, to_v2, rest, q_out); return;
       case 4: launch_lanes<4>(b, st, a, in, last, to_v2, rest, q_out); return;
@@ -2147,6 +2164,10 @@ template <bool kLiveOut>
 void launch_lambda(const StepPlan& plan, cudaStream_t st, const StepArgs& a, int in) {
   const ListShape sh(plan, FLUID_KERNEL_LAMBDA);
   const int b = sh.block;
+  if (sh.ieee) {
+    k_lambda<4, kLiveOut, true><<<list_grid(a, b, 1), b, 0, st>>>(a, in);
+    return;
+  }
   switch (sh.lanes) {
     case 2: k_lambda_lanes<2, kLiveOut><<<list_grid(a, b, 2), b, 0, st>>>(a, in); return;
     case 4: k_lambda_lanes<4, kLiveOut><<<list_grid(a, b, 4), b, 0, st>>>(a, in); return;
@@ -2185,6 +2206,10 @@ template <int kLive>
 void launch_omega(const StepPlan& plan, cudaStream_t st, const StepArgs& a) {
   const ListShape sh(plan, FLUID_KERNEL_OMEGA);
   const int b = sh.block;
+  if (sh.ieee) {
+    k_omega<4, kLive, true><<<list_grid(a, b, 1), b, 0, st>>>(a);
+    return;
+  }
   switch (sh.lanes) {
     case 2: k_omega_lanes<2, kLive><<<list_grid(a, b, 2), b, 0, st>>>(a); return;
     case 4: k_omega_lanes<4, kLive><<<list_grid(a, b, 4), b, 0, st>>>(a); return;
@@ -2203,6 +2228,10 @@ void launch_omega(const StepPlan& plan, cudaStream_t st, const StepArgs& a) {
 void launch_eta(const StepPlan& plan, cudaStream_t st, const StepArgs& a, int rest) {
   const ListShape sh(plan, FLUID_KERNEL_ETA);
   const int b = sh.block;
+  if (sh.ieee) {
+    k_eta<4, true><<<list_grid(a, b, 1), b, 0, st>>>(a, rest);
+    return;
+  }
   switch (sh.lanes) {
     case 2: k_eta_lanes<2><<<list_grid(a, b, 2), b, 0, st>>>(a, rest); return;
     case 4: k_eta_lanes<4><<<list_grid(a, b, 4), b, 0, st>>>(a, rest); return;

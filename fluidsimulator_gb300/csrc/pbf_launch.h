@@ -32,6 +32,10 @@ struct StepPlan {
   // List entries per lane the list build stages in shared memory; a warp with
   // a longer list is finished by a second scan of its candidates.
   int stage_rows = kStageRowsDefault;
+  // Some scene's clamped r^2 range, [(0.01 h)^2, h^2), lies outside the
+  // range where the list passes' square root is checked against sqrtf (only
+  // scenes whose kernel constants overflow or vanish): their passes use sqrtf.
+  bool ieee_sqrt = false;
   // Per-kernel launch shape (indexed by FLUID_KERNEL_*), chosen by the
   // autotuner: neighbour entries fetched ahead (2, 4, 8; 1 when set
   // explicitly) in the list passes, and threads per block (128, 256, 512)

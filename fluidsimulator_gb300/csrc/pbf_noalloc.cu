@@ -174,6 +174,7 @@ extern "C" int fluid_gb300_step_noalloc(const fluid_params* params, int64_t coun
   plan.radix_bits = 8;
   plan.radix_passes = 3;  // keys < FLUID_NOALLOC_MAX_CELLS = 2^18
   plan.scorr_pow = shared_scorr_pow(&c, 1);
+  plan.ieee_sqrt = c.exact_sqrt != 0;
   LaunchMarks marks;      // profiling off
 
   if (cudaMemcpyAsync(const_cast<SceneConst*>(a.sc), &c, sizeof(c), cudaMemcpyHostToDevice, st) != cudaSuccess)

@@ -135,6 +135,7 @@ SceneConst make_scene_const(const fluid_params& p, int first, int count) {
   c.all_pairs = p.use_uniform_grid ? 0 : 1;
   c.first_slot = first;
   c.neg_zero = -0.0f;
+  c.exact_sqrt = rn_sqrt_covers(c.min_r2, c.h2) ? 0 : 1;
   c.count = count;
   for (int q = 0; q < p.plane_count; ++q) {
     c.planes[q] = make_float4(p.plane_nx[q], p.plane_ny[q], p.plane_nz[q], p.plane_d[q]);
@@ -1061,6 +1062,8 @@ class Solver {
     }
     plan_.radix_passes = std::max(1, (bits_for(grid_cap_) + plan_.radix_bits - 1) / plan_.radix_bits);
     plan_.scorr_pow = shared_scorr_pow(sc_host_.data(), S_);
+    plan_.ieee_sqrt = false;
+    for (const auto& c : sc_host_) plan_.ieee_sqrt |= c.exact_sqrt != 0;
   }
 
   void advance_times(int steps) {

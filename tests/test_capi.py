@@ -60,6 +60,31 @@ def test_struct_layout_matches_header(tmp_path):
     assert out[2 + len(fields):] == [getattr(FluidStats, f).offset for f in sfields]
 
 
+def test_rn_sqrt_range_covers_every_scene_with_finite_kernels(tmp_path):
+    """A scene's list passes take the fast per-pair square root (rn_sqrt,
+    compared with the IEEE square root over its whole checked range on the
+    GPU) when the clamped r^2 range [(0.01 h)^2, h^2) lies in that range.
+    That holds for every h from 1e-12 to 1e18, far wider than the h for which
+    the kernels' float constants are finite (h^9 and h^6 neither overflow nor
+    flush to zero: about 1e-4 to 1e4); h = 1e-14 and 1e19 take sqrtf."""
+    src = tmp_path / "covers.cpp"
+    src.write_text("\n".join([
+        '#include <cstdio>', '#include <cstdlib>', '#include "pbf_sqrt.cuh"',
+        "int main(int argc, char** argv) {",
+        "  for (int k = 1; k < argc; ++k) {",
+        "    const float h = std::strtof(argv[k], nullptr);",
+        "    const float min_r = 0.01f * h;",  # as the solver's scene constants
+        '    std::printf("%d\\n", fgb::rn_sqrt_covers(min_r * min_r, h * h) ? 1 : 0);',
+        "  }",
+        "  return 0; }"]))
+    exe = tmp_path / "covers"
+    subprocess.run(["g++", "-std=c++17", "-I", os.path.join(ROOT, "fluidsimulator_gb300", "csrc"), "-I",
+                    os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    hs = [f"{10.0 ** e:g}" for e in range(-12, 19)]
+    out = subprocess.run([str(exe), *hs, "1e-14", "1e19"], capture_output=True, text=True, check=True).stdout.split()
+    assert out == ["1"] * len(hs) + ["0", "0"]
+
+
 def test_status_strings(cuda_lib):
     for code in range(10):
         assert cuda_lib.fluid_status_string(code)
