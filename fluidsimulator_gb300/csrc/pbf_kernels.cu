@@ -129,7 +129,8 @@ __device__ __forceinline__ float spiky(const SceneConst& c, float r) {
 
 // r from r^2 with the 0.01 h floor (core.cpp:303), correctly rounded:
 // rn_sqrt (checked over every scene's clamped r^2 range unless the step's
-// plan says otherwise), or sqrtf in the kIeee instantiations.
+// plan says otherwise), or sqrtf in the kIeee instantiations and the
+// vorticity pass.
 template <bool kIeee = false>
 __device__ __forceinline__ float clamped_r(const SceneConst& c, float r2) {
   const float x = r2 < c.min_r2 ? c.min_r2 : r2;
@@ -1509,7 +1510,10 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_xsph(StepArg
 // Vorticity omega and |omega| (core.cpp:472-508). kLive: 1 = only the live
 // ones among the first entries (live bits from XSPH, same positions); 2 =
 // record the live bits for the eta pass (no XSPH this step).
-template <int U, int kLive, bool kIeee = false>
+// Takes sqrtf for r in every scene (the same bits as rn_sqrt where that is
+// checked): with rn_sqrt this pass ran 0.672 ms against 0.625 at the collapsed
+// 125k step, the same at the 1M lattice step.
+template <int U, int kLive>
 __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_omega(StepArgs a) {
   if (failed(a.status)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1529,7 +1533,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_omega(StepAr
       const float dx = xi.x - r.x.x, dy = xi.y - r.x.y, dz = xi.z - r.x.z;
       const float r2 = dist2(dx, dy, dz);
       if (r2 < h2) {
-        const float gf = spiky(c, clamped_r<kIeee>(c, r2));
+        const float gf = spiky(c, clamped_r<true>(c, r2));
         const float gx = gf * dx, gy = gf * dy, gz = gf * dz;
         const float ux = r.v.x - vi.x, uy = r.v.y - vi.y, uz = r.v.z - vi.z;
         ox += uy * gz - uz * gy;
@@ -1544,7 +1548,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_omega(StepAr
       const PairGeom g = pair_geom(px, py, pz, ra.x, rb.x, nz);
       const bool oka = g.r2.x < h2, okb = g.r2.y < h2;
       if (!oka && !okb) return 0u;
-      const float2 gf = spiky_pair<kIeee>(c, g.r2, nz);
+      const float2 gf = spiky_pair<true>(c, g.r2, nz);
       const float2 gx = pmul(gf, g.dx, nz), gy = pmul(gf, g.dy, nz), gz = pmul(gf, g.dz, nz);
       const float2 ux = psub(make_float2(ra.v.x, rb.v.x), f2(vi.x));
       const float2 uy = psub(make_float2(ra.v.y, rb.v.y), f2(vi.y));
@@ -1934,7 +1938,7 @@ __global__ void __launch_bounds__(kMaxBlock, FGB_LIST_MIN_BLOCKS) k_omega_lanes(
     const float r2 = dist2(dx, dy, dz);
     t.live = in_list && r2 < h2;
     if (t.live) {
-      const float gf = spiky(c, clamped_r(c, r2));
+      const float gf = spiky(c, clamped_r<true>(c, r2));
       const float gx = gf * dx, gy = gf * dy, gz = gf * dz;
       const float ux = r.v.x - vi.x, uy = r.v.y - vi.y, uz = r.v.z - vi.z;
       t.f[0] = uy * gz - uz * gy;
@@ -2097,8 +2101,9 @@ inline int list_grid(const StepArgs& a, int block, int lanes) {
 // Launch shape of list kernel k in the plan: block size, records fetched
 // ahead (one lane per particle) and lanes per particle.
 // A list pass's launch shape. ieee: some scene's clamped r^2 range lies
-// outside rn_sqrt's checked range, so the passes that take square roots run
-// their one-lane, four-ahead form with sqrtf (any shape gives the same bits).
+// outside rn_sqrt's checked range, so lambda, delta and eta run their
+// one-lane, four-ahead form with sqrtf (any shape gives the same bits; the
+// vorticity pass takes sqrtf in every form).
 struct ListShape {
   int block, unroll, lanes;
   bool ieee;
@@ -2206,10 +2211,6 @@ template <int kLive>
 void launch_omega(const StepPlan& plan, cudaStream_t st, const StepArgs& a) {
   const ListShape sh(plan, FLUID_KERNEL_OMEGA);
   const int b = sh.block;
-  if (sh.ieee) {
-    k_omega<4, kLive, true><<<list_grid(a, b, 1), b, 0, st>>>(a);
-    return;
-  }
   switch (sh.lanes) {
     case 2: k_omega_lanes<2, kLive><<<list_grid(a, b, 2), b, 0, st>>>(a); return;
     case 4: k_omega_lanes<4, kLive><<<list_grid(a, b, 4), b, 0, st>>>(a); return;
