@@ -85,6 +85,32 @@ def test_rn_sqrt_range_covers_every_scene_with_finite_kernels(tmp_path):
     assert out == ["1"] * len(hs) + ["0", "0"]
 
 
+def test_default_lanes_by_particle_count(tmp_path):
+    """StepPlan::size_for, the untuned solver's lanes per particle: 8 in
+    lambda and delta up to 16,384 particles in all, 4 up to 32,768, 1 above;
+    1 in every other pass."""
+    src = tmp_path / "lanes.cpp"
+    src.write_text("\n".join([
+        '#include <cstdio>', '#include <cstdlib>', '#include "pbf_launch.h"',
+        "int main(int argc, char** argv) {",
+        "  for (int k = 1; k < argc; ++k) {",
+        "    fgb::StepPlan p;",
+        "    p.size_for(std::atoll(argv[k]));",
+        '    std::printf("%d %d %d %d %d\\n", p.lanes[FLUID_KERNEL_LAMBDA], p.lanes[FLUID_KERNEL_DELTA],',
+        "                p.lanes[FLUID_KERNEL_XSPH], p.lanes[FLUID_KERNEL_OMEGA], p.lanes[FLUID_KERNEL_ETA]);",
+        "  }",
+        "  return 0; }"]))
+    exe = tmp_path / "lanes"
+    cuda_inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
+    subprocess.run(["g++", "-std=c++17", "-I", os.path.join(ROOT, "fluidsimulator_gb300", "csrc"), "-I",
+                    os.path.join(ROOT, "include"), "-I", cuda_inc, str(src), "-o", str(exe)], check=True)
+    counts = [1, 4096, 16384, 16385, 32768, 32769, 1_000_000]
+    out = subprocess.run([str(exe), *map(str, counts)], capture_output=True, text=True, check=True).stdout.split("\n")
+    want = {1: 8, 4096: 8, 16384: 8, 16385: 4, 32768: 4, 32769: 1, 1_000_000: 1}
+    for n, line in zip(counts, out):
+        assert [int(x) for x in line.split()] == [want[n], want[n], 1, 1, 1], (n, line)
+
+
 def test_status_strings(cuda_lib):
     for code in range(10):
         assert cuda_lib.fluid_status_string(code)
